@@ -1,0 +1,107 @@
+// acum_internal.h -- declarations shared by the CUDA translation units and the C++ host
+// layer of libacum.  Not part of the public ABI (include/acum.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/acum.h"
+
+namespace acum {
+
+// Record layout of one element-step for the tonal kernels: 5 groups of 4 reals, so a
+// lane reads its step with 128-bit (FP32) or 2x128-bit (FP64) loads.
+//   g0: x, y, z, dsD          (dsD   = D1 * ds,              D1 = 1/(4 pi a0))
+//   g1: Mx, My, Mz, M2        (M     = V / a0,  M2 = |V|^2 / a0^2)
+//   g2: Mdx, Mdy, Mdz, ATD    (Md    = Vdot / a0, ATD = D1 * rho0 * (V.n) * a0 * ds)
+//   g3: Lx, Ly, Lz, Lm        (L     = P n,  Lm = L.V / a0)
+//   g4: Ldx, Ldy, Ldz, 0      (Ldot  = Pdot n + P ndot)
+// In HBM the records are tiled [element][window][group][32 steps][4]: a (element,
+// 32-step window) tile is contiguous (2560 B in FP32, 5120 B in FP64), which is what one
+// bulk (TMA) copy moves into shared memory.
+constexpr int kGroups = 5;
+constexpr int kWin = 32;
+constexpr int kFields = 18;  // x,y,z,ds, n(3), ndot(3), V(3), Vdot(3), P, Pdot
+
+struct DeviceErr {
+    unsigned int bits;
+    unsigned int disc, order, nonfinite, timeout;
+};
+
+struct TonalGeom {
+    int E, Epad, T, nW, O;
+    double a0, rho, oM, dPsi, dTau, lpi;  // dPsi in radians
+    double vinf[3];
+};
+
+struct TonalTile {
+    int W;      // observers (warps) per block
+    int SE;     // elements per pipeline stage
+    int NS;     // pipeline stages
+    int chunk;  // elements per work item (multiple of SE)
+    int nchunk;
+    int items;
+    size_t smem;
+};
+
+// preprocessing (tonal.cu)
+struct PrepArgs {
+    const float* raw;      // [surf][T][E_i][8] device
+    const int* surf_of;    // not used
+    int nsurf;
+    const long long* raw_off;  // device: start (floats) of each surface's rows
+    const int* e_surf;     // device: surface of each global element
+    const int* e_local;    // device: element index within its surface
+    const int* e_count;    // device: E_i per surface
+    int E, Epad, T, nW;
+    double a0, rho, pscale, cfd, dTau;
+    int periodic, lowpass;
+    double gauss[13];
+    float* ser;            // scratch [E][8][T] float
+    double* rec64;         // [Epad][nW][5][32][4] or null
+    float* rec32;          // [Epad][nW][5][32][4] or null
+    double* fields;        // optional [E][T][18]
+};
+cudaError_t launch_prep(const PrepArgs& a, cudaStream_t s);
+
+// records straight from reference-layout AoS arrays (for the drop-in entry points)
+struct AosArgs {
+    const void* X;  // float or double, AoS as variables.cu:54
+    const void* N;
+    const void* V;
+    const void* PR;
+    int is_double;
+    const long long* xoff;  // device per-element start of its X rows (floats)
+    const long long* noff;
+    const long long* voff;
+    const long long* proff;
+    int E, Epad, T, nW;
+    double a0, rho;
+    double* rec64;
+    float* rec32;
+};
+cudaError_t launch_aos_records(const AosArgs& a, cudaStream_t s);
+
+struct TonalRun {
+    TonalGeom g;
+    TonalTile t;
+    const void* rec;      // rec64 or rec32
+    const double* obs64;  // [O][3]
+    const float* obs32;
+    double* acc;          // [O][T][2] (zeroed when nchunk > 1)
+    DeviceErr* err;
+    int precision;
+};
+cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int num_sms, size_t smem_optin);
+cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s);
+// acc [O][T][2] -> pT/pL/pA [T][O]; mode 0 overwrite double, 1 accumulate double,
+// 2 accumulate float (drop-in)
+cudaError_t launch_finalize(const double* acc, int O, int T, void* pT, void* pL, void* pA, int mode,
+                            cudaStream_t s);
+
+// misc
+void gauss_taps(double* w);
+
+}  // namespace acum

@@ -1,0 +1,875 @@
+// tonal.cu -- sm_103a kernels of the tonal (FW-H thickness + loading) path.
+//
+//  prep_kernel         preprocess_imper (preprocess.cu:228-413) on the GPU in FP64, one
+//                      block per element: scaling, make_periodic, optional lowpass,
+//                      periodic d/dtau of P, n, x and of the velocity; writes the tiled
+//                      FP64 and FP32 records the tonal kernels stream.
+//  aos_record_kernel   the same records from the reference's AoS arrays (drop-in entry).
+//  tonal_kernel<F64>   the hot loop (core.cu:18-259 semantics).  A block owns W observers,
+//                      one warp each, and a chunk of elements.  Lane = source step inside
+//                      a 32-step window.  Element tiles are moved into shared memory by
+//                      bulk TMA copies (cp.async.bulk + mbarrier complete_tx), shared by
+//                      the W observer warps.  Each lane evaluates the Farassat-1A
+//                      integrand and the observer time of its step; the periodic hat-
+//                      function binning of core.cu:166-231 is done as its equivalent, the
+//                      piecewise-linear interpolation of the retarded-time signal onto the
+//                      bin grid: lane tau fills the bins in (t(tau-1), t(tau)] from its own
+//                      sample and its left neighbour's (one warp shuffle), so lanes never
+//                      collide and each warp accumulates into its own observer's bins in
+//                      shared memory with plain read-modify-writes -- no atomics.  The
+//                      block adds its bins to global memory once at the end.
+//  finalize_kernel     [obs][bin][2] sums -> pT/pL/pA [bin][obs] (main.cu:224 layout).
+//
+// Precision forms.  F64: every quantity in double, observer time in radians as the
+// reference forms it; matches the reference's FP64 build.  Mixed: the integrand in FP32;
+// the observer time carried as an integer bin index plus an FP32 fraction built from a
+// float-float product (no rounding beyond that of the FP32 retarded time); the bin sums
+// as float-float pairs (TwoSum) in shared memory, added in FP64 at the flush.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <type_traits>
+
+#include "acum_internal.h"
+
+namespace acum {
+
+// ------------------------------------------------------------------ helpers
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Every wait on a barrier is bounded: after kMaxSpin polls the wait gives up, records
+// ACUM_DEVERR_TIMEOUT and the kernel unwinds instead of hanging.
+constexpr long kMaxSpin = 1L << 24;
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity)
+{
+    for (long it = 0; it < kMaxSpin; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// bulk TMA copy global -> shared, completion signalled on `bar` (bytes % 16 == 0,
+// both addresses 16-byte aligned)
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void flag(DeviceErr* e, unsigned bit, unsigned* counter)
+{
+    atomicOr(&e->bits, bit);
+    atomicAdd(counter, 1u);
+}
+
+// TwoSum (Knuth): s + err == a + b exactly; accumulates the rounding error into lo.
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float b)
+{
+    float s = hi + b;
+    float bb = s - hi;
+    float err = (hi - (s - bb)) + (b - bb);
+    hi = s;
+    lo += err;
+}
+
+struct dbl4 {
+    double x, y, z, w;
+};
+
+// ------------------------------------------------------------ preprocessing
+
+// One block per element.  Shared memory: the element's rows [T][8] as float, then two
+// double series (P and a ping-pong buffer for the filters).
+__global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
+{
+    extern __shared__ __align__(16) unsigned char sm[];
+    const int T = a.T;
+    float* rows = reinterpret_cast<float*>(sm);                  // [T][8]
+    double* P = reinterpret_cast<double*>(sm + (size_t)T * 32);  // [T]
+    double* Q = P + T;                                           // [T]
+    const int e = blockIdx.x;
+    const int s = a.e_surf[e];
+    const int j = a.e_local[e];
+    const int Es = a.e_count[s];
+    const float* base = a.raw + a.raw_off[s];
+    for (int t = threadIdx.x; t < T; t += blockDim.x) {
+        const float4* src = reinterpret_cast<const float4*>(base + ((size_t)t * Es + j) * 8);
+        float4 v0 = src[0], v1 = src[1];
+        float4* dst = reinterpret_cast<float4*>(rows + (size_t)t * 8);
+        dst[0] = v0;
+        dst[1] = v1;
+    }
+    __syncthreads();
+    // scaled pressure (preprocess.cu:279)
+    for (int t = threadIdx.x; t < T; t += blockDim.x) P[t] = (double)rows[t * 8 + 3] * a.pscale;
+    __syncthreads();
+    // make_periodic (mathfunc.cu:165-206): cubic through the end mismatch
+    {
+        double p0 = P[0], p1 = P[1], pm = P[T - 2], pn = P[T - 1];
+        const double g0 = p0 - (p1 - p0);  // linear extrapolation before the first sample
+        double k2 = pn, k1 = g0, s2 = pn - pm, s1 = p0 - g0;
+        int xm = T;
+        double dd = k1, cc = s1 - s2;
+        double bb = -2.0 * (s1 - s2) / xm - 3.0 * (k1 - k2) / xm / xm;
+        double aa = -bb / xm - (s1 - s2) / xm / xm - (k1 - k2) / xm / xm / xm;
+        __syncthreads();
+        for (int t = threadIdx.x; t < T; t += blockDim.x) {
+            int i = t + 1;
+            double cub = aa * i * i * i + bb * i * i + cc * i + dd;
+            P[t] = P[t] - (cub - k2);
+        }
+        __syncthreads();
+    }
+    if (a.lowpass == 1) {
+        // two passes of (3-point periodic median, 13-tap periodic Gaussian)
+        // (preprocess.cu:323-333, mathfunc.cu:208-341 and 375-421)
+        for (int pass = 0; pass < 2; ++pass) {
+            for (int t = threadIdx.x; t < T; t += blockDim.x) {
+                double l = P[t == 0 ? T - 1 : t - 1], m = P[t], r = P[t == T - 1 ? 0 : t + 1];
+                double hi = l > m ? l : m;
+                hi = hi > r ? hi : r;
+                double lo = l < m ? l : m;
+                lo = lo < r ? lo : r;
+                Q[t] = (l < hi && l > lo) ? l : ((m < hi && m > lo) ? m : r);
+            }
+            __syncthreads();
+            for (int t = threadIdx.x; t < T; t += blockDim.x) {
+                double acc = 0.0;
+                for (int k = 0; k < 13; ++k) {
+                    int q = t + k - 6;
+                    if (q < 0) q += T;
+                    else if (q > T - 1) q -= T;
+                    acc += a.gauss[k] * Q[q];
+                }
+                P[t] = acc;
+            }
+            __syncthreads();
+        }
+    }
+    const double two_dt = 2.0 * a.dTau;
+    const double D1 = 1.0 / (4.0 * M_PI * a.a0);
+    for (int t = threadIdx.x; t < T; t += blockDim.x) {
+        const int tm = t == 0 ? T - 1 : t - 1, tp = t == T - 1 ? 0 : t + 1;
+        const int tmm = tm == 0 ? T - 1 : tm - 1, tpp = tp == T - 1 ? 0 : tp + 1;
+        double Pd;
+        if (a.periodic == 1) {
+            Pd = (P[tp] - P[tm]) / two_dt;
+        } else {
+            // central interior, ends by cubic extrapolation (mathfunc.cu:142-159)
+            auto cd = [&](int k) { return (P[k + 1] - P[k - 1]) / two_dt; };
+            if (t == 0) Pd = 3 * cd(1) - 3 * cd(2) + cd(3);
+            else if (t == T - 1) Pd = 3 * cd(T - 2) - 3 * cd(T - 3) + cd(T - 4);
+            else Pd = cd(t);
+        }
+        const float* r0 = rows + (size_t)t * 8;
+        const float* rm = rows + (size_t)tm * 8;
+        const float* rp = rows + (size_t)tp * 8;
+        const float* rmm = rows + (size_t)tmm * 8;
+        const float* rpp = rows + (size_t)tpp * 8;
+        double x[3], n[3], nd[3], v[3], vd[3];
+        for (int c = 0; c < 3; ++c) {
+            x[c] = (double)r0[c] * a.cfd;
+            n[c] = (double)r0[5 + c];
+            nd[c] = ((double)rp[5 + c] - (double)rm[5 + c]) / two_dt;
+            double xp = (double)rp[c] * a.cfd, xm = (double)rm[c] * a.cfd;
+            double xpp = (double)rpp[c] * a.cfd, xmm = (double)rmm[c] * a.cfd;
+            v[c] = (xp - xm) / two_dt;
+            double vp = (xpp - x[c]) / two_dt, vm = (x[c] - xmm) / two_dt;
+            vd[c] = (vp - vm) / two_dt;
+        }
+        const double ds = (double)r0[4] * a.cfd * a.cfd;
+        const double Pt = P[t];
+        if (a.fields) {
+            double* f = a.fields + ((size_t)e * T + t) * kFields;
+            f[0] = x[0]; f[1] = x[1]; f[2] = x[2]; f[3] = ds;
+            f[4] = n[0]; f[5] = n[1]; f[6] = n[2];
+            f[7] = nd[0]; f[8] = nd[1]; f[9] = nd[2];
+            f[10] = v[0]; f[11] = v[1]; f[12] = v[2];
+            f[13] = vd[0]; f[14] = vd[1]; f[15] = vd[2];
+            f[16] = Pt; f[17] = Pd;
+        }
+        // records
+        const double ia0 = 1.0 / a.a0;
+        double rec[20];
+        rec[0] = x[0]; rec[1] = x[1]; rec[2] = x[2]; rec[3] = D1 * ds;
+        rec[4] = v[0] * ia0; rec[5] = v[1] * ia0; rec[6] = v[2] * ia0;
+        rec[7] = (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) * ia0 * ia0;
+        rec[8] = vd[0] * ia0; rec[9] = vd[1] * ia0; rec[10] = vd[2] * ia0;
+        rec[11] = D1 * a.rho * (v[0] * n[0] + v[1] * n[1] + v[2] * n[2]) * a.a0 * ds;
+        double L[3], Ld[3];
+        for (int c = 0; c < 3; ++c) {
+            L[c] = Pt * n[c];
+            Ld[c] = Pd * n[c] + Pt * nd[c];
+        }
+        rec[12] = L[0]; rec[13] = L[1]; rec[14] = L[2];
+        rec[15] = (L[0] * v[0] + L[1] * v[1] + L[2] * v[2]) * ia0;
+        rec[16] = Ld[0]; rec[17] = Ld[1]; rec[18] = Ld[2]; rec[19] = 0.0;
+        const int w = t / kWin, lane = t % kWin;
+        const size_t tile = ((size_t)e * a.nW + w) * (kGroups * kWin * 4);
+        for (int q = 0; q < kGroups; ++q) {
+            const size_t off = tile + ((size_t)q * kWin + lane) * 4;
+            if (a.rec64) {
+                double2* d = reinterpret_cast<double2*>(a.rec64 + off);
+                d[0] = make_double2(rec[4 * q], rec[4 * q + 1]);
+                d[1] = make_double2(rec[4 * q + 2], rec[4 * q + 3]);
+            }
+            if (a.rec32) {
+                *reinterpret_cast<float4*>(a.rec32 + off) =
+                    make_float4((float)rec[4 * q], (float)rec[4 * q + 1], (float)rec[4 * q + 2], (float)rec[4 * q + 3]);
+            }
+        }
+    }
+}
+
+cudaError_t launch_prep(const PrepArgs& a, cudaStream_t s)
+{
+    size_t smem = (size_t)a.T * 32 + (size_t)a.T * 16;
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        cudaError_t err = cudaFuncSetAttribute(prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err != cudaSuccess) return err;
+        configured = smem;
+    }
+    prep_kernel<<<a.E, 256, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+// records from the reference's AoS arrays; one thread per (element, step)
+template <typename S>
+__global__ void aos_record_kernel(AosArgs a)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)a.E * a.T) return;
+    const int e = (int)(idx / a.T), t = (int)(idx % a.T);
+    const S* X = reinterpret_cast<const S*>(a.X) + a.xoff[e] + (size_t)t * 4;
+    const S* N = reinterpret_cast<const S*>(a.N) + a.noff[e] + (size_t)t * 6;
+    const S* V = reinterpret_cast<const S*>(a.V) + a.voff[e] + (size_t)t * 6;
+    const S* PR = reinterpret_cast<const S*>(a.PR) + a.proff[e] + (size_t)t * 2;
+    const double D1 = 1.0 / (4.0 * M_PI * a.a0), ia0 = 1.0 / a.a0;
+    double x[3] = {(double)X[0], (double)X[1], (double)X[2]}, ds = (double)X[3];
+    double n[3] = {(double)N[0], (double)N[1], (double)N[2]}, nd[3] = {(double)N[3], (double)N[4], (double)N[5]};
+    double v[3] = {(double)V[0], (double)V[1], (double)V[2]}, vd[3] = {(double)V[3], (double)V[4], (double)V[5]};
+    double Pt = (double)PR[0], Pd = (double)PR[1];
+    double rec[20];
+    rec[0] = x[0]; rec[1] = x[1]; rec[2] = x[2]; rec[3] = D1 * ds;
+    rec[4] = v[0] * ia0; rec[5] = v[1] * ia0; rec[6] = v[2] * ia0;
+    rec[7] = (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) * ia0 * ia0;
+    rec[8] = vd[0] * ia0; rec[9] = vd[1] * ia0; rec[10] = vd[2] * ia0;
+    rec[11] = D1 * a.rho * (v[0] * n[0] + v[1] * n[1] + v[2] * n[2]) * a.a0 * ds;
+    for (int c = 0; c < 3; ++c) {
+        rec[12 + c] = Pt * n[c];
+        rec[16 + c] = Pd * n[c] + Pt * nd[c];
+    }
+    rec[15] = (rec[12] * v[0] + rec[13] * v[1] + rec[14] * v[2]) * ia0;
+    rec[19] = 0.0;
+    const int w = t / kWin, lane = t % kWin;
+    const size_t tile = ((size_t)e * a.nW + w) * (kGroups * kWin * 4);
+    for (int q = 0; q < kGroups; ++q) {
+        const size_t off = tile + ((size_t)q * kWin + lane) * 4;
+        if (a.rec64) {
+            double2* d = reinterpret_cast<double2*>(a.rec64 + off);
+            d[0] = make_double2(rec[4 * q], rec[4 * q + 1]);
+            d[1] = make_double2(rec[4 * q + 2], rec[4 * q + 3]);
+        }
+        if (a.rec32)
+            *reinterpret_cast<float4*>(a.rec32 + off) =
+                make_float4((float)rec[4 * q], (float)rec[4 * q + 1], (float)rec[4 * q + 2], (float)rec[4 * q + 3]);
+    }
+}
+
+cudaError_t launch_aos_records(const AosArgs& a, cudaStream_t s)
+{
+    long long n = (long long)a.E * a.T;
+    int blocks = (int)((n + 255) / 256);
+    if (a.is_double) aos_record_kernel<double><<<blocks, 256, 0, s>>>(a);
+    else aos_record_kernel<float><<<blocks, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------- tonal kernel
+
+struct KParams {
+    const void* rec;
+    int Epad, T, nW, O;
+    const float* obs32;
+    const double* obs64;
+    // mixed constants
+    float a0f, alphaf, ialphaf, vxf, vyf, vzf, kbhi, kblo, invTf;
+    // FP64 constants
+    double a0, alpha, ialpha, vx, vy, vz, dTau, oM, dPsi, lpi;
+    int W, NS, chunk, nchunk, obs_tiles;
+    double* acc;
+    DeviceErr* err;
+};
+
+struct SmpF {
+    int k;      // integer part of the observer time in bins (unwrapped)
+    float f;    // fraction in [0, 1)
+    float pt, pl;
+};
+
+struct SmpD {
+    int nb;     // floor(t / dPsi)
+    double t;   // observer time [rad]
+    double pt, pl;
+};
+
+// Farassat-1A integrand with U = V and the normal-velocity rates forced to 0
+// (core.cu:93-154), rearranged around K = Mdot_r + (a0/r)(Mr - M^2):
+//   pThick = ATD/r * G^3 * K
+//   pLoad  = dsD/r * G^2 * (Ldot_r + (a0/r)(L_r - L_M) + L_r G K),  G = 1/(1-Mr)
+// where the records carry D1 = 1/(4 pi a0) inside ATD and dsD.
+__device__ __forceinline__ SmpF sample_mixed(const float4& g0, const float4& g1, const float4& g2, const float4& g3,
+                                             const float4& g4, float ox, float oy, float oz, const KParams& p,
+                                             int tau)
+{
+    const float dx = ox - g0.x, dy = oy - g0.y, dz = oz - g0.z;
+    const float c = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float beta = fmaf(dx, p.vxf, fmaf(dy, p.vyf, dz * p.vzf));
+    // retarded time: positive root of (|v|^2 - a0^2) t^2 - 2 beta t + c = 0 (core.cu:261-279)
+    const float q2 = fmaf(beta, beta, p.alphaf * c);
+    const float s = q2 * rsqrtf(q2);
+    const float tr = (s - beta) * p.ialphaf;
+    const float rx = fmaf(-p.vxf, tr, dx), ry = fmaf(-p.vyf, tr, dy), rz = fmaf(-p.vzf, tr, dz);
+    const float r = p.a0f * tr;
+    const float ir = __fdividef(1.0f, r);
+    const float Mr = fmaf(g1.x, rx, fmaf(g1.y, ry, g1.z * rz)) * ir;
+    const float Mdr = fmaf(g2.x, rx, fmaf(g2.y, ry, g2.z * rz)) * ir;
+    const float Lr = fmaf(g3.x, rx, fmaf(g3.y, ry, g3.z * rz)) * ir;
+    const float Ldr = fmaf(g4.x, rx, fmaf(g4.y, ry, g4.z * rz)) * ir;
+    const float G = __fdividef(1.0f, 1.0f - Mr);
+    const float qa = p.a0f * ir;
+    const float K = fmaf(qa, Mr - g1.w, Mdr);
+    const float base = ir * G * G;
+    SmpF o;
+    o.pt = g2.w * base * G * K;
+    o.pl = g0.w * base * fmaf(Lr * G, K, fmaf(qa, Lr - g3.w, Ldr));
+    // observer time in bins: tau + tr * (oM / dPsi), the product kept as a float pair
+    const float ph = tr * p.kbhi;
+    const float pe = fmaf(tr, p.kbhi, -ph) + tr * p.kblo;
+    const float n0 = floorf(ph);
+    float f = (ph - n0) + pe;
+    int k = tau + (int)n0;
+    if (f >= 1.0f) { f -= 1.0f; k += 1; }
+    else if (f < 0.0f) { f += 1.0f; k -= 1; }
+    o.k = k;
+    o.f = f;
+    return o;
+}
+
+__device__ __forceinline__ SmpD sample_f64(const dbl4& g0, const dbl4& g1, const dbl4& g2, const dbl4& g3,
+                                           const dbl4& g4, double ox, double oy, double oz, const KParams& p, int tau)
+{
+    const double dx = ox - g0.x, dy = oy - g0.y, dz = oz - g0.z;
+    const double c = dx * dx + dy * dy + dz * dz;
+    const double beta = dx * p.vx + dy * p.vy + dz * p.vz;
+    const double s = sqrt(beta * beta + p.alpha * c);
+    const double tr = (s - beta) * p.ialpha;
+    const double rx = dx - p.vx * tr, ry = dy - p.vy * tr, rz = dz - p.vz * tr;
+    const double r = p.a0 * tr;
+    const double ir = 1.0 / r;
+    const double Mr = (g1.x * rx + g1.y * ry + g1.z * rz) * ir;
+    const double Mdr = (g2.x * rx + g2.y * ry + g2.z * rz) * ir;
+    const double Lr = (g3.x * rx + g3.y * ry + g3.z * rz) * ir;
+    const double Ldr = (g4.x * rx + g4.y * ry + g4.z * rz) * ir;
+    const double G = 1.0 / (1.0 - Mr);
+    const double qa = p.a0 * ir;
+    const double K = Mdr + qa * (Mr - g1.w);
+    const double base = ir * G * G;
+    SmpD o;
+    o.pt = g2.w * base * G * K;
+    o.pl = g0.w * base * (Ldr + qa * (Lr - g3.w) + Lr * G * K);
+    // observer time (core.cu:156) and its bin floor
+    o.t = (tau * p.dTau + tr) * p.oM;
+    o.nb = (int)floor(o.t / p.dPsi);
+    return o;
+}
+
+__device__ __forceinline__ int wrap_bin(int n, int T, float invT)
+{
+    int q = __float2int_rz((float)n * invT);
+    int r = n - q * T;
+    if (r < 0) r += T;
+    else if (r >= T) r -= T;
+    return r;
+}
+
+// bins n with u(prev) < n <= u(cur), value interpolated between the two samples
+__device__ __forceinline__ void deposit_mixed(float4* acc, int T, float invT, const SmpF& a, const SmpF& b, int kshift,
+                                              DeviceErr* err)
+{
+    const int kb = b.k + kshift;
+    const int cnt = kb - a.k;
+    const float du = (float)cnt + (b.f - a.f);
+    // one step never spans a whole period of bins for |Mr| < 1; anything else is bad
+    // geometry (or a non-finite time) and must not turn into a long loop
+    if (!(du > 0.0f) || cnt > T) {
+        flag(err, ACUM_DEVERR_ORDER, &err->order);
+        return;
+    }
+    if (!(fabsf(b.pt) < 3.0e38f) || !(fabsf(b.pl) < 3.0e38f)) {
+        flag(err, ACUM_DEVERR_NONFINITE, &err->nonfinite);
+        return;
+    }
+    const float inv = __fdividef(1.0f, du);
+    const float dT = b.pt - a.pt, dL = b.pl - a.pl;
+    int idx = wrap_bin(a.k + 1, T, invT);
+    for (int m = 1; m <= cnt; ++m) {
+        const float w = ((float)m - a.f) * inv;
+        const float vT = fmaf(w, dT, a.pt), vL = fmaf(w, dL, a.pl);
+        float4 s = acc[idx];
+        ff_add(s.x, s.y, vT);
+        ff_add(s.z, s.w, vL);
+        acc[idx] = s;
+        if (++idx == T) idx = 0;
+    }
+}
+
+__device__ __forceinline__ void deposit_f64(double2* acc, int T, const KParams& p, const SmpD& a, const SmpD& b,
+                                            double tshift, int nshift, DeviceErr* err)
+{
+    const double tb = b.t + tshift;
+    const int nbb = b.nb + nshift;
+    if (!(tb > a.t) || nbb - a.nb > T || nbb - a.nb < 0) {
+        flag(err, ACUM_DEVERR_ORDER, &err->order);
+        return;
+    }
+    if (!(fabs(b.pt) < 1e300) || !(fabs(b.pl) < 1e300)) {
+        flag(err, ACUM_DEVERR_NONFINITE, &err->nonfinite);
+        return;
+    }
+    const double inv = 1.0 / (tb - a.t);
+    const double dT = b.pt - a.pt, dL = b.pl - a.pl;
+    int idx = (a.nb + 1) % T;
+    if (idx < 0) idx += T;
+    for (int n = a.nb + 1; n <= nbb; ++n) {
+        const double w = (n * p.dPsi - a.t) * inv;
+        double2 s = acc[idx];
+        s.x += a.pt + w * dT;
+        s.y += a.pl + w * dL;
+        acc[idx] = s;
+        if (++idx == T) idx = 0;
+    }
+}
+
+template <typename S>
+__device__ __forceinline__ S shfl_smp(const S& v, int src);
+template <>
+__device__ __forceinline__ SmpF shfl_smp<SmpF>(const SmpF& v, int src)
+{
+    SmpF o;
+    o.k = __shfl_sync(0xffffffffu, v.k, src);
+    o.f = __shfl_sync(0xffffffffu, v.f, src);
+    o.pt = __shfl_sync(0xffffffffu, v.pt, src);
+    o.pl = __shfl_sync(0xffffffffu, v.pl, src);
+    return o;
+}
+template <>
+__device__ __forceinline__ SmpD shfl_smp<SmpD>(const SmpD& v, int src)
+{
+    SmpD o;
+    o.nb = __shfl_sync(0xffffffffu, v.nb, src);
+    o.t = __shfl_sync(0xffffffffu, v.t, src);
+    o.pt = __shfl_sync(0xffffffffu, v.pt, src);
+    o.pl = __shfl_sync(0xffffffffu, v.pl, src);
+    return o;
+}
+template <typename S>
+__device__ __forceinline__ S shfl_up_smp(const S& v);
+template <>
+__device__ __forceinline__ SmpF shfl_up_smp<SmpF>(const SmpF& v)
+{
+    SmpF o;
+    o.k = __shfl_up_sync(0xffffffffu, v.k, 1);
+    o.f = __shfl_up_sync(0xffffffffu, v.f, 1);
+    o.pt = __shfl_up_sync(0xffffffffu, v.pt, 1);
+    o.pl = __shfl_up_sync(0xffffffffu, v.pl, 1);
+    return o;
+}
+template <>
+__device__ __forceinline__ SmpD shfl_up_smp<SmpD>(const SmpD& v)
+{
+    SmpD o;
+    o.nb = __shfl_up_sync(0xffffffffu, v.nb, 1);
+    o.t = __shfl_up_sync(0xffffffffu, v.t, 1);
+    o.pt = __shfl_up_sync(0xffffffffu, v.pt, 1);
+    o.pl = __shfl_up_sync(0xffffffffu, v.pl, 1);
+    return o;
+}
+
+template <bool F64, int SE>
+__global__ void __launch_bounds__(512, 1) tonal_kernel(const KParams p)
+{
+    using Real = typename std::conditional<F64, double, float>::type;
+    using Smp = typename std::conditional<F64, SmpD, SmpF>::type;
+    using Acc = typename std::conditional<F64, double2, float4>::type;
+    constexpr int kTile = kGroups * kWin * 4;  // reals per (element, window) tile
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ int s_abort;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int W = p.W, T = p.T, NS = p.NS, nW = p.nW;
+    Acc* acc_all = reinterpret_cast<Acc*>(smem);
+    Real* stages = reinterpret_cast<Real*>(smem + (size_t)W * T * 16);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)W * T * 16 + (size_t)NS * SE * kTile * sizeof(Real));
+    Acc* acc = acc_all + (size_t)warp * T;
+
+    const int item = blockIdx.x;
+    const int ot = item % p.obs_tiles, ec = item / p.obs_tiles;
+    const int o = ot * W + warp;
+    const bool obs_ok = o < p.O;
+    const int e0 = ec * p.chunk;
+    const int e1 = min(e0 + p.chunk, p.Epad);
+    const int ngroups = e1 > e0 ? (e1 - e0) / SE : 0;
+    const int N = ngroups * nW;
+
+    for (int i = threadIdx.x; i < W * T; i += blockDim.x) {
+        if constexpr (F64) acc_all[i] = make_double2(0.0, 0.0);
+        else acc_all[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NS; ++s) mbar_init(&bars[s], 1);
+        mbar_fence_init();
+        s_abort = 0;
+    }
+    __syncthreads();
+
+    const Real* rec = reinterpret_cast<const Real*>(p.rec);
+    const uint32_t tile_bytes = kTile * sizeof(Real);
+    int issued = 0;
+    auto issue = [&](int i) {
+        const int s = i % NS, g = i / nW, w = i % nW;
+        mbar_expect_tx(&bars[s], tile_bytes * SE);
+        for (int j = 0; j < SE; ++j) {
+            const int e = e0 + g * SE + j;
+            bulk_g2s(stages + ((size_t)s * SE + j) * kTile, rec + ((size_t)e * nW + w) * kTile, tile_bytes, &bars[s]);
+        }
+    };
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < NS - 1 && i < N; ++i) issue(i);
+        issued = min(NS - 1, N);
+    }
+
+    Real ox = 0, oy = 0, oz = 0;
+    if (obs_ok) {
+        if constexpr (F64) {
+            ox = p.obs64[3 * o]; oy = p.obs64[3 * o + 1]; oz = p.obs64[3 * o + 2];
+        } else {
+            ox = p.obs32[3 * o]; oy = p.obs32[3 * o + 1]; oz = p.obs32[3 * o + 2];
+        }
+    }
+    Smp carry[SE], first[SE];
+    const float invT = 1.0f / (float)T;
+
+    int done = 0;
+    for (int i = 0; i < N; ++i) {
+        if (threadIdx.x == 0 && i + NS - 1 < N) {
+            issue(i + NS - 1);
+            issued = i + NS;
+        }
+        const int s = i % NS;
+        // the wait result is made warp-uniform before any shuffle below
+        const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&bars[s], (uint32_t)((i / NS) & 1)));
+        if (!ok && lane == 0) {
+            s_abort = 1;
+            flag(p.err, ACUM_DEVERR_TIMEOUT, &p.err->timeout);
+        }
+        const int w = i % nW;
+        const int tau = w * kWin + lane;
+        const bool valid = tau < T;
+        if (ok && obs_ok) {
+            const Real* st = stages + (size_t)s * SE * kTile;
+            Smp cur[SE];
+#pragma unroll
+            for (int j = 0; j < SE; ++j) {
+                const Real* tl = st + (size_t)j * kTile + lane * 4;
+                if constexpr (F64) {
+                    dbl4 g[kGroups];
+#pragma unroll
+                    for (int q = 0; q < kGroups; ++q) {
+                        const double2* pp = reinterpret_cast<const double2*>(tl + q * kWin * 4);
+                        double2 u0 = pp[0], u1 = pp[1];
+                        g[q] = dbl4{u0.x, u0.y, u1.x, u1.y};
+                    }
+                    cur[j] = sample_f64(g[0], g[1], g[2], g[3], g[4], ox, oy, oz, p, tau);
+                } else {
+                    float4 g[kGroups];
+#pragma unroll
+                    for (int q = 0; q < kGroups; ++q) g[q] = *reinterpret_cast<const float4*>(tl + q * kWin * 4);
+                    cur[j] = sample_mixed(g[0], g[1], g[2], g[3], g[4], ox, oy, oz, p, tau);
+                }
+            }
+            const int last = min(31, T - 1 - w * kWin);
+#pragma unroll
+            for (int j = 0; j < SE; ++j) {
+                Smp prev = shfl_up_smp(cur[j]);
+                if (lane == 0) prev = carry[j];
+                const bool has_prev = valid && (lane > 0 || w > 0);
+                if constexpr (F64) {
+                    if (has_prev) deposit_f64(acc, T, p, prev, cur[j], 0.0, 0, p.err);
+                } else {
+                    if (has_prev) deposit_mixed(acc, T, invT, prev, cur[j], 0, p.err);
+                }
+                if (w == 0) first[j] = shfl_smp(cur[j], 0);
+                carry[j] = shfl_smp(cur[j], last);
+                if (w == nW - 1 && lane == 0) {
+                    // the periodic wrap: (t(T-1), t(0) + period] (core.cu:173-194)
+                    if constexpr (F64) {
+                        SmpD f0 = first[j];
+                        const double tw = f0.t + p.lpi;
+                        const int nw = (int)floor(tw / p.dPsi);
+                        deposit_f64(acc, T, p, carry[j], f0, p.lpi, nw - f0.nb, p.err);
+                    } else {
+                        deposit_mixed(acc, T, invT, carry[j], first[j], T, p.err);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        done = i + 1;
+        if (s_abort) break;
+    }
+    if (s_abort) {
+        // drain the copies still in flight before the block exits (bounded)
+        if (threadIdx.x == 0)
+            for (int i = done; i < issued; ++i) (void)mbar_wait_bounded(&bars[i % NS], (uint32_t)((i / NS) & 1));
+        __syncthreads();
+        return;
+    }
+    // flush this block's bins
+    if (obs_ok) {
+        double* g = p.acc + (size_t)o * T * 2;
+        for (int n = lane; n < T; n += 32) {
+            double vT, vL;
+            if constexpr (F64) {
+                double2 a = acc[n];
+                vT = a.x;
+                vL = a.y;
+            } else {
+                float4 a = acc[n];
+                vT = (double)a.x + (double)a.y;
+                vL = (double)a.z + (double)a.w;
+            }
+            if (p.nchunk == 1) {
+                reinterpret_cast<double2*>(g)[n] = make_double2(vT, vL);
+            } else {
+                atomicAdd(g + 2 * n, vT);
+                atomicAdd(g + 2 * n + 1, vL);
+            }
+        }
+    }
+}
+
+constexpr int kSE32 = 4;
+constexpr int kSE64 = 2;
+
+static size_t tonal_smem(int W, int T, int NS, int SE, int real_bytes)
+{
+    return (size_t)W * T * 16 + (size_t)NS * SE * kGroups * kWin * 4 * real_bytes + (size_t)NS * 8;
+}
+
+cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int num_sms, size_t smem_optin)
+{
+    const bool f64 = r.precision == ACUM_PLAIN_FP64;
+    const int rb = f64 ? 8 : 4;
+    const int SE = f64 ? kSE64 : kSE32;
+    (void)SE_req;
+    const int NS = 3;
+    const int T = r.g.T;
+    int W = W_req > 0 ? W_req : 16;
+    W = std::min(W, 16);
+    while (W > 1 && tonal_smem(W, T, NS, SE, rb) > smem_optin) --W;
+    if (tonal_smem(W, T, NS, SE, rb) > smem_optin) return cudaErrorInvalidValue;
+    if (W_req <= 0) {
+        // do not spread few observers over many idle warps
+        W = std::max(1, std::min(W, r.g.O));
+    }
+    TonalTile& t = r.t;
+    t.W = W;
+    t.SE = SE;
+    t.NS = NS;
+    t.smem = tonal_smem(W, T, NS, SE, rb);
+    const int obs_tiles = (r.g.O + W - 1) / W;
+    const int per_sm = std::max(1, (int)((228 * 1024) / (t.smem + 1024)));
+    const int slots = num_sms * per_sm;
+    const int groups = r.g.Epad / SE;
+    const int ips = items_per_sm > 0 ? items_per_sm : 4;
+    // number of element chunks: enough work items to fill the machine; among the
+    // candidates prefer the one with the smallest wave-quantisation loss
+    int best = 1;
+    double best_cost = 1e30;
+    const int maxc = std::max(1, std::min(groups, std::max(1, (ips * slots + obs_tiles - 1) / obs_tiles)));
+    for (int c = 1; c <= maxc; ++c) {
+        const long items = (long)obs_tiles * c;
+        const double waves = (double)items / slots;
+        const double eff = waves / std::ceil(waves);
+        const double cost = 1.0 / eff + 0.002 * c;
+        if (cost < best_cost) {
+            best_cost = cost;
+            best = c;
+        }
+    }
+    t.nchunk = best;
+    const int gpc = (groups + best - 1) / best;
+    t.chunk = gpc * SE;
+    t.nchunk = (groups + gpc - 1) / gpc;
+    t.items = obs_tiles * t.nchunk;
+    return cudaSuccess;
+}
+
+template <bool F64, int SE>
+static cudaError_t launch_t(const KParams& kp, int items, int threads, size_t smem, cudaStream_t s)
+{
+    static size_t configured = 0;
+    if (smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(tonal_kernel<F64, SE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    tonal_kernel<F64, SE><<<items, threads, smem, s>>>(kp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s)
+{
+    KParams kp;
+    const TonalGeom& g = r.g;
+    kp.rec = r.rec;
+    kp.Epad = g.Epad;
+    kp.T = g.T;
+    kp.nW = g.nW;
+    kp.O = g.O;
+    kp.obs32 = r.obs32;
+    kp.obs64 = r.obs64;
+    const double alpha = g.a0 * g.a0 - (g.vinf[0] * g.vinf[0] + g.vinf[1] * g.vinf[1] + g.vinf[2] * g.vinf[2]);
+    kp.a0 = g.a0;
+    kp.alpha = alpha;
+    kp.ialpha = 1.0 / alpha;
+    kp.vx = g.vinf[0];
+    kp.vy = g.vinf[1];
+    kp.vz = g.vinf[2];
+    kp.dTau = g.dTau;
+    kp.oM = g.oM;
+    kp.dPsi = g.dPsi;
+    kp.lpi = g.T * g.dPsi;
+    kp.a0f = (float)g.a0;
+    kp.alphaf = (float)alpha;
+    kp.ialphaf = (float)(1.0 / alpha);
+    kp.vxf = (float)g.vinf[0];
+    kp.vyf = (float)g.vinf[1];
+    kp.vzf = (float)g.vinf[2];
+    const double kb = g.oM / g.dPsi;  // bins per second of retarded time
+    kp.kbhi = (float)kb;
+    kp.kblo = (float)(kb - (double)kp.kbhi);
+    kp.invTf = 1.0f / (float)g.T;
+    kp.W = r.t.W;
+    kp.NS = r.t.NS;
+    kp.chunk = r.t.chunk;
+    kp.nchunk = r.t.nchunk;
+    kp.obs_tiles = (g.O + r.t.W - 1) / r.t.W;
+    kp.acc = r.acc;
+    kp.err = r.err;
+    const int threads = 32 * r.t.W;
+    if (r.precision == ACUM_PLAIN_FP64) return launch_t<true, kSE64>(kp, r.t.items, threads, r.t.smem, s);
+    return launch_t<false, kSE32>(kp, r.t.items, threads, r.t.smem, s);
+}
+
+// ------------------------------------------------------------------ finalize
+
+__global__ void finalize_kernel(const double* __restrict__ acc, int O, int T, void* pT, void* pL, void* pA, int mode)
+{
+    __shared__ double tT[32][33], tL[32][33];
+    const int o0 = blockIdx.y * 32, n0 = blockIdx.x * 32;
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int o = o0 + k, n = n0 + threadIdx.x;
+        double a = 0, b = 0;
+        if (o < O && n < T) {
+            double2 v = reinterpret_cast<const double2*>(acc)[(size_t)o * T + n];
+            a = v.x;
+            b = v.y;
+        }
+        tT[k][threadIdx.x] = a;
+        tL[k][threadIdx.x] = b;
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int n = n0 + k, o = o0 + threadIdx.x;
+        if (n >= T || o >= O) continue;
+        const double a = tT[threadIdx.x][k], b = tL[threadIdx.x][k];
+        const size_t q = (size_t)n * O + o;
+        if (mode == 0) {
+            if (pT) reinterpret_cast<double*>(pT)[q] = a;
+            if (pL) reinterpret_cast<double*>(pL)[q] = b;
+            if (pA) reinterpret_cast<double*>(pA)[q] = a + b;
+        } else if (mode == 1) {
+            if (pT) reinterpret_cast<double*>(pT)[q] += a;
+            if (pL) reinterpret_cast<double*>(pL)[q] += b;
+            if (pA) reinterpret_cast<double*>(pA)[q] += a + b;
+        } else {
+            if (pT) reinterpret_cast<float*>(pT)[q] += (float)a;
+            if (pL) reinterpret_cast<float*>(pL)[q] += (float)b;
+            if (pA) reinterpret_cast<float*>(pA)[q] += (float)(a + b);
+        }
+    }
+}
+
+cudaError_t launch_finalize(const double* acc, int O, int T, void* pT, void* pL, void* pA, int mode, cudaStream_t s)
+{
+    dim3 grid((T + 31) / 32, (O + 31) / 32), block(32, 8);
+    finalize_kernel<<<grid, block, 0, s>>>(acc, O, T, pT, pL, pA, mode);
+    return cudaGetLastError();
+}
+
+void gauss_taps(double* w)
+{
+    // mathfunc.cu:350-370 with n_win = 13: sigma = 2, normalised
+    const double sd = (13 - 1) / 6.0, amp = 1.0 / (std::sqrt(2.0 * M_PI) * sd);
+    double tot = 0.0;
+    for (int j = 0; j < 13; ++j) {
+        const double x = j - 6;
+        w[j] = amp * std::exp(-0.5 * (x * x) / sd / sd);
+        tot += w[j];
+    }
+    for (int j = 0; j < 13; ++j) w[j] = w[j] / tot;
+}
+
+}  // namespace acum

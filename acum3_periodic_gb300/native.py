@@ -1,0 +1,313 @@
+"""ctypes binding of libacum.so (include/acum.h).
+
+The library is built in-tree by `acum3_periodic_gb300.build.build()`.  Loading fails
+loudly (RuntimeError) if it is missing or if no CUDA device is present: there is no CPU
+fallback for any of these calls.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .build import LIB
+
+PLAIN_FP64 = 0
+MIXED = 1
+
+DEVERR_DISC = 0x1
+DEVERR_ORDER = 0x2
+DEVERR_NONFINITE = 0x4
+DEVERR_TIMEOUT = 0x8
+
+ERRORS = {-1: "ACUM_ERR_INVALID", -2: "ACUM_ERR_IO", -3: "ACUM_ERR_CUDA", -4: "ACUM_ERR_NOMEM",
+          -5: "ACUM_ERR_STATE", -6: "ACUM_ERR_TIMEOUT", -7: "ACUM_ERR_GEOMETRY", -8: "ACUM_ERR_UNSUPPORTED"}
+
+_DP = C.POINTER(C.c_double)
+_FP = C.POINTER(C.c_float)
+_IP = C.POINTER(C.c_int)
+
+
+class AcumError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "?"), code, msg))
+        self.code = code
+
+
+class Inputs(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("a0", "rhoRef", "pRef", "oM", "dPsi", "Minf", "Mref", "xy_angle",
+                                          "xz_angle", "CFDscale", "OBSscale")] + \
+               [(k, C.c_int) for k in ("nTime", "impermeable", "periodic", "lowpass", "BB_noise")]
+
+
+class BBDesc(C.Structure):
+    _fields_ = [("nsurf", C.c_int), ("t_del", C.c_int),
+                ("span", _DP), ("omega", _DP), ("psi_offset", _DP), ("rotate", _DP), ("translate", _DP),
+                ("ccw", _IP), ("trip", _IP), ("nsect", _IP), ("geom", _FP), ("data", _FP),
+                ("ns_t", _IP), ("na_t", _IP), ("nm_t", _IP), ("nr_t", _IP),
+                ("sect_t", _FP), ("aoa_t", _FP), ("mach_t", _FP), ("re_t", _FP), ("table", _FP)]
+
+
+_lib = None
+
+# every symbol of include/acum.h with its ctypes signature (restype, argtypes)
+SIGNATURES = {
+    "acum_version": (C.c_int, []),
+    "acum_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int]),
+    "acum_destroy": (C.c_int, [C.c_void_p]),
+    "acum_last_error": (C.c_char_p, [C.c_void_p]),
+    "acum_last_global_error": (C.c_char_p, []),
+    "acum_load_deck": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "acum_set_deck": (C.c_int, [C.c_void_p, C.POINTER(Inputs), C.c_int, _FP, C.c_int, _IP, C.c_void_p, C.c_int]),
+    "acum_update_surfaces": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "acum_set_bb": (C.c_int, [C.c_void_p, C.POINTER(BBDesc)]),
+    "acum_get_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
+    "acum_preprocess": (C.c_int, [C.c_void_p]),
+    "acum_get_fields": (C.c_int, [C.c_void_p, _DP]),
+    "acum_tonal": (C.c_int, [C.c_void_p, C.c_int, _DP, _DP, _DP]),
+    "acum_tonal_from_host": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "acum_tonal_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "acum_surfaces_device_ptr": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "acum_mark_surfaces_changed": (C.c_int, [C.c_void_p]),
+    "acum_sync": (C.c_int, [C.c_void_p]),
+    "acum_bpm": (C.c_int, [C.c_void_p, C.c_int, _DP, _DP]),
+    "acum_write_outputs": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "acum_tonal_adjoint": (C.c_int, [C.c_void_p, C.c_int, _DP, _DP, _DP, _DP, _DP]),
+    "acum_device_error_word": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.c_int]),
+    "acum_last_timing": (C.c_int, [C.c_void_p, C.c_int, _DP, C.POINTER(C.c_longlong)]),
+    "acum_set_tile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "acum_host_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t]),
+    "acum_host_free": (C.c_int, [C.c_void_p]),
+    "acum_find_pressure_time_history": (C.c_int, [C.c_void_p] * 9 + [C.c_int] + [C.c_void_p] * 5 +
+                                        [C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_void_p,
+                                         C.c_float, C.c_void_p]),
+    "acum_find_pressure_time_history_f64": (C.c_int, [C.c_void_p] * 9 + [C.c_int] + [C.c_void_p] * 5 +
+                                            [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                             C.c_void_p, C.c_double, C.c_void_p]),
+    "acum_preprocess_imper": (C.c_int, [C.c_void_p] * 4 + [C.c_int] + [C.c_void_p] * 5 +
+                              [C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int]),
+    "acum_find_bb_noise": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_float] + [C.c_void_p] * 26 +
+                           [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_float,
+                            C.c_void_p, C.c_void_p]),
+    "acum_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int]),
+    "acum_batch_destroy": (C.c_int, [C.c_void_p]),
+    "acum_batch_last_error": (C.c_char_p, [C.c_void_p]),
+    "acum_batch_add": (C.c_int, [C.c_void_p, C.POINTER(Inputs), C.c_int, _FP, C.c_int, _IP, C.c_void_p, _IP]),
+    "acum_batch_prepare": (C.c_int, [C.c_void_p]),
+    "acum_batch_run": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "acum_batch_result": (C.c_int, [C.c_void_p, C.c_int, _DP]),
+    "acum_batch_timing": (C.c_int, [C.c_void_p, _DP, C.POINTER(C.c_longlong)]),
+    "acum_batch_set_tile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+}
+
+
+def lib(build_if_missing: bool = True):
+    """The loaded library.  Builds it in-tree first if it is not there."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            if not build_if_missing:
+                raise RuntimeError("libacum.so is not built (%s); run __graft_entry__.build()" % LIB)
+            from .build import build
+            build()
+        L = C.CDLL(LIB)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a, t=_DP):
+    return a.ctypes.data_as(t)
+
+
+def inputs_of(deck) -> Inputs:
+    s = Inputs()
+    for k in ("a0", "rhoRef", "pRef", "oM", "dPsi", "Minf", "Mref", "xy_angle", "xz_angle", "CFDscale",
+              "OBSscale"):
+        setattr(s, k, float(np.float32(getattr(deck, k))))
+    s.nTime, s.impermeable, s.periodic, s.lowpass, s.BB_noise = (
+        deck.nTime, deck.impermeable, deck.periodic, deck.lowpass, deck.BB_noise)
+    return s
+
+
+class Context:
+    """One acum_ctx on one GPU."""
+
+    def __init__(self, device: int = 0):
+        self.L = lib()
+        h = C.c_void_p()
+        rc = self.L.acum_create(C.byref(h), device)
+        if rc != 0:
+            raise AcumError(rc, self.L.acum_last_global_error().decode())
+        self.h = h
+        self.T = self.O = self.E = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.acum_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc):
+        if rc != 0:
+            raise AcumError(rc, self.L.acum_last_error(self.h).decode())
+
+    def _sizes(self):
+        s = (C.c_longlong * 6)()
+        self._ck(self.L.acum_get_sizes(self.h, s))
+        self.nsurf, self.T, self.O, self.E, self.nbb, self.has_bb = (int(v) for v in s)
+
+    # ---- deck
+    def set_deck(self, deck, bb: bool = True):
+        obs = np.ascontiguousarray(deck.obs_file, dtype=np.float32)
+        ne = np.array(deck.elements, dtype=np.int32)
+        raw = deck.raw_surfaces()
+        inp = inputs_of(deck)
+        self._ck(self.L.acum_set_deck(self.h, C.byref(inp), deck.nObs, _p(obs, _FP), deck.nSurf, _p(ne, _IP),
+                                      raw.ctypes.data_as(C.c_void_p), 0))
+        self._sizes()
+        if bb and deck.BB_noise == 1:
+            self.set_bb(deck)
+        return self
+
+    def set_deck_raw_device(self, deck, raw_dev_ptr: int):
+        obs = np.ascontiguousarray(deck.obs_file, dtype=np.float32)
+        ne = np.array(deck.elements, dtype=np.int32)
+        inp = inputs_of(deck)
+        self._ck(self.L.acum_set_deck(self.h, C.byref(inp), deck.nObs, _p(obs, _FP), deck.nSurf, _p(ne, _IP),
+                                      C.c_void_p(raw_dev_ptr), 1))
+        self._sizes()
+        return self
+
+    def load_deck(self, path: str):
+        self._ck(self.L.acum_load_deck(self.h, os.fsencode(path)))
+        self._sizes()
+        return self
+
+    def set_bb(self, deck):
+        bb = deck.bb
+        self._bb_keep = k = dict(
+            span=np.array([b.span for b in bb], np.float64), omega=np.array([b.omega for b in bb], np.float64),
+            psi=np.array([b.psi_offset for b in bb], np.float64),
+            rot=np.array([b.rotate for b in bb], np.float64).reshape(-1),
+            tra=np.array([b.translate for b in bb], np.float64).reshape(-1),
+            ccw=np.array([b.ccw for b in bb], np.int32), trip=np.array([b.trip for b in bb], np.int32),
+            nsect=np.array([b.nsect for b in bb], np.int32),
+            geom=np.concatenate([b.geom.reshape(-1) for b in bb]).astype(np.float32),
+            data=np.concatenate([b.data.reshape(-1) for b in bb]).astype(np.float32),
+            ns=np.array([b.t_data.shape[0] for b in bb], np.int32),
+            na=np.array([b.t_data.shape[3] for b in bb], np.int32),
+            nm=np.array([b.t_data.shape[1] for b in bb], np.int32),
+            nr=np.array([b.t_data.shape[2] for b in bb], np.int32),
+            sect=np.concatenate([b.t_sect for b in bb]).astype(np.float32),
+            aoa=np.concatenate([b.t_aoa for b in bb]).astype(np.float32),
+            mach=np.concatenate([b.t_mach for b in bb]).astype(np.float32),
+            re=np.concatenate([b.t_re for b in bb]).astype(np.float32),
+            table=np.concatenate([b.t_data.reshape(-1) for b in bb]).astype(np.float32))
+        d = BBDesc()
+        d.nsurf, d.t_del = len(bb), deck.t_del
+        d.span, d.omega, d.psi_offset = _p(k["span"]), _p(k["omega"]), _p(k["psi"])
+        d.rotate, d.translate = _p(k["rot"]), _p(k["tra"])
+        d.ccw, d.trip, d.nsect = _p(k["ccw"], _IP), _p(k["trip"], _IP), _p(k["nsect"], _IP)
+        d.geom, d.data = _p(k["geom"], _FP), _p(k["data"], _FP)
+        d.ns_t, d.na_t, d.nm_t, d.nr_t = (_p(k[x], _IP) for x in ("ns", "na", "nm", "nr"))
+        d.sect_t, d.aoa_t, d.mach_t, d.re_t, d.table = (_p(k[x], _FP) for x in ("sect", "aoa", "mach", "re",
+                                                                                  "table"))
+        self._ck(self.L.acum_set_bb(self.h, C.byref(d)))
+        self._sizes()
+
+    # ---- runs
+    def preprocess(self):
+        self._ck(self.L.acum_preprocess(self.h))
+
+    def fields(self) -> np.ndarray:
+        out = np.zeros((self.E, self.T, 18))
+        self._ck(self.L.acum_get_fields(self.h, _p(out)))
+        return out
+
+    def tonal(self, precision: int = MIXED):
+        pT, pL, pA = (np.zeros((self.T, self.O)) for _ in range(3))
+        self._ck(self.L.acum_tonal(self.h, precision, _p(pT), _p(pL), _p(pA)))
+        return pT, pL, pA
+
+    def tonal_from_host(self, precision: int, raw_ptr: int, pA_ptr: int):
+        self._ck(self.L.acum_tonal_from_host(self.h, precision, C.c_void_p(raw_ptr), C.c_void_p(pA_ptr)))
+
+    def tonal_device(self, precision: int, pT_ptr: int, pL_ptr: int, pA_ptr: int):
+        self._ck(self.L.acum_tonal_device(self.h, precision, C.c_void_p(pT_ptr), C.c_void_p(pL_ptr),
+                                          C.c_void_p(pA_ptr)))
+
+    def mark_surfaces_changed(self):
+        self._ck(self.L.acum_mark_surfaces_changed(self.h))
+
+    def sync(self):
+        self._ck(self.L.acum_sync(self.h))
+
+    def bpm(self, aa_mode: int = 0):
+        spl = np.zeros((self.O, 42, 7))
+        oas = np.zeros(self.O)
+        self._ck(self.L.acum_bpm(self.h, aa_mode, _p(spl), _p(oas)))
+        return spl, oas
+
+    def adjoint(self, precision: int = PLAIN_FP64, dJ_dpA: np.ndarray = None):
+        J = np.zeros(1)
+        gcp = np.zeros((self.E, self.T))
+        gx = np.zeros((self.E, self.T, 3))
+        gn = np.zeros((self.E, self.T, 3))
+        dj = None if dJ_dpA is None else np.ascontiguousarray(dJ_dpA, dtype=np.float64)
+        self._ck(self.L.acum_tonal_adjoint(self.h, precision, None if dj is None else _p(dj), _p(J), _p(gcp),
+                                           _p(gx), _p(gn)))
+        return float(J[0]), gcp, gx, gn
+
+    def write_outputs(self, path: str):
+        self._ck(self.L.acum_write_outputs(self.h, os.fsencode(path)))
+
+    def set_tile(self, obs_per_block=0, elems_per_stage=0, items_per_sm=0):
+        self._ck(self.L.acum_set_tile(self.h, obs_per_block, elems_per_stage, items_per_sm))
+
+    def timing(self, which: int):
+        ms = C.c_double()
+        n = C.c_longlong()
+        self._ck(self.L.acum_last_timing(self.h, which, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def error_word(self, reset: bool = False) -> int:
+        w = C.c_uint32()
+        self._ck(self.L.acum_device_error_word(self.h, C.byref(w), int(reset)))
+        return w.value
+
+
+class PinnedBuffer:
+    """Page-locked host memory from acum_host_alloc, viewed as a numpy array."""
+
+    def __init__(self, shape, dtype):
+        self.L = lib()
+        n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        p = C.c_void_p()
+        rc = self.L.acum_host_alloc(C.byref(p), max(n, 1))
+        if rc != 0:
+            raise AcumError(rc, self.L.acum_last_global_error().decode())
+        self.ptr = p.value
+        buf = (C.c_char * max(n, 1)).from_address(self.ptr)
+        self.array = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+
+    def close(self):
+        if self.ptr:
+            self.array = None
+            self.L.acum_host_free(C.c_void_p(self.ptr))
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

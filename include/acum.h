@@ -1,0 +1,240 @@
+/*
+ * acum.h -- C ABI of the GB300-native ACUM-3 periodic acoustic path.
+ *
+ * Two families of entry points:
+ *
+ *  1. Reference-shaped drop-ins.  Same arguments, same meaning and the same accumulate
+ *     semantics as the two hot-path calls of the reference driver, so a maintainer can
+ *     swap them in at main.cu:360 and main.cu:274 with no other change:
+ *       acum_find_pressure_time_history      replaces core.cu:18 (launched at main.cu:360)
+ *       acum_find_pressure_time_history_f64  the same call on the FP64 build's arrays
+ *       acum_find_bb_noise                   replaces bb_core.cu:11 (called at main.cu:274)
+ *       acum_preprocess_imper                replaces preprocess.cu:228 on caller arrays
+ *
+ *  2. A context API that owns the deck on the device and runs the whole path: the file
+ *     readers and writers keep the reference's formats (io.cu), preprocessing and all
+ *     compute run on the GPU, and the adjoint and batched forms are reachable here.
+ *
+ * Conventions: every call returns int status (ACUM_OK = 0, negative = error class) and
+ * never exits the process; acum_last_error() gives the message of the last failure of a
+ * context, acum_last_global_error() that of a context-free call.  Pointers documented as
+ * "device" must be CUDA device (or managed) memory of the context's device; "host"
+ * pointers are ordinary or pinned host memory.  All arrays are dense, C order.  A
+ * context is used by one host thread at a time; different contexts are independent.
+ */
+#ifndef ACUM_H
+#define ACUM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ACUM_OK 0
+#define ACUM_ERR_INVALID (-1)     /* bad argument or inconsistent sizes */
+#define ACUM_ERR_IO (-2)          /* deck file missing or malformed */
+#define ACUM_ERR_CUDA (-3)        /* CUDA runtime error (message has the CUDA error) */
+#define ACUM_ERR_NOMEM (-4)       /* device or host allocation failed */
+#define ACUM_ERR_STATE (-5)       /* call out of order (e.g. a run before a deck) */
+#define ACUM_ERR_TIMEOUT (-6)     /* a bounded device wait ran out; the context stays usable */
+#define ACUM_ERR_GEOMETRY (-7)    /* invalid geometry met on the device (see error word) */
+#define ACUM_ERR_UNSUPPORTED (-8) /* option outside what this build implements */
+
+/* precision of the tonal forms */
+#define ACUM_PLAIN_FP64 0 /* FP64 end to end; matches the reference's FP64 build */
+#define ACUM_MIXED 1      /* FP32 integrand, float-float observer time, compensated bin sums */
+
+/* bits of the device error word (acum_device_error_word) */
+#define ACUM_DEVERR_DISC 0x1u       /* negative discriminant in the retarded-time solve */
+#define ACUM_DEVERR_ORDER 0x2u      /* observer time not increasing between steps (|Mr| >= 1) */
+#define ACUM_DEVERR_NONFINITE 0x4u  /* non-finite integrand */
+#define ACUM_DEVERR_TIMEOUT 0x8u    /* a bounded shared-memory pipeline wait ran out */
+
+typedef struct acum_ctx acum_ctx;
+
+/* ---------------------------------------------------------------- context */
+
+int acum_create(acum_ctx** out, int device);
+int acum_destroy(acum_ctx* ctx);
+const char* acum_last_error(const acum_ctx* ctx);
+const char* acum_last_global_error(void);
+int acum_version(void);
+
+/* The `input` file's settings (io.cu:12-101).  Angles in degrees, as in the file. */
+typedef struct {
+    double a0, rhoRef, pRef, oM, dPsi, Minf, Mref, xy_angle, xz_angle, CFDscale, OBSscale;
+    int nTime, impermeable, periodic, lowpass, BB_noise;
+} acum_inputs;
+
+/* Reads input, obs.dat, surfaces/surface_*.dat (and input_BB, BB_inputs/ when
+ * BB_noise = 1) from `dir` with the semantics of io.cu (read_inputs, read_observers,
+ * read_surf, read_BB_inputs).  Replaces any deck already in the context. */
+int acum_load_deck(acum_ctx* ctx, const char* dir);
+
+/* The same deck from memory.  `obs_file` [nobs][3] are obs.dat values (OBSscale is
+ * applied as read_observers does); `raw` holds the surface_*.dat rows of all surfaces,
+ * surface after surface, each [nTime][nelem[i]][8] = x,y,z,Cp,A,nx,ny,nz.  The arrays are
+ * copied; `raw` may be pinned host memory or device memory (raw_on_device = 1). */
+int acum_set_deck(acum_ctx* ctx, const acum_inputs* in, int nobs, const float* obs_file, int nsurf,
+                  const int* nelem, const float* raw, int raw_on_device);
+
+/* Replaces only the surface rows (same sizes as the deck), e.g. for a new flight state;
+ * host or device memory.  Marks the deck for re-preprocessing. */
+int acum_update_surfaces(acum_ctx* ctx, const float* raw, int raw_on_device);
+
+/* Broadband inputs from memory (read_BB_inputs layout, io.cu:337-700).  Per BB surface
+ * i: span, omega, ccw, psi_offset, trip, rotate[3], translate[3]; nsect[i] sections with
+ * geom [nsect][4] = r/R, y/R, z/R, c/R and data [nTime][nsect][7] = BLT_s, BLT_p, DT_s,
+ * DT_p, cn, cc, theta as in the file (cn, cc are divided by (r/R)^2 here when omega != 0,
+ * as the reader does); tables of sizes ns_t, na_t, nm_t, nr_t with axes sect/aoa/mach/re
+ * and data [ns_t][nm_t][nr_t][na_t][7] = cl, cd, cm, bl_u, bl_l, disp_u, disp_l.  All
+ * per-surface arrays are concatenated surface after surface. */
+typedef struct {
+    int nsurf, t_del;
+    const double *span, *omega, *psi_offset, *rotate, *translate;
+    const int *ccw, *trip, *nsect;
+    const float *geom, *data;
+    const int *ns_t, *na_t, *nm_t, *nr_t;
+    const float *sect_t, *aoa_t, *mach_t, *re_t, *table;
+} acum_bb_desc;
+int acum_set_bb(acum_ctx* ctx, const acum_bb_desc* bb);
+
+/* sizes: out[0]=nSurf, [1]=nTime, [2]=nObs, [3]=elements, [4]=BB sections, [5]=BB_noise */
+int acum_get_sizes(const acum_ctx* ctx, long long* out);
+
+/* Uploads what is not on the device yet and runs preprocess_imper's steps on the GPU
+ * (scaling, make_periodic, optional lowpass, d/dtau), building both record layouts. */
+int acum_preprocess(acum_ctx* ctx);
+
+/* Copies the preprocessed per-element-step fields back, [elements][nTime][18] =
+ * x,y,z,ds, n(3), ndot(3), V(3), Vdot(3), P, Pdot (the contents of Xham/Nham/Vham/PRham). */
+int acum_get_fields(acum_ctx* ctx, double* host_fields);
+
+/* Tonal noise.  Outputs [nTime][nObs] (main.cu:224 layout), overwritten, host memory;
+ * any of pT/pL/pA may be NULL.  Preprocesses first if needed. */
+int acum_tonal(acum_ctx* ctx, int precision, double* pT, double* pL, double* pA);
+
+/* The whole tonal path from host buffers in one call: copies `raw` (same layout as
+ * acum_set_deck, host memory, pinned for full speed) to the device, preprocesses, runs
+ * the kernels and copies pA [nTime][nObs] back.  The deck's sizes must not change. */
+int acum_tonal_from_host(acum_ctx* ctx, int precision, const float* raw, double* pA_host);
+
+/* Tonal with device outputs [nTime][nObs], on the context stream; no host sync.  With
+ * all three pointers NULL the results stay in the context's own device buffer. */
+int acum_tonal_device(acum_ctx* ctx, int precision, double* d_pT, double* d_pL, double* d_pA);
+
+/* Device address of the context's copy of the surface rows (acum_set_deck layout), so a
+ * solver on the same GPU can write new rows in place; call acum_mark_surfaces_changed
+ * afterwards so the next run preprocesses them again. */
+int acum_surfaces_device_ptr(acum_ctx* ctx, float** p);
+int acum_mark_surfaces_changed(acum_ctx* ctx);
+
+/* Waits for the context's stream (all runs issued so far). */
+int acum_sync(acum_ctx* ctx);
+
+/* Broadband: BBspl [nObs][42][7] and BBoaspl [nObs] in dB (bb_core.cu:563-583 layout),
+ * host memory, overwritten (the -100 dB seeding of main.cu:256-266 is applied inside).
+ * aa_mode selects the convected emission time of bb_core.cu:517-520: 0 uses
+ * aa = a0^2 - |vInf|^2 (the formula's intent), 1 uses aa = 0 (the value the reference's
+ * uninitialised variable takes in a zero-initialising build). */
+int acum_bpm(acum_ctx* ctx, int aa_mode, double* BBspl, double* BBoaspl);
+
+/* Writes pT.out, pL.out, pA.out (io.cu:137-203) and, if broadband was run,
+ * bb_oaspl.out and bb_spl.dat (io.cu:702-796) into `dir`, byte-format compatible. */
+int acum_write_outputs(acum_ctx* ctx, const char* dir);
+
+/* Adjoint of J = sum_obs mean_bins(pA^2) with respect to the surface rows: gradients
+ * [elements][nTime] for Cp, [elements][nTime][3] for positions and normals (file
+ * coordinates, before CFDscale), host memory.  J is returned in *J.  Requires
+ * lowpass = 0.  dJ_dpA may be NULL (the objective above) or [nTime][nObs] host. */
+int acum_tonal_adjoint(acum_ctx* ctx, int precision, const double* dJ_dpA, double* J, double* g_cp, double* g_x,
+                       double* g_n);
+
+/* Device error word (ACUM_DEVERR_* bits) accumulated since the last reset. */
+int acum_device_error_word(acum_ctx* ctx, uint32_t* out, int reset);
+
+/* Timing of the last run's kernels, measured with CUDA events on the launching stream:
+ * which = 0 tonal kernel, 1 preprocess, 2 finalize, 3 bpm, 4 adjoint, 5 whole call.
+ * *launches is the number of kernel launches of this library in the last run. */
+int acum_last_timing(const acum_ctx* ctx, int which, double* ms, long long* launches);
+
+/* Tile shape of the tonal kernels (0 = let the library choose): observers per block and
+ * elements per pipeline stage.  Used by the autotuner. */
+int acum_set_tile(acum_ctx* ctx, int obs_per_block, int elems_per_stage, int items_per_sm);
+
+/* Pinned host memory for staging (cudaHostAlloc); free with acum_host_free. */
+int acum_host_alloc(void** p, size_t bytes);
+int acum_host_free(void* p);
+
+/* ------------------------------------------------- reference-shaped drop-ins */
+
+/* Replaces findPressureTimeHistory (core.cu:18) as launched at main.cu:360: the same
+ * arguments, all device pointers, FP32 storage; accumulates into pT, pL, pA [nTime][nObs].
+ * The arrays are those preprocess_imper produced (AoS Xham/Nham/Vham/PRham with the
+ * XPtr/NPtr/VPtr/PRPtr offsets and E[] counts, all in device memory as the reference
+ * passes them).  Runs the mixed-precision kernel; `stream` may be NULL (default stream).
+ * Synchronises the stream before returning. */
+int acum_find_pressure_time_history(const float* rObs, const float* tObs, float* pT, float* pL, float* pA,
+                                    const float* Xham, const float* Nham, const float* Vham, const float* PRham,
+                                    int nSurf, const int* XPtr, const int* NPtr, const int* VPtr, const int* PRPtr,
+                                    const int* E, int nObs, int nTime, float dPsi, float dTau, float a0,
+                                    float rhoRef, const float* vInf, float oM, void* stream);
+
+/* The same call on the FP64 build's arrays (every `float` of core.cu:18 a `double`);
+ * runs the plain FP64 kernel. */
+int acum_find_pressure_time_history_f64(const double* rObs, const double* tObs, double* pT, double* pL,
+                                        double* pA, const double* Xham, const double* Nham, const double* Vham,
+                                        const double* PRham, int nSurf, const int* XPtr, const int* NPtr,
+                                        const int* VPtr, const int* PRPtr, const int* E, int nObs, int nTime,
+                                        double dPsi, double dTau, double a0, double rhoRef, const double* vInf,
+                                        double oM, void* stream);
+
+/* Replaces preprocess_imper (preprocess.cu:228) on caller arrays: host AoS Xham [etot*
+ * nTime*4], Nham [*6], Vham [*6], PRham [*2] laid out with the reference's XPtr/NPtr/
+ * VPtr/PRPtr offsets (E[] counts, host); updated in place with the same meaning. */
+int acum_preprocess_imper(float* Xham, float* Nham, float* Vham, float* PRham, int nSurf, const int* XPtr,
+                          const int* NPtr, const int* VPtr, const int* PRPtr, const int* E, int nTime, float dTau,
+                          float a0, float rhoRef, float Mref, float CFDscale, int periodic, int lowpass);
+
+/* Replaces findBBnoise (bb_core.cu:11) as called at main.cu:274: the same 39 arguments,
+ * host pointers, FP32 storage; BBspl [nObs][nf2][7] and BBoaspl [nObs] are updated as the
+ * reference does (they arrive seeded, normally with -100 dB).  Computes on the GPU with
+ * aa_mode 0 (see acum_bpm). */
+int acum_find_bb_noise(int nSurf_BB, int nObs, int nTime, float dTau, const float* span, const float* omega,
+                       const int* ccw, const float* psi_offset, const int* trip, const float* rotate,
+                       const float* translate, const int* xsPtr, const int* dsPtr, const int* nsect,
+                       const float* xyzcR, const float* bbdata, const int* nsect_t, const int* nmach_t,
+                       const int* naoa_t, const int* nre_t, const int* aPtr, const int* mPtr, const int* rPtr,
+                       const int* sPtr, const int* dPtr, const float* sect_t, const float* mach_t, const float* aoa_t,
+                       const float* re_t, const float* bbdata_t, int t_del, const float* vInf, const float* rObs,
+                       const float* tObs, int nf2, const float* ff, float a0, float* BBspl, float* BBoaspl);
+
+/* --------------------------------------------------------------- batching */
+
+typedef struct acum_batch acum_batch;
+
+/* A batch holds many decks (cases) resident on one device and runs their tonal solves
+ * in one persistent launch (optionally replayed from a CUDA graph). */
+int acum_batch_create(acum_batch** out, int device);
+int acum_batch_destroy(acum_batch* b);
+const char* acum_batch_last_error(const acum_batch* b);
+/* Adds a case (same argument meaning as acum_set_deck); returns its index in *case_id. */
+int acum_batch_add(acum_batch* b, const acum_inputs* in, int nobs, const float* obs_file, int nsurf,
+                   const int* nelem, const float* raw, int* case_id);
+/* Preprocesses every case (once). */
+int acum_batch_prepare(acum_batch* b);
+/* mode 0: one persistent launch over all cases; 1: one launch per case; 2: the persistent
+ * launch captured once into a CUDA graph and replayed. */
+int acum_batch_run(acum_batch* b, int precision, int mode);
+/* pA [nTime_c][nObs_c] of one case after a run, host memory. */
+int acum_batch_result(acum_batch* b, int case_id, double* pA);
+/* Kernel time of the last run (CUDA events on the launching stream) and launch count. */
+int acum_batch_timing(const acum_batch* b, double* ms, long long* launches);
+int acum_batch_set_tile(acum_batch* b, int obs_per_block, int elems_per_stage, int items_per_sm);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ACUM_H */

@@ -1,0 +1,167 @@
+"""Tonal path on the GPU (through the C ABI) against the oracle and the golden vectors
+of the reference's FP64 build.
+
+Tolerances: the plain FP64 form must agree per bin to 1e-10 relative, normalised as
+|p - ref| / max(|ref|, 1e-6 max_t|ref|); the mixed form is held to a per-bin error of
+1e-4 of the observer's RMS and to the OASPL bound of 0.05 dB (observed: far below)."""
+import os
+
+import numpy as np
+import pytest
+
+from acum3_periodic_gb300 import synth
+from acum3_periodic_gb300.deck import read_deck
+from oracle import oracle as O
+
+from conftest import GOLDEN
+from metrics import oaspl_db, per_bin_rel, per_bin_rms
+
+pytestmark = pytest.mark.gpu
+
+F64_TOL = 1e-10
+MIXED_RMS_TOL = 1e-4
+OASPL_TOL_DB = 0.05
+
+TONAL = ["tonal_hover", "tonal_flight_lowpass", "bb_tdel2", "bb_tdel1_lbl_cw", "bb_tdel0_hover"]
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from acum3_periodic_gb300 import native
+    c = native.Context(0)
+    yield c
+    c.close()
+
+
+def _golden(name):
+    return read_deck(os.path.join(GOLDEN, "decks", name)), np.load(os.path.join(GOLDEN, name + ".npz"))
+
+
+@pytest.mark.parametrize("name", TONAL)
+def test_preprocess_fields_match_reference(ctx, name):
+    d, g = _golden(name)
+    ctx.set_deck(d, bb=False)
+    f = ctx.fields()
+    np.testing.assert_array_equal(f[:, :, 0:3], g["fields_X"][:, :, 0:3])
+    for sl, key in ((slice(3, 4), None), (slice(4, 10), "fields_N"), (slice(10, 16), "fields_V"),
+                    (slice(16, 18), "fields_P")):
+        want = g["fields_X"][:, :, 3:4] if key is None else g[key]
+        np.testing.assert_allclose(f[:, :, sl], want, rtol=0, atol=1e-12 * np.abs(want).max())
+
+
+@pytest.mark.parametrize("name", TONAL)
+def test_fp64_matches_reference_build(ctx, name):
+    from acum3_periodic_gb300 import native
+    d, g = _golden(name)
+    ctx.set_deck(d, bb=False)
+    pT, pL, pA = ctx.tonal(native.PLAIN_FP64)
+    for k, v in (("pT", pT), ("pL", pL), ("pA", pA)):
+        err = per_bin_rel(v, g[k + "_f64"]).max()
+        assert err < F64_TOL, (k, err)
+    assert ctx.error_word(reset=True) == 0
+
+
+@pytest.mark.parametrize("name", TONAL)
+def test_mixed_against_fp64_reference(ctx, name):
+    from acum3_periodic_gb300 import native
+    d, g = _golden(name)
+    ctx.set_deck(d, bb=False)
+    pT, pL, pA = ctx.tonal(native.MIXED)
+    ref = g["pA_f64"]
+    assert per_bin_rms(pA, ref).max() < MIXED_RMS_TOL
+    assert np.abs(oaspl_db(pA) - oaspl_db(ref)).max() < OASPL_TOL_DB
+    np.testing.assert_allclose(pA, pT + pL, rtol=0, atol=1e-12 * np.abs(pA).max())
+
+
+@pytest.mark.parametrize("cfg,rep,scale", [
+    (0, 31, dict(n_span=7, n_chord_side=5, ntime=45, nobs=13)),        # T not a multiple of 32
+    (1, 32, dict(n_span=5, n_chord_side=3, ntime=64, nobs=37, bb_nsect=4, bb_small=True, n_bb=1)),
+    (3, 33, dict(n_span=9, n_chord_side=4, ntime=90, nobs=21)),
+])
+def test_random_decks_against_oracle(ctx, cfg, rep, scale):
+    from acum3_periodic_gb300 import native
+    d = synth.config_deck(cfg, replicate=rep, scale=scale)
+    oT, oL, oA, bad = O.tonal(d)
+    assert bad == 0
+    ctx.set_deck(d, bb=False)
+    pT, pL, pA = ctx.tonal(native.PLAIN_FP64)
+    assert per_bin_rel(pA, oA).max() < F64_TOL
+    assert per_bin_rel(pT, oT).max() < F64_TOL
+    mT, mL, mA = ctx.tonal(native.MIXED)
+    assert per_bin_rms(mA, oA).max() < MIXED_RMS_TOL
+    assert np.abs(oaspl_db(mA) - oaspl_db(oA)).max() < OASPL_TOL_DB
+
+
+def test_config0_full_size(ctx):
+    """Workload 0 at its full size (2 x 1200 elements, 360 steps, 16 observers)."""
+    from acum3_periodic_gb300 import native
+    d = synth.config_deck(0)
+    oT, oL, oA, bad = O.tonal(d)
+    ctx.set_deck(d, bb=False)
+    pT, pL, pA = ctx.tonal(native.PLAIN_FP64)
+    assert per_bin_rel(pA, oA).max() < F64_TOL
+    mT, mL, mA = ctx.tonal(native.MIXED)
+    assert np.abs(oaspl_db(mA) - oaspl_db(oA)).max() < OASPL_TOL_DB
+    assert per_bin_rms(mA, oA).max() < MIXED_RMS_TOL
+
+
+def test_linearity_in_cp_and_blade_periodicity(ctx):
+    """pL is linear in Cp and pT does not depend on it; two identical blades half a
+    revolution apart give a pA that repeats every half revolution."""
+    from acum3_periodic_gb300 import native
+    d = synth.config_deck(0, replicate=40, scale=dict(n_span=4, n_chord_side=3, ntime=48, nobs=5))
+    ctx.set_deck(d, bb=False)
+    pT, pL, pA = ctx.tonal(native.PLAIN_FP64)
+    for s in d.surfaces:
+        s[:, :, 3] *= 2.5
+    ctx.set_deck(d, bb=False)
+    qT, qL, qA = ctx.tonal(native.PLAIN_FP64)
+    np.testing.assert_allclose(qT, pT, rtol=0, atol=1e-12 * np.abs(pT).max())
+    np.testing.assert_allclose(qL, 2.5 * pL, rtol=0, atol=1e-11 * np.abs(pL).max())
+    # identical blades: make blade 1's Cp the same as blade 0's, shifted by T/2 steps
+    s0, s1 = d.surfaces
+    s1[:, :, 3] = np.roll(s0[:, :, 3], d.nTime // 2, axis=0)
+    ctx.set_deck(d, bb=False)
+    _, _, rA = ctx.tonal(native.PLAIN_FP64)
+    np.testing.assert_allclose(rA, np.roll(rA, d.nTime // 2, axis=0), rtol=0, atol=1e-9 * np.abs(rA).max())
+
+
+def test_element_permutation_invariance(ctx):
+    from acum3_periodic_gb300 import native
+    d = synth.config_deck(3, replicate=41, scale=dict(n_span=5, n_chord_side=3, ntime=40, nobs=6))
+    ctx.set_deck(d, bb=False)
+    _, _, pA = ctx.tonal(native.PLAIN_FP64)
+    perm = np.array(synth.uniform(5, 1, d.surfaces[0].shape[1]).argsort())
+    d.surfaces[0] = np.ascontiguousarray(d.surfaces[0][:, perm, :])
+    ctx.set_deck(d, bb=False)
+    _, _, qA = ctx.tonal(native.PLAIN_FP64)
+    np.testing.assert_allclose(qA, pA, rtol=0, atol=1e-12 * np.abs(pA).max())
+
+
+def test_load_deck_and_write_outputs(ctx, tmp_path):
+    """The file-format drop-in: load a deck directory, write pT/pL/pA.out."""
+    from acum3_periodic_gb300 import native
+    import shutil
+    src = os.path.join(GOLDEN, "decks", "tonal_hover")
+    dst = tmp_path / "deck"
+    shutil.copytree(src, dst)
+    ctx.load_deck(str(dst))
+    pT, pL, pA = ctx.tonal(native.PLAIN_FP64)
+    ctx.write_outputs(str(dst))
+    g = np.load(os.path.join(GOLDEN, "tonal_hover.npz"))
+    lines = open(dst / "pA.out").read().splitlines()
+    assert lines[0] == "# ntime nobs"
+    T, Ob = (int(x) for x in lines[1].split())
+    assert (T, Ob) == g["pA_f64"].shape
+    vals = np.array([[float(x) for x in l.split()] for l in lines[2:]])
+    np.testing.assert_allclose(vals[:, 1:], g["pA_f64"], rtol=1e-8, atol=1e-8 * np.abs(g["pA_f64"]).max())
+    assert lines[3].startswith(" ") and "E" in lines[3]
+
+
+def test_timing_and_launch_count(ctx):
+    from acum3_periodic_gb300 import native
+    d = synth.config_deck(0, replicate=42, scale=dict(n_span=4, n_chord_side=3, ntime=36, nobs=4))
+    ctx.set_deck(d, bb=False)
+    ctx.tonal(native.MIXED)
+    ms, launches = ctx.timing(0)
+    assert ms > 0 and launches >= 3
