@@ -380,7 +380,9 @@ int acum_ctx::run_tonal(int precision, double* d_pT, double* d_pL, double* d_pA)
     r.acc = d_acc.p;
     r.err = d_err.p;
     last_tile = r.t;
-    if (r.t.nchunk > 1) CK(this, cudaMemsetAsync(d_acc.p, 0, (size_t)nobs * T * 2 * 8, stream));
+    // the mixed form always adds into the FP64 sums; the FP64 form stores when one block
+    // owns an observer's whole element range
+    if (r.t.nchunk > 1 || !f64) CK(this, cudaMemsetAsync(d_acc.p, 0, (size_t)nobs * T * 2 * 8, stream));
     CK(this, cudaEventRecord(ev[EV_TONAL0], stream));
     CK(this, launch_tonal(r, stream));
     CK(this, cudaEventRecord(ev[EV_TONAL1], stream));
@@ -697,7 +699,7 @@ int find_pth(const S* rObs, const S* tObs, S* pT, S* pL, S* pA, const S* Xham, c
     CK(nullptr, c->d_acc.ensure((size_t)nObs * nTime * 2));
     r.acc = c->d_acc.p;
     r.err = c->d_err.p;
-    if (r.t.nchunk > 1) CK(nullptr, cudaMemsetAsync(c->d_acc.p, 0, (size_t)nObs * nTime * 16, st));
+    if (r.t.nchunk > 1 || !f64) CK(nullptr, cudaMemsetAsync(c->d_acc.p, 0, (size_t)nObs * nTime * 16, st));
     CK(nullptr, launch_tonal(r, st));
     CK(nullptr, launch_finalize(c->d_acc.p, nObs, nTime, pT, pL, pA, f64 ? 1 : 2, st));
     CK(nullptr, cudaStreamSynchronize(st));

@@ -43,6 +43,7 @@ struct TonalTile {
     int chunk;  // elements per work item (multiple of SE)
     int nchunk;
     int items;
+    int flush_elems;  // mixed: elements summed in FP32 before the FP64 flush
     size_t smem;
 };
 

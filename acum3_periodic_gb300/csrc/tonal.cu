@@ -72,6 +72,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
     return ok != 0;
 }
 
+constexpr int kMaxStages = 8;
+
 // Every wait on a barrier is bounded: after kMaxSpin polls the wait gives up, records
 // ACUM_DEVERR_TIMEOUT and the kernel unwinds instead of hanging.
 constexpr long kMaxSpin = 1L << 24;
@@ -335,7 +337,7 @@ struct KParams {
     float a0f, alphaf, ialphaf, vxf, vyf, vzf, kbhi, kblo, invTf;
     // FP64 constants
     double a0, alpha, ialpha, vx, vy, vz, dTau, oM, dPsi, lpi;
-    int W, NS, chunk, nchunk, obs_tiles;
+    int W, NS, chunk, nchunk, obs_tiles, flush_groups;
     double* acc;
     DeviceErr* err;
 };
@@ -432,34 +434,36 @@ __device__ __forceinline__ int wrap_bin(int n, int T, float invT)
     return r;
 }
 
-// bins n with u(prev) < n <= u(cur), value interpolated between the two samples
-__device__ __forceinline__ void deposit_mixed(float4* acc, int T, float invT, const SmpF& a, const SmpF& b, int kshift,
+// bins n with u(prev) < n <= u(cur), value interpolated between the two samples.  For
+// |Mr| < 1 an interval holds at most 2 bins (u(cur) - u(prev) = 1 - Mr < 2), so the first
+// bin is unrolled and the loop only runs for the second (or, for invalid input, is cut
+// off by the count bound).
+__device__ __forceinline__ void deposit_mixed(float2* acc, int T, float invT, const SmpF& a, const SmpF& b, int kshift,
                                               DeviceErr* err)
 {
-    const int kb = b.k + kshift;
-    const int cnt = kb - a.k;
+    const int cnt = b.k + kshift - a.k;
     const float du = (float)cnt + (b.f - a.f);
-    // one step never spans a whole period of bins for |Mr| < 1; anything else is bad
-    // geometry (or a non-finite time) and must not turn into a long loop
-    if (!(du > 0.0f) || cnt > T) {
-        flag(err, ACUM_DEVERR_ORDER, &err->order);
-        return;
-    }
-    if (!(fabsf(b.pt) < 3.0e38f) || !(fabsf(b.pl) < 3.0e38f)) {
-        flag(err, ACUM_DEVERR_NONFINITE, &err->nonfinite);
+    if (cnt <= 0 || cnt > T || !(du > 0.0f)) {
+        // no bin in the interval (cnt == 0, du > 0) is normal; everything else is bad
+        // geometry or a non-finite time and must not turn into a long loop
+        if (!(cnt == 0 && du > 0.0f)) flag(err, ACUM_DEVERR_ORDER, &err->order);
         return;
     }
     const float inv = __fdividef(1.0f, du);
     const float dT = b.pt - a.pt, dL = b.pl - a.pl;
     int idx = wrap_bin(a.k + 1, T, invT);
-    for (int m = 1; m <= cnt; ++m) {
-        const float w = ((float)m - a.f) * inv;
-        const float vT = fmaf(w, dT, a.pt), vL = fmaf(w, dL, a.pl);
-        float4 s = acc[idx];
-        ff_add(s.x, s.y, vT);
-        ff_add(s.z, s.w, vL);
-        acc[idx] = s;
+    float w = (1.0f - a.f) * inv;
+    float2 s = acc[idx];
+    s.x += fmaf(w, dT, a.pt);
+    s.y += fmaf(w, dL, a.pl);
+    acc[idx] = s;
+    for (int m = 2; m <= cnt; ++m) {
         if (++idx == T) idx = 0;
+        w = ((float)m - a.f) * inv;
+        s = acc[idx];
+        s.x += fmaf(w, dT, a.pt);
+        s.y += fmaf(w, dL, a.pl);
+        acc[idx] = s;
     }
 }
 
@@ -470,10 +474,6 @@ __device__ __forceinline__ void deposit_f64(double2* acc, int T, const KParams& 
     const int nbb = b.nb + nshift;
     if (!(tb > a.t) || nbb - a.nb > T || nbb - a.nb < 0) {
         flag(err, ACUM_DEVERR_ORDER, &err->order);
-        return;
-    }
-    if (!(fabs(b.pt) < 1e300) || !(fabs(b.pl) < 1e300)) {
-        flag(err, ACUM_DEVERR_NONFINITE, &err->nonfinite);
         return;
     }
     const double inv = 1.0 / (tb - a.t);
@@ -535,21 +535,52 @@ __device__ __forceinline__ SmpD shfl_up_smp<SmpD>(const SmpD& v)
     return o;
 }
 
+__host__ __device__ __forceinline__ size_t acc_region_bytes(int W, int T, int acc_bytes)
+{
+    return ((size_t)W * T * acc_bytes + 127) / 128 * 128;
+}
+
+// Adds a warp's bins to the global FP64 sums [obs][bin][2] and clears them.  `direct`
+// stores instead of adding (the block is the only writer of these sums).
+__device__ __forceinline__ void flush_bins(float2* acc, double* g, int T, int lane, bool direct, DeviceErr* err)
+{
+    __syncwarp();
+    for (int n = lane; n < T; n += 32) {
+        const float2 v = acc[n];
+        if (!(fabsf(v.x) < 3.0e38f) || !(fabsf(v.y) < 3.0e38f)) flag(err, ACUM_DEVERR_NONFINITE, &err->nonfinite);
+        if (direct) {
+            reinterpret_cast<double2*>(g)[n] = make_double2((double)v.x, (double)v.y);
+        } else if (v.x != 0.0f || v.y != 0.0f) {
+            atomicAdd(g + 2 * n, (double)v.x);
+            atomicAdd(g + 2 * n + 1, (double)v.y);
+        }
+        acc[n] = make_float2(0.f, 0.f);
+    }
+    __syncwarp();
+}
+
 template <bool F64, int SE>
 __global__ void __launch_bounds__(512, 1) tonal_kernel(const KParams p)
 {
     using Real = typename std::conditional<F64, double, float>::type;
     using Smp = typename std::conditional<F64, SmpD, SmpF>::type;
-    using Acc = typename std::conditional<F64, double2, float4>::type;
+    using Acc = typename std::conditional<F64, double2, float2>::type;
+    constexpr int kAccBytes = sizeof(Acc);
     constexpr int kTile = kGroups * kWin * 4;  // reals per (element, window) tile
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ int s_abort;
+    __shared__ int s_release[kMaxStages];  // warps done with the stage in each slot
+    __shared__ int s_last[kMaxStages];     // last stage issued into each slot (for the drain)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nwarps = blockDim.x >> 5;
     const int W = p.W, T = p.T, NS = p.NS, nW = p.nW;
     Acc* acc_all = reinterpret_cast<Acc*>(smem);
-    Real* stages = reinterpret_cast<Real*>(smem + (size_t)W * T * 16);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)W * T * 16 + (size_t)NS * SE * kTile * sizeof(Real));
+    // stages start on a 128-byte boundary: they are bulk-copy destinations (16-byte
+    // alignment required) read with 128-bit loads, and W*T*8 need not be a multiple of 16
+    const size_t stage_off = acc_region_bytes(W, T, kAccBytes);
+    Real* stages = reinterpret_cast<Real*>(smem + stage_off);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + stage_off + (size_t)NS * SE * kTile * sizeof(Real));
     Acc* acc = acc_all + (size_t)warp * T;
 
     const int item = blockIdx.x;
@@ -563,10 +594,14 @@ __global__ void __launch_bounds__(512, 1) tonal_kernel(const KParams p)
 
     for (int i = threadIdx.x; i < W * T; i += blockDim.x) {
         if constexpr (F64) acc_all[i] = make_double2(0.0, 0.0);
-        else acc_all[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        else acc_all[i] = make_float2(0.f, 0.f);
     }
     if (threadIdx.x == 0) {
-        for (int s = 0; s < NS; ++s) mbar_init(&bars[s], 1);
+        for (int s = 0; s < NS; ++s) {
+            mbar_init(&bars[s], 1);
+            s_release[s] = 0;
+            s_last[s] = -1;
+        }
         mbar_fence_init();
         s_abort = 0;
     }
@@ -574,19 +609,18 @@ __global__ void __launch_bounds__(512, 1) tonal_kernel(const KParams p)
 
     const Real* rec = reinterpret_cast<const Real*>(p.rec);
     const uint32_t tile_bytes = kTile * sizeof(Real);
-    int issued = 0;
+    // stage i = (element group i / nW, window i % nW) goes into slot i % NS
     auto issue = [&](int i) {
         const int s = i % NS, g = i / nW, w = i % nW;
+        s_last[s] = i;
         mbar_expect_tx(&bars[s], tile_bytes * SE);
         for (int j = 0; j < SE; ++j) {
             const int e = e0 + g * SE + j;
             bulk_g2s(stages + ((size_t)s * SE + j) * kTile, rec + ((size_t)e * nW + w) * kTile, tile_bytes, &bars[s]);
         }
     };
-    if (threadIdx.x == 0) {
-        for (int i = 0; i < NS - 1 && i < N; ++i) issue(i);
-        issued = min(NS - 1, N);
-    }
+    if (threadIdx.x == 0)
+        for (int i = 0; i < NS && i < N; ++i) issue(i);
 
     Real ox = 0, oy = 0, oz = 0;
     if (obs_ok) {
@@ -599,50 +633,50 @@ __global__ void __launch_bounds__(512, 1) tonal_kernel(const KParams p)
     Smp carry[SE], first[SE];
     const float invT = 1.0f / (float)T;
 
-    int done = 0;
+    // counters advanced incrementally (no per-stage integer division)
+    int s = 0, w = 0, g = 0, since_flush = 0;
+    uint32_t par = 0;
     for (int i = 0; i < N; ++i) {
-        if (threadIdx.x == 0 && i + NS - 1 < N) {
-            issue(i + NS - 1);
-            issued = i + NS;
-        }
-        const int s = i % NS;
         // the wait result is made warp-uniform before any shuffle below
-        const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&bars[s], (uint32_t)((i / NS) & 1)));
-        if (!ok && lane == 0) {
-            s_abort = 1;
-            flag(p.err, ACUM_DEVERR_TIMEOUT, &p.err->timeout);
+        const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&bars[s], par));
+        if (!ok) {
+            if (lane == 0) {
+                s_abort = 1;
+                flag(p.err, ACUM_DEVERR_TIMEOUT, &p.err->timeout);
+            }
+            break;
         }
-        const int w = i % nW;
+        if (*(volatile int*)&s_abort) break;
         const int tau = w * kWin + lane;
         const bool valid = tau < T;
-        if (ok && obs_ok) {
+        if (obs_ok) {
             const Real* st = stages + (size_t)s * SE * kTile;
             Smp cur[SE];
 #pragma unroll
             for (int j = 0; j < SE; ++j) {
                 const Real* tl = st + (size_t)j * kTile + lane * 4;
                 if constexpr (F64) {
-                    dbl4 g[kGroups];
+                    dbl4 gg[kGroups];
 #pragma unroll
                     for (int q = 0; q < kGroups; ++q) {
                         const double2* pp = reinterpret_cast<const double2*>(tl + q * kWin * 4);
                         double2 u0 = pp[0], u1 = pp[1];
-                        g[q] = dbl4{u0.x, u0.y, u1.x, u1.y};
+                        gg[q] = dbl4{u0.x, u0.y, u1.x, u1.y};
                     }
-                    cur[j] = sample_f64(g[0], g[1], g[2], g[3], g[4], ox, oy, oz, p, tau);
+                    cur[j] = sample_f64(gg[0], gg[1], gg[2], gg[3], gg[4], ox, oy, oz, p, tau);
                 } else {
-                    float4 g[kGroups];
+                    float4 gg[kGroups];
 #pragma unroll
-                    for (int q = 0; q < kGroups; ++q) g[q] = *reinterpret_cast<const float4*>(tl + q * kWin * 4);
-                    cur[j] = sample_mixed(g[0], g[1], g[2], g[3], g[4], ox, oy, oz, p, tau);
+                    for (int q = 0; q < kGroups; ++q) gg[q] = *reinterpret_cast<const float4*>(tl + q * kWin * 4);
+                    cur[j] = sample_mixed(gg[0], gg[1], gg[2], gg[3], gg[4], ox, oy, oz, p, tau);
                 }
             }
             const int last = min(31, T - 1 - w * kWin);
+            const bool has_prev = valid && (lane > 0 || w > 0);
 #pragma unroll
             for (int j = 0; j < SE; ++j) {
                 Smp prev = shfl_up_smp(cur[j]);
                 if (lane == 0) prev = carry[j];
-                const bool has_prev = valid && (lane > 0 || w > 0);
                 if constexpr (F64) {
                     if (has_prev) deposit_f64(acc, T, p, prev, cur[j], 0.0, 0, p.err);
                 } else {
@@ -662,48 +696,68 @@ __global__ void __launch_bounds__(512, 1) tonal_kernel(const KParams p)
                     }
                 }
             }
+            if constexpr (!F64) {
+                // FP32 partial sums cover at most `flush_groups` element groups before
+                // they are added to the FP64 sums in global memory
+                if (w == nW - 1 && (++since_flush == p.flush_groups || g == ngroups - 1)) {
+                    flush_bins(acc, p.acc + (size_t)o * T * 2, T, lane, false, p.err);
+                    since_flush = 0;
+                }
+            }
         }
-        __syncthreads();
-        done = i + 1;
-        if (s_abort) break;
+        // release the slot; the last warp to finish with it refills it with stage i + NS
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence_block();
+            if (atomicAdd(&s_release[s], 1) == nwarps - 1) {
+                s_release[s] = 0;
+                if (i + NS < N) issue(i + NS);
+            }
+        }
+        if (++s == NS) {
+            s = 0;
+            par ^= 1u;
+        }
+        if (++w == nW) {
+            w = 0;
+            ++g;
+        }
     }
+    __syncthreads();
     if (s_abort) {
-        // drain the copies still in flight before the block exits (bounded)
+        // drain the copies still in flight before the block exits (bounded waits)
         if (threadIdx.x == 0)
-            for (int i = done; i < issued; ++i) (void)mbar_wait_bounded(&bars[i % NS], (uint32_t)((i / NS) & 1));
+            for (int k = 0; k < NS; ++k)
+                if (s_last[k] >= 0) (void)mbar_wait_bounded(&bars[k], (uint32_t)((s_last[k] / NS) & 1));
         __syncthreads();
         return;
     }
-    // flush this block's bins
-    if (obs_ok) {
-        double* g = p.acc + (size_t)o * T * 2;
-        for (int n = lane; n < T; n += 32) {
-            double vT, vL;
-            if constexpr (F64) {
-                double2 a = acc[n];
-                vT = a.x;
-                vL = a.y;
-            } else {
-                float4 a = acc[n];
-                vT = (double)a.x + (double)a.y;
-                vL = (double)a.z + (double)a.w;
-            }
-            if (p.nchunk == 1) {
-                reinterpret_cast<double2*>(g)[n] = make_double2(vT, vL);
-            } else {
-                atomicAdd(g + 2 * n, vT);
-                atomicAdd(g + 2 * n + 1, vL);
+    // flush this block's bins (the mixed form flushed inside the loop)
+    if constexpr (F64) {
+        if (obs_ok) {
+            double* gsum = p.acc + (size_t)o * T * 2;
+            for (int n = lane; n < T; n += 32) {
+                const double2 a = acc[n];
+                if (!(fabs(a.x) < 1e300) || !(fabs(a.y) < 1e300)) flag(p.err, ACUM_DEVERR_NONFINITE, &p.err->nonfinite);
+                if (p.nchunk == 1) {
+                    reinterpret_cast<double2*>(gsum)[n] = a;
+                } else {
+                    atomicAdd(gsum + 2 * n, a.x);
+                    atomicAdd(gsum + 2 * n + 1, a.y);
+                }
             }
         }
     }
 }
 
 constexpr int kSE32 = 4;
+static_assert(kMaxStages >= 4, "stage bookkeeping");
 constexpr int kSE64 = 2;
 
 static size_t tonal_smem(int W, int T, int NS, int SE, int real_bytes)
 {
-    return (size_t)W * T * 16 + (size_t)NS * SE * kGroups * kWin * 4 * real_bytes + (size_t)NS * 8;
+    const int acc_bytes = real_bytes == 8 ? 16 : 8;  // double2 or float2 per bin
+    return acc_region_bytes(W, T, acc_bytes) + (size_t)NS * SE * kGroups * kWin * 4 * real_bytes + (size_t)NS * 8;
 }
 
 cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int num_sms, size_t smem_optin)
@@ -712,17 +766,20 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
     const int rb = f64 ? 8 : 4;
     const int SE = f64 ? kSE64 : kSE32;
     (void)SE_req;
-    const int NS = 3;
+    const int NS = 4;
     const int T = r.g.T;
     int W = W_req > 0 ? W_req : 16;
     W = std::min(W, 16);
-    while (W > 1 && tonal_smem(W, T, NS, SE, rb) > smem_optin) --W;
-    if (tonal_smem(W, T, NS, SE, rb) > smem_optin) return cudaErrorInvalidValue;
+    // keep 1 KB of the per-block limit for the kernel's static shared memory
+    const size_t budget = smem_optin - 1024;
+    while (W > 1 && tonal_smem(W, T, NS, SE, rb) > budget) --W;
+    if (tonal_smem(W, T, NS, SE, rb) > budget) return cudaErrorInvalidValue;
     if (W_req <= 0) {
         // do not spread few observers over many idle warps
         W = std::max(1, std::min(W, r.g.O));
     }
     TonalTile& t = r.t;
+    t.flush_elems = f64 ? 1 << 30 : 64;
     t.W = W;
     t.SE = SE;
     t.NS = NS;
@@ -806,6 +863,7 @@ cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s)
     kp.chunk = r.t.chunk;
     kp.nchunk = r.t.nchunk;
     kp.obs_tiles = (g.O + r.t.W - 1) / r.t.W;
+    kp.flush_groups = std::max(1, r.t.flush_elems / r.t.SE);
     kp.acc = r.acc;
     kp.err = r.err;
     const int threads = 32 * r.t.W;

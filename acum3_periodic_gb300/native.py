@@ -77,6 +77,7 @@ SIGNATURES = {
     "acum_device_error_word": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.c_int]),
     "acum_last_timing": (C.c_int, [C.c_void_p, C.c_int, _DP, C.POINTER(C.c_longlong)]),
     "acum_set_tile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "acum_measure_peak": (C.c_int, [C.c_int, C.c_int, _DP]),
     "acum_host_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t]),
     "acum_host_free": (C.c_int, [C.c_void_p]),
     "acum_find_pressure_time_history": (C.c_int, [C.c_void_p] * 9 + [C.c_int] + [C.c_void_p] * 5 +
@@ -284,6 +285,14 @@ class Context:
         w = C.c_uint32()
         self._ck(self.L.acum_device_error_word(self.h, C.byref(w), int(reset)))
         return w.value
+
+
+def measure_peak(device: int, which: int) -> float:
+    v = C.c_double()
+    rc = lib().acum_measure_peak(device, which, C.byref(v))
+    if rc != 0:
+        raise AcumError(rc, "acum_measure_peak failed")
+    return v.value
 
 
 class PinnedBuffer:

@@ -1,0 +1,306 @@
+"""Benchmark of the tonal hot path on the large workload (workload 2: 4 blades x 8000
+panels = 32000 elements, 1440 steps per revolution, 4096 observers; seeded synthetic
+rotor, see acum3_periodic_gb300/synth.py).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+GB300 arm (default).  One step = one pass of the tonal path over the deck with the
+surface rows already resident in HBM: GPU preprocessing (preprocess_imper) + the
+mixed-precision tonal kernel + the finalize transpose, i.e. acum_tonal_device.  `value`
+is element*observer*step evaluations per second over K timed steps (inputs larger than
+L2: 1.47 GB of surface rows and 2.9 GB of records per step).  `e2e` times the same
+metric through acum_tonal_from_host: pinned host rows in, pA out, copies inside.  The
+plain FP64 form is timed on every 8th observer (512) of the same deck, and the mixed
+result is compared with it there (OASPL dB and per-bin error).  `cpu_baseline` times
+the oracle port (the C restatement of the reference path) on this host's cores on a
+bounded sample of the same deck.
+
+Reference arm (--impl reference).  The reference's CPU implementation of the path: the
+oracle port in oracle/acum_oracle.c (the reference's own sources cannot be compiled on
+the GPU host: the reference tree is not there), all host threads, on bounded samples of
+the same workload; rank 0 only under torchrun.
+
+Multi-GPU: replicas (weak scaling) -- each rank solves the whole workload on its own
+GPU; no collective on the data path; value = all ranks' evaluations / max rank time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "elem·obs·step evals/s: mixed vs FP64 at ≤0.05 dB OASPL; adjoint/fwd ratio"
+ALG_FLOPS_PER_EVAL = 102  # FP ops per tonal evaluation (integrand + observer time + deposits)
+WORKLOAD = "workload 2: 4-blade rotor, 32000 elements, 1440 steps/rev, 4096 observers, tonal mixed precision"
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return ws, rank, local, dist
+    return 1, 0, 0, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms in the background."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.out = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.out.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for l in self.out:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def cpu_baseline(deck, nobs_sample: int, nthreads: int):
+    """The oracle port (C, FP64, reference algorithm) on the first `nobs_sample`
+    observers of the deck, with `nthreads` host threads; returns evals/s and details."""
+    from oracle import oracle as O
+    sub = deck.subset_observers(np.arange(nobs_sample))
+    inputs = O.TonalInputs(sub)
+    t0 = time.perf_counter()
+    fields = O.preprocess(sub, inputs)
+    t1 = time.perf_counter()
+    O.tonal(sub, nthreads=nthreads, fields=fields, inputs=inputs)
+    t2 = time.perf_counter()
+    evals = sub.E * sub.nTime * sub.nObs
+    return evals / (t2 - t0), dict(evals=evals, seconds=t2 - t0, preprocess_s=t1 - t0)
+
+
+def run_reference(args, deck, ws, rank, dist):
+    if rank != 0:
+        return
+    nth = os.cpu_count() or 1
+    nobs = max(nth, 16)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, info = cpu_baseline(deck, nobs, nth)
+        if i >= args.warmup:
+            vals.append(info["seconds"])
+    sec = float(np.mean(vals))
+    evals = deck.E * deck.nTime * nobs
+    value = evals / sec
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded rotor deck)",
+        "config": {"workload": WORKLOAD, "elements": deck.E, "steps": deck.nTime, "observers": deck.nObs},
+        "cpu_baseline": {"value": value, "unit": "evals/s", "cores": nth, "kind": "port",
+                         "sample": "first %d of %d observers x all %d elements x %d steps per step (%d evals); "
+                                   "oracle/acum_oracle.c, FP64, %d threads" % (nobs, deck.nObs, deck.E, deck.nTime,
+                                                                               evals, nth)},
+        "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--fp64-every", type=int, default=8, help="time the FP64 form on every n-th observer")
+    ap.add_argument("--cpu-obs", type=int, default=16, help="observers in the CPU-baseline sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--small", action="store_true", help="a reduced deck (for profiling runs)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if not args.small else args.warmup
+
+    ws, rank, local, dist = dist_init()
+    from acum3_periodic_gb300 import synth
+    scale = dict(n_span=25, n_chord_side=10, ntime=1440, nobs=512) if args.small else None
+    deck = synth.config_deck(2, scale=scale)
+
+    if args.impl == "reference":
+        run_reference(args, deck, ws, rank, dist)
+        return
+
+    from acum3_periodic_gb300 import native
+    ctx = native.Context(local)
+    ctx.set_deck(deck, bb=False)
+    evals = deck.tonal_evals()
+
+    def step():
+        ctx.mark_surfaces_changed()
+        ctx.tonal_device(native.MIXED, 0, 0, 0)
+
+    for _ in range(args.warmup):
+        step()
+    ctx.sync()
+    sampler = ClockSampler(local)
+    sampler.start()
+    kern_ms, prep_ms, fin_ms, launches = [], [], [], 0
+    barrier(dist)
+    ctx.sync()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+        ctx.sync()
+        kern_ms.append(ctx.timing(0)[0])
+        prep_ms.append(ctx.timing(1)[0])
+        fin_ms.append(ctx.timing(2)[0])
+        launches += ctx.timing(0)[1]
+    ctx.sync()
+    barrier(dist)
+    elapsed = max_over_ranks(dist, time.perf_counter() - t0)
+    clocks = sampler.stop()
+    value = ws * evals * args.steps / elapsed
+    ms_per_step = elapsed / args.steps * 1e3
+
+    # end to end through the C ABI from pinned host memory
+    raw = deck.raw_surfaces()
+    pin_raw = native.PinnedBuffer(raw.shape, np.float32)
+    pin_raw.array[:] = raw
+    pin_pA = native.PinnedBuffer((deck.nTime, deck.nObs), np.float64)
+    ctx.tonal_from_host(native.MIXED, pin_raw.ptr, pin_pA.ptr)
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.tonal_from_host(native.MIXED, pin_raw.ptr, pin_pA.ptr)
+    barrier(dist)
+    e2e_elapsed = max_over_ranks(dist, time.perf_counter() - t0)
+    e2e_value = ws * evals * args.steps / e2e_elapsed
+    mixed_pA = np.array(pin_pA.array)
+
+    # plain FP64 on every n-th observer of the same deck, and the accuracy of the mixed form
+    sel = np.arange(0, deck.nObs, args.fp64_every)
+    sub = deck.subset_observers(sel)
+    ctx64 = native.Context(local)
+    ctx64.set_deck(sub, bb=False)
+    ctx64.tonal(native.PLAIN_FP64)
+    t0 = time.perf_counter()
+    _, _, pA64 = ctx64.tonal(native.PLAIN_FP64)
+    fp64_sec = time.perf_counter() - t0
+    fp64_kern = ctx64.timing(0)[0] / 1e3
+    fp64_value = sub.tonal_evals() / fp64_sec
+    ref = pA64
+    mix = mixed_pA[:, sel]
+    oas = lambda p: 10 * np.log10(np.mean(p ** 2, axis=0) / 4e-10)
+    oaspl_err = float(np.max(np.abs(oas(mix) - oas(ref))))
+    rms = np.sqrt(np.mean(ref ** 2, axis=0, keepdims=True))
+    bin_rms_err = float(np.max(np.abs(mix - ref) / rms))
+    scale_ = np.maximum(np.abs(ref), 1e-6 * np.abs(ref).max(axis=0, keepdims=True))
+    bin_rel_err = float(np.median(np.abs(mix - ref) / scale_))
+
+    # roofline of the dominant kernel (the mixed tonal kernel), CUDA-event timed
+    kms = float(np.mean(kern_ms))
+    fp32_peak = native.measure_peak(local, 0)
+    fp64_peak = native.measure_peak(local, 1)
+    achieved = ALG_FLOPS_PER_EVAL * evals / (kms * 1e-3) / 1e12
+    rec_bytes = deck.E * deck.nTime * 20 * 4
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded rotor deck)",
+        "config": {"workload": WORKLOAD, "elements": deck.E, "steps": deck.nTime, "observers": deck.nObs,
+                   "precision": "mixed", "l2": "inputs larger than L2 (1.47 GB rows, 3.7 GB records per step)",
+                   "parallelism": "replicas" if ws > 1 else "1 GPU"},
+        "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": int(raw.nbytes),
+                "d2h_bytes_per_step": int(deck.nTime * deck.nObs * 8)},
+        "gpu_launches": int(launches),
+        "kernels_ms_per_step": {"preprocess": float(np.mean(prep_ms)), "tonal_mixed": kms,
+                                "finalize": float(np.mean(fin_ms))},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak, "traffic": None,
+                     "peak_source": "measured FP32 FMA throughput of this GPU (acum_measure_peak); "
+                                    "MEASURED_PEAKS.json holds no CUDA-core FP32 peak",
+                     "algorithmic_flops_per_eval": ALG_FLOPS_PER_EVAL,
+                     "hbm_view": {"record_bytes_per_launch": rec_bytes,
+                                  "achieved_gbs": rec_bytes / (kms * 1e-3) / 1e9}},
+        "fp64": {"evals_per_s": fp64_value, "kernel_evals_per_s": sub.tonal_evals() / fp64_kern,
+                 "observers": int(len(sel)), "fp64_peak_tflops": fp64_peak,
+                 "kernel_frac_of_fp64_peak": ALG_FLOPS_PER_EVAL * sub.tonal_evals() / fp64_kern / 1e12 / fp64_peak},
+        "mixed_over_fp64": value / fp64_value,
+        "accuracy_vs_fp64": {"oaspl_max_err_db": oaspl_err, "per_bin_err_over_rms_max": bin_rms_err,
+                             "per_bin_rel_err_median": bin_rel_err, "observers_compared": int(len(sel))},
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu:
+        nth = os.cpu_count() or 1
+        v, info = cpu_baseline(deck, args.cpu_obs, nth)
+        out["cpu_baseline"] = {"value": v, "unit": "evals/s", "cores": nth, "kind": "port",
+                               "sample": "first %d of %d observers x all elements x all steps (%d evals), "
+                                         "oracle/acum_oracle.c FP64 incl. its preprocessing" % (
+                                             args.cpu_obs, deck.nObs, info["evals"])}
+    if rank == 0:
+        print(json.dumps(out))
+    pin_raw.close()
+    pin_pA.close()
+    ctx.close()
+    ctx64.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

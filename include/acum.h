@@ -164,6 +164,10 @@ int acum_last_timing(const acum_ctx* ctx, int which, double* ms, long long* laun
  * elements per pipeline stage.  Used by the autotuner. */
 int acum_set_tile(acum_ctx* ctx, int obs_per_block, int elems_per_stage, int items_per_sm);
 
+/* Measured FMA throughput of `device` in TFLOP/s: which = 0 FP32, 1 FP64 (a short
+ * FMA-chain kernel timed with CUDA events; the CUDA-core peaks of the roofline). */
+int acum_measure_peak(int device, int which, double* tflops);
+
 /* Pinned host memory for staging (cudaHostAlloc); free with acum_host_free. */
 int acum_host_alloc(void** p, size_t bytes);
 int acum_host_free(void* p);
