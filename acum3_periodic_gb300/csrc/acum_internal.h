@@ -44,6 +44,7 @@ struct TonalTile {
     int nchunk;
     int items;
     int flush_elems;  // mixed: elements summed in FP32 before the FP64 flush
+    int opw;          // observers per warp
     size_t smem;
 };
 

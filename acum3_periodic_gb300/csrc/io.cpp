@@ -310,7 +310,7 @@ bool read_bb(const std::string& dir, int nsurf, int ntime, BBDeck& bb, std::stri
         std::string b;
         if (!slurp(fn, b)) return set_err(err, "Unable to open " + fn);
         int nt = 0, ns = 0;
-        if (sscanf(b.c_str(), "%d %d", &nt, &ns) != 2 || ns < 2) return set_err(err, "Bad header in " + fn);
+        if (sscanf(b.c_str(), "%d %d", &nt, &ns) != 2 || ns < 3) return set_err(err, "Bad header in " + fn);
         bb.nsect[i] = ns;
         const char* p = b.c_str();
         const char* end = p + b.size();

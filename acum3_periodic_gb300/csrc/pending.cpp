@@ -3,26 +3,14 @@
 #include "ctx.h"
 
 namespace acum {
-void release_bpm_state(acum_ctx*) {}
 void release_adj_state(acum_ctx*) {}
 }  // namespace acum
 
 using namespace acum;
 
-extern "C" int acum_set_bb(acum_ctx* ctx, const acum_bb_desc*) { return fail(ctx, ACUM_ERR_UNSUPPORTED, "not built yet"); }
-extern "C" int acum_bpm(acum_ctx* ctx, int, double*, double*) { return fail(ctx, ACUM_ERR_UNSUPPORTED, "not built yet"); }
 extern "C" int acum_tonal_adjoint(acum_ctx* ctx, int, const double*, double*, double*, double*, double*)
 {
     return fail(ctx, ACUM_ERR_UNSUPPORTED, "not built yet");
-}
-extern "C" int acum_find_bb_noise(int, int, int, float, const float*, const float*, const int*, const float*,
-                                  const int*, const float*, const float*, const int*, const int*, const int*,
-                                  const float*, const float*, const int*, const int*, const int*, const int*,
-                                  const int*, const int*, const int*, const int*, const int*, const float*,
-                                  const float*, const float*, const float*, const float*, int, const float*,
-                                  const float*, const float*, int, const float*, float, float*, float*)
-{
-    return fail(nullptr, ACUM_ERR_UNSUPPORTED, "not built yet");
 }
 extern "C" int acum_batch_create(acum_batch**, int) { return fail(nullptr, ACUM_ERR_UNSUPPORTED, "not built yet"); }
 extern "C" int acum_batch_destroy(acum_batch*) { return ACUM_OK; }

@@ -750,7 +750,217 @@ __global__ void __launch_bounds__(512, 1) tonal_kernel(const KParams p)
     }
 }
 
+// ----------------------------------------------------------- mixed kernel v2
+//
+// The mixed form's kernel.  Each warp serves OPW observers, so a record loaded from
+// shared memory feeds OPW evaluations, and each lane carries OPW x SE independent
+// samples per stage (instruction-level parallelism in place of more warps).  The left
+// neighbour of lane l's sample comes from one rotating shuffle (lane l-1); lane 0 keeps
+// what it received in the previous window (the previous window's lane 31), and the first
+// sample of an element stays in lane 0 for the periodic wrap at its end.
+
+// RMW of one bin of a warp's observer row
+__device__ __forceinline__ void add_bin(float2* acc, int idx, float w, float pt, float dT, float pl, float dL)
+{
+    float2 v = acc[idx];
+    v.x += fmaf(w, dT, pt);
+    v.y += fmaf(w, dL, pl);
+    acc[idx] = v;
+}
+
+// bins in (u(a), u(b) + kshift]; cnt <= 2 whenever |Mr| < 1, handled without a loop
+__device__ __forceinline__ void deposit_v2(float2* acc, int T, float invT, const SmpF& a, const SmpF& b, int kshift,
+                                           bool active, DeviceErr* err)
+{
+    const int cnt = b.k + kshift - a.k;
+    const float du = (float)cnt + (b.f - a.f);
+    const bool fast = active && cnt >= 1 && cnt <= 2 && du > 0.0f;
+    if (fast) {
+        const float inv = __fdividef(1.0f, du);
+        const float dT = b.pt - a.pt, dL = b.pl - a.pl;
+        int idx = wrap_bin(a.k + 1, T, invT);
+        const float w1 = (1.0f - a.f) * inv;
+        add_bin(acc, idx, w1, a.pt, dT, a.pl, dL);
+        if (cnt == 2) {
+            if (++idx == T) idx = 0;
+            add_bin(acc, idx, w1 + inv, a.pt, dT, a.pl, dL);
+        }
+    } else if (active && !(cnt == 0 && du > 0.0f)) {
+        // more than two bins in one step (a step faster than the bin rate: |Mr| > 1) or a
+        // decreasing / non-finite observer time
+        if (cnt > 2 && cnt <= T && du > 0.0f) {
+            const float inv = __fdividef(1.0f, du);
+            const float dT = b.pt - a.pt, dL = b.pl - a.pl;
+            int idx = wrap_bin(a.k + 1, T, invT);
+            for (int m = 1; m <= cnt; ++m) {
+                add_bin(acc, idx, ((float)m - a.f) * inv, a.pt, dT, a.pl, dL);
+                if (++idx == T) idx = 0;
+            }
+        } else {
+            flag(err, ACUM_DEVERR_ORDER, &err->order);
+        }
+    }
+}
+
+__device__ __forceinline__ SmpF shfl_idx(const SmpF& v, int src)
+{
+    SmpF o;
+    o.k = __shfl_sync(0xffffffffu, v.k, src);
+    o.f = __shfl_sync(0xffffffffu, v.f, src);
+    o.pt = __shfl_sync(0xffffffffu, v.pt, src);
+    o.pl = __shfl_sync(0xffffffffu, v.pl, src);
+    return o;
+}
+
+template <int OPW, int SE>
+__global__ void __launch_bounds__(OPW == 1 ? 512 : 256, 1) tonal_mixed_kernel(const KParams p)
+{
+    constexpr int kTile = kGroups * kWin * 4;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ int s_abort;
+    __shared__ int s_release[kMaxStages];
+    __shared__ int s_last[kMaxStages];
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nwarps = blockDim.x >> 5;
+    const int W = p.W;  // observers per block = nwarps * OPW
+    const int T = p.T, NS = p.NS, nW = p.nW;
+    float2* acc_all = reinterpret_cast<float2*>(smem);
+    const size_t stage_off = acc_region_bytes(W, T, 8);
+    float* stages = reinterpret_cast<float*>(smem + stage_off);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + stage_off + (size_t)NS * SE * kTile * sizeof(float));
+
+    const int item = blockIdx.x;
+    const int ot = item % p.obs_tiles, ec = item / p.obs_tiles;
+    const int e0 = ec * p.chunk;
+    const int e1 = min(e0 + p.chunk, p.Epad);
+    const int ngroups = e1 > e0 ? (e1 - e0) / SE : 0;
+    const int N = ngroups * nW;
+
+    for (int i = threadIdx.x; i < W * T; i += blockDim.x) acc_all[i] = make_float2(0.f, 0.f);
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NS; ++s) {
+            mbar_init(&bars[s], 1);
+            s_release[s] = 0;
+            s_last[s] = -1;
+        }
+        mbar_fence_init();
+        s_abort = 0;
+    }
+    __syncthreads();
+
+    const float* rec = reinterpret_cast<const float*>(p.rec);
+    const uint32_t tile_bytes = kTile * sizeof(float);
+    auto issue = [&](int i) {
+        const int s = i % NS, g = i / nW, w = i % nW;
+        s_last[s] = i;
+        mbar_expect_tx(&bars[s], tile_bytes * SE);
+        for (int j = 0; j < SE; ++j) {
+            const int e = e0 + g * SE + j;
+            bulk_g2s(stages + ((size_t)s * SE + j) * kTile, rec + ((size_t)e * nW + w) * kTile, tile_bytes, &bars[s]);
+        }
+    };
+    if (threadIdx.x == 0)
+        for (int i = 0; i < NS && i < N; ++i) issue(i);
+
+    float ox[OPW], oy[OPW], oz[OPW];
+    bool oks[OPW];
+    float2* acc[OPW];
+#pragma unroll
+    for (int q = 0; q < OPW; ++q) {
+        const int o = ot * W + warp * OPW + q;
+        oks[q] = o < p.O;
+        const int oc = oks[q] ? o : 0;
+        ox[q] = p.obs32[3 * oc];
+        oy[q] = p.obs32[3 * oc + 1];
+        oz[q] = p.obs32[3 * oc + 2];
+        acc[q] = acc_all + (size_t)(warp * OPW + q) * T;
+    }
+    SmpF carry[OPW][SE], first[OPW][SE];
+    const float invT = 1.0f / (float)T;
+
+    int s = 0, w = 0, g = 0, since_flush = 0;
+    uint32_t par = 0;
+    for (int i = 0; i < N; ++i) {
+        const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&bars[s], par));
+        if (!ok) {
+            if (lane == 0) {
+                s_abort = 1;
+                flag(p.err, ACUM_DEVERR_TIMEOUT, &p.err->timeout);
+            }
+            break;
+        }
+        if (*(volatile int*)&s_abort) break;
+        const int tau = w * kWin + lane;
+        const bool valid = tau < T;
+        const float* st = stages + (size_t)s * SE * kTile;
+        SmpF cur[OPW][SE];
+#pragma unroll
+        for (int j = 0; j < SE; ++j) {
+            const float* tl = st + (size_t)j * kTile + lane * 4;
+            float4 gg[kGroups];
+#pragma unroll
+            for (int q = 0; q < kGroups; ++q) gg[q] = *reinterpret_cast<const float4*>(tl + q * kWin * 4);
+#pragma unroll
+            for (int q = 0; q < OPW; ++q)
+                cur[q][j] = sample_mixed(gg[0], gg[1], gg[2], gg[3], gg[4], ox[q], oy[q], oz[q], p, tau);
+        }
+        const bool first_win = w == 0, last_win = w == nW - 1;
+        const int rot_src = (lane + 31) & 31;
+#pragma unroll
+        for (int q = 0; q < OPW; ++q) {
+#pragma unroll
+            for (int j = 0; j < SE; ++j) {
+                const SmpF rot = shfl_idx(cur[q][j], rot_src);
+                const SmpF prev = lane == 0 ? carry[q][j] : rot;
+                deposit_v2(acc[q], T, invT, prev, cur[q][j], 0, oks[q] && valid && !(first_win && lane == 0), p.err);
+                carry[q][j] = rot;
+                if (first_win && lane == 0) first[q][j] = cur[q][j];
+                if (last_win) {
+                    // the periodic wrap: (t(T-1), t(0) + period] (core.cu:173-194)
+                    const SmpF lastS = shfl_idx(cur[q][j], min(31, T - 1 - w * kWin));
+                    if (lane == 0) deposit_v2(acc[q], T, invT, lastS, first[q][j], T, oks[q], p.err);
+                }
+            }
+        }
+        // FP32 partial sums cover at most `flush_groups` element groups before they are
+        // added to the FP64 sums in global memory
+        if (last_win && (++since_flush == p.flush_groups || g == ngroups - 1)) {
+#pragma unroll
+            for (int q = 0; q < OPW; ++q)
+                if (oks[q])
+                    flush_bins(acc[q], p.acc + (size_t)(ot * W + warp * OPW + q) * T * 2, T, lane, false, p.err);
+            since_flush = 0;
+        }
+        // release the slot; the last warp to finish with it refills it with stage i + NS
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence_block();
+            if (atomicAdd(&s_release[s], 1) == nwarps - 1) {
+                s_release[s] = 0;
+                if (i + NS < N) issue(i + NS);
+            }
+        }
+        if (++s == NS) {
+            s = 0;
+            par ^= 1u;
+        }
+        if (++w == nW) {
+            w = 0;
+            ++g;
+        }
+    }
+    __syncthreads();
+    if (s_abort) {
+        if (threadIdx.x == 0)
+            for (int k = 0; k < NS; ++k)
+                if (s_last[k] >= 0) (void)mbar_wait_bounded(&bars[k], (uint32_t)((s_last[k] / NS) & 1));
+        __syncthreads();
+    }
+}
+
 constexpr int kSE32 = 4;
+constexpr int kOPW = 1;
 static_assert(kMaxStages >= 4, "stage bookkeeping");
 constexpr int kSE64 = 2;
 
@@ -766,18 +976,22 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
     const int rb = f64 ? 8 : 4;
     const int SE = f64 ? kSE64 : kSE32;
     (void)SE_req;
+    // mixed: two observers per warp; W below counts observers per block
+    const int opw = f64 ? 1 : kOPW;
+    r.t.opw = opw;
     const int NS = 4;
     const int T = r.g.T;
     int W = W_req > 0 ? W_req : 16;
     W = std::min(W, 16);
     // keep 1 KB of the per-block limit for the kernel's static shared memory
     const size_t budget = smem_optin - 1024;
-    while (W > 1 && tonal_smem(W, T, NS, SE, rb) > budget) --W;
+    while (W > opw && tonal_smem(W, T, NS, SE, rb) > budget) W -= opw;
     if (tonal_smem(W, T, NS, SE, rb) > budget) return cudaErrorInvalidValue;
     if (W_req <= 0) {
         // do not spread few observers over many idle warps
-        W = std::max(1, std::min(W, r.g.O));
+        W = std::max(opw, std::min(W, (r.g.O + opw - 1) / opw * opw));
     }
+    W = (W + opw - 1) / opw * opw;
     TonalTile& t = r.t;
     t.flush_elems = f64 ? 1 << 30 : 64;
     t.W = W;
@@ -866,9 +1080,17 @@ cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s)
     kp.flush_groups = std::max(1, r.t.flush_elems / r.t.SE);
     kp.acc = r.acc;
     kp.err = r.err;
-    const int threads = 32 * r.t.W;
-    if (r.precision == ACUM_PLAIN_FP64) return launch_t<true, kSE64>(kp, r.t.items, threads, r.t.smem, s);
-    return launch_t<false, kSE32>(kp, r.t.items, threads, r.t.smem, s);
+    if (r.precision == ACUM_PLAIN_FP64) return launch_t<true, kSE64>(kp, r.t.items, 32 * r.t.W, r.t.smem, s);
+    const int threads = 32 * (r.t.W / kOPW);
+    static size_t configured = 0;
+    if (r.t.smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(tonal_mixed_kernel<kOPW, kSE32>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r.t.smem);
+        if (e != cudaSuccess) return e;
+        configured = r.t.smem;
+    }
+    tonal_mixed_kernel<kOPW, kSE32><<<r.t.items, threads, r.t.smem, s>>>(kp);
+    return cudaGetLastError();
 }
 
 // ------------------------------------------------------------------ finalize
