@@ -231,8 +231,13 @@ def add_bb(deck: Deck, spec: RotorSpec, nsect: int, t_del: int, trip: int, seed:
     for b in range(spec.blades if n_bb is None else n_bb):
         geom = np.stack([rr, np.zeros(nsect), np.zeros(nsect), chord / spec.radius], -1).astype(np.float32)
         data = np.zeros((T, nsect, 7), np.float32)
-        cn = 0.2 + 0.6 * uniform(seed, 500 + b, nsect)
-        cc = -0.02 + 0.04 * uniform(seed, 600 + b, nsect)
+        # local section coefficients cn in [0.2, 0.8] and cc in [-0.02, 0.02]; the file holds
+        # them normalised by the tip dynamic pressure, i.e. times (r/R)^2, which the reader
+        # divides out again (io.cu:509-512).  (Taken literally as file values they would mean
+        # cl ~ 20 at the root, where the reference's fixed-point angle-of-attack solve does not
+        # converge and the result depends on the last bits of cos/sin.)
+        cn = (0.2 + 0.6 * uniform(seed, 500 + b, nsect)) * rr ** 2
+        cc = (-0.02 + 0.04 * uniform(seed, 600 + b, nsect)) * rr ** 2
         if t_del == 0:
             # boundary-layer thicknesses given directly (BLT/DT suction, pressure) [m]
             base = 0.01 * chord

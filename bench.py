@@ -172,6 +172,7 @@ def main():
     ap.add_argument("--cpu-obs", type=int, default=16, help="observers in the CPU-baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--small", action="store_true", help="a reduced deck (for profiling runs)")
+    ap.add_argument("--no-bpm", action="store_true", help="skip the broadband leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if not args.small else args.warmup
 
@@ -285,6 +286,35 @@ def main():
                              "per_bin_rel_err_median": bin_rel_err, "observers_compared": int(len(sel))},
         "clocks": clocks,
     }
+    # broadband (BPM) path on the same workload's broadband deck (4 x 50 sections)
+    if deck.BB_noise == 1 and not args.no_bpm:
+        ctx.set_bb(deck)
+        ctx.bpm(0)
+        bt = []
+        for _ in range(max(1, args.steps // 2)):
+            t0 = time.perf_counter()
+            spl, oas = ctx.bpm(0)
+            bt.append(time.perf_counter() - t0)
+        bpm_kernel_ms = ctx.timing(3)[0]
+        nsec = sum(b.nsect for b in deck.bb)
+        bpm_evals = nsec * deck.nObs * deck.nTime * 42
+        bsel = np.arange(0, deck.nObs, max(1, deck.nObs // 8))[:8]
+        bpm = {"metric": "section·observer·band evals/s (per source step)", "sections": nsec,
+               "evals": bpm_evals, "evals_per_s": bpm_evals / float(np.mean(bt)),
+               "kernel_evals_per_s": bpm_evals / (bpm_kernel_ms * 1e-3), "kernel_ms": bpm_kernel_ms,
+               "per_section_observer_band_per_s": bpm_evals / float(np.mean(bt)) / deck.nTime}
+        if not args.no_cpu:
+            from oracle import oracle as O
+            sub = deck.subset_observers(bsel)
+            nth = os.cpu_count() or 1
+            t0 = time.perf_counter()
+            ospl, ooas = O.bpm(sub, aa_mode=0, nthreads=nth)
+            cpu_s = time.perf_counter() - t0
+            bpm["oaspl_max_err_db"] = float(np.max(np.abs(oas[bsel] - ooas)))
+            bpm["band_total_max_err_db"] = float(np.max(np.abs(spl[bsel, :, 0] - ospl[:, :, 0])))
+            bpm["cpu_baseline"] = {"evals_per_s": nsec * len(bsel) * deck.nTime * 42 / cpu_s, "cores": nth,
+                                   "kind": "port", "sample": "%d observers x all sections, steps, bands" % len(bsel)}
+        out["bpm"] = bpm
     if rank == 0 and not args.no_cpu:
         nth = os.cpu_count() or 1
         v, info = cpu_baseline(deck, args.cpu_obs, nth)

@@ -1013,3 +1013,33 @@ int acumo_bpm_prep(const acumo_bpm* B, int is_req, double* u, double* alpha, dou
     }
     return -1;
 }
+
+/* Exposes the blade positions of BB surface `is`: quarter chord xyz and trailing edge
+ * xyzt, each [sect][step][3] (bb_core.cu:79-164). */
+int acumo_bpm_geom(const acumo_bpm* B, int is_req, double* xyz, double* xyzt)
+{
+    int xs = 0, as = 0, ss = 0, ms = 0, rs = 0;
+    size_t ds = 0, dt = 0;
+    for (int is = 0; is < B->nsurf; is++) {
+        int ns = B->nsect[is];
+        o_table T;
+        T.ns = B->nsect_t[is]; T.na = B->naoa_t[is]; T.nm = B->nmach_t[is]; T.nr = B->nre_t[is];
+        T.sect = B->sect_t + ss; T.aoa = B->aoa_t + as; T.mach = B->mach_t + ms; T.re = B->re_t + rs;
+        T.data = B->bbdata_t + dt;
+        if (is == is_req) {
+            size_t n = (size_t)ns * B->ntime;
+            o_bbsurf S;
+            S.xyz = xyz; S.xyzt = xyzt;
+            S.u = (double*)malloc(sizeof(double) * n); S.alpha = (double*)malloc(sizeof(double) * n);
+            S.cla = (double*)malloc(sizeof(double) * n); S.bl = (double*)malloc(sizeof(double) * n * 4);
+            o_bpm_surface_prep(B, is, B->xyzcR + 4 * (size_t)xs, B->bbdata + ds, &T, &S);
+            free(S.u); free(S.alpha); free(S.cla); free(S.bl);
+            return 0;
+        }
+        xs += ns;
+        ds += (size_t)ns * B->ntime * 7;
+        ss += T.ns; as += T.na; ms += T.nm; rs += T.nr;
+        dt += (size_t)T.ns * T.na * T.nm * T.nr * 7;
+    }
+    return -1;
+}

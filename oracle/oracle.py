@@ -58,6 +58,7 @@ def lib():
         L.acumo_tonal_run.argtypes = [C.POINTER(_Tonal), _DP, _DP, C.c_int, C.c_int, _DP, _DP, _DP, C.c_int]
         L.acumo_bpm_run.argtypes = [C.POINTER(_Bpm), _DP, C.c_int, C.c_int, _DP, _DP, C.c_int]
         L.acumo_bpm_prep.argtypes = [C.POINTER(_Bpm), C.c_int, _DP, _DP, _DP, _DP]
+        L.acumo_bpm_geom.argtypes = [C.POINTER(_Bpm), C.c_int, _DP, _DP]
         L.acumo_bb_curve.argtypes = [C.c_int, _DP, _DP, C.c_int]
         L.acumo_g5comp.argtypes = [C.c_double, C.c_double]
         L.acumo_g5comp.restype = C.c_double
@@ -180,6 +181,15 @@ def bpm_prep(deck, surface: int, aa_mode: int = 0):
     u = np.zeros((ns, T)); al = np.zeros((ns, T)); cla = np.zeros((ns, T)); bl = np.zeros((ns, T, 4))
     lib().acumo_bpm_prep(C.byref(I.s), surface, _p(u), _p(al), _p(cla), _p(bl))
     return u, al, cla, bl
+
+
+def bpm_geom(deck, surface: int):
+    """quarter-chord and trailing-edge positions [sect][step][3] of one BB surface."""
+    I = BpmInputs(deck, 0)
+    ns = deck.bb[surface].nsect
+    xyz = np.zeros((ns, deck.nTime, 3)); xyzt = np.zeros((ns, deck.nTime, 3))
+    lib().acumo_bpm_geom(C.byref(I.s), surface, _p(xyz), _p(xyzt))
+    return xyz, xyzt
 
 
 def bb_curve(which: int, x: np.ndarray) -> np.ndarray:
