@@ -1,0 +1,202 @@
+// noalloc.cu -- acum_find_pressure_time_history_noalloc: the reference-shaped tonal
+// drop-in for callers that must not allocate memory.
+//
+// Who needs it: code that runs where allocation is not allowed or not safe -- inside a
+// host callback or a custom allocator's own call path, in a solver that has handed all
+// device memory to a pool it does not share, or between the capture of stream work
+// that must not be split by cudaMalloc/cudaFree (which synchronise the device).  Such a
+// caller still owns and passes its inputs and outputs; what the computation needs besides
+// them (the tiled per-step records and the FP64 bin sums) lives here in one fixed array
+// of device memory that every GPU loading this library reserves until process exit.
+//
+// Limits and behaviour:
+//  * the scratch array is kNoAllocBytes = 128 MiB per device; a call whose records
+//    (80 bytes per element-step, elements rounded up to 4 and steps to 32) plus FP64 bin
+//    sums (16 bytes per observer-step) exceed it is rejected with ACUM_ERR_INVALID and a
+//    message that gives both sizes;
+//  * the first call on a device looks up the array's device address (cudaGetSymbolAddress)
+//    with that device current; make that first call before capturing stream work into a
+//    CUDA graph;
+//  * every call reuses the same array and leaves its contents behind; the call clears
+//    what must start at zero itself, and two calls whose GPU work overlaps (different
+//    streams or threads without ordering) race on the array -- serialise them;
+//  * no cudaMalloc/cudaFree, no host heap allocation: the small per-surface arrays are
+//    read into fixed stack buffers (at most kMaxSurfaces surfaces).
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "acum_internal.h"
+#include "ctx.h"
+
+namespace acum {
+
+constexpr size_t kNoAllocBytes = 128ull << 20;
+constexpr int kMaxSurfaces = 256;
+constexpr int kMaxDevices = 64;
+
+// the scratch: tiled records first, then the [obs][step][2] FP64 bin sums
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+static std::mutex g_na_mu;
+static void* g_na_ptr[kMaxDevices];
+static char g_na_msg[256];
+
+// Records straight from the reference's AoS arrays; the element's surface and offsets
+// are found from E[] and the X/N/V/PR pointer arrays on the device (no host tables).
+__global__ void noalloc_records_kernel(const float* __restrict__ X, const float* __restrict__ N,
+                                       const float* __restrict__ V, const float* __restrict__ PR,
+                                       const int* __restrict__ E, const int* __restrict__ XPtr,
+                                       const int* __restrict__ NPtr, const int* __restrict__ VPtr,
+                                       const int* __restrict__ PRPtr, int nSurf, int Etot, int T, int nW, double a0,
+                                       double rho, float* __restrict__ rec)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)Etot * T) return;
+    const int e = (int)(idx / T), t = (int)(idx % T);
+    int s = 0, base = 0;
+    while (s < nSurf - 1 && e >= base + E[s]) {
+        base += E[s];
+        ++s;
+    }
+    const int j = e - base;
+    const float* x = X + XPtr[s] + (size_t)j * T * 4 + (size_t)t * 4;
+    const float* n = N + NPtr[s] + (size_t)j * T * 6 + (size_t)t * 6;
+    const float* v = V + VPtr[s] + (size_t)j * T * 6 + (size_t)t * 6;
+    const float* pr = PR + PRPtr[s] + (size_t)j * T * 2 + (size_t)t * 2;
+    const double D1 = 1.0 / (4.0 * M_PI * a0), ia0 = 1.0 / a0;
+    const double vx = v[0], vy = v[1], vz = v[2], nx = n[0], ny = n[1], nz = n[2], P = pr[0], Pd = pr[1];
+    const double ds = x[3];
+    const double L[3] = {P * nx, P * ny, P * nz};
+    double r[20];
+    r[0] = x[0]; r[1] = x[1]; r[2] = x[2]; r[3] = D1 * ds;
+    r[4] = vx * ia0; r[5] = vy * ia0; r[6] = vz * ia0; r[7] = (vx * vx + vy * vy + vz * vz) * ia0 * ia0;
+    r[8] = (double)v[3] * ia0; r[9] = (double)v[4] * ia0; r[10] = (double)v[5] * ia0;
+    r[11] = D1 * rho * (vx * nx + vy * ny + vz * nz) * a0 * ds;
+    r[12] = L[0]; r[13] = L[1]; r[14] = L[2]; r[15] = (L[0] * vx + L[1] * vy + L[2] * vz) * ia0;
+    r[16] = Pd * nx + P * (double)n[3]; r[17] = Pd * ny + P * (double)n[4]; r[18] = Pd * nz + P * (double)n[5];
+    r[19] = 0.0;
+    const int w = t / kWin, lane = t % kWin;
+    const size_t tile = ((size_t)e * nW + w) * (kGroups * kWin * 4);
+    for (int q = 0; q < kGroups; ++q)
+        *reinterpret_cast<float4*>(rec + tile + ((size_t)q * kWin + lane) * 4) =
+            make_float4((float)r[4 * q], (float)r[4 * q + 1], (float)r[4 * q + 2], (float)r[4 * q + 3]);
+}
+
+}  // namespace acum
+
+using namespace acum;
+
+extern "C" const char* acum_noalloc_last_error(void) { return g_na_msg; }
+
+extern "C" int acum_find_pressure_time_history_noalloc(const float* rObs, const float* tObs, float* pT, float* pL,
+                                                       float* pA, const float* Xham, const float* Nham,
+                                                       const float* Vham, const float* PRham, int nSurf,
+                                                       const int* XPtr, const int* NPtr, const int* VPtr,
+                                                       const int* PRPtr, const int* E, int nObs, int nTime,
+                                                       float dPsi, float dTau, float a0, float rhoRef,
+                                                       const float* vInf, float oM, void* stream)
+{
+    (void)tObs;
+    auto bad = [](int code, const char* m) {
+        snprintf(g_na_msg, sizeof g_na_msg, "%s", m);
+        return code;
+    };
+    if (!rObs || !pT || !pL || !pA || !Xham || !Nham || !Vham || !PRham || !XPtr || !NPtr || !VPtr || !PRPtr || !E ||
+        !vInf)
+        return bad(ACUM_ERR_INVALID, "findPressureTimeHistory_noalloc: null argument");
+    if (nSurf <= 0 || nSurf > kMaxSurfaces || nObs <= 0 || nTime < 6)
+        return bad(ACUM_ERR_INVALID, "findPressureTimeHistory_noalloc: sizes (1..256 surfaces, nTime >= 6)");
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+        return bad(ACUM_ERR_CUDA, "findPressureTimeHistory_noalloc: no current device");
+    void* scratch = nullptr;
+    {
+        // set-up once per device, with that device current
+        std::lock_guard<std::mutex> lk(g_na_mu);
+        if (!g_na_ptr[dev]) {
+            cudaError_t e = cudaGetSymbolAddress(&g_na_ptr[dev], g_noalloc_scratch);
+            if (e != cudaSuccess) {
+                g_na_ptr[dev] = nullptr;
+                snprintf(g_na_msg, sizeof g_na_msg, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+                return ACUM_ERR_CUDA;
+            }
+        }
+        scratch = g_na_ptr[dev];
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    int hE[kMaxSurfaces];
+    float hv[3];
+    if (cudaMemcpyAsync(hE, E, nSurf * sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(hv, vInf, 3 * sizeof(float), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return bad(ACUM_ERR_CUDA, "findPressureTimeHistory_noalloc: reading E/vInf failed");
+    long long Et = 0;
+    for (int i = 0; i < nSurf; ++i) {
+        if (hE[i] < 0) return bad(ACUM_ERR_INVALID, "findPressureTimeHistory_noalloc: negative element count");
+        Et += hE[i];
+    }
+    if (Et <= 0) return bad(ACUM_ERR_INVALID, "findPressureTimeHistory_noalloc: no elements");
+    const int nW = (nTime + kWin - 1) / kWin;
+    const long long Epad = (Et + 3) / 4 * 4;
+    const size_t rec_bytes = (size_t)Epad * nW * kGroups * kWin * 4 * sizeof(float);
+    const size_t acc_off = (rec_bytes + 255) / 256 * 256;
+    const size_t acc_bytes = (size_t)nObs * nTime * 2 * sizeof(double);
+    if (acc_off + acc_bytes > kNoAllocBytes) {
+        snprintf(g_na_msg, sizeof g_na_msg,
+                 "findPressureTimeHistory_noalloc: needs %zu bytes of scratch (records %zu + sums %zu), the "
+                 "maximum is %zu",
+                 acc_off + acc_bytes, rec_bytes, acc_bytes, kNoAllocBytes);
+        return ACUM_ERR_INVALID;
+    }
+    float* rec = reinterpret_cast<float*>(scratch);
+    double* acc = reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(scratch) + acc_off);
+    // the array keeps the previous call's contents: clear the record padding and the sums
+    if (cudaMemsetAsync(rec, 0, rec_bytes, st) != cudaSuccess || cudaMemsetAsync(acc, 0, acc_bytes, st) != cudaSuccess)
+        return bad(ACUM_ERR_CUDA, "findPressureTimeHistory_noalloc: clearing scratch failed");
+    const long long n = Et * nTime;
+    noalloc_records_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(Xham, Nham, Vham, PRham, E, XPtr, NPtr, VPtr,
+                                                                   PRPtr, nSurf, (int)Et, nTime, nW, a0, rhoRef,
+                                                                   rec);
+    int sms = 0, optin = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    TonalRun r;
+    memset(&r, 0, sizeof(r));
+    r.g.E = (int)Et;
+    r.g.Epad = (int)Epad;
+    r.g.T = nTime;
+    r.g.nW = nW;
+    r.g.O = nObs;
+    r.g.a0 = a0;
+    r.g.rho = rhoRef;
+    r.g.oM = oM;
+    r.g.dPsi = dPsi;
+    r.g.dTau = dTau;
+    r.g.lpi = nTime * (double)dPsi;
+    for (int q = 0; q < 3; ++q) r.g.vinf[q] = hv[q];
+    r.precision = ACUM_MIXED;
+    if (plan_tonal(r, 0, 0, 0, sms, (size_t)optin) != cudaSuccess)
+        return bad(ACUM_ERR_UNSUPPORTED, "findPressureTimeHistory_noalloc: no tile shape fits this nTime");
+    r.rec = rec;
+    r.obs32 = rObs;
+    r.obs64 = nullptr;
+    r.acc = acc;
+    // the device error word lives in the scratch too (after the sums), cleared per call
+    const size_t err_off = (acc_off + acc_bytes + 255) / 256 * 256;
+    if (err_off + sizeof(DeviceErr) > kNoAllocBytes)
+        return bad(ACUM_ERR_INVALID, "findPressureTimeHistory_noalloc: no room for the error word");
+    r.err = reinterpret_cast<DeviceErr*>(reinterpret_cast<unsigned char*>(scratch) + err_off);
+    if (cudaMemsetAsync(r.err, 0, sizeof(DeviceErr), st) != cudaSuccess)
+        return bad(ACUM_ERR_CUDA, "findPressureTimeHistory_noalloc: clearing scratch failed");
+    if (launch_tonal(r, st) != cudaSuccess || launch_finalize(acc, nObs, nTime, pT, pL, pA, 2, st) != cudaSuccess)
+        return bad(ACUM_ERR_CUDA, "findPressureTimeHistory_noalloc: launch failed");
+    DeviceErr h;
+    if (cudaMemcpyAsync(&h, r.err, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return bad(ACUM_ERR_CUDA, "findPressureTimeHistory_noalloc: kernel failed");
+    if (h.bits & ACUM_DEVERR_TIMEOUT) return bad(ACUM_ERR_TIMEOUT, "a bounded shared-memory pipeline wait ran out");
+    return ACUM_OK;
+}

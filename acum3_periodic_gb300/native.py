@@ -86,6 +86,10 @@ SIGNATURES = {
     "acum_find_pressure_time_history_f64": (C.c_int, [C.c_void_p] * 9 + [C.c_int] + [C.c_void_p] * 5 +
                                             [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                              C.c_void_p, C.c_double, C.c_void_p]),
+    "acum_find_pressure_time_history_noalloc": (C.c_int, [C.c_void_p] * 9 + [C.c_int] + [C.c_void_p] * 5 +
+                                                [C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float,
+                                                 C.c_void_p, C.c_float, C.c_void_p]),
+    "acum_noalloc_last_error": (C.c_char_p, []),
     "acum_preprocess_imper": (C.c_int, [C.c_void_p] * 4 + [C.c_int] + [C.c_void_p] * 5 +
                               [C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int]),
     "acum_find_bb_noise": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_float] + [C.c_void_p] * 26 +

@@ -195,6 +195,25 @@ int acum_find_pressure_time_history_f64(const double* rObs, const double* tObs, 
                                         double dPsi, double dTau, double a0, double rhoRef, const double* vInf,
                                         double oM, void* stream);
 
+/* The same call as acum_find_pressure_time_history for callers that cannot allocate
+ * memory (no counterpart in the reference): code running where cudaMalloc/cudaFree are
+ * not allowed or would synchronise work that must not be split, or a solver whose device
+ * memory is all in its own pool.  It allocates nothing -- no cudaMalloc, no host heap --
+ * and uses a fixed 128 MiB scratch array in device memory that every GPU loading this
+ * library holds until exit.  Limit: records (80 B per element-step, elements rounded up to
+ * 4 and steps to 32) plus 16 B per observer-step must fit in 128 MiB, else ACUM_ERR_INVALID
+ * (acum_noalloc_last_error() gives the sizes); at most 256 surfaces.  The first call on a
+ * device looks up the scratch address (with that device current), so make it before any
+ * stream capture.  All calls share the scratch: calls whose GPU work overlaps race, so
+ * serialise them.  tObs is not read (the grid is t*dPsi, as main.cu:248 builds it). */
+int acum_find_pressure_time_history_noalloc(const float* rObs, const float* tObs, float* pT, float* pL, float* pA,
+                                            const float* Xham, const float* Nham, const float* Vham,
+                                            const float* PRham, int nSurf, const int* XPtr, const int* NPtr,
+                                            const int* VPtr, const int* PRPtr, const int* E, int nObs, int nTime,
+                                            float dPsi, float dTau, float a0, float rhoRef, const float* vInf,
+                                            float oM, void* stream);
+const char* acum_noalloc_last_error(void);
+
 /* Replaces preprocess_imper (preprocess.cu:228) on caller arrays: host AoS Xham [etot*
  * nTime*4], Nham [*6], Vham [*6], PRham [*2] laid out with the reference's XPtr/NPtr/
  * VPtr/PRPtr offsets (E[] counts, host); updated in place with the same meaning. */
