@@ -1,0 +1,519 @@
+// adjoint.cu -- hand-written adjoint of the tonal path.
+//
+// Objective J = sum_obs mean_bins pA^2 (or any J given by dJ/dpA).  Its gradient with
+// respect to the surface rows (Cp, positions, normals per element and step) is formed in
+// three steps:
+//
+//  1. forward: the tonal kernels give pA; g[obs][bin] = dJ/dpA (= 2 pA / T).
+//  2. adjoint_kernel: one warp per (element, window of 32 lanes), looping over every
+//     observer.  Lane l holds the sample of unwrapped step tau = 30 w - 1 + l, so each
+//     sample at lanes 1..30 has both of its interpolation intervals inside the window
+//     (windows overlap by two lanes and need no carried state; the periodic wrap comes
+//     from the unwrapped tau).  Per observer the lane recomputes the forward integrand and
+//     observer time of its sample (nothing is stored from the forward), gathers g at the
+//     <= 2 bins of its interval (t(tau-1), t(tau)], forms the interval's contributions to
+//     dJ/dp and dJ/dt of both end samples (the hat weights and their derivatives), takes
+//     its right neighbour's half through one shuffle, and runs the reverse of the
+//     integrand by hand.  The 19 cotangents of its step's record fields accumulate in
+//     registers over all observers and are written once: no atomics.
+//  3. adjoint_chain_kernel: one block per element, FP64: record cotangents -> cotangents of
+//     x, ds, n, ndot, V, Vdot, P, Pdot -> through the transposes of the periodic central
+//     differences (V = Dx, Vdot = D^2 x, ndot = Dn, Pdot = DP), of make_periodic and of the
+//     scalings -> dJ/dCp, dJ/dx, dJ/dn in file coordinates.
+//
+// Records as the forward builds them (tonal.cu):
+//   g0 = x, y, z, dsD   g1 = M(3), M2   g2 = Md(3), ATD   g3 = L(3), Lm   g4 = Ld(3), 0
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "acum_internal.h"
+#include "ctx.h"
+
+namespace acum {
+
+constexpr int kAdjStride = 30;  // new samples per window
+constexpr int kCot = 19;        // record-field cotangents per element-step
+
+struct AdjDev {
+    const void* rec;  // forward record tiles [Epad][nW][5][32][4]
+    int E, nW, T, O, nWa;
+    const void* obs;  // [O][3]
+    const void* g;    // [O][T]
+    double a0, alpha, ialpha, vx, vy, vz, dTau, oM, dPsi, kb;
+    double* cot;      // [E][T][19] FP64
+};
+
+template <typename R>
+struct V3 {
+    R x, y, z;
+};
+
+// forward integrand with the intermediates the reverse pass needs
+template <typename R>
+struct Fwd {
+    R dx, dy, dz, c, beta, s, tr, rx, ry, rz, ir, Mr, Mdr, Lr, Ldr, G, qa, K, base, Y, pt, pl, t;
+};
+
+template <typename R>
+__device__ __forceinline__ void load_rec(const R* rec, int nW, int e, int step, R* f)
+{
+    const R* tile = rec + ((size_t)e * nW + step / kWin) * (kGroups * kWin * 4);
+    const int lane = step % kWin;
+#pragma unroll
+    for (int q = 0; q < kGroups; ++q)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) f[4 * q + c] = tile[((size_t)q * kWin + lane) * 4 + c];
+}
+
+template <typename R>
+__device__ __forceinline__ Fwd<R> forward(const R* f, R ox, R oy, R oz, const AdjDev& p, int tau)
+{
+    Fwd<R> a;
+    const R vx = (R)p.vx, vy = (R)p.vy, vz = (R)p.vz, a0 = (R)p.a0;
+    a.dx = ox - f[0];
+    a.dy = oy - f[1];
+    a.dz = oz - f[2];
+    a.c = a.dx * a.dx + a.dy * a.dy + a.dz * a.dz;
+    a.beta = a.dx * vx + a.dy * vy + a.dz * vz;
+    a.s = sqrt(a.beta * a.beta + (R)p.alpha * a.c);
+    a.tr = (a.s - a.beta) * (R)p.ialpha;
+    a.rx = a.dx - vx * a.tr;
+    a.ry = a.dy - vy * a.tr;
+    a.rz = a.dz - vz * a.tr;
+    const R r = a0 * a.tr;
+    a.ir = (R)1 / r;
+    a.Mr = (f[4] * a.rx + f[5] * a.ry + f[6] * a.rz) * a.ir;
+    a.Mdr = (f[8] * a.rx + f[9] * a.ry + f[10] * a.rz) * a.ir;
+    a.Lr = (f[12] * a.rx + f[13] * a.ry + f[14] * a.rz) * a.ir;
+    a.Ldr = (f[16] * a.rx + f[17] * a.ry + f[18] * a.rz) * a.ir;
+    a.G = (R)1 / ((R)1 - a.Mr);
+    a.qa = a0 * a.ir;
+    a.K = a.Mdr + a.qa * (a.Mr - f[7]);
+    a.base = a.ir * a.G * a.G;
+    a.Y = a.Ldr + a.qa * (a.Lr - f[15]) + a.Lr * a.G * a.K;
+    a.pt = f[11] * a.base * a.G * a.K;
+    a.pl = f[3] * a.base * a.Y;
+    // observer time [rad] as core.cu:156 forms it
+    a.t = ((R)tau * (R)p.dTau + a.tr) * (R)p.oM;
+    return a;
+}
+
+// reverse of `forward` for dJ/dp (p = pT + pL) = pb and dJ/dt = tb; adds the record
+// cotangents into acc[19] (order of the record fields)
+template <typename R>
+__device__ __forceinline__ void reverse(const R* f, const Fwd<R>& a, R pb, R tb, const AdjDev& p, R* acc)
+{
+    const R a0 = (R)p.a0, vx = (R)p.vx, vy = (R)p.vy, vz = (R)p.vz;
+    // pt = ATD * base * G * K
+    R baseb = pb * f[11] * a.G * a.K;
+    R Gb = pb * f[11] * a.base * a.K;
+    R Kb = pb * f[11] * a.base * a.G;
+    acc[11] += pb * a.base * a.G * a.K;
+    // pl = dsD * base * Y,  Y = Ldr + qa (Lr - Lm) + Lr G K
+    acc[3] += pb * a.base * a.Y;
+    baseb += pb * f[3] * a.Y;
+    const R Yb = pb * f[3] * a.base;
+    R Ldrb = Yb;
+    R qab = Yb * (a.Lr - f[15]);
+    R Lrb = Yb * (a.qa + a.G * a.K);
+    acc[15] -= Yb * a.qa;
+    Gb += Yb * a.Lr * a.K;
+    Kb += Yb * a.Lr * a.G;
+    // base = ir G^2
+    R irb = baseb * a.G * a.G;
+    Gb += baseb * (R)2 * a.ir * a.G;
+    // K = Mdr + qa (Mr - M2)
+    R Mdrb = Kb;
+    qab += Kb * (a.Mr - f[7]);
+    R Mrb = Kb * a.qa;
+    acc[7] -= Kb * a.qa;
+    // qa = a0 ir
+    irb += qab * a0;
+    // G = 1/(1 - Mr)
+    Mrb += Gb * a.G * a.G;
+    // the four projections X.r_hat = (X . rv) ir
+    R rvx = 0, rvy = 0, rvz = 0;
+    auto proj = [&](int i0, R sb, R val) {
+        acc[i0] += sb * a.ir * a.rx;
+        acc[i0 + 1] += sb * a.ir * a.ry;
+        acc[i0 + 2] += sb * a.ir * a.rz;
+        rvx += sb * a.ir * f[i0];
+        rvy += sb * a.ir * f[i0 + 1];
+        rvz += sb * a.ir * f[i0 + 2];
+        irb += sb * val / a.ir;  // (X . rv) = val / ir
+    };
+    proj(4, Mrb, a.Mr);
+    proj(8, Mdrb, a.Mdr);
+    proj(12, Lrb, a.Lr);
+    proj(16, Ldrb, a.Ldr);
+    // ir = 1 / (a0 tr), t = (tau dTau + tr) oM
+    R trb = -irb * a.ir * a.ir * a0 + tb * (R)p.oM;
+    // rv = d - v tr
+    R dxb = rvx, dyb = rvy, dzb = rvz;
+    trb -= rvx * vx + rvy * vy + rvz * vz;
+    // tr = (s - beta) / alpha,  s = sqrt(beta^2 + alpha c)
+    const R sb = trb * (R)p.ialpha;
+    R betab = -trb * (R)p.ialpha;
+    const R q2b = sb / ((R)2 * a.s);
+    betab += q2b * (R)2 * a.beta;
+    const R cb = q2b * (R)p.alpha;
+    dxb += betab * vx + cb * (R)2 * a.dx;
+    dyb += betab * vy + cb * (R)2 * a.dy;
+    dzb += betab * vz + cb * (R)2 * a.dz;
+    // d = obs - x
+    acc[0] -= dxb;
+    acc[1] -= dyb;
+    acc[2] -= dzb;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128) adjoint_kernel(AdjDev p)
+{
+    const int warp_g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp_g >= p.E * p.nWa) return;  // warp-uniform
+    const int e = warp_g / p.nWa, w = warp_g % p.nWa;
+    const int tau = kAdjStride * w - 1 + lane;  // unwrapped step of this lane's sample
+    const int step = ((tau % p.T) + p.T) % p.T;
+    const bool owner = lane >= 1 && lane <= kAdjStride && tau >= 0 && tau < p.T;
+    R f[20];
+    load_rec<R>(reinterpret_cast<const R*>(p.rec), p.nW, e, step, f);
+    R acc[kCot];
+#pragma unroll
+    for (int k = 0; k < kCot; ++k) acc[k] = 0;
+    const R* obs = reinterpret_cast<const R*>(p.obs);
+    const R* gg = reinterpret_cast<const R*>(p.g);
+    const R dPsi = (R)p.dPsi;
+    for (int o = 0; o < p.O; ++o) {
+        const Fwd<R> a = forward<R>(f, obs[3 * o], obs[3 * o + 1], obs[3 * o + 2], p, tau);
+        const R pc = a.pt + a.pl;
+        const R tp = __shfl_up_sync(0xffffffffu, a.t, 1);
+        const R pp = __shfl_up_sync(0xffffffffu, pc, 1);
+        // interval (t(tau-1), t(tau)] of this lane: bins n with tp < n dPsi <= t
+        R rp = 0, lp = 0, rt = 0, lt = 0;
+        if (lane >= 1 && a.t > tp) {
+            const int n0 = (int)floor(tp / dPsi) + 1, n1 = (int)floor(a.t / dPsi);
+            const R inv = (R)1 / (a.t - tp);
+            const R dp = pc - pp;
+            const R* grow = gg + (size_t)o * p.T;
+            for (int n = n0; n <= n1 && n - n0 < 4; ++n) {
+                const R g = grow[((n % p.T) + p.T) % p.T];
+                const R wgt = ((R)n * dPsi - tp) * inv;
+                rp += g * wgt;
+                lp += g * ((R)1 - wgt);
+                // d value / d t(tau) = -dp w / dt,  d value / d t(tau-1) = -dp (1 - w) / dt
+                rt -= g * dp * wgt * inv;
+                lt -= g * dp * ((R)1 - wgt) * inv;
+            }
+        }
+        const R pb = rp + __shfl_down_sync(0xffffffffu, lp, 1);
+        const R tb = rt + __shfl_down_sync(0xffffffffu, lt, 1);
+        if (owner) reverse<R>(f, a, pb, tb, p, acc);
+    }
+    if (owner) {
+        double* out = p.cot + ((size_t)e * p.T + step) * kCot;
+#pragma unroll
+        for (int k = 0; k < kCot; ++k) out[k] = (double)acc[k];
+    }
+}
+
+// g[o][n] = 2 (pT + pL) / T from the forward sums [o][n][2], and J's terms
+__global__ void adj_seed_kernel(const double* __restrict__ acc, int O, int T, double* __restrict__ g64,
+                                float* __restrict__ g32, double* __restrict__ jrow)
+{
+    const int o = blockIdx.x;
+    double s = 0.0;
+    for (int n = threadIdx.x; n < T; n += blockDim.x) {
+        const double pa = acc[((size_t)o * T + n) * 2] + acc[((size_t)o * T + n) * 2 + 1];
+        s += pa * pa;
+        const double g = 2.0 * pa / T;
+        if (g64) g64[(size_t)o * T + n] = g;
+        if (g32) g32[(size_t)o * T + n] = (float)g;
+    }
+    __shared__ double red[256];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+        if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) jrow[o] = red[0] / T;
+}
+
+// Record cotangents -> file-level gradients, one block per element, FP64.
+struct ChainDev {
+    const double* cot;     // [E][T][19]
+    const double* fields;  // [E][T][18] from the preprocessing
+    int E, T, periodic;
+    double a0, rho, pscale, cfd, dTau;
+    double* gcp;  // [E][T]
+    double* gx;   // [E][T][3]
+    double* gn;   // [E][T][3]
+};
+
+__global__ void __launch_bounds__(256) adjoint_chain_kernel(ChainDev c)
+{
+    extern __shared__ double sm[];
+    const int T = c.T;
+    // per element series of field cotangents: V(3), Vd(3), nd(3), P, Pd
+    double* bV = sm;            // [3][T]
+    double* bVd = bV + 3 * T;   // [3][T]
+    double* bnd = bVd + 3 * T;  // [3][T]
+    double* bP = bnd + 3 * T;   // [T]
+    double* bPd = bP + T;       // [T]
+    double* tmp = bPd + T;      // [3][T]
+    const int e = blockIdx.x;
+    const double D1 = 1.0 / (4.0 * M_PI * c.a0), ia0 = 1.0 / c.a0;
+    const double two_dt = 2.0 * c.dTau;
+    // local chain at each step
+    for (int t = threadIdx.x; t < T; t += blockDim.x) {
+        const double* k = c.cot + ((size_t)e * T + t) * kCot;
+        const double* f = c.fields + ((size_t)e * T + t) * kFields;
+        const double n[3] = {f[4], f[5], f[6]}, nd[3] = {f[7], f[8], f[9]}, V[3] = {f[10], f[11], f[12]};
+        const double ds = f[3], P = f[16], Pd = f[17];
+        const double Vn = V[0] * n[0] + V[1] * n[1] + V[2] * n[2];
+        double gV[3], gVd[3], gN[3], gNd[3], gP = 0.0, gPd = 0.0;
+        for (int i = 0; i < 3; ++i) {
+            // M = V/a0, M2 = |V|^2/a0^2, Md = Vd/a0
+            gV[i] = k[4 + i] * ia0 + k[7] * 2.0 * V[i] * ia0 * ia0;
+            gVd[i] = k[8 + i] * ia0;
+            // ATD = D1 rho (V.n) a0 ds
+            gV[i] += k[11] * D1 * c.rho * c.a0 * ds * n[i];
+            gN[i] = k[11] * D1 * c.rho * c.a0 * ds * V[i];
+            // L = P n, Lm = P (n.V)/a0, Ld = Pd n + P nd
+            gN[i] += k[12 + i] * P + k[15] * P * V[i] * ia0 + k[16 + i] * Pd;
+            gV[i] += k[15] * P * n[i] * ia0;
+            gNd[i] = k[16 + i] * P;
+            gP += k[12 + i] * n[i] + k[16 + i] * nd[i];
+            gPd += k[16 + i] * n[i];
+        }
+        gP += k[15] * Vn * ia0;
+        for (int i = 0; i < 3; ++i) {
+            bV[i * T + t] = gV[i];
+            bVd[i * T + t] = gVd[i];
+            bnd[i * T + t] = gNd[i];
+            // direct position and normal cotangents (positions scaled by CFDscale)
+            c.gx[((size_t)e * T + t) * 3 + i] = k[i] * c.cfd;  // completed below
+            c.gn[((size_t)e * T + t) * 3 + i] = gN[i];
+        }
+        bP[t] = gP;
+        bPd[t] = gPd;
+    }
+    __syncthreads();
+    // transposes of the periodic central difference: D^T v[k] = (v[k-1] - v[k+1]) / (2 dt)
+    auto DT = [&](const double* v, int k) {
+        const int km = k == 0 ? T - 1 : k - 1, kp = k == T - 1 ? 0 : k + 1;
+        return (v[km] - v[kp]) / two_dt;
+    };
+    // Vd = D V: bV += D^T bVd
+    for (int t = threadIdx.x; t < T; t += blockDim.x)
+        for (int i = 0; i < 3; ++i) tmp[i * T + t] = bV[i * T + t] + DT(bVd + i * T, t);
+    __syncthreads();
+    // V = D x, x scaled by CFDscale
+    for (int t = threadIdx.x; t < T; t += blockDim.x)
+        for (int i = 0; i < 3; ++i) c.gx[((size_t)e * T + t) * 3 + i] += DT(tmp + i * T, t) * c.cfd;
+    // nd = D n
+    for (int t = threadIdx.x; t < T; t += blockDim.x)
+        for (int i = 0; i < 3; ++i) c.gn[((size_t)e * T + t) * 3 + i] += DT(bnd + i * T, t);
+    __syncthreads();
+    // Pd = D P (periodic) or the biased form
+    if (c.periodic == 1) {
+        for (int t = threadIdx.x; t < T; t += blockDim.x) tmp[t] = bP[t] + DT(bPd, t);
+    } else {
+        // du[0] = 3 c1 - 3 c2 + c3, du[T-1] = 3 c(T-2) - 3 c(T-3) + c(T-4), interior central
+        // (mathfunc.cu:142-159); transpose through the interior central differences
+        for (int t = threadIdx.x; t < T; t += blockDim.x) {
+            // weight of du[k] (k interior) after folding the two end rows
+            auto w = [&](int k) {
+                double v = bPd[k];
+                if (k == 1) v += 3 * bPd[0];
+                if (k == 2) v += -3 * bPd[0];
+                if (k == 3) v += bPd[0];
+                if (k == T - 2) v += 3 * bPd[T - 1];
+                if (k == T - 3) v += -3 * bPd[T - 1];
+                if (k == T - 4) v += bPd[T - 1];
+                return v;
+            };
+            // u[t] appears in du[t-1] (+1/(2dt)) and du[t+1] (-1/(2dt)) for interior rows
+            double acc = bP[t];
+            if (t - 1 >= 1 && t - 1 <= T - 2) acc += w(t - 1) / two_dt;
+            if (t + 1 >= 1 && t + 1 <= T - 2) acc -= w(t + 1) / two_dt;
+            tmp[t] = acc;
+        }
+    }
+    __syncthreads();
+    // make_periodic (mathfunc.cu:165-206): P'[k] = P[k] - (cubic(k+1) - k2), the cubic
+    // linear in k1 = 2 P0 - P1, k2 = P[T-1], s1 = P1 - P0, s2 = P[T-1] - P[T-2]
+    if (threadIdx.x == 0) {
+        const double xm = T;
+        double sk1 = 0, sk2 = 0, ss1 = 0, ss2 = 0;
+        for (int k = 0; k < T; ++k) {
+            const double i = k + 1, b = tmp[k];
+            // cubic = aa i^3 + bb i^2 + cc i + dd with
+            // dd = k1, cc = s1 - s2, bb = -2(s1-s2)/xm - 3(k1-k2)/xm^2,
+            // aa = -bb/xm - (s1-s2)/xm^2 - (k1-k2)/xm^3; P' = P - cubic + k2
+            const double dbb_ds = -2.0 / xm, dbb_dk = -3.0 / (xm * xm);
+            const double daa_ds = -dbb_ds / xm - 1.0 / (xm * xm), daa_dk = -dbb_dk / xm - 1.0 / (xm * xm * xm);
+            const double dc_ds = daa_ds * i * i * i + dbb_ds * i * i + i;  // d cubic / d(s1-s2)
+            const double dc_dk = daa_dk * i * i * i + dbb_dk * i * i;      // d cubic / d(k1-k2), besides dd
+            // P' = P - cubic + k2: d/dk1 = -(dc_dk + 1), d/dk2 = dc_dk + 1, d/ds1 = -dc_ds, d/ds2 = dc_ds
+            sk1 += b * (-(dc_dk + 1.0));
+            sk2 += b * (dc_dk + 1.0);
+            ss1 += b * (-dc_ds);
+            ss2 += b * dc_ds;
+        }
+        // k1 = 2 P0 - P1, s1 = P1 - P0, k2 = P[T-1], s2 = P[T-1] - P[T-2]
+        tmp[0] += 2.0 * sk1 - ss1;
+        tmp[1] += -sk1 + ss1;
+        tmp[T - 1] += sk2 + ss2;
+        tmp[T - 2] += -ss2;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < T; t += blockDim.x) c.gcp[(size_t)e * T + t] = tmp[t] * c.pscale;
+}
+
+struct AdjState {
+    DBuf<double> cot, g64, jrow, gcp, gx, gn;
+    DBuf<float> g32;
+    DBuf<double> obs64;
+};
+
+static AdjState* adj_state(acum_ctx* c)
+{
+    if (!c->adj_state) c->adj_state = new AdjState();
+    return reinterpret_cast<AdjState*>(c->adj_state);
+}
+
+void release_adj_state(acum_ctx* c)
+{
+    if (!c->adj_state) return;
+    AdjState* s = adj_state(c);
+    s->cot.release(); s->g64.release(); s->jrow.release(); s->gcp.release(); s->gx.release(); s->gn.release();
+    s->g32.release(); s->obs64.release();
+    delete s;
+    c->adj_state = nullptr;
+}
+
+}  // namespace acum
+
+using namespace acum;
+
+#define CKA(call)                                              \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+extern "C" int acum_tonal_adjoint(acum_ctx* ctx, int precision, const double* dJ_dpA, double* J, double* g_cp,
+                                  double* g_x, double* g_n)
+{
+    if (!ctx) return ACUM_ERR_INVALID;
+    if (!ctx->have_deck) return fail(ctx, ACUM_ERR_STATE, "no deck");
+    if (precision != ACUM_PLAIN_FP64 && precision != ACUM_MIXED) return fail(ctx, ACUM_ERR_INVALID, "precision");
+    if (ctx->in.lowpass == 1)
+        return fail(ctx, ACUM_ERR_UNSUPPORTED, "the adjoint is built for lowpass = 0 (no median filter transpose)");
+    DeviceGuard gd(ctx->device);
+    AdjState* s = adj_state(ctx);
+    const int T = ctx->T, O = ctx->nobs;
+    const long long E = ctx->E;
+    const bool f64 = precision == ACUM_PLAIN_FP64;
+    ctx->begin_run();
+    // forward (both record layouts are built; the FP64 fields feed the chain kernel)
+    int rc = ctx->ensure_prep(f64, !f64, true);
+    if (rc) return rc;
+    const size_t n = (size_t)T * O;
+    CKA(ctx->d_out.ensure(3 * n));
+    rc = ctx->run_tonal(precision, ctx->d_out.p, ctx->d_out.p + n, ctx->d_out.p + 2 * n);
+    if (rc) return rc;
+    cudaStream_t st = ctx->stream;
+    CKA(s->jrow.ensure(O));
+    CKA(s->g64.ensure(n));
+    CKA(s->g32.ensure(n));
+    adj_seed_kernel<<<O, 256, 0, st>>>(ctx->d_acc.p, O, T, s->g64.p, s->g32.p, s->jrow.p);
+    if (dJ_dpA) {
+        // caller's cotangent [T][O] -> [O][T]
+        std::vector<double> gt(n);
+        for (int t = 0; t < T; ++t)
+            for (int o = 0; o < O; ++o) gt[(size_t)o * T + t] = dJ_dpA[(size_t)t * O + o];
+        std::vector<float> g32(n);
+        for (size_t i = 0; i < n; ++i) g32[i] = (float)gt[i];
+        CKA(cudaMemcpyAsync(s->g64.p, gt.data(), n * 8, cudaMemcpyHostToDevice, st));
+        CKA(cudaMemcpyAsync(s->g32.p, g32.data(), n * 4, cudaMemcpyHostToDevice, st));
+        CKA(cudaStreamSynchronize(st));
+    }
+    AdjDev p;
+    memset(&p, 0, sizeof(p));
+    p.E = (int)E;
+    p.nW = ctx->nW;
+    p.T = T;
+    p.O = O;
+    p.nWa = (T + kAdjStride - 1) / kAdjStride;
+    p.a0 = ctx->in.a0;
+    p.vx = ctx->der.vinf[0];
+    p.vy = ctx->der.vinf[1];
+    p.vz = ctx->der.vinf[2];
+    p.alpha = p.a0 * p.a0 - (p.vx * p.vx + p.vy * p.vy + p.vz * p.vz);
+    p.ialpha = 1.0 / p.alpha;
+    p.dTau = ctx->der.dTau;
+    p.oM = ctx->der.oM;
+    p.dPsi = ctx->der.dPsi;
+    CKA(s->cot.ensure((size_t)E * T * kCot));
+    p.cot = s->cot.p;
+    const long long warps = E * p.nWa;
+    const int blocks = (int)((warps * 32 + 127) / 128);
+    CKA(cudaEventRecord(ctx->ev[EV_ADJ0], st));
+    if (f64) {
+        p.rec = ctx->d_rec64.p;
+        p.obs = ctx->d_obs64.p;
+        p.g = s->g64.p;
+        adjoint_kernel<double><<<blocks, 128, 0, st>>>(p);
+    } else {
+        p.rec = ctx->d_rec32.p;
+        p.obs = ctx->d_obs32.p;
+        p.g = s->g32.p;
+        adjoint_kernel<float><<<blocks, 128, 0, st>>>(p);
+    }
+    CKA(cudaEventRecord(ctx->ev[EV_ADJ1], st));
+    CKA(cudaGetLastError());
+    ChainDev c;
+    c.cot = s->cot.p;
+    c.fields = ctx->d_fields.p;
+    c.E = (int)E;
+    c.T = T;
+    c.periodic = ctx->in.periodic;
+    c.a0 = ctx->in.a0;
+    c.rho = ctx->in.rhoRef;
+    c.pscale = 0.5 * ctx->in.rhoRef * (ctx->in.Mref * ctx->in.Mref) * (ctx->in.a0 * ctx->in.a0);
+    c.cfd = ctx->in.CFDscale;
+    c.dTau = ctx->der.dTau;
+    CKA(s->gcp.ensure((size_t)E * T));
+    CKA(s->gx.ensure((size_t)E * T * 3));
+    CKA(s->gn.ensure((size_t)E * T * 3));
+    c.gcp = s->gcp.p;
+    c.gx = s->gx.p;
+    c.gn = s->gn.p;
+    const size_t smem = (size_t)T * 14 * sizeof(double);
+    if (smem > 48 * 1024) CKA(cudaFuncSetAttribute(adjoint_chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)smem));
+    adjoint_chain_kernel<<<(int)E, 256, smem, st>>>(c);
+    CKA(cudaGetLastError());
+    ctx->launches += 3;
+    ctx->adj_timed = true;
+    std::vector<double> jr(O);
+    CKA(cudaMemcpyAsync(jr.data(), s->jrow.p, O * 8, cudaMemcpyDeviceToHost, st));
+    if (g_cp) CKA(cudaMemcpyAsync(g_cp, s->gcp.p, (size_t)E * T * 8, cudaMemcpyDeviceToHost, st));
+    if (g_x) CKA(cudaMemcpyAsync(g_x, s->gx.p, (size_t)E * T * 24, cudaMemcpyDeviceToHost, st));
+    if (g_n) CKA(cudaMemcpyAsync(g_n, s->gn.p, (size_t)E * T * 24, cudaMemcpyDeviceToHost, st));
+    rc = ctx->finish_run();
+    if (rc) return rc;
+    if (J) {
+        double j = 0;
+        for (int o = 0; o < O; ++o) j += jr[o];
+        *J = j;
+    }
+    return ACUM_OK;
+}

@@ -3,15 +3,10 @@
 #include "ctx.h"
 
 namespace acum {
-void release_adj_state(acum_ctx*) {}
 }  // namespace acum
 
 using namespace acum;
 
-extern "C" int acum_tonal_adjoint(acum_ctx* ctx, int, const double*, double*, double*, double*, double*)
-{
-    return fail(ctx, ACUM_ERR_UNSUPPORTED, "not built yet");
-}
 extern "C" int acum_batch_create(acum_batch**, int) { return fail(nullptr, ACUM_ERR_UNSUPPORTED, "not built yet"); }
 extern "C" int acum_batch_destroy(acum_batch*) { return ACUM_OK; }
 extern "C" const char* acum_batch_last_error(const acum_batch*) { return "not built yet"; }

@@ -85,7 +85,9 @@ class TonalInputs:
     def __init__(self, deck):
         d = deck.derived()
         self.nelem = np.array(deck.elements, dtype=np.int32)
-        self.raw = deck.raw_surfaces().astype(np.float64)
+        # widened without a float32 round trip, so float64 rows (finite-difference
+        # perturbations) keep their precision
+        self.raw = np.concatenate([np.asarray(x, dtype=np.float64).reshape(-1) for x in deck.surfaces])
         self.obs = deck.observers().astype(np.float64).reshape(-1)
         s = _Tonal()
         s.nsurf, s.ntime, s.nobs = deck.nSurf, deck.nTime, deck.nObs

@@ -1,0 +1,147 @@
+"""Hand-written adjoint of the tonal path (acum_tonal_adjoint) on workload 3 (2 blades x
+2400 panels, 360 steps, 256 observers on a 10R sphere, tip Mach 0.6, Minf 0.05).
+
+Objective J = sum_obs mean_bins pA^2.  Checks: the FP64 adjoint against central finite
+differences in FP64 with relative step 1e-6 at 64 seeded coordinates (Cp, positions,
+normals), tolerance 1e-5 relative; the FP32 adjoint against the FP64 one; J itself; and a
+torch.autograd.Function built on the ABI (only here, in the test harness).
+
+Finite differences are formed element-locally: perturbing one coordinate changes only
+that element's contribution c to pA, so J(+h) - J(-h) = sum (c+ - c-)(2 pA_rest + c+ + c-)/T
+exactly, with c+/- from the FP64 oracle on a one-element deck -- the two full sums never
+have to be subtracted."""
+import numpy as np
+import pytest
+
+from acum3_periodic_gb300 import synth
+from acum3_periodic_gb300.deck import Deck
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+FD_REL_TOL = 1e-5
+REL_STEP = 1e-6
+
+
+def one_element_deck(d, e):
+    """The deck restricted to global element e (same settings and observers)."""
+    s = 0
+    while e >= d.surfaces[s].shape[1]:
+        e -= d.surfaces[s].shape[1]
+        s += 1
+    sub = Deck(**{k: getattr(d, k) for k in d.__dataclass_fields__})
+    sub.surfaces = [np.ascontiguousarray(d.surfaces[s][:, e:e + 1, :])]
+    sub.BB_noise = 0
+    sub.bb = []
+    return sub, s, e
+
+
+def element_pA(d1):
+    _, _, pA, bad = O.tonal(d1, nthreads=8)
+    return pA
+
+
+@pytest.fixture(scope="module")
+def workload3():
+    from acum3_periodic_gb300 import native
+    d = synth.config_deck(3)
+    ctx = native.Context(0)
+    ctx.set_deck(d, bb=False)
+    _, _, pA = ctx.tonal(native.PLAIN_FP64)
+    J, gcp, gx, gn = ctx.adjoint(native.PLAIN_FP64)
+    yield d, ctx, pA, (J, gcp, gx, gn)
+    ctx.close()
+
+
+def test_objective(workload3):
+    d, ctx, pA, (J, gcp, gx, gn) = workload3
+    np.testing.assert_allclose(J, np.sum(np.mean(pA ** 2, axis=0)), rtol=1e-12)
+
+
+def test_fp64_adjoint_against_finite_differences(workload3):
+    d, ctx, pA, (J, gcp, gx, gn) = workload3
+    T = d.nTime
+    u = synth.uniform(3003, 1, 64 * 4).reshape(64, 4)
+    errs = []
+    for k in range(64):
+        e = int(u[k, 0] * d.E)
+        t = int(u[k, 1] * T)
+        kind = int(u[k, 2] * 3)           # 0 Cp, 1 position, 2 normal
+        comp = int(u[k, 3] * 3)
+        d1, s, el = one_element_deck(d, e)
+        col = 3 if kind == 0 else (comp if kind == 1 else 5 + comp)
+        v0 = float(d1.surfaces[0][t, 0, col])
+        h = REL_STEP * max(abs(v0), 1e-2)
+        base = element_pA(d1)
+        rest = pA - base
+        cs = []
+        for sign in (+1, -1):
+            d2, _, _ = one_element_deck(d, e)
+            arr = d2.surfaces[0].astype(np.float64)
+            arr[t, 0, col] = v0 + sign * h
+            # keep float64 precision of the perturbed value in the oracle inputs
+            d2.surfaces = [arr]
+            cs.append(element_pA(d2))
+        cp_, cm_ = cs
+        fd = np.sum((cp_ - cm_) * (2 * rest + cp_ + cm_)) / T / (2 * h)
+        adj = gcp[e, t] if kind == 0 else (gx[e, t, comp] if kind == 1 else gn[e, t, comp])
+        errs.append((abs(adj - fd) / max(abs(fd), 1e-30), kind, adj, fd))
+    worst = max(errs, key=lambda x: x[0])
+    assert worst[0] < FD_REL_TOL, worst
+
+
+def test_fp32_adjoint_against_fp64(workload3):
+    from acum3_periodic_gb300 import native
+    d, ctx, pA, (J, gcp, gx, gn) = workload3
+    J32, g32, x32, n32 = ctx.adjoint(native.MIXED)
+    assert abs(J32 - J) / J < 1e-5
+    for a, b in ((g32, gcp), (x32, gx), (n32, gn)):
+        rel = np.linalg.norm(a - b) / np.linalg.norm(b)
+        assert rel < 1e-3, rel
+
+
+def test_adjoint_cost_ratio(workload3):
+    from acum3_periodic_gb300 import native
+    d, ctx, pA, _ = workload3
+    ctx.tonal(native.PLAIN_FP64)
+    fwd_ms = ctx.timing(0)[0]
+    ctx.adjoint(native.PLAIN_FP64)
+    adj_ms = ctx.timing(4)[0]
+    assert adj_ms > 0 and fwd_ms > 0
+    # recorded for the measurement report; the bound below only guards regressions
+    assert adj_ms / fwd_ms < 20
+
+
+def test_autograd_function_wrapper(workload3):
+    """dJ/dCp through a torch.autograd.Function whose backward calls acum_tonal_adjoint
+    with the incoming dJ/dpA (harness only; the library itself has no torch types)."""
+    torch = pytest.importorskip("torch")
+    from acum3_periodic_gb300 import native
+    d, ctx, pA, (J, gcp, gx, gn) = workload3
+    E, T = d.E, d.nTime
+
+    class TonalCp(torch.autograd.Function):
+        @staticmethod
+        def forward(fctx, cp):
+            c = cp.detach().cpu().numpy()
+            a = 0
+            for s_ in d.surfaces:
+                b = a + s_.shape[1]
+                s_[:, :, 3] = c[a:b].T.astype(np.float32)
+                a = b
+            ctx.set_deck(d, bb=False)
+            _, _, p = ctx.tonal(native.PLAIN_FP64)
+            return torch.from_numpy(p)
+
+        @staticmethod
+        def backward(fctx, grad_pA):
+            _, g, _, _ = ctx.adjoint(native.PLAIN_FP64, dJ_dpA=grad_pA.numpy())
+            return torch.from_numpy(g)
+
+    cp0 = np.concatenate([s_[:, :, 3].T for s_ in d.surfaces], axis=0).astype(np.float64)  # [E][T]
+    cp = torch.tensor(cp0, requires_grad=True)
+    p = TonalCp.apply(cp)
+    Jt = (p ** 2).mean(dim=0).sum()
+    Jt.backward()
+    np.testing.assert_allclose(float(Jt), J, rtol=1e-12)
+    np.testing.assert_allclose(cp.grad.numpy(), gcp, rtol=1e-9, atol=1e-12 * np.abs(gcp).max())
