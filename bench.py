@@ -16,8 +16,8 @@ the oracle port (the C restatement of the reference path) on this host's cores o
 bounded sample of the same deck.
 
 Reference arm (--impl reference).  The reference's CPU implementation of the path: the
-oracle port in oracle/acum_oracle.c (the reference's own sources cannot be compiled on
-the GPU host: the reference tree is not there), all host threads, on bounded samples of
+oracle port in oracle/acum_oracle.c (the reference's sources are not shipped with this
+package, so its own build cannot be timed where the benchmark runs), all host threads, on bounded samples of
 the same workload; rank 0 only under torchrun.
 
 Multi-GPU: replicas (weak scaling) -- each rank solves the whole workload on its own
@@ -135,10 +135,11 @@ def cpu_baseline(deck, nobs_sample: int, nthreads: int):
     return evals / (t2 - t0), dict(evals=evals, seconds=t2 - t0, preprocess_s=t1 - t0)
 
 
-def adjoint_leg(native, device, with_fd=True, n_fd=16):
+def adjoint_leg(native, device):
     """Workload 3 (2 x 2400 elements, 360 steps, 256 observers): cost of the hand-written
-    adjoint of J = sum_obs mean_bins pA^2 relative to the forward, and its error against
-    element-local central finite differences (FP64, relative step 1e-6)."""
+    adjoint of J = sum_obs mean_bins pA^2 relative to the forward (kernel times by CUDA
+    events on the launching stream), and the FP32 gradient's error against the FP64 one.
+    The finite-difference check of the FP64 gradient lives in the GPU tests."""
     from acum3_periodic_gb300 import synth
     d = synth.config_deck(3)
     ctx = native.Context(device)
@@ -160,37 +161,6 @@ def adjoint_leg(native, device, with_fd=True, n_fd=16):
         else:
             res[name]["grad_rel_err_vs_fp64"] = float(max(np.linalg.norm(x - y) / np.linalg.norm(y)
                                                           for x, y in zip((gcp, gx, gn), g64[1:])))
-    if with_fd:
-        from oracle import oracle as O
-        from acum3_periodic_gb300.deck import Deck
-        _, _, pA = ctx.tonal(native.PLAIN_FP64)
-        J, gcp, gx, gn = g64
-        u = synth.uniform(3003, 1, n_fd * 4).reshape(n_fd, 4)
-        worst = 0.0
-        for k in range(n_fd):
-            e, t = int(u[k, 0] * d.E), int(u[k, 1] * d.nTime)
-            kind, comp = int(u[k, 2] * 3), int(u[k, 3] * 3)
-            s, el = 0, e
-            while el >= d.surfaces[s].shape[1]:
-                el -= d.surfaces[s].shape[1]
-                s += 1
-            col = 3 if kind == 0 else (comp if kind == 1 else 5 + comp)
-
-            def contrib(val=None):
-                sub = Deck(**{kk: getattr(d, kk) for kk in d.__dataclass_fields__})
-                arr = d.surfaces[s][:, el:el + 1, :].astype(np.float64)
-                if val is not None:
-                    arr[t, 0, col] = val
-                sub.surfaces = [arr]
-                return O.tonal(sub, nthreads=os.cpu_count() or 1)[2]
-
-            v0 = float(d.surfaces[s][t, el, col])
-            h = 1e-6 * max(abs(v0), 1e-2)
-            c0, cp_, cm_ = contrib(), contrib(v0 + h), contrib(v0 - h)
-            fd = np.sum((cp_ - cm_) * (2 * (pA - c0) + cp_ + cm_)) / d.nTime / (2 * h)
-            adj = gcp[e, t] if kind == 0 else (gx[e, t, comp] if kind == 1 else gn[e, t, comp])
-            worst = max(worst, abs(adj - fd) / abs(fd))
-        res["fd_check"] = {"coordinates": n_fd, "max_rel_err": worst, "rel_step": 1e-6}
     ctx.close()
     return res
 
@@ -377,7 +347,7 @@ def main():
                                    "kind": "port", "sample": "%d observers x all sections, steps, bands" % len(bsel)}
         out["bpm"] = bpm
     if not args.no_adjoint:
-        out["adjoint"] = adjoint_leg(native, local, with_fd=not args.no_cpu)
+        out["adjoint"] = adjoint_leg(native, local)
     if rank == 0 and not args.no_cpu:
         nth = os.cpu_count() or 1
         v, info = cpu_baseline(deck, args.cpu_obs, nth)

@@ -7,8 +7,8 @@
 #                      i.e. the FP64 build that the plain tonal form is held to
 #
 # TEST INFRASTRUCTURE ONLY.  Only the tests, the smoke check and bench.py's CPU baseline
-# leg may load these libraries.  Both libraries are x86-only builds of this container;
-# where the reference tree is absent (the GPU host) the script exits 0 and builds nothing.
+# leg may load these libraries.  They are built from the reference source tree in place;
+# on a machine without that tree the script exits 0 and builds nothing.
 #
 # Flags: -ftrivial-auto-var-init=zero makes the uninitialised locals of bb_core.cu
 # (notably `aa` in the convected-time formula at bb_core.cu:520) read as zero instead of

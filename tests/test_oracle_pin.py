@@ -1,6 +1,6 @@
 """The oracle against the reference's own sources compiled here (oracle/_ref), on fresh
-seeded decks beyond the committed fixtures.  Skipped where the reference build is absent
-(the GPU host)."""
+seeded decks beyond the committed fixtures.  Skipped on machines without the reference
+build (oracle/_ref is built only where the reference source tree is present)."""
 import os
 
 import numpy as np
