@@ -155,8 +155,24 @@ class Deck:
         return (self.obs_file.astype(np.float32) * s).astype(np.float32)
 
     def raw_surfaces(self) -> np.ndarray:
-        """All surfaces concatenated surface-major: [sum_i nTime*E_i*8] float32."""
-        return np.concatenate([s.reshape(-1) for s in self.surfaces]).astype(np.float32)
+        """All surfaces concatenated surface-major: [sum_i nTime*E_i*8] float32.  When the
+        surfaces are consecutive float32 views of one buffer (as the synthetic decks are
+        built) that buffer is returned without a copy."""
+        ss = self.surfaces
+        b = ss[0].base if ss and isinstance(ss[0], np.ndarray) else None
+        if (b is not None and b.dtype == np.float32 and b.ndim == 1 and b.flags.c_contiguous
+                and all(s.dtype == np.float32 and s.base is b and s.flags.c_contiguous for s in ss)
+                and sum(s.size for s in ss) == b.size):
+            off = 0
+            ok = True
+            for s in ss:
+                if s.__array_interface__["data"][0] != b.__array_interface__["data"][0] + 4 * off:
+                    ok = False
+                    break
+                off += s.size
+            if ok:
+                return b
+        return np.concatenate([s.reshape(-1) for s in ss]).astype(np.float32)
 
     def subset_observers(self, idx) -> "Deck":
         d = Deck(**{k: getattr(self, k) for k in self.__dataclass_fields__})

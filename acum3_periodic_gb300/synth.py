@@ -32,18 +32,30 @@ _M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
 def _splitmix(x: np.ndarray) -> np.ndarray:
     with np.errstate(over="ignore"):
         z = x + np.uint64(0x9E3779B97F4A7C15)
-        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
-        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
-        return z ^ (z >> np.uint64(31))
+        t = z >> np.uint64(30)
+        z ^= t
+        z *= np.uint64(0xBF58476D1CE4E5B9)
+        np.right_shift(z, np.uint64(27), out=t)
+        z ^= t
+        z *= np.uint64(0x94D049BB133111EB)
+        np.right_shift(z, np.uint64(31), out=t)
+        z ^= t
+        return z
 
 
 def uniform(seed: int, stream: int, n: int) -> np.ndarray:
     """n doubles in (0, 1) from (seed, stream); platform independent."""
     key = _splitmix(np.array([(seed & 0xFFFFFFFF) * 1000003 + stream], dtype=np.uint64))[0]
     with np.errstate(over="ignore"):
-        ctr = np.arange(n, dtype=np.uint64) * np.uint64(0xD1B54A32D192ED03) + key
+        ctr = np.arange(n, dtype=np.uint64)
+        ctr *= np.uint64(0xD1B54A32D192ED03)
+        ctr += key
     z = _splitmix(ctr)
-    return ((z >> np.uint64(11)).astype(np.float64) + 0.5) * (1.0 / 9007199254740992.0)
+    z >>= np.uint64(11)
+    out = z.astype(np.float64)
+    out += 0.5
+    out *= 1.0 / 9007199254740992.0
+    return out
 
 
 def normal(seed: int, stream: int, n: int) -> np.ndarray:
@@ -144,20 +156,28 @@ def rotor_surfaces(spec: RotorSpec, seed: int) -> List[np.ndarray]:
     if spec.cp_local_q:
         cp0 = cp0 * rr ** 2
     psi_t = np.deg2rad(f32(spec.dpsi_deg)) * np.arange(T)
+    # all blades in one buffer (surface-major, the layout the library takes), so the
+    # concatenated rows need no second copy
+    raw = np.empty(spec.blades * T * E * 8, dtype=np.float32)
+    tmpl = np.zeros((E, 8), np.float32)
+    tmpl[:, 2] = cen[:, 2]
+    tmpl[:, 4] = area
+    tmpl[:, 7] = nrm[:, 2]
+    rot = np.stack([cen[:, 0], cen[:, 1], nrm[:, 0], nrm[:, 1]], 0)
     out = []
     for b in range(spec.blades):
         psi = psi_t + 2.0 * math.pi * b / spec.blades
-        c, s = np.cos(psi)[:, None], np.sin(psi)[:, None]
-        arr = np.empty((T, E, 8), dtype=np.float32)
-        arr[:, :, 0] = cen[None, :, 0] * c - cen[None, :, 1] * s
-        arr[:, :, 1] = cen[None, :, 0] * s + cen[None, :, 1] * c
-        arr[:, :, 2] = np.broadcast_to(cen[None, :, 2], (T, E))
+        cs, sn = np.cos(psi), np.sin(psi)
+        arr = raw[b * T * E * 8:(b + 1) * T * E * 8].reshape(T, E, 8)
+        arr[:] = tmpl[None]
+        for t in range(T):
+            a = arr[t]
+            a[:, 0] = rot[0] * cs[t] - rot[1] * sn[t]
+            a[:, 1] = rot[0] * sn[t] + rot[1] * cs[t]
+            a[:, 5] = rot[2] * cs[t] - rot[3] * sn[t]
+            a[:, 6] = rot[2] * sn[t] + rot[3] * cs[t]
         noise = normal(seed, 100 + b, T * E).reshape(T, E) * 0.01
         arr[:, :, 3] = cp0[None, :] + noise
-        arr[:, :, 4] = area[None, :]
-        arr[:, :, 5] = nrm[None, :, 0] * c - nrm[None, :, 1] * s
-        arr[:, :, 6] = nrm[None, :, 0] * s + nrm[None, :, 1] * c
-        arr[:, :, 7] = np.broadcast_to(nrm[None, :, 2], (T, E))
         out.append(arr)
     return out
 
