@@ -29,8 +29,8 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-Wall", "-Wno-unused-function", "-I" + os.path.join(CUDA_HOME, "include"),
              "-I" + os.path.join(ROOT, "include"), "-pthread"]
 
-CU_SOURCES = ["tonal.cu", "bpm.cu", "adjoint.cu", "batch.cu", "probe.cu", "noalloc.cu"]
-CPP_SOURCES = ["abi.cpp", "io.cpp", "pending.cpp"]
+CU_SOURCES = ["tonal.cu", "bpm.cu", "adjoint.cu", "probe.cu", "noalloc.cu"]
+CPP_SOURCES = ["abi.cpp", "io.cpp", "batch.cpp"]
 
 
 def _sources():

@@ -121,7 +121,7 @@ extern "C" int acum_destroy(acum_ctx* ctx)
         cudaStreamSynchronize(ctx->stream);
         ctx->release_all();
         for (int i = 0; i < kNumEvents; ++i) cudaEventDestroy(ctx->ev[i]);
-        cudaStreamDestroy(ctx->stream);
+        if (ctx->owns_stream) cudaStreamDestroy(ctx->stream);
     }
     delete ctx;
     return ACUM_OK;
@@ -275,6 +275,7 @@ int acum_ctx::ensure_prep(bool need64, bool need32, bool need_fields)
     DeviceGuard g(device);
     const bool do64 = need64 && !rec64_ok, do32 = need32 && !rec32_ok;
     if (!do64 && !do32 && !need_fields) return ACUM_OK;
+    if (!d_raw.p) return fail(this, ACUM_ERR_STATE, "the surface rows were released after preprocessing");
     if (T > 4096) return fail(this, ACUM_ERR_UNSUPPORTED, "nTime above 4096 is not supported by the preprocessing");
     const size_t nrec = (size_t)Epad * nW * kGroups * kWin * 4;
     if (do64) {
@@ -434,6 +435,13 @@ extern "C" int acum_mark_surfaces_changed(acum_ctx* ctx)
 {
     if (!ctx) return ACUM_ERR_INVALID;
     ctx->invalidate();
+    return ACUM_OK;
+}
+
+extern "C" int acum_stream(acum_ctx* ctx, void** stream)
+{
+    if (!ctx || !stream) return ACUM_ERR_INVALID;
+    *stream = (void*)ctx->stream;
     return ACUM_OK;
 }
 

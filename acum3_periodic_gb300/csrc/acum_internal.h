@@ -98,6 +98,41 @@ struct TonalRun {
 };
 cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int num_sms, size_t smem_optin);
 cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s);
+
+// Constants of one tonal launch (one case), as the kernels read them.
+struct KParams {
+    const void* rec;
+    int Epad, T, nW, O;
+    const float* obs32;
+    const double* obs64;
+    // mixed constants
+    float a0f, alphaf, ialphaf, vxf, vyf, vzf, kbhi, kblo, invTf;
+    // FP64 constants
+    double a0, alpha, ialpha, vx, vy, vz, dTau, oM, dPsi, lpi;
+    int W, NS, chunk, nchunk, obs_tiles, flush_groups;
+    double* acc;
+    DeviceErr* err;
+};
+void fill_kparams(const TonalRun& r, KParams& kp);
+
+// Batched (persistent) mixed launch over many cases.  Work item = (case, observer tile,
+// element range [e0, e1)); the kernel takes items in array order from *counter.
+struct BatchItem {
+    int c, ot, e0, e1;
+};
+constexpr int kBatchNS = 4;
+// dynamic shared memory of the persistent kernel for W observers per block, elements per
+// stage SE and the longest case's nTime
+size_t batch_smem(int W, int SE, int Tmax);
+cudaError_t launch_tonal_batch(const KParams* d_cases, const BatchItem* d_items, int nitems, int* d_counter, int W,
+                               int SE, int Tmax, int grid, cudaStream_t s);
+// acc [O][T][2] of every case -> pA [T][O] (overwrite)
+struct FinCase {
+    const double* acc;
+    double* pA;
+    int O, T, tiles_o, tile0;
+};
+cudaError_t launch_finalize_batch(const FinCase* d_cases, int ncase, int total_tiles, cudaStream_t s);
 // acc [O][T][2] -> pT/pL/pA [T][O]; mode 0 overwrite double, 1 accumulate double,
 // 2 accumulate float (drop-in)
 cudaError_t launch_finalize(const double* acc, int O, int T, void* pT, void* pL, void* pA, int mode,

@@ -1,0 +1,516 @@
+// batch.cpp -- many decks on one device, solved by one persistent launch (acum_batch_*).
+//
+// Each case is an ordinary context (deck upload, GPU preprocessing into the mixed-form
+// records) that shares the batch's stream; its surface rows are dropped once the records
+// exist.  The batch owns one pool of FP64 bin sums and one pool of pA results, the
+// per-case kernel constants, and the work list of the persistent kernel:
+//   item = (case, observer tile of W observers, element range)
+// with the element range of each case cut so that all items cost about the same
+// (total evaluations / (SMs x items_per_sm)), and the list sorted largest first so that
+// the blocks' dynamic pick-up ends with the small items (no tail of one big item).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <numeric>
+#include <vector>
+
+#include "acum_internal.h"
+#include "ctx.h"
+
+using namespace acum;
+
+struct acum_batch {
+    int device = 0;
+    int num_sms = 0;
+    size_t smem_optin = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::string err;
+    std::vector<acum_ctx*> cases;
+
+    // tile shape and plan
+    int W = 16, SE = 4, ips = 8;
+    bool planned = false;
+    int Tmax = 0;
+    int nitems = 0;
+    std::vector<BatchItem> items;
+    std::vector<size_t> acc_off, out_off;
+    int fin_tiles = 0;
+    DBuf<double> d_acc, d_out;
+    DBuf<KParams> d_kp;
+    DBuf<BatchItem> d_items;
+    DBuf<FinCase> d_fin;
+    DBuf<int> d_counter;
+    DBuf<DeviceErr> d_err;
+    size_t acc_doubles = 0, out_doubles = 0;
+
+    // graph of the persistent run (mode 2)
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+
+    double last_ms = 0;
+    long long last_launches = 0;
+    bool have_result = false;
+    int last_mode = -1;
+
+    void drop_graph()
+    {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
+        gexec = nullptr;
+        graph = nullptr;
+    }
+};
+
+namespace {
+
+int bfail(acum_batch* b, int code, const std::string& msg)
+{
+    if (b) b->err = msg;
+    return fail(nullptr, code, msg);
+}
+
+int bcuda(acum_batch* b, cudaError_t e, const char* what)
+{
+    return bfail(b, ACUM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define BK(b, call)                                        \
+    do {                                                   \
+        cudaError_t e_ = (call);                           \
+        if (e_ != cudaSuccess) return bcuda(b, e_, #call); \
+    } while (0)
+
+// TonalRun of case c with the batch's tile shape (the fields the kernels read)
+TonalRun case_run(const acum_batch* b, const acum_ctx* c, double* acc)
+{
+    TonalRun r;
+    memset(&r, 0, sizeof(r));
+    r.g.E = (int)c->E;
+    r.g.Epad = c->Epad;
+    r.g.T = c->T;
+    r.g.nW = c->nW;
+    r.g.O = c->nobs;
+    r.g.a0 = c->in.a0;
+    r.g.rho = c->in.rhoRef;
+    r.g.oM = c->der.oM;
+    r.g.dPsi = c->der.dPsi;
+    r.g.dTau = c->der.dTau;
+    r.g.lpi = c->T * c->der.dPsi;
+    for (int k = 0; k < 3; ++k) r.g.vinf[k] = c->der.vinf[k];
+    r.precision = ACUM_MIXED;
+    r.t.W = b->W;
+    r.t.SE = b->SE;
+    r.t.NS = kBatchNS;
+    r.t.flush_elems = 64;
+    r.t.opw = 1;
+    r.t.chunk = c->Epad;
+    r.t.nchunk = 1;
+    r.rec = c->d_rec32.p;
+    r.obs32 = c->d_obs32.p;
+    r.obs64 = c->d_obs64.p;
+    r.acc = acc;
+    r.err = b->d_err.p;
+    return r;
+}
+
+// the work list for a tile shape, largest item first
+void build_items(const acum_batch* b, int W, int SE, int ips, std::vector<BatchItem>& out)
+{
+    out.clear();
+    double total = 0;
+    for (const acum_ctx* c : b->cases) total += (double)((c->nobs + W - 1) / W) * W * c->Epad * c->T;
+    const double target = total / ((double)b->num_sms * ips);
+    struct Cost {
+        double cost;
+        BatchItem it;
+    };
+    std::vector<Cost> v;
+    for (size_t ci = 0; ci < b->cases.size(); ++ci) {
+        const acum_ctx* c = b->cases[ci];
+        const int tiles = (c->nobs + W - 1) / W;
+        const int groups = c->Epad / SE;
+        const double per_tile = (double)W * c->Epad * c->T;
+        int nchunk = (int)std::ceil(per_tile / std::max(target, 1.0));
+        nchunk = std::max(1, std::min(nchunk, groups));
+        const int gpc = (groups + nchunk - 1) / nchunk;
+        for (int ot = 0; ot < tiles; ++ot) {
+            const int wobs = std::min(W, c->nobs - ot * W);
+            for (int g0 = 0; g0 < groups; g0 += gpc) {
+                const int e0 = g0 * SE, e1 = std::min(groups, g0 + gpc) * SE;
+                v.push_back({(double)wobs * (e1 - e0) * c->T, BatchItem{(int)ci, ot, e0, e1}});
+            }
+        }
+    }
+    std::stable_sort(v.begin(), v.end(), [](const Cost& a, const Cost& b2) { return a.cost > b2.cost; });
+    out.reserve(v.size());
+    for (const Cost& x : v) out.push_back(x.it);
+}
+
+bool shape_fits(const acum_batch* b, int W, int SE)
+{
+    // keep 1 KB of the per-block limit for the kernel's static shared memory
+    return batch_smem(W, SE, b->Tmax) + 1024 <= b->smem_optin;
+}
+
+int plan(acum_batch* b)
+{
+    if (b->cases.empty()) return bfail(b, ACUM_ERR_STATE, "the batch has no cases");
+    DeviceGuard g(b->device);
+    b->Tmax = 0;
+    for (const acum_ctx* c : b->cases) b->Tmax = std::max(b->Tmax, c->T);
+    if (!shape_fits(b, b->W, b->SE))
+        return bfail(b, ACUM_ERR_INVALID, "tile shape does not fit in shared memory for the longest case");
+    // pools of sums and results
+    const size_t n = b->cases.size();
+    b->acc_off.assign(n, 0);
+    b->out_off.assign(n, 0);
+    size_t acc = 0, out = 0;
+    for (size_t i = 0; i < n; ++i) {
+        b->acc_off[i] = acc;
+        b->out_off[i] = out;
+        acc += (size_t)b->cases[i]->nobs * b->cases[i]->T * 2;
+        out += (size_t)b->cases[i]->nobs * b->cases[i]->T;
+    }
+    b->acc_doubles = acc;
+    b->out_doubles = out;
+    BK(b, b->d_acc.ensure(acc));
+    BK(b, b->d_out.ensure(out));
+    // per-case constants
+    std::vector<KParams> kp(n);
+    std::vector<FinCase> fin(n);
+    int tiles = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const acum_ctx* c = b->cases[i];
+        TonalRun r = case_run(b, c, b->d_acc.p + b->acc_off[i]);
+        fill_kparams(r, kp[i]);
+        fin[i].acc = b->d_acc.p + b->acc_off[i];
+        fin[i].pA = b->d_out.p + b->out_off[i];
+        fin[i].O = c->nobs;
+        fin[i].T = c->T;
+        fin[i].tiles_o = (c->nobs + 31) / 32;
+        fin[i].tile0 = tiles;
+        tiles += fin[i].tiles_o * ((c->T + 31) / 32);
+    }
+    b->fin_tiles = tiles;
+    build_items(b, b->W, b->SE, b->ips, b->items);
+    b->nitems = (int)b->items.size();
+    BK(b, b->d_kp.ensure(n));
+    BK(b, b->d_fin.ensure(n));
+    BK(b, b->d_items.ensure(b->items.size()));
+    BK(b, cudaMemcpy(b->d_kp.p, kp.data(), n * sizeof(KParams), cudaMemcpyHostToDevice));
+    BK(b, cudaMemcpy(b->d_fin.p, fin.data(), n * sizeof(FinCase), cudaMemcpyHostToDevice));
+    BK(b, cudaMemcpy(b->d_items.p, b->items.data(), b->items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice));
+    b->drop_graph();
+    b->planned = true;
+    return ACUM_OK;
+}
+
+// memset of the counter and the sums, the persistent kernel, the finalize
+int enqueue_persistent(acum_batch* b, const BatchItem* d_items, int nitems, bool finalize)
+{
+    BK(b, cudaMemsetAsync(b->d_counter.p, 0, sizeof(int), b->stream));
+    BK(b, cudaMemsetAsync(b->d_acc.p, 0, b->acc_doubles * 8, b->stream));
+    BK(b, launch_tonal_batch(b->d_kp.p, d_items, nitems, b->d_counter.p, b->W, b->SE, b->Tmax, b->num_sms,
+                             b->stream));
+    if (finalize) BK(b, launch_finalize_batch(b->d_fin.p, (int)b->cases.size(), b->fin_tiles, b->stream));
+    return ACUM_OK;
+}
+
+int check_err(acum_batch* b)
+{
+    DeviceErr h;
+    BK(b, cudaMemcpy(&h, b->d_err.p, sizeof(h), cudaMemcpyDeviceToHost));
+    if (h.bits & ACUM_DEVERR_TIMEOUT) {
+        cudaMemset(b->d_err.p, 0, sizeof(DeviceErr));
+        return bfail(b, ACUM_ERR_TIMEOUT, "a bounded shared-memory pipeline wait ran out; results are incomplete");
+    }
+    return ACUM_OK;
+}
+
+}  // namespace
+
+extern "C" int acum_batch_create(acum_batch** out, int device)
+{
+    if (!out) return fail(nullptr, ACUM_ERR_INVALID, "acum_batch_create: null out");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(nullptr, ACUM_ERR_CUDA, "acum_batch_create: no CUDA device");
+    if (device < 0 || device >= ndev) return fail(nullptr, ACUM_ERR_INVALID, "acum_batch_create: bad device index");
+    std::unique_ptr<acum_batch> b(new acum_batch());
+    b->device = device;
+    DeviceGuard g(device);
+    BK(nullptr, cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, device));
+    int optin = 0;
+    BK(nullptr, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+    b->smem_optin = (size_t)optin;
+    BK(nullptr, cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    BK(nullptr, cudaEventCreate(&b->ev0));
+    BK(nullptr, cudaEventCreate(&b->ev1));
+    BK(nullptr, b->d_counter.ensure(1));
+    BK(nullptr, b->d_err.ensure(1));
+    BK(nullptr, cudaMemset(b->d_err.p, 0, sizeof(DeviceErr)));
+    *out = b.release();
+    return ACUM_OK;
+}
+
+extern "C" int acum_batch_destroy(acum_batch* b)
+{
+    if (!b) return ACUM_OK;
+    {
+        DeviceGuard g(b->device);
+        cudaStreamSynchronize(b->stream);
+        b->drop_graph();
+        for (acum_ctx* c : b->cases) acum_destroy(c);
+        b->d_acc.release();
+        b->d_out.release();
+        b->d_kp.release();
+        b->d_items.release();
+        b->d_fin.release();
+        b->d_counter.release();
+        b->d_err.release();
+        cudaEventDestroy(b->ev0);
+        cudaEventDestroy(b->ev1);
+        cudaStreamDestroy(b->stream);
+    }
+    delete b;
+    return ACUM_OK;
+}
+
+extern "C" const char* acum_batch_last_error(const acum_batch* b) { return b ? b->err.c_str() : ""; }
+
+extern "C" int acum_batch_add(acum_batch* b, const acum_inputs* in, int nobs, const float* obs_file, int nsurf,
+                              const int* nelem, const float* raw, int* case_id)
+{
+    if (!b || !in || !obs_file || !nelem || !raw) return bfail(b, ACUM_ERR_INVALID, "acum_batch_add: null argument");
+    if (nsurf <= 0 || nobs <= 0 || in->nTime < 6) return bfail(b, ACUM_ERR_INVALID, "acum_batch_add: bad sizes");
+    long long E = 0;
+    for (int i = 0; i < nsurf; ++i) {
+        if (nelem[i] < 0) return bfail(b, ACUM_ERR_INVALID, "acum_batch_add: negative element count");
+        E += nelem[i];
+    }
+    if (E <= 0) return bfail(b, ACUM_ERR_INVALID, "acum_batch_add: no elements");
+    DeviceGuard g(b->device);
+    // what the case holds while it is added (rows + records) and afterwards (records,
+    // sums, results), against the device's free memory with 1 GiB to spare
+    const long long T = in->nTime, nW = (T + kWin - 1) / kWin, Epad = (E + 3) / 4 * 4;
+    const double rows = (double)E * T * 8 * 4, recs = (double)Epad * nW * kGroups * kWin * 4 * 4;
+    const double sums = (double)nobs * T * 8 * 3;
+    size_t free_b = 0, total_b = 0;
+    BK(b, cudaMemGetInfo(&free_b, &total_b));
+    if (rows + recs + sums + (double)(1ull << 30) > (double)free_b)
+        return bfail(b, ACUM_ERR_NOMEM, "acum_batch_add: not enough free device memory for this case");
+    acum_ctx* c = nullptr;
+    int rc = acum_create(&c, b->device);
+    if (rc) return bfail(b, rc, std::string("acum_batch_add: ") + acum_last_global_error());
+    cudaStreamDestroy(c->stream);
+    c->stream = b->stream;
+    c->owns_stream = false;
+    rc = acum_set_deck(c, in, nobs, obs_file, nsurf, nelem, raw, 0);
+    if (!rc) {
+        c->begin_run();
+        rc = c->ensure_prep(false, true, false);
+    }
+    if (!rc && cudaStreamSynchronize(b->stream) != cudaSuccess) rc = cuda_fail(c, cudaGetLastError(), "prep");
+    if (rc) {
+        std::string m = c->err;
+        acum_destroy(c);
+        return bfail(b, rc, "acum_batch_add: " + m);
+    }
+    c->d_raw.release();
+    b->cases.push_back(c);
+    b->planned = false;
+    b->have_result = false;
+    b->drop_graph();
+    if (case_id) *case_id = (int)b->cases.size() - 1;
+    return ACUM_OK;
+}
+
+extern "C" int acum_batch_count(const acum_batch* b, int* ncase)
+{
+    if (!b || !ncase) return ACUM_ERR_INVALID;
+    *ncase = (int)b->cases.size();
+    return ACUM_OK;
+}
+
+extern "C" int acum_batch_prepare(acum_batch* b)
+{
+    if (!b) return ACUM_ERR_INVALID;
+    return plan(b);
+}
+
+extern "C" int acum_batch_run(acum_batch* b, int precision, int mode)
+{
+    if (!b) return ACUM_ERR_INVALID;
+    if (precision != ACUM_MIXED) return bfail(b, ACUM_ERR_UNSUPPORTED, "batched runs are mixed precision only");
+    if (mode < 0 || mode > 2) return bfail(b, ACUM_ERR_INVALID, "mode must be 0, 1 or 2");
+    if (!b->planned) {
+        int rc = plan(b);
+        if (rc) return rc;
+    }
+    DeviceGuard g(b->device);
+    long long launches = 0;
+    if (mode == 2 && !b->gexec) {
+        BK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = enqueue_persistent(b, b->d_items.p, b->nitems, true);
+        cudaGraph_t gr = nullptr;
+        cudaError_t e = cudaStreamEndCapture(b->stream, &gr);
+        if (rc) {
+            if (gr) cudaGraphDestroy(gr);
+            return rc;
+        }
+        BK(b, e);
+        b->graph = gr;
+        BK(b, cudaGraphInstantiate(&b->gexec, b->graph, 0));
+    }
+    BK(b, cudaEventRecord(b->ev0, b->stream));
+    if (mode == 0) {
+        int rc = enqueue_persistent(b, b->d_items.p, b->nitems, true);
+        if (rc) return rc;
+        launches = 2;
+    } else if (mode == 2) {
+        BK(b, cudaGraphLaunch(b->gexec, b->stream));
+        launches = 2;
+    } else {
+        for (size_t i = 0; i < b->cases.size(); ++i) {
+            acum_ctx* c = b->cases[i];
+            c->begin_run();
+            int rc = c->run_tonal(ACUM_MIXED, nullptr, nullptr, b->d_out.p + b->out_off[i]);
+            if (rc) return bfail(b, rc, "case " + std::to_string(i) + ": " + c->err);
+            launches += c->launches;
+        }
+    }
+    BK(b, cudaEventRecord(b->ev1, b->stream));
+    BK(b, cudaStreamSynchronize(b->stream));
+    float ms = 0;
+    BK(b, cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    b->last_ms = ms;
+    b->last_launches = launches;
+    b->last_mode = mode;
+    int rc = check_err(b);
+    if (mode == 1)
+        for (acum_ctx* c : b->cases) {
+            int r2 = c->finish_run();
+            if (r2 && !rc) rc = bfail(b, r2, c->err);
+        }
+    if (rc) return rc;
+    b->have_result = true;
+    return ACUM_OK;
+}
+
+extern "C" int acum_batch_result(acum_batch* b, int case_id, double* pA)
+{
+    if (!b || !pA) return ACUM_ERR_INVALID;
+    if (case_id < 0 || case_id >= (int)b->cases.size()) return bfail(b, ACUM_ERR_INVALID, "bad case index");
+    if (!b->have_result) return bfail(b, ACUM_ERR_STATE, "no run yet");
+    DeviceGuard g(b->device);
+    const acum_ctx* c = b->cases[case_id];
+    BK(b, cudaMemcpy(pA, b->d_out.p + b->out_off[case_id], (size_t)c->nobs * c->T * 8, cudaMemcpyDeviceToHost));
+    return ACUM_OK;
+}
+
+extern "C" int acum_batch_timing(const acum_batch* b, double* ms, long long* launches)
+{
+    if (!b) return ACUM_ERR_INVALID;
+    if (ms) *ms = b->last_ms;
+    if (launches) *launches = b->last_launches;
+    return ACUM_OK;
+}
+
+extern "C" int acum_batch_case_timing(const acum_batch* b, int case_id, double* ms)
+{
+    if (!b || !ms) return ACUM_ERR_INVALID;
+    if (case_id < 0 || case_id >= (int)b->cases.size()) return ACUM_ERR_INVALID;
+    if (b->last_mode != 1) return ACUM_ERR_STATE;
+    return acum_last_timing(b->cases[case_id], 0, ms, nullptr);
+}
+
+extern "C" int acum_batch_set_tile(acum_batch* b, int obs_per_block, int elems_per_stage, int items_per_sm)
+{
+    if (!b) return ACUM_ERR_INVALID;
+    if (obs_per_block < 0 || obs_per_block > 16 || items_per_sm < 0 ||
+        (elems_per_stage != 0 && elems_per_stage != 2 && elems_per_stage != 4))
+        return bfail(b, ACUM_ERR_INVALID, "acum_batch_set_tile: obs_per_block 1..16, elems_per_stage 2 or 4");
+    if (obs_per_block) b->W = obs_per_block;
+    if (elems_per_stage) b->SE = elems_per_stage;
+    if (items_per_sm) b->ips = items_per_sm;
+    b->planned = false;
+    b->drop_graph();
+    return ACUM_OK;
+}
+
+extern "C" int acum_batch_get_tile(const acum_batch* b, int* obs_per_block, int* elems_per_stage, int* items_per_sm)
+{
+    if (!b) return ACUM_ERR_INVALID;
+    if (obs_per_block) *obs_per_block = b->W;
+    if (elems_per_stage) *elems_per_stage = b->SE;
+    if (items_per_sm) *items_per_sm = b->ips;
+    return ACUM_OK;
+}
+
+extern "C" int acum_batch_autotune(acum_batch* b, int sample_stride, double* best_ms)
+{
+    if (!b) return ACUM_ERR_INVALID;
+    if (b->cases.empty()) return bfail(b, ACUM_ERR_STATE, "the batch has no cases");
+    if (sample_stride < 1) return bfail(b, ACUM_ERR_INVALID, "sample_stride must be >= 1");
+    DeviceGuard g(b->device);
+    b->Tmax = 0;
+    for (const acum_ctx* c : b->cases) b->Tmax = std::max(b->Tmax, c->T);
+    const int Ws[] = {8, 12, 16}, SEs[] = {2, 4}, IPS[] = {4, 8, 16};
+    double best = 1e300;
+    int bw = b->W, bse = b->SE, bips = b->ips;
+    DBuf<BatchItem> d_sample;
+    for (int W : Ws)
+        for (int SE : SEs) {
+            if (!shape_fits(b, W, SE)) continue;
+            for (int ips : IPS) {
+                b->W = W;
+                b->SE = SE;
+                b->ips = ips;
+                int rc = plan(b);
+                if (rc) return rc;
+                std::vector<BatchItem> s;
+                double frac_num = 0, frac_den = 0;
+                for (size_t k = 0; k < b->items.size(); ++k) {
+                    const BatchItem& it = b->items[k];
+                    const double cost = (double)(it.e1 - it.e0) * b->cases[it.c]->T;
+                    frac_den += cost;
+                    if (k % sample_stride == 0) {
+                        s.push_back(it);
+                        frac_num += cost;
+                    }
+                }
+                BK(b, d_sample.ensure(s.size()));
+                BK(b, cudaMemcpy(d_sample.p, s.data(), s.size() * sizeof(BatchItem), cudaMemcpyHostToDevice));
+                float ms = 0;
+                for (int rep = 0; rep < 2; ++rep) {  // the first launch warms up
+                    BK(b, cudaEventRecord(b->ev0, b->stream));
+                    rc = enqueue_persistent(b, d_sample.p, (int)s.size(), false);
+                    if (rc) return rc;
+                    BK(b, cudaEventRecord(b->ev1, b->stream));
+                    BK(b, cudaStreamSynchronize(b->stream));
+                    BK(b, cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+                }
+                rc = check_err(b);
+                if (rc) return rc;
+                const double est = ms * (frac_den / std::max(frac_num, 1.0));
+                if (est < best) {
+                    best = est;
+                    bw = W;
+                    bse = SE;
+                    bips = ips;
+                }
+            }
+        }
+    d_sample.release();
+    b->W = bw;
+    b->SE = bse;
+    b->ips = bips;
+    int rc = plan(b);
+    if (rc) return rc;
+    b->have_result = false;
+    if (best_ms) *best_ms = best;
+    return ACUM_OK;
+}

@@ -69,6 +69,7 @@ struct acum_ctx {
     int num_sms = 0;
     size_t smem_optin = 0;
     cudaStream_t stream = nullptr;
+    bool owns_stream = true;  // false for the cases of a batch, which run on its stream
     cudaEvent_t ev[acum::kNumEvents];
     std::string err;
 

@@ -30,6 +30,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <type_traits>
 
 #include "acum_internal.h"
@@ -327,20 +328,6 @@ cudaError_t launch_aos_records(const AosArgs& a, cudaStream_t s)
 }
 
 // ------------------------------------------------------------- tonal kernel
-
-struct KParams {
-    const void* rec;
-    int Epad, T, nW, O;
-    const float* obs32;
-    const double* obs64;
-    // mixed constants
-    float a0f, alphaf, ialphaf, vxf, vyf, vzf, kbhi, kblo, invTf;
-    // FP64 constants
-    double a0, alpha, ialpha, vx, vy, vz, dTau, oM, dPsi, lpi;
-    int W, NS, chunk, nchunk, obs_tiles, flush_groups;
-    double* acc;
-    DeviceErr* err;
-};
 
 struct SmpF {
     int k;      // integer part of the observer time in bins (unwrapped)
@@ -812,48 +799,42 @@ __device__ __forceinline__ SmpF shfl_idx(const SmpF& v, int src)
     return o;
 }
 
+// Block-wide shared state of the mixed kernels besides the dynamic shared memory.
+struct MixedShared {
+    int abort;
+    int release[kMaxStages];
+    int last[kMaxStages];
+};
+
+// One work item of the mixed form: observers [ot*W, ot*W + W) and elements [e0, e1)
+// (a multiple of SE) of the case `p`.  The dynamic shared memory holds the warps' FP32
+// bin rows (W x acc_T float2, laid out for the item's T) followed by the NS-stage ring;
+// `stage_off` is where the ring starts (fixed for a launch).  `gbase` counts the stages
+// the block has consumed before this item, so consecutive items of a persistent block
+// continue the mbarrier phases of the same ring.  On entry every slot is free and all
+// bin rows are zero; on return (without abort) the same holds again.
 template <int OPW, int SE>
-__global__ void __launch_bounds__(OPW == 1 ? 512 : 256, 1) tonal_mixed_kernel(const KParams p)
+__device__ __forceinline__ void mixed_item(const KParams& p, int ot, int e0, int e1, unsigned char* smem,
+                                           size_t stage_off, MixedShared& sh, unsigned& gbase)
 {
     constexpr int kTile = kGroups * kWin * 4;
-    extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ int s_abort;
-    __shared__ int s_release[kMaxStages];
-    __shared__ int s_last[kMaxStages];
-
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nwarps = blockDim.x >> 5;
     const int W = p.W;  // observers per block = nwarps * OPW
     const int T = p.T, NS = p.NS, nW = p.nW;
     float2* acc_all = reinterpret_cast<float2*>(smem);
-    const size_t stage_off = acc_region_bytes(W, T, 8);
     float* stages = reinterpret_cast<float*>(smem + stage_off);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + stage_off + (size_t)NS * SE * kTile * sizeof(float));
-
-    const int item = blockIdx.x;
-    const int ot = item % p.obs_tiles, ec = item / p.obs_tiles;
-    const int e0 = ec * p.chunk;
-    const int e1 = min(e0 + p.chunk, p.Epad);
     const int ngroups = e1 > e0 ? (e1 - e0) / SE : 0;
     const int N = ngroups * nW;
-
-    for (int i = threadIdx.x; i < W * T; i += blockDim.x) acc_all[i] = make_float2(0.f, 0.f);
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < NS; ++s) {
-            mbar_init(&bars[s], 1);
-            s_release[s] = 0;
-            s_last[s] = -1;
-        }
-        mbar_fence_init();
-        s_abort = 0;
-    }
-    __syncthreads();
+    const unsigned g0 = gbase;
 
     const float* rec = reinterpret_cast<const float*>(p.rec);
     const uint32_t tile_bytes = kTile * sizeof(float);
     auto issue = [&](int i) {
-        const int s = i % NS, g = i / nW, w = i % nW;
-        s_last[s] = i;
+        const unsigned gi = g0 + (unsigned)i;
+        const int s = (int)(gi % (unsigned)NS), g = i / nW, w = i % nW;
+        sh.last[s] = (int)gi;
         mbar_expect_tx(&bars[s], tile_bytes * SE);
         for (int j = 0; j < SE; ++j) {
             const int e = e0 + g * SE + j;
@@ -877,20 +858,20 @@ __global__ void __launch_bounds__(OPW == 1 ? 512 : 256, 1) tonal_mixed_kernel(co
         acc[q] = acc_all + (size_t)(warp * OPW + q) * T;
     }
     SmpF carry[OPW][SE], first[OPW][SE];
-    const float invT = 1.0f / (float)T;
+    const float invT = p.invTf;
 
-    int s = 0, w = 0, g = 0, since_flush = 0;
-    uint32_t par = 0;
+    int s = (int)(g0 % (unsigned)NS), w = 0, g = 0, since_flush = 0;
+    uint32_t par = (g0 / (unsigned)NS) & 1u;
     for (int i = 0; i < N; ++i) {
         const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&bars[s], par));
         if (!ok) {
             if (lane == 0) {
-                s_abort = 1;
+                sh.abort = 1;
                 flag(p.err, ACUM_DEVERR_TIMEOUT, &p.err->timeout);
             }
             break;
         }
-        if (*(volatile int*)&s_abort) break;
+        if (*(volatile int*)&sh.abort) break;
         const int tau = w * kWin + lane;
         const bool valid = tau < T;
         const float* st = stages + (size_t)s * SE * kTile;
@@ -936,8 +917,8 @@ __global__ void __launch_bounds__(OPW == 1 ? 512 : 256, 1) tonal_mixed_kernel(co
         __syncwarp();
         if (lane == 0) {
             __threadfence_block();
-            if (atomicAdd(&s_release[s], 1) == nwarps - 1) {
-                s_release[s] = 0;
+            if (atomicAdd(&sh.release[s], 1) == nwarps - 1) {
+                sh.release[s] = 0;
                 if (i + NS < N) issue(i + NS);
             }
         }
@@ -950,12 +931,89 @@ __global__ void __launch_bounds__(OPW == 1 ? 512 : 256, 1) tonal_mixed_kernel(co
             ++g;
         }
     }
+    gbase = g0 + (unsigned)N;
+}
+
+__device__ __forceinline__ void mixed_init(unsigned char* smem, size_t stage_off, int NS, int SE, MixedShared& sh)
+{
+    constexpr int kTile = kGroups * kWin * 4;
+    float2* acc_all = reinterpret_cast<float2*>(smem);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + stage_off + (size_t)NS * SE * kTile * sizeof(float));
+    for (size_t i = threadIdx.x; i < stage_off / sizeof(float2); i += blockDim.x) acc_all[i] = make_float2(0.f, 0.f);
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NS; ++s) {
+            mbar_init(&bars[s], 1);
+            sh.release[s] = 0;
+            sh.last[s] = -1;
+        }
+        mbar_fence_init();
+        sh.abort = 0;
+    }
     __syncthreads();
-    if (s_abort) {
-        if (threadIdx.x == 0)
-            for (int k = 0; k < NS; ++k)
-                if (s_last[k] >= 0) (void)mbar_wait_bounded(&bars[k], (uint32_t)((s_last[k] / NS) & 1));
+}
+
+// After an abort: wait (bounded) for the copies still in flight before the block exits.
+__device__ __forceinline__ void mixed_drain(unsigned char* smem, size_t stage_off, int NS, int SE, MixedShared& sh)
+{
+    constexpr int kTile = kGroups * kWin * 4;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + stage_off + (size_t)NS * SE * kTile * sizeof(float));
+    if (threadIdx.x == 0)
+        for (int k = 0; k < NS; ++k)
+            if (sh.last[k] >= 0) (void)mbar_wait_bounded(&bars[k], (uint32_t)(((unsigned)sh.last[k] / NS) & 1u));
+    __syncthreads();
+}
+
+template <int OPW, int SE>
+__global__ void __launch_bounds__(OPW == 1 ? 512 : 256, 1) tonal_mixed_kernel(const KParams p)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ MixedShared sh;
+    const size_t stage_off = acc_region_bytes(p.W, p.T, 8);
+    mixed_init(smem, stage_off, p.NS, SE, sh);
+    const int item = blockIdx.x;
+    const int ot = item % p.obs_tiles, ec = item / p.obs_tiles;
+    const int e0 = ec * p.chunk;
+    const int e1 = min(e0 + p.chunk, p.Epad);
+    unsigned gbase = 0;
+    mixed_item<OPW, SE>(p, ot, e0, e1, smem, stage_off, sh, gbase);
+    __syncthreads();
+    if (sh.abort) mixed_drain(smem, stage_off, p.NS, SE, sh);
+}
+
+// Persistent form over many cases: one block per SM takes work items from a shared
+// counter (largest first, as the host sorts them) until none are left.  Item k is
+// (case, observer tile, first element, end element); the case's constants are copied
+// into shared memory at the start of each item.
+
+template <int SE>
+__global__ void __launch_bounds__(512, 1)
+    tonal_batch_kernel(const KParams* __restrict__ cases, const BatchItem* __restrict__ items, int nitems,
+                       int* counter, int NS, size_t stage_off)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ MixedShared sh;
+    __shared__ __align__(16) KParams sp;
+    __shared__ BatchItem s_it;
+    mixed_init(smem, stage_off, NS, SE, sh);
+    unsigned gbase = 0;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const int k = atomicAdd(counter, 1);
+            s_it = k < nitems ? items[k] : BatchItem{-1, 0, 0, 0};
+        }
         __syncthreads();
+        const BatchItem it = s_it;
+        if (it.c < 0) break;
+        constexpr int kWords = (int)(sizeof(KParams) / sizeof(int));
+        for (int k = threadIdx.x; k < kWords; k += blockDim.x)
+            reinterpret_cast<int*>(&sp)[k] = reinterpret_cast<const int*>(cases + it.c)[k];
+        __syncthreads();
+        mixed_item<1, SE>(sp, it.ot, it.e0, it.e1, smem, stage_off, sh, gbase);
+        __syncthreads();
+        if (sh.abort) {
+            mixed_drain(smem, stage_off, NS, SE, sh);
+            break;
+        }
     }
 }
 
@@ -1040,9 +1098,9 @@ static cudaError_t launch_t(const KParams& kp, int items, int threads, size_t sm
     return cudaGetLastError();
 }
 
-cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s)
+void fill_kparams(const TonalRun& r, KParams& kp)
 {
-    KParams kp;
+    memset(&kp, 0, sizeof(kp));
     const TonalGeom& g = r.g;
     kp.rec = r.rec;
     kp.Epad = g.Epad;
@@ -1080,6 +1138,12 @@ cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s)
     kp.flush_groups = std::max(1, r.t.flush_elems / r.t.SE);
     kp.acc = r.acc;
     kp.err = r.err;
+}
+
+cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s)
+{
+    KParams kp;
+    fill_kparams(r, kp);
     if (r.precision == ACUM_PLAIN_FP64) return launch_t<true, kSE64>(kp, r.t.items, 32 * r.t.W, r.t.smem, s);
     const int threads = 32 * (r.t.W / kOPW);
     static size_t configured = 0;
@@ -1091,6 +1155,44 @@ cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s)
     }
     tonal_mixed_kernel<kOPW, kSE32><<<r.t.items, threads, r.t.smem, s>>>(kp);
     return cudaGetLastError();
+}
+
+size_t batch_smem(int W, int SE, int Tmax)
+{
+    return acc_region_bytes(W, Tmax, 8) + (size_t)kBatchNS * SE * kGroups * kWin * 4 * sizeof(float) +
+           (size_t)kBatchNS * 8;
+}
+
+template <int SE>
+static cudaError_t launch_batch_t(const KParams* d_cases, const BatchItem* d_items, int nitems, int* d_counter, int W,
+                                  int Tmax, int grid, cudaStream_t s)
+{
+    static size_t configured = 0;
+    const size_t smem = batch_smem(W, SE, Tmax);
+    if (smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(tonal_batch_kernel<SE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    // as many resident blocks per SM as shared memory and registers allow
+    int per_sm = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<SE>, 32 * W, smem) != cudaSuccess ||
+        per_sm < 1)
+        per_sm = 1;
+    tonal_batch_kernel<SE><<<grid * per_sm, 32 * W, smem, s>>>(d_cases, d_items, nitems, d_counter, kBatchNS,
+                                                               acc_region_bytes(W, Tmax, 8));
+    return cudaGetLastError();
+}
+
+// grid = SMs; the launch puts as many blocks on each SM as fit
+cudaError_t launch_tonal_batch(const KParams* d_cases, const BatchItem* d_items, int nitems, int* d_counter, int W,
+                               int SE, int Tmax, int grid, cudaStream_t s)
+{
+    if (W < 1 || W > 16 || grid < 1) return cudaErrorInvalidValue;
+    if (SE == 2) return launch_batch_t<2>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s);
+    if (SE == 4) return launch_batch_t<4>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s);
+    return cudaErrorInvalidValue;
 }
 
 // ------------------------------------------------------------------ finalize
@@ -1136,6 +1238,44 @@ cudaError_t launch_finalize(const double* acc, int O, int T, void* pT, void* pL,
 {
     dim3 grid((T + 31) / 32, (O + 31) / 32), block(32, 8);
     finalize_kernel<<<grid, block, 0, s>>>(acc, O, T, pT, pL, pA, mode);
+    return cudaGetLastError();
+}
+
+// One block per 32 x 32 (observer, bin) tile of some case; the case is found by binary
+// search over the cases' first tile indices.
+__global__ void finalize_batch_kernel(const FinCase* __restrict__ cases, int ncase)
+{
+    __shared__ double tA[32][33];
+    int lo = 0, hi = ncase - 1;
+    const int tile = blockIdx.x;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (cases[mid].tile0 <= tile) lo = mid;
+        else hi = mid - 1;
+    }
+    const FinCase c = cases[lo];
+    const int local = tile - c.tile0;
+    const int o0 = (local % c.tiles_o) * 32, n0 = (local / c.tiles_o) * 32;
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int o = o0 + k, n = n0 + threadIdx.x;
+        double a = 0;
+        if (o < c.O && n < c.T) {
+            const double2 v = reinterpret_cast<const double2*>(c.acc)[(size_t)o * c.T + n];
+            a = v.x + v.y;
+        }
+        tA[k][threadIdx.x] = a;
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int n = n0 + k, o = o0 + threadIdx.x;
+        if (n < c.T && o < c.O) c.pA[(size_t)n * c.O + o] = tA[threadIdx.x][k];
+    }
+}
+
+cudaError_t launch_finalize_batch(const FinCase* d_cases, int ncase, int total_tiles, cudaStream_t s)
+{
+    if (ncase < 1 || total_tiles < 1) return cudaErrorInvalidValue;
+    finalize_batch_kernel<<<total_tiles, dim3(32, 8), 0, s>>>(d_cases, ncase);
     return cudaGetLastError();
 }
 

@@ -71,6 +71,7 @@ SIGNATURES = {
     "acum_surfaces_device_ptr": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "acum_mark_surfaces_changed": (C.c_int, [C.c_void_p]),
     "acum_sync": (C.c_int, [C.c_void_p]),
+    "acum_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "acum_bpm": (C.c_int, [C.c_void_p, C.c_int, _DP, _DP]),
     "acum_write_outputs": (C.c_int, [C.c_void_p, C.c_char_p]),
     "acum_tonal_adjoint": (C.c_int, [C.c_void_p, C.c_int, _DP, _DP, _DP, _DP, _DP]),
@@ -104,6 +105,10 @@ SIGNATURES = {
     "acum_batch_result": (C.c_int, [C.c_void_p, C.c_int, _DP]),
     "acum_batch_timing": (C.c_int, [C.c_void_p, _DP, C.POINTER(C.c_longlong)]),
     "acum_batch_set_tile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "acum_batch_get_tile": (C.c_int, [C.c_void_p, _IP, _IP, _IP]),
+    "acum_batch_count": (C.c_int, [C.c_void_p, _IP]),
+    "acum_batch_case_timing": (C.c_int, [C.c_void_p, C.c_int, _DP]),
+    "acum_batch_autotune": (C.c_int, [C.c_void_p, C.c_int, _DP]),
 }
 
 
@@ -257,6 +262,12 @@ class Context:
     def sync(self):
         self._ck(self.L.acum_sync(self.h))
 
+    def stream_ptr(self) -> int:
+        """The cudaStream_t the context issues its runs on, as an integer."""
+        p = C.c_void_p()
+        self._ck(self.L.acum_stream(self.h, C.byref(p)))
+        return int(p.value or 0)
+
     def bpm(self, aa_mode: int = 0):
         spl = np.zeros((self.O, 42, 7))
         oas = np.zeros(self.O)
@@ -297,6 +308,86 @@ def measure_peak(device: int, which: int) -> float:
     if rc != 0:
         raise AcumError(rc, "acum_measure_peak failed")
     return v.value
+
+
+class Batch:
+    """One acum_batch on one GPU: many decks solved by one persistent launch."""
+
+    def __init__(self, device: int = 0):
+        self.L = lib()
+        h = C.c_void_p()
+        rc = self.L.acum_batch_create(C.byref(h), device)
+        if rc != 0:
+            raise AcumError(rc, self.L.acum_last_global_error().decode())
+        self.h = h
+        self.shapes = []  # (nTime, nObs, evals) per case
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.acum_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc):
+        if rc != 0:
+            raise AcumError(rc, self.L.acum_batch_last_error(self.h).decode())
+
+    def add(self, deck) -> int:
+        """Uploads and preprocesses one deck; its rows are not kept on the device."""
+        obs = np.ascontiguousarray(deck.obs_file, dtype=np.float32)
+        ne = np.array([s.shape[1] for s in deck.surfaces], np.int32)
+        raw = np.ascontiguousarray(deck.raw_surfaces(), dtype=np.float32)
+        cid = C.c_int()
+        inp = inputs_of(deck)
+        self._ck(self.L.acum_batch_add(self.h, C.byref(inp), obs.shape[0], _p(obs, _FP), len(ne), _p(ne, _IP),
+                                       raw.ctypes.data_as(C.c_void_p), C.byref(cid)))
+        self.shapes.append((deck.nTime, deck.nObs, deck.tonal_evals()))
+        return cid.value
+
+    def count(self) -> int:
+        n = C.c_int()
+        self._ck(self.L.acum_batch_count(self.h, C.byref(n)))
+        return n.value
+
+    def prepare(self):
+        self._ck(self.L.acum_batch_prepare(self.h))
+
+    def set_tile(self, obs_per_block=0, elems_per_stage=0, items_per_sm=0):
+        self._ck(self.L.acum_batch_set_tile(self.h, obs_per_block, elems_per_stage, items_per_sm))
+
+    def tile(self):
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        self._ck(self.L.acum_batch_get_tile(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    def autotune(self, sample_stride: int = 16) -> float:
+        ms = C.c_double()
+        self._ck(self.L.acum_batch_autotune(self.h, sample_stride, C.byref(ms)))
+        return ms.value
+
+    def run(self, mode: int = 2, precision: int = MIXED):
+        self._ck(self.L.acum_batch_run(self.h, precision, mode))
+
+    def result(self, case: int) -> np.ndarray:
+        T, O, _ = self.shapes[case]
+        out = np.empty((T, O), np.float64)
+        self._ck(self.L.acum_batch_result(self.h, case, _p(out)))
+        return out
+
+    def timing(self):
+        ms, n = C.c_double(), C.c_longlong()
+        self._ck(self.L.acum_batch_timing(self.h, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def case_ms(self, case: int) -> float:
+        ms = C.c_double()
+        self._ck(self.L.acum_batch_case_timing(self.h, case, C.byref(ms)))
+        return ms.value
 
 
 class PinnedBuffer:

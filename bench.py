@@ -120,6 +120,33 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
+class StreamTimer:
+    """CUDA events recorded on a context's own stream (the stream its runs are issued on),
+    with the device synchronised on both sides of the timed region."""
+
+    def __init__(self, ctx, device: int):
+        import torch
+        self.torch = torch
+        self.ctx = ctx
+        self.dev = torch.device("cuda", device)
+        self.stream = torch.cuda.ExternalStream(ctx.stream_ptr(), device=self.dev)
+        self.e0 = torch.cuda.Event(enable_timing=True)
+        self.e1 = torch.cuda.Event(enable_timing=True)
+
+    def start(self):
+        self.ctx.sync()
+        self.torch.cuda.synchronize(self.dev)
+        self.e0.record(self.stream)
+
+    def stop(self) -> float:
+        """Seconds between start() and now on the context's stream."""
+        self.e1.record(self.stream)
+        self.e1.synchronize()
+        self.ctx.sync()
+        self.torch.cuda.synchronize(self.dev)
+        return self.e0.elapsed_time(self.e1) * 1e-3
+
+
 def cpu_baseline(deck, nobs_sample: int, nthreads: int):
     """The oracle port (C, FP64, reference algorithm) on the first `nobs_sample`
     observers of the deck, with `nthreads` host threads; returns evals/s and details."""
@@ -165,6 +192,66 @@ def adjoint_leg(native, device):
     return res
 
 
+def batch_leg(native, device, steps=1, inflight=6):
+    """Workload 4: 64 seeded rotor cases (2-6 blades, 500-20000 elements per blade, 180-1440
+    steps, 64-2048 observers) resident on the GPU and solved in mixed precision (a) by one
+    persistent launch replayed from a CUDA graph, tile shape from the autotuner, and (b) by
+    one launch per case.  Decks are generated on host threads (a bounded number in flight)
+    and added one by one; only their records stay on the device."""
+    from concurrent.futures import ThreadPoolExecutor
+    from acum3_periodic_gb300 import synth
+    ncase = len(synth.batch_specs())
+    b = native.Batch(device)
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(inflight) as ex:
+        futs = [ex.submit(synth.batch_deck, c) for c in range(min(inflight, ncase))]
+        nxt = len(futs)
+        for c in range(ncase):
+            d = futs[c].result()
+            futs[c] = None
+            b.add(d)
+            del d
+            if nxt < ncase:
+                futs.append(ex.submit(synth.batch_deck, nxt))
+                nxt += 1
+    gen_s = time.perf_counter() - t0
+    evals = np.array([e for (_, _, e) in b.shapes], np.float64)
+    total = float(evals.sum())
+    t0 = time.perf_counter()
+    est_ms = b.autotune(sample_stride=32)
+    tune_s = time.perf_counter() - t0
+    tile = b.tile()
+    res = {"workload": "workload 4: 64 rotor cases, one persistent launch (CUDA graph) vs one launch per case",
+           "cases": ncase, "evals": total, "deck_generation_s": gen_s, "autotune_s": tune_s,
+           "tile": {"obs_per_block": tile[0], "elems_per_stage": tile[1], "items_per_sm": tile[2]},
+           "autotune_estimate_ms": est_ms}
+    for name, mode in (("persistent_graph", 2), ("per_case", 1)):
+        b.run(mode=mode)
+        ms = []
+        for _ in range(steps):
+            b.run(mode=mode)
+            ms.append(b.timing()[0])
+        m = float(np.median(ms))
+        res[name] = {"ms": m, "evals_per_s": total / (m * 1e-3), "gpu_launches": b.timing()[1],
+                     "fp32_tflops": ALG_FLOPS_PER_EVAL * total / (m * 1e-3) / 1e12}
+        if mode == 1:
+            case_ms = np.array([b.case_ms(i) for i in range(ncase)])
+            per = evals / (case_ms * 1e-3)
+            res[name]["per_case_evals_per_s"] = {"min": float(per.min()), "median": float(np.median(per)),
+                                                 "max": float(per.max())}
+            res["per_case"]["per_case"] = [[int(b.shapes[i][0]), int(b.shapes[i][1]), float(evals[i]),
+                                            float(case_ms[i])] for i in range(ncase)]
+            res["per_case"]["per_case_columns"] = ["nTime", "nObs", "evals", "kernel_ms"]
+            last = [b.result(i) for i in (0, ncase // 2, ncase - 1)]
+    b.run(mode=2)
+    rms = lambda p, r: float(np.max(np.abs(p - r) / np.sqrt(np.mean(r ** 2, axis=0, keepdims=True))))
+    res["persistent_vs_per_case_bin_err_over_rms_max"] = max(
+        rms(b.result(i), r) for i, r in zip((0, ncase // 2, ncase - 1), last))
+    res["speedup_persistent_over_per_case"] = res["per_case"]["ms"] / res["persistent_graph"]["ms"]
+    b.close()
+    return res
+
+
 def run_reference(args, deck, ws, rank, dist):
     if rank != 0:
         return
@@ -204,6 +291,8 @@ def main():
     ap.add_argument("--small", action="store_true", help="a reduced deck (for profiling runs)")
     ap.add_argument("--no-bpm", action="store_true", help="skip the broadband leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg (workload 3)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched leg (workload 4)")
+    ap.add_argument("--batch-steps", type=int, default=1, help="timed runs per mode of the batched leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if not args.small else args.warmup
 
@@ -231,19 +320,17 @@ def main():
     sampler = ClockSampler(local)
     sampler.start()
     kern_ms, prep_ms, fin_ms, launches = [], [], [], 0
+    timer = StreamTimer(ctx, local)
     barrier(dist)
-    ctx.sync()
-    t0 = time.perf_counter()
+    timer.start()
     for _ in range(args.steps):
         step()
-        ctx.sync()
         kern_ms.append(ctx.timing(0)[0])
         prep_ms.append(ctx.timing(1)[0])
         fin_ms.append(ctx.timing(2)[0])
         launches += ctx.timing(0)[1]
-    ctx.sync()
+    elapsed = max_over_ranks(dist, timer.stop())
     barrier(dist)
-    elapsed = max_over_ranks(dist, time.perf_counter() - t0)
     clocks = sampler.stop()
     value = ws * evals * args.steps / elapsed
     ms_per_step = elapsed / args.steps * 1e3
@@ -255,11 +342,11 @@ def main():
     pin_pA = native.PinnedBuffer((deck.nTime, deck.nObs), np.float64)
     ctx.tonal_from_host(native.MIXED, pin_raw.ptr, pin_pA.ptr)
     barrier(dist)
-    t0 = time.perf_counter()
+    timer.start()
     for _ in range(args.steps):
         ctx.tonal_from_host(native.MIXED, pin_raw.ptr, pin_pA.ptr)
+    e2e_elapsed = max_over_ranks(dist, timer.stop())
     barrier(dist)
-    e2e_elapsed = max_over_ranks(dist, time.perf_counter() - t0)
     e2e_value = ws * evals * args.steps / e2e_elapsed
     mixed_pA = np.array(pin_pA.array)
 
@@ -268,10 +355,12 @@ def main():
     sub = deck.subset_observers(sel)
     ctx64 = native.Context(local)
     ctx64.set_deck(sub, bb=False)
-    ctx64.tonal(native.PLAIN_FP64)
-    t0 = time.perf_counter()
     _, _, pA64 = ctx64.tonal(native.PLAIN_FP64)
-    fp64_sec = time.perf_counter() - t0
+    timer64 = StreamTimer(ctx64, local)
+    timer64.start()
+    ctx64.mark_surfaces_changed()
+    ctx64.tonal_device(native.PLAIN_FP64, 0, 0, 0)
+    fp64_sec = timer64.stop()
     fp64_kern = ctx64.timing(0)[0] / 1e3
     fp64_value = sub.tonal_evals() / fp64_sec
     ref = pA64
@@ -323,9 +412,9 @@ def main():
         ctx.bpm(0)
         bt = []
         for _ in range(max(1, args.steps // 2)):
-            t0 = time.perf_counter()
+            timer.start()
             spl, oas = ctx.bpm(0)
-            bt.append(time.perf_counter() - t0)
+            bt.append(timer.stop())
         bpm_kernel_ms = ctx.timing(3)[0]
         nsec = sum(b.nsect for b in deck.bb)
         bpm_evals = nsec * deck.nObs * deck.nTime * 42
@@ -355,12 +444,17 @@ def main():
                                "sample": "first %d of %d observers x all elements x all steps (%d evals), "
                                          "oracle/acum_oracle.c FP64 incl. its preprocessing" % (
                                              args.cpu_obs, deck.nObs, info["evals"])}
-    if rank == 0:
-        print(json.dumps(out))
     pin_raw.close()
     pin_pA.close()
     ctx.close()
     ctx64.close()
+    if not args.no_batch:
+        try:
+            out["batch"] = batch_leg(native, local, args.batch_steps)
+        except native.AcumError as e:  # e.g. not enough device memory for all cases
+            out["batch"] = {"error": str(e)}
+    if rank == 0:
+        print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()
 

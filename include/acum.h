@@ -133,6 +133,9 @@ int acum_mark_surfaces_changed(acum_ctx* ctx);
 
 /* Waits for the context's stream (all runs issued so far). */
 int acum_sync(acum_ctx* ctx);
+/* The context's CUDA stream (a cudaStream_t), on which every run of the context is
+ * issued; a caller may record events on it or order its own work after it. */
+int acum_stream(acum_ctx* ctx, void** stream);
 
 /* Broadband: BBspl [nObs][42][7] and BBoaspl [nObs] in dB (bb_core.cu:563-583 layout),
  * host memory, overwritten (the -100 dB seeding of main.cu:256-266 is applied inside).
@@ -236,26 +239,47 @@ int acum_find_bb_noise(int nSurf_BB, int nObs, int nTime, float dTau, const floa
 
 /* --------------------------------------------------------------- batching */
 
+/* No reference counterpart: the reference solves one deck per process (main.cu).  A batch
+ * holds many independent decks ("cases") resident on one device and runs all their tonal
+ * solves (mixed precision) in one persistent launch: one block per SM takes work items
+ * (case, observer tile, element range) from a device counter, largest first.  The tile
+ * shape -- observers per block, elements per pipeline stage, work items per SM -- is set
+ * by acum_batch_set_tile or chosen by acum_batch_autotune. */
 typedef struct acum_batch acum_batch;
 
-/* A batch holds many decks (cases) resident on one device and runs their tonal solves
- * in one persistent launch (optionally replayed from a CUDA graph). */
 int acum_batch_create(acum_batch** out, int device);
 int acum_batch_destroy(acum_batch* b);
 const char* acum_batch_last_error(const acum_batch* b);
-/* Adds a case (same argument meaning as acum_set_deck); returns its index in *case_id. */
+/* Adds a case (same argument meaning as acum_set_deck with host rows) and preprocesses it
+ * on the device at once; the rows are not kept, only the mixed-form records (2560 bytes
+ * per element and 32 steps).  Fails with ACUM_ERR_NOMEM, adding nothing, when the
+ * device has less free memory than the case needs plus 1 GiB.  *case_id = its index. */
 int acum_batch_add(acum_batch* b, const acum_inputs* in, int nobs, const float* obs_file, int nsurf,
                    const int* nelem, const float* raw, int* case_id);
-/* Preprocesses every case (once). */
+int acum_batch_count(const acum_batch* b, int* ncase);
+/* Builds the work list for the current tile shape (done by acum_batch_run if needed). */
 int acum_batch_prepare(acum_batch* b);
-/* mode 0: one persistent launch over all cases; 1: one launch per case; 2: the persistent
- * launch captured once into a CUDA graph and replayed. */
+/* precision must be ACUM_MIXED.  mode 0: one persistent launch over all cases (plus
+ * one zeroing of the sums and one finalize launch); 1: one launch per case (the
+ * single-deck path, case after case on one stream); 2: mode 0 captured once into a CUDA
+ * graph and replayed. */
 int acum_batch_run(acum_batch* b, int precision, int mode);
 /* pA [nTime_c][nObs_c] of one case after a run, host memory. */
 int acum_batch_result(acum_batch* b, int case_id, double* pA);
-/* Kernel time of the last run (CUDA events on the launching stream) and launch count. */
+/* Device time of the last run (CUDA events on the batch's stream around all of its
+ * work) and the number of kernels it launched. */
 int acum_batch_timing(const acum_batch* b, double* ms, long long* launches);
+/* Device time of one case's tonal kernel in the last mode-1 run. */
+int acum_batch_case_timing(const acum_batch* b, int case_id, double* ms);
+/* obs_per_block 1..16, elems_per_stage 2 or 4, items_per_sm >= 1 (0 keeps a value). */
 int acum_batch_set_tile(acum_batch* b, int obs_per_block, int elems_per_stage, int items_per_sm);
+int acum_batch_get_tile(const acum_batch* b, int* obs_per_block, int* elems_per_stage, int* items_per_sm);
+/* Times the persistent launch for each candidate tile shape on a sample of its work
+ * items (every `sample_stride`-th, largest first; 1 = all), keeps the fastest and
+ * returns its estimated full-batch time in *best_ms.  Candidates: obs_per_block in
+ * {8, 12, 16} x elems_per_stage in {2, 4} x items_per_sm in {4, 8, 16}, skipping shapes
+ * whose shared memory does not fit. */
+int acum_batch_autotune(acum_batch* b, int sample_stride, double* best_ms);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,148 @@
+"""Batched tonal solves (acum_batch_*): many decks in one persistent launch.
+
+Cases are drawn like the 64-case batched workload (2-6 blades, uneven element, step and
+observer counts, tip Mach 0.4-0.7, Minf 0-0.2) but shrunk so that the FP64 oracle
+finishes in seconds.  Checks: every case of the persistent launch (direct and CUDA-graph
+replay) against the same deck solved alone through the single-deck mixed path and
+against the FP64 oracle; one launch per case (mode 1) against the persistent launch; all
+tile shapes the autotuner may pick; the autotuner itself; and the error paths."""
+import numpy as np
+import pytest
+
+from acum3_periodic_gb300 import synth
+from metrics import oaspl_db, per_bin_rms
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+CASES = (0, 5, 11, 17, 23, 42)
+SHRINK = dict(n_span=12, n_chord_side=6, nobs=40)
+# mixed form against FP64 (the tonal tests' bounds)
+OASPL_DB = 0.05
+BIN_RMS = 2e-3
+# two mixed solves of the same deck that differ only in how the elements are cut into
+# work items (FP32 partial sums flushed at different element boundaries)
+SAME_FORM_RMS = 1e-5
+
+
+def shrunk(case):
+    d = synth.batch_deck(case, shrink=dict(SHRINK))
+    return d
+
+
+@pytest.fixture(scope="module")
+def batch():
+    from acum3_periodic_gb300 import native
+    decks = [shrunk(c) for c in CASES]
+    b = native.Batch(0)
+    for d in decks:
+        b.add(d)
+    yield b, decks
+    b.close()
+
+
+@pytest.fixture(scope="module")
+def singles(batch):
+    from acum3_periodic_gb300 import native
+    _, decks = batch
+    ctx = native.Context(0)
+    out = []
+    for d in decks:
+        ctx.set_deck(d, bb=False)
+        out.append(ctx.tonal(native.MIXED)[2])
+    ctx.close()
+    return out
+
+
+def test_shapes_are_uneven(batch):
+    b, decks = batch
+    assert b.count() == len(CASES)
+    assert len({d.nTime for d in decks}) > 2
+    assert len({d.E for d in decks}) > 2
+
+
+def test_persistent_matches_single_deck_path(batch, singles):
+    b, decks = batch
+    b.set_tile(16, 4, 8)
+    b.run(mode=0)
+    for i, d in enumerate(decks):
+        got = b.result(i)
+        assert got.shape == (d.nTime, d.nObs)
+        assert per_bin_rms(got, singles[i]).max() < SAME_FORM_RMS, i
+
+
+def test_graph_replay_matches_and_repeats(batch, singles):
+    b, decks = batch
+    b.run(mode=2)
+    first = [b.result(i) for i in range(len(decks))]
+    b.run(mode=2)
+    for i in range(len(decks)):
+        assert per_bin_rms(first[i], singles[i]).max() < SAME_FORM_RMS
+        assert per_bin_rms(b.result(i), first[i]).max() < 1e-12
+    ms, launches = b.timing()
+    assert ms > 0 and launches == 2
+
+
+def test_one_launch_per_case_matches(batch, singles):
+    b, decks = batch
+    b.run(mode=1)
+    for i in range(len(decks)):
+        assert per_bin_rms(b.result(i), singles[i]).max() < 1e-12
+        assert b.case_ms(i) > 0
+    _, launches = b.timing()
+    assert launches == 2 * len(decks)
+
+
+def test_against_fp64_oracle(batch):
+    b, decks = batch
+    b.run(mode=0)
+    for i in (0, 3, 5):
+        _, _, ref, _ = O.tonal(decks[i], nthreads=8)
+        got = b.result(i)
+        assert np.max(np.abs(oaspl_db(got) - oaspl_db(ref))) < OASPL_DB
+        assert per_bin_rms(got, ref).max() < BIN_RMS
+
+
+@pytest.mark.parametrize("W,SE,ips", [(8, 2, 4), (12, 4, 16), (16, 2, 8), (5, 4, 1)])
+def test_tile_shapes_agree(batch, singles, W, SE, ips):
+    b, decks = batch
+    b.set_tile(W, SE, ips)
+    assert b.tile() == (W, SE, ips)
+    b.run(mode=0)
+    for i in range(len(decks)):
+        assert per_bin_rms(b.result(i), singles[i]).max() < SAME_FORM_RMS, (W, SE, ips, i)
+
+
+def test_autotune(batch, singles):
+    b, decks = batch
+    est = b.autotune(sample_stride=2)
+    W, SE, ips = b.tile()
+    assert W in (8, 12, 16) and SE in (2, 4) and ips in (4, 8, 16)
+    assert est > 0
+    b.run(mode=2)
+    for i in range(len(decks)):
+        assert per_bin_rms(b.result(i), singles[i]).max() < SAME_FORM_RMS
+
+
+def test_errors():
+    from acum3_periodic_gb300 import native
+    b = native.Batch(0)
+    with pytest.raises(native.AcumError):
+        b.run(mode=0)  # no cases
+    b.add(shrunk(0))
+    with pytest.raises(native.AcumError):
+        b.run(mode=0, precision=native.PLAIN_FP64)
+    with pytest.raises(native.AcumError):
+        b.run(mode=3)
+    with pytest.raises(native.AcumError):
+        b.set_tile(17, 4, 8)
+    with pytest.raises(native.AcumError):
+        b.set_tile(8, 3, 8)
+    with pytest.raises(native.AcumError):
+        b.result(0)  # no run yet
+    b.run(mode=0)
+    with pytest.raises(native.AcumError):
+        b.result(1)
+    with pytest.raises(native.AcumError):
+        b.case_ms(0)  # last run was not one launch per case
+    b.close()
