@@ -257,10 +257,25 @@ extern "C" int acum_get_sizes(const acum_ctx* ctx, long long* out)
     return ACUM_OK;
 }
 
+extern "C" int acum_last_plan(const acum_ctx* ctx, int* out)
+{
+    if (!ctx || !out) return ACUM_ERR_INVALID;
+    if (!ctx->have_tonal_plan) return ACUM_ERR_STATE;
+    const TonalTile& t = ctx->last_tile;
+    out[0] = t.W;
+    out[1] = t.SE;
+    out[2] = t.NS;
+    out[3] = t.chunk;
+    out[4] = t.nchunk;
+    out[5] = t.items;
+    return ACUM_OK;
+}
+
 extern "C" int acum_set_tile(acum_ctx* ctx, int obs_per_block, int elems_per_stage, int items_per_sm)
 {
     if (!ctx) return ACUM_ERR_INVALID;
-    if (obs_per_block < 0 || obs_per_block > 16 || items_per_sm < 0 || items_per_sm > 64)
+    if (obs_per_block < 0 || obs_per_block > 16 || items_per_sm < 0 || items_per_sm > 64 ||
+        (elems_per_stage != 0 && elems_per_stage != 2 && elems_per_stage != 4))
         return fail(ctx, ACUM_ERR_INVALID, "acum_set_tile: out of range");
     ctx->tile_W = obs_per_block;
     ctx->tile_SE = elems_per_stage;
@@ -381,6 +396,7 @@ int acum_ctx::run_tonal(int precision, double* d_pT, double* d_pL, double* d_pA)
     r.acc = d_acc.p;
     r.err = d_err.p;
     last_tile = r.t;
+    have_tonal_plan = true;
     // the mixed form always adds into the FP64 sums; the FP64 form stores when one block
     // owns an observer's whole element range
     if (r.t.nchunk > 1 || !f64) CK(this, cudaMemsetAsync(d_acc.p, 0, (size_t)nobs * T * 2 * 8, stream));

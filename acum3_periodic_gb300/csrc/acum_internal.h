@@ -107,6 +107,7 @@ struct KParams {
     const double* obs64;
     // mixed constants
     float a0f, alphaf, ialphaf, vxf, vyf, vzf, kbhi, kblo, invTf;
+    unsigned tmod;  // ceil(2^32 / T): bin index modulo T by multiply-high
     // FP64 constants
     double a0, alpha, ialpha, vx, vy, vz, dTau, oM, dPsi, lpi;
     int W, NS, chunk, nchunk, obs_tiles, flush_groups;

@@ -107,6 +107,7 @@ struct acum_ctx {
     bool prep_timed = false, tonal_timed = false, bpm_timed = false, adj_timed = false, call_timed = false;
     int tile_W = 0, tile_SE = 0, tile_ips = 0;
     acum::TonalTile last_tile;
+    bool have_tonal_plan = false;
 
     // broadband / adjoint state lives in their own translation units
     void* bpm_state = nullptr;

@@ -30,6 +30,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <type_traits>
 
@@ -813,7 +814,95 @@ struct MixedShared {
 // the block has consumed before this item, so consecutive items of a persistent block
 // continue the mbarrier phases of the same ring.  On entry every slot is free and all
 // bin rows are zero; on return (without abort) the same holds again.
-template <int OPW, int SE>
+// Lean forms of the observer time and the deposit: the integer part of the observer time
+// is rounded to nearest by the 1.5 * 2^23 addition (exact for |x| < 2^22, checked), so the
+// fraction lies in [-0.5, 0.5]; the bin index is reduced modulo T by a multiply-high with
+// m = ceil(2^32 / T).  Both stay on the FMA and integer pipes.
+constexpr float kRound = 12582912.0f;  // 1.5 * 2^23
+constexpr int kRoundBits = 0x4B400000;
+
+__device__ __forceinline__ SmpF sample_mixed_lean(const float4& g0, const float4& g1, const float4& g2,
+                                                  const float4& g3, const float4& g4, float ox, float oy, float oz,
+                                                  const KParams& p, int tau, DeviceErr* err)
+{
+    const float dx = ox - g0.x, dy = oy - g0.y, dz = oz - g0.z;
+    const float c = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float beta = fmaf(dx, p.vxf, fmaf(dy, p.vyf, dz * p.vzf));
+    const float q2 = fmaf(beta, beta, p.alphaf * c);
+    const float s = q2 * rsqrtf(q2);
+    const float tr = (s - beta) * p.ialphaf;
+    const float rx = fmaf(-p.vxf, tr, dx), ry = fmaf(-p.vyf, tr, dy), rz = fmaf(-p.vzf, tr, dz);
+    const float r = p.a0f * tr;
+    const float ir = __fdividef(1.0f, r);
+    const float Mr = fmaf(g1.x, rx, fmaf(g1.y, ry, g1.z * rz)) * ir;
+    const float Mdr = fmaf(g2.x, rx, fmaf(g2.y, ry, g2.z * rz)) * ir;
+    const float Lr = fmaf(g3.x, rx, fmaf(g3.y, ry, g3.z * rz)) * ir;
+    const float Ldr = fmaf(g4.x, rx, fmaf(g4.y, ry, g4.z * rz)) * ir;
+    const float G = __fdividef(1.0f, 1.0f - Mr);
+    const float qa = p.a0f * ir;
+    const float K = fmaf(qa, Mr - g1.w, Mdr);
+    const float base = ir * G * G;
+    SmpF o;
+    o.pt = g2.w * base * G * K;
+    o.pl = g0.w * base * fmaf(Lr * G, K, fmaf(qa, Lr - g3.w, Ldr));
+    // observer time in bins: tau + tr * (oM / dPsi) = k + f, the product kept as a float pair
+    const float ph = tr * p.kbhi;
+    const float pe = fmaf(tr, p.kbhi, -ph) + tr * p.kblo;
+    if (!(ph < 4.0e6f)) flag(err, ACUM_DEVERR_ORDER, &err->order);  // outside the rounding's range
+    const float t = __fadd_rn(ph, kRound);
+    o.k = tau + (__float_as_int(t) - kRoundBits);
+    o.f = (ph - __fsub_rn(t, kRound)) + pe;
+    return o;
+}
+
+__device__ __forceinline__ int mod_T(int n, int T, unsigned m)
+{
+    // 0 <= n < 2^24: the multiply-high quotient is floor(n / T) or one more
+    int r = n - (int)__umulhi((unsigned)n, m) * T;
+    return r < 0 ? r + T : r;
+}
+
+__device__ __forceinline__ float small_int_to_float(int v)
+{
+    return __int_as_float(v + kRoundBits) - kRound;  // exact for |v| < 2^22
+}
+
+// bins n with u(a) < n <= u(b) + kshift, u = k + f with f in [-0.5, 0.5]
+__device__ __forceinline__ void deposit_lean(float2* acc, int T, unsigned tm, const SmpF& a, const SmpF& b,
+                                             int kshift, bool active, DeviceErr* err)
+{
+    const int dk = b.k + kshift - a.k;
+    const bool a_up = a.f >= 0.0f;  // floor(u(a)) = k(a) - 1 + a_up
+    const int cnt = dk + (b.f < 0.0f ? 0 : 1) - (a_up ? 1 : 0);
+    const float du = small_int_to_float(dk) + (b.f - a.f);
+    const bool fast = active && cnt >= 1 && cnt <= 2 && du > 0.0f;
+    if (fast) {
+        const float inv = __fdividef(1.0f, du);
+        const float dT = b.pt - a.pt, dL = b.pl - a.pl;
+        int idx = mod_T(a.k + (a_up ? 1 : 0), T, tm);
+        const float w1 = ((a_up ? 1.0f : 0.0f) - a.f) * inv;
+        add_bin(acc, idx, w1, a.pt, dT, a.pl, dL);
+        if (cnt == 2) {
+            if (++idx == T) idx = 0;
+            add_bin(acc, idx, w1 + inv, a.pt, dT, a.pl, dL);
+        }
+    } else if (active && !(cnt == 0 && du > 0.0f)) {
+        if (cnt > 2 && cnt <= T && du > 0.0f) {
+            const float inv = __fdividef(1.0f, du);
+            const float dT = b.pt - a.pt, dL = b.pl - a.pl;
+            int idx = mod_T(a.k + (a_up ? 1 : 0), T, tm);
+            const float f0 = (a_up ? 1.0f : 0.0f) - a.f;
+            for (int m = 0; m < cnt; ++m) {
+                add_bin(acc, idx, (f0 + (float)m) * inv, a.pt, dT, a.pl, dL);
+                if (++idx == T) idx = 0;
+            }
+        } else {
+            flag(err, ACUM_DEVERR_ORDER, &err->order);
+        }
+    }
+}
+
+template <int OPW, int SE, bool LEAN>
 __device__ __forceinline__ void mixed_item(const KParams& p, int ot, int e0, int e1, unsigned char* smem,
                                            size_t stage_off, MixedShared& sh, unsigned& gbase)
 {
@@ -883,8 +972,13 @@ __device__ __forceinline__ void mixed_item(const KParams& p, int ot, int e0, int
 #pragma unroll
             for (int q = 0; q < kGroups; ++q) gg[q] = *reinterpret_cast<const float4*>(tl + q * kWin * 4);
 #pragma unroll
-            for (int q = 0; q < OPW; ++q)
-                cur[q][j] = sample_mixed(gg[0], gg[1], gg[2], gg[3], gg[4], ox[q], oy[q], oz[q], p, tau);
+            for (int q = 0; q < OPW; ++q) {
+                if (LEAN)
+                    cur[q][j] = sample_mixed_lean(gg[0], gg[1], gg[2], gg[3], gg[4], ox[q], oy[q], oz[q], p, tau,
+                                                  p.err);
+                else
+                    cur[q][j] = sample_mixed(gg[0], gg[1], gg[2], gg[3], gg[4], ox[q], oy[q], oz[q], p, tau);
+            }
         }
         const bool first_win = w == 0, last_win = w == nW - 1;
         const int rot_src = (lane + 31) & 31;
@@ -894,13 +988,18 @@ __device__ __forceinline__ void mixed_item(const KParams& p, int ot, int e0, int
             for (int j = 0; j < SE; ++j) {
                 const SmpF rot = shfl_idx(cur[q][j], rot_src);
                 const SmpF prev = lane == 0 ? carry[q][j] : rot;
-                deposit_v2(acc[q], T, invT, prev, cur[q][j], 0, oks[q] && valid && !(first_win && lane == 0), p.err);
+                const bool act = oks[q] && valid && !(first_win && lane == 0);
+                if (LEAN) deposit_lean(acc[q], T, p.tmod, prev, cur[q][j], 0, act, p.err);
+                else deposit_v2(acc[q], T, invT, prev, cur[q][j], 0, act, p.err);
                 carry[q][j] = rot;
                 if (first_win && lane == 0) first[q][j] = cur[q][j];
                 if (last_win) {
                     // the periodic wrap: (t(T-1), t(0) + period] (core.cu:173-194)
                     const SmpF lastS = shfl_idx(cur[q][j], min(31, T - 1 - w * kWin));
-                    if (lane == 0) deposit_v2(acc[q], T, invT, lastS, first[q][j], T, oks[q], p.err);
+                    if (lane == 0) {
+                        if (LEAN) deposit_lean(acc[q], T, p.tmod, lastS, first[q][j], T, oks[q], p.err);
+                        else deposit_v2(acc[q], T, invT, lastS, first[q][j], T, oks[q], p.err);
+                    }
                 }
             }
         }
@@ -963,7 +1062,7 @@ __device__ __forceinline__ void mixed_drain(unsigned char* smem, size_t stage_of
     __syncthreads();
 }
 
-template <int OPW, int SE>
+template <int OPW, int SE, bool LEAN>
 __global__ void __launch_bounds__(OPW == 1 ? 512 : 256, 1) tonal_mixed_kernel(const KParams p)
 {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -975,7 +1074,7 @@ __global__ void __launch_bounds__(OPW == 1 ? 512 : 256, 1) tonal_mixed_kernel(co
     const int e0 = ec * p.chunk;
     const int e1 = min(e0 + p.chunk, p.Epad);
     unsigned gbase = 0;
-    mixed_item<OPW, SE>(p, ot, e0, e1, smem, stage_off, sh, gbase);
+    mixed_item<OPW, SE, LEAN>(p, ot, e0, e1, smem, stage_off, sh, gbase);
     __syncthreads();
     if (sh.abort) mixed_drain(smem, stage_off, p.NS, SE, sh);
 }
@@ -985,7 +1084,7 @@ __global__ void __launch_bounds__(OPW == 1 ? 512 : 256, 1) tonal_mixed_kernel(co
 // (case, observer tile, first element, end element); the case's constants are copied
 // into shared memory at the start of each item.
 
-template <int SE>
+template <int SE, bool LEAN>
 __global__ void __launch_bounds__(512, 1)
     tonal_batch_kernel(const KParams* __restrict__ cases, const BatchItem* __restrict__ items, int nitems,
                        int* counter, int NS, size_t stage_off)
@@ -1008,7 +1107,7 @@ __global__ void __launch_bounds__(512, 1)
         for (int k = threadIdx.x; k < kWords; k += blockDim.x)
             reinterpret_cast<int*>(&sp)[k] = reinterpret_cast<const int*>(cases + it.c)[k];
         __syncthreads();
-        mixed_item<1, SE>(sp, it.ot, it.e0, it.e1, smem, stage_off, sh, gbase);
+        mixed_item<1, SE, LEAN>(sp, it.ot, it.e0, it.e1, smem, stage_off, sh, gbase);
         __syncthreads();
         if (sh.abort) {
             mixed_drain(smem, stage_off, NS, SE, sh);
@@ -1032,24 +1131,31 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
 {
     const bool f64 = r.precision == ACUM_PLAIN_FP64;
     const int rb = f64 ? 8 : 4;
-    const int SE = f64 ? kSE64 : kSE32;
-    (void)SE_req;
-    // mixed: two observers per warp; W below counts observers per block
+    // mixed: elements per stage 2 or 4 (default 4); FP64: 2
+    const int SE = f64 ? kSE64 : (SE_req == 2 ? 2 : kSE32);
     const int opw = f64 ? 1 : kOPW;
     r.t.opw = opw;
-    const int NS = 4;
     const int T = r.g.T;
     int W = W_req > 0 ? W_req : 16;
     W = std::min(W, 16);
     // keep 1 KB of the per-block limit for the kernel's static shared memory
     const size_t budget = smem_optin - 1024;
-    while (W > opw && tonal_smem(W, T, NS, SE, rb) > budget) W -= opw;
-    if (tonal_smem(W, T, NS, SE, rb) > budget) return cudaErrorInvalidValue;
+    while (W > opw && tonal_smem(W, T, 4, SE, rb) > budget) W -= opw;
+    if (tonal_smem(W, T, 4, SE, rb) > budget) return cudaErrorInvalidValue;
     if (W_req <= 0) {
         // do not spread few observers over many idle warps
         W = std::max(opw, std::min(W, (r.g.O + opw - 1) / opw * opw));
     }
     W = (W + opw - 1) / opw * opw;
+    // mixed: as many ring stages (4..8) as the shared memory left over by the bins holds,
+    // without lowering the blocks per SM (registers, ~128 per thread, allow 65536 / (128 *
+    // 32 W) blocks of W warps)
+    int NS = 4;
+    if (!f64) {
+        const auto per_sm_at = [&](int ns) { return (int)((228 * 1024) / (tonal_smem(W, T, ns, SE, rb) + 1024)); };
+        const int resident = std::max(1, std::min(per_sm_at(4), 65536 / (128 * 32 * (W / opw))));
+        while (NS < kMaxStages && tonal_smem(W, T, NS + 1, SE, rb) <= budget && per_sm_at(NS + 1) >= resident) ++NS;
+    }
     TonalTile& t = r.t;
     t.flush_elems = f64 ? 1 << 30 : 64;
     t.W = W;
@@ -1098,6 +1204,31 @@ static cudaError_t launch_t(const KParams& kp, int items, int threads, size_t sm
     return cudaGetLastError();
 }
 
+template <int SE, bool LEAN>
+static cudaError_t launch_mixed_t(const KParams& kp, int items, int threads, size_t smem, cudaStream_t s)
+{
+    static size_t configured = 0;
+    if (smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(tonal_mixed_kernel<kOPW, SE, LEAN>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    tonal_mixed_kernel<kOPW, SE, LEAN><<<items, threads, smem, s>>>(kp);
+    return cudaGetLastError();
+}
+
+// the mixed kernel's form: lean (integer-pipe observer time and bin wrap) unless
+// ACUM_MIXED_FORM=classic selects the float-modulo form (kept for comparison)
+static bool mixed_lean()
+{
+    static const int v = [] {
+        const char* e = getenv("ACUM_MIXED_FORM");
+        return (e && strcmp(e, "classic") == 0) ? 0 : 1;
+    }();
+    return v != 0;
+}
+
 void fill_kparams(const TonalRun& r, KParams& kp)
 {
     memset(&kp, 0, sizeof(kp));
@@ -1130,6 +1261,7 @@ void fill_kparams(const TonalRun& r, KParams& kp)
     kp.kbhi = (float)kb;
     kp.kblo = (float)(kb - (double)kp.kbhi);
     kp.invTf = 1.0f / (float)g.T;
+    kp.tmod = (unsigned)((0x100000000ull + (unsigned long long)g.T - 1) / (unsigned long long)g.T);
     kp.W = r.t.W;
     kp.NS = r.t.NS;
     kp.chunk = r.t.chunk;
@@ -1146,15 +1278,12 @@ cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s)
     fill_kparams(r, kp);
     if (r.precision == ACUM_PLAIN_FP64) return launch_t<true, kSE64>(kp, r.t.items, 32 * r.t.W, r.t.smem, s);
     const int threads = 32 * (r.t.W / kOPW);
-    static size_t configured = 0;
-    if (r.t.smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(tonal_mixed_kernel<kOPW, kSE32>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r.t.smem);
-        if (e != cudaSuccess) return e;
-        configured = r.t.smem;
+    if (mixed_lean()) {
+        if (r.t.SE == 2) return launch_mixed_t<2, true>(kp, r.t.items, threads, r.t.smem, s);
+        return launch_mixed_t<kSE32, true>(kp, r.t.items, threads, r.t.smem, s);
     }
-    tonal_mixed_kernel<kOPW, kSE32><<<r.t.items, threads, r.t.smem, s>>>(kp);
-    return cudaGetLastError();
+    if (r.t.SE == 2) return launch_mixed_t<2, false>(kp, r.t.items, threads, r.t.smem, s);
+    return launch_mixed_t<kSE32, false>(kp, r.t.items, threads, r.t.smem, s);
 }
 
 size_t batch_smem(int W, int SE, int Tmax)
@@ -1163,25 +1292,26 @@ size_t batch_smem(int W, int SE, int Tmax)
            (size_t)kBatchNS * 8;
 }
 
-template <int SE>
+template <int SE, bool LEAN>
 static cudaError_t launch_batch_t(const KParams* d_cases, const BatchItem* d_items, int nitems, int* d_counter, int W,
                                   int Tmax, int grid, cudaStream_t s)
 {
     static size_t configured = 0;
     const size_t smem = batch_smem(W, SE, Tmax);
     if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(tonal_batch_kernel<SE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(tonal_batch_kernel<SE, LEAN>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
     // as many resident blocks per SM as shared memory and registers allow
     int per_sm = 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<SE>, 32 * W, smem) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<SE, LEAN>, 32 * W, smem) !=
+            cudaSuccess ||
         per_sm < 1)
         per_sm = 1;
-    tonal_batch_kernel<SE><<<grid * per_sm, 32 * W, smem, s>>>(d_cases, d_items, nitems, d_counter, kBatchNS,
-                                                               acc_region_bytes(W, Tmax, 8));
+    tonal_batch_kernel<SE, LEAN><<<grid * per_sm, 32 * W, smem, s>>>(d_cases, d_items, nitems, d_counter, kBatchNS,
+                                                                     acc_region_bytes(W, Tmax, 8));
     return cudaGetLastError();
 }
 
@@ -1190,8 +1320,13 @@ cudaError_t launch_tonal_batch(const KParams* d_cases, const BatchItem* d_items,
                                int SE, int Tmax, int grid, cudaStream_t s)
 {
     if (W < 1 || W > 16 || grid < 1) return cudaErrorInvalidValue;
-    if (SE == 2) return launch_batch_t<2>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s);
-    if (SE == 4) return launch_batch_t<4>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s);
+    const bool lean = mixed_lean();
+    if (SE == 2)
+        return lean ? launch_batch_t<2, true>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s)
+                    : launch_batch_t<2, false>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s);
+    if (SE == 4)
+        return lean ? launch_batch_t<4, true>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s)
+                    : launch_batch_t<4, false>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s);
     return cudaErrorInvalidValue;
 }
 

@@ -71,6 +71,7 @@ SIGNATURES = {
     "acum_surfaces_device_ptr": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "acum_mark_surfaces_changed": (C.c_int, [C.c_void_p]),
     "acum_sync": (C.c_int, [C.c_void_p]),
+    "acum_last_plan": (C.c_int, [C.c_void_p, _IP]),
     "acum_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "acum_bpm": (C.c_int, [C.c_void_p, C.c_int, _DP, _DP]),
     "acum_write_outputs": (C.c_int, [C.c_void_p, C.c_char_p]),
@@ -289,6 +290,12 @@ class Context:
 
     def set_tile(self, obs_per_block=0, elems_per_stage=0, items_per_sm=0):
         self._ck(self.L.acum_set_tile(self.h, obs_per_block, elems_per_stage, items_per_sm))
+
+    def last_plan(self) -> dict:
+        v = (C.c_int * 6)()
+        self._ck(self.L.acum_last_plan(self.h, v))
+        keys = ("obs_per_block", "elems_per_stage", "stages", "elems_per_item", "element_chunks", "work_items")
+        return dict(zip(keys, (int(x) for x in v)))
 
     def timing(self, which: int):
         ms = C.c_double()

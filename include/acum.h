@@ -163,9 +163,12 @@ int acum_device_error_word(acum_ctx* ctx, uint32_t* out, int reset);
  * *launches is the number of kernel launches of this library in the last run. */
 int acum_last_timing(const acum_ctx* ctx, int which, double* ms, long long* launches);
 
-/* Tile shape of the tonal kernels (0 = let the library choose): observers per block and
- * elements per pipeline stage.  Used by the autotuner. */
+/* Tile shape of the tonal kernels (0 = let the library choose): observers per block
+ * (1..16), elements per pipeline stage (mixed form: 2 or 4) and work items per SM. */
 int acum_set_tile(acum_ctx* ctx, int obs_per_block, int elems_per_stage, int items_per_sm);
+/* The plan of the last tonal run: out[0] observers per block, [1] elements per stage,
+ * [2] pipeline stages, [3] elements per work item, [4] element chunks, [5] work items. */
+int acum_last_plan(const acum_ctx* ctx, int* out);
 
 /* Measured FMA throughput of `device` in TFLOP/s: which = 0 FP32, 1 FP64 (a short
  * FMA-chain kernel timed with CUDA events; the CUDA-core peaks of the roofline). */
