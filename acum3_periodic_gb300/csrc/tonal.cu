@@ -1,30 +1,34 @@
 // tonal.cu -- sm_103a kernels of the tonal (FW-H thickness + loading) path.
 //
-//  prep_kernel         preprocess_imper (preprocess.cu:228-413) on the GPU in FP64, one
-//                      block per element: scaling, make_periodic, optional lowpass,
-//                      periodic d/dtau of P, n, x and of the velocity; writes the tiled
-//                      FP64 and FP32 records the tonal kernels stream.
-//  aos_record_kernel   the same records from the reference's AoS arrays (drop-in entry).
-//  tonal_kernel<F64>   the hot loop (core.cu:18-259 semantics).  A block owns W observers,
-//                      one warp each, and a chunk of elements.  Lane = source step inside
-//                      a 32-step window.  Element tiles are moved into shared memory by
-//                      bulk TMA copies (cp.async.bulk + mbarrier complete_tx), shared by
-//                      the W observer warps.  Each lane evaluates the Farassat-1A
-//                      integrand and the observer time of its step; the periodic hat-
-//                      function binning of core.cu:166-231 is done as its equivalent, the
-//                      piecewise-linear interpolation of the retarded-time signal onto the
-//                      bin grid: lane tau fills the bins in (t(tau-1), t(tau)] from its own
-//                      sample and its left neighbour's (one warp shuffle), so lanes never
-//                      collide and each warp accumulates into its own observer's bins in
-//                      shared memory with plain read-modify-writes -- no atomics.  The
-//                      block adds its bins to global memory once at the end.
-//  finalize_kernel     [obs][bin][2] sums -> pT/pL/pA [bin][obs] (main.cu:224 layout).
+//  prep_kernel          preprocess_imper (preprocess.cu:228-413) on the GPU in FP64, one
+//                       block per element: scaling, make_periodic, optional lowpass,
+//                       periodic d/dtau of P, n, x and of the velocity; writes the tiled
+//                       FP64 and FP32 records the tonal kernels stream.
+//  aos_record_kernel    the same records from the reference's AoS arrays (drop-in entry).
+//  tonal_mixed_kernel   the hot loop of the mixed form (core.cu:18-259 semantics).  A
+//                       block owns W observers, one warp each, and a range of elements.
+//                       Lane = source step inside a 32-step window.  Element tiles are
+//                       moved into shared memory by bulk TMA copies (cp.async.bulk +
+//                       mbarrier complete_tx) into a ring of NS stages shared by the W
+//                       observer warps; the last warp done with a stage refills it.  Each
+//                       lane evaluates the Farassat-1A integrand and the observer time of
+//                       its step; the periodic hat-function binning of core.cu:166-231 is
+//                       done as its equivalent, the piecewise-linear interpolation of the
+//                       retarded-time signal onto the bin grid: lane tau fills the bins in
+//                       (t(tau-1), t(tau)] from its own sample and its left neighbour's
+//                       (one warp shuffle), so lanes never collide and each warp adds into
+//                       its own observer's bins in shared memory with plain read-modify-
+//                       writes -- no atomics.
+//  tonal_batch_kernel   the same work items of many decks in one persistent launch.
+//  tonal_f64_kernel     the plain FP64 form, same structure.
+//  finalize_kernel      [obs][bin][2] sums -> pT/pL/pA [bin][obs] (main.cu:224 layout).
 //
-// Precision forms.  F64: every quantity in double, observer time in radians as the
+// Precision forms.  FP64: every quantity in double, observer time in radians as the
 // reference forms it; matches the reference's FP64 build.  Mixed: the integrand in FP32;
 // the observer time carried as an integer bin index plus an FP32 fraction built from a
-// float-float product (no rounding beyond that of the FP32 retarded time); the bin sums
-// as float-float pairs (TwoSum) in shared memory, added in FP64 at the flush.
+// float-float product (no rounding beyond that of the FP32 retarded time); bin sums in
+// FP32 in shared memory over at most 64 elements, then added into FP64 sums in global
+// memory.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -32,7 +36,6 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
-#include <type_traits>
 
 #include "acum_internal.h"
 
@@ -102,16 +105,6 @@ __device__ __forceinline__ void flag(DeviceErr* e, unsigned bit, unsigned* count
 {
     atomicOr(&e->bits, bit);
     atomicAdd(counter, 1u);
-}
-
-// TwoSum (Knuth): s + err == a + b exactly; accumulates the rounding error into lo.
-__device__ __forceinline__ void ff_add(float& hi, float& lo, float b)
-{
-    float s = hi + b;
-    float bb = s - hi;
-    float err = (hi - (s - bb)) + (b - bb);
-    hi = s;
-    lo += err;
 }
 
 struct dbl4 {
@@ -422,39 +415,6 @@ __device__ __forceinline__ int wrap_bin(int n, int T, float invT)
     return r;
 }
 
-// bins n with u(prev) < n <= u(cur), value interpolated between the two samples.  For
-// |Mr| < 1 an interval holds at most 2 bins (u(cur) - u(prev) = 1 - Mr < 2), so the first
-// bin is unrolled and the loop only runs for the second (or, for invalid input, is cut
-// off by the count bound).
-__device__ __forceinline__ void deposit_mixed(float2* acc, int T, float invT, const SmpF& a, const SmpF& b, int kshift,
-                                              DeviceErr* err)
-{
-    const int cnt = b.k + kshift - a.k;
-    const float du = (float)cnt + (b.f - a.f);
-    if (cnt <= 0 || cnt > T || !(du > 0.0f)) {
-        // no bin in the interval (cnt == 0, du > 0) is normal; everything else is bad
-        // geometry or a non-finite time and must not turn into a long loop
-        if (!(cnt == 0 && du > 0.0f)) flag(err, ACUM_DEVERR_ORDER, &err->order);
-        return;
-    }
-    const float inv = __fdividef(1.0f, du);
-    const float dT = b.pt - a.pt, dL = b.pl - a.pl;
-    int idx = wrap_bin(a.k + 1, T, invT);
-    float w = (1.0f - a.f) * inv;
-    float2 s = acc[idx];
-    s.x += fmaf(w, dT, a.pt);
-    s.y += fmaf(w, dL, a.pl);
-    acc[idx] = s;
-    for (int m = 2; m <= cnt; ++m) {
-        if (++idx == T) idx = 0;
-        w = ((float)m - a.f) * inv;
-        s = acc[idx];
-        s.x += fmaf(w, dT, a.pt);
-        s.y += fmaf(w, dL, a.pl);
-        acc[idx] = s;
-    }
-}
-
 __device__ __forceinline__ void deposit_f64(double2* acc, int T, const KParams& p, const SmpD& a, const SmpD& b,
                                             double tshift, int nshift, DeviceErr* err)
 {
@@ -547,13 +507,13 @@ __device__ __forceinline__ void flush_bins(float2* acc, double* g, int T, int la
     __syncwarp();
 }
 
-template <bool F64, int SE>
-__global__ void __launch_bounds__(512, 1) tonal_kernel(const KParams p)
+// The plain FP64 form.  Same structure as the mixed kernel below (one observer per
+// warp, lane = step of a 32-step window, element tiles by bulk copy into an NS-stage
+// ring), everything in double; the bins are FP64 in shared memory and written once per
+// block at the end.
+template <int SE>
+__global__ void __launch_bounds__(512, 1) tonal_f64_kernel(const KParams p)
 {
-    using Real = typename std::conditional<F64, double, float>::type;
-    using Smp = typename std::conditional<F64, SmpD, SmpF>::type;
-    using Acc = typename std::conditional<F64, double2, float2>::type;
-    constexpr int kAccBytes = sizeof(Acc);
     constexpr int kTile = kGroups * kWin * 4;  // reals per (element, window) tile
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ int s_abort;
@@ -563,13 +523,13 @@ __global__ void __launch_bounds__(512, 1) tonal_kernel(const KParams p)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nwarps = blockDim.x >> 5;
     const int W = p.W, T = p.T, NS = p.NS, nW = p.nW;
-    Acc* acc_all = reinterpret_cast<Acc*>(smem);
+    double2* acc_all = reinterpret_cast<double2*>(smem);
     // stages start on a 128-byte boundary: they are bulk-copy destinations (16-byte
-    // alignment required) read with 128-bit loads, and W*T*8 need not be a multiple of 16
-    const size_t stage_off = acc_region_bytes(W, T, kAccBytes);
-    Real* stages = reinterpret_cast<Real*>(smem + stage_off);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + stage_off + (size_t)NS * SE * kTile * sizeof(Real));
-    Acc* acc = acc_all + (size_t)warp * T;
+    // alignment required) read with 128-bit loads
+    const size_t stage_off = acc_region_bytes(W, T, 16);
+    double* stages = reinterpret_cast<double*>(smem + stage_off);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + stage_off + (size_t)NS * SE * kTile * sizeof(double));
+    double2* acc = acc_all + (size_t)warp * T;
 
     const int item = blockIdx.x;
     const int ot = item % p.obs_tiles, ec = item / p.obs_tiles;
@@ -580,10 +540,7 @@ __global__ void __launch_bounds__(512, 1) tonal_kernel(const KParams p)
     const int ngroups = e1 > e0 ? (e1 - e0) / SE : 0;
     const int N = ngroups * nW;
 
-    for (int i = threadIdx.x; i < W * T; i += blockDim.x) {
-        if constexpr (F64) acc_all[i] = make_double2(0.0, 0.0);
-        else acc_all[i] = make_float2(0.f, 0.f);
-    }
+    for (int i = threadIdx.x; i < W * T; i += blockDim.x) acc_all[i] = make_double2(0.0, 0.0);
     if (threadIdx.x == 0) {
         for (int s = 0; s < NS; ++s) {
             mbar_init(&bars[s], 1);
@@ -595,8 +552,8 @@ __global__ void __launch_bounds__(512, 1) tonal_kernel(const KParams p)
     }
     __syncthreads();
 
-    const Real* rec = reinterpret_cast<const Real*>(p.rec);
-    const uint32_t tile_bytes = kTile * sizeof(Real);
+    const double* rec = reinterpret_cast<const double*>(p.rec);
+    const uint32_t tile_bytes = kTile * sizeof(double);
     // stage i = (element group i / nW, window i % nW) goes into slot i % NS
     auto issue = [&](int i) {
         const int s = i % NS, g = i / nW, w = i % nW;
@@ -610,19 +567,16 @@ __global__ void __launch_bounds__(512, 1) tonal_kernel(const KParams p)
     if (threadIdx.x == 0)
         for (int i = 0; i < NS && i < N; ++i) issue(i);
 
-    Real ox = 0, oy = 0, oz = 0;
+    double ox = 0, oy = 0, oz = 0;
     if (obs_ok) {
-        if constexpr (F64) {
-            ox = p.obs64[3 * o]; oy = p.obs64[3 * o + 1]; oz = p.obs64[3 * o + 2];
-        } else {
-            ox = p.obs32[3 * o]; oy = p.obs32[3 * o + 1]; oz = p.obs32[3 * o + 2];
-        }
+        ox = p.obs64[3 * o];
+        oy = p.obs64[3 * o + 1];
+        oz = p.obs64[3 * o + 2];
     }
-    Smp carry[SE], first[SE];
-    const float invT = 1.0f / (float)T;
+    SmpD carry[SE], first[SE];
 
     // counters advanced incrementally (no per-stage integer division)
-    int s = 0, w = 0, g = 0, since_flush = 0;
+    int s = 0, w = 0;
     uint32_t par = 0;
     for (int i = 0; i < N; ++i) {
         // the wait result is made warp-uniform before any shuffle below
@@ -638,58 +592,35 @@ __global__ void __launch_bounds__(512, 1) tonal_kernel(const KParams p)
         const int tau = w * kWin + lane;
         const bool valid = tau < T;
         if (obs_ok) {
-            const Real* st = stages + (size_t)s * SE * kTile;
-            Smp cur[SE];
+            const double* st = stages + (size_t)s * SE * kTile;
+            SmpD cur[SE];
 #pragma unroll
             for (int j = 0; j < SE; ++j) {
-                const Real* tl = st + (size_t)j * kTile + lane * 4;
-                if constexpr (F64) {
-                    dbl4 gg[kGroups];
+                const double* tl = st + (size_t)j * kTile + lane * 4;
+                dbl4 gg[kGroups];
 #pragma unroll
-                    for (int q = 0; q < kGroups; ++q) {
-                        const double2* pp = reinterpret_cast<const double2*>(tl + q * kWin * 4);
-                        double2 u0 = pp[0], u1 = pp[1];
-                        gg[q] = dbl4{u0.x, u0.y, u1.x, u1.y};
-                    }
-                    cur[j] = sample_f64(gg[0], gg[1], gg[2], gg[3], gg[4], ox, oy, oz, p, tau);
-                } else {
-                    float4 gg[kGroups];
-#pragma unroll
-                    for (int q = 0; q < kGroups; ++q) gg[q] = *reinterpret_cast<const float4*>(tl + q * kWin * 4);
-                    cur[j] = sample_mixed(gg[0], gg[1], gg[2], gg[3], gg[4], ox, oy, oz, p, tau);
+                for (int q = 0; q < kGroups; ++q) {
+                    const double2* pp = reinterpret_cast<const double2*>(tl + q * kWin * 4);
+                    double2 u0 = pp[0], u1 = pp[1];
+                    gg[q] = dbl4{u0.x, u0.y, u1.x, u1.y};
                 }
+                cur[j] = sample_f64(gg[0], gg[1], gg[2], gg[3], gg[4], ox, oy, oz, p, tau);
             }
             const int last = min(31, T - 1 - w * kWin);
             const bool has_prev = valid && (lane > 0 || w > 0);
 #pragma unroll
             for (int j = 0; j < SE; ++j) {
-                Smp prev = shfl_up_smp(cur[j]);
+                SmpD prev = shfl_up_smp(cur[j]);
                 if (lane == 0) prev = carry[j];
-                if constexpr (F64) {
-                    if (has_prev) deposit_f64(acc, T, p, prev, cur[j], 0.0, 0, p.err);
-                } else {
-                    if (has_prev) deposit_mixed(acc, T, invT, prev, cur[j], 0, p.err);
-                }
+                if (has_prev) deposit_f64(acc, T, p, prev, cur[j], 0.0, 0, p.err);
                 if (w == 0) first[j] = shfl_smp(cur[j], 0);
                 carry[j] = shfl_smp(cur[j], last);
                 if (w == nW - 1 && lane == 0) {
                     // the periodic wrap: (t(T-1), t(0) + period] (core.cu:173-194)
-                    if constexpr (F64) {
-                        SmpD f0 = first[j];
-                        const double tw = f0.t + p.lpi;
-                        const int nw = (int)floor(tw / p.dPsi);
-                        deposit_f64(acc, T, p, carry[j], f0, p.lpi, nw - f0.nb, p.err);
-                    } else {
-                        deposit_mixed(acc, T, invT, carry[j], first[j], T, p.err);
-                    }
-                }
-            }
-            if constexpr (!F64) {
-                // FP32 partial sums cover at most `flush_groups` element groups before
-                // they are added to the FP64 sums in global memory
-                if (w == nW - 1 && (++since_flush == p.flush_groups || g == ngroups - 1)) {
-                    flush_bins(acc, p.acc + (size_t)o * T * 2, T, lane, false, p.err);
-                    since_flush = 0;
+                    SmpD f0 = first[j];
+                    const double tw = f0.t + p.lpi;
+                    const int nw = (int)floor(tw / p.dPsi);
+                    deposit_f64(acc, T, p, carry[j], f0, p.lpi, nw - f0.nb, p.err);
                 }
             }
         }
@@ -706,10 +637,7 @@ __global__ void __launch_bounds__(512, 1) tonal_kernel(const KParams p)
             s = 0;
             par ^= 1u;
         }
-        if (++w == nW) {
-            w = 0;
-            ++g;
-        }
+        if (++w == nW) w = 0;
     }
     __syncthreads();
     if (s_abort) {
@@ -720,19 +648,17 @@ __global__ void __launch_bounds__(512, 1) tonal_kernel(const KParams p)
         __syncthreads();
         return;
     }
-    // flush this block's bins (the mixed form flushed inside the loop)
-    if constexpr (F64) {
-        if (obs_ok) {
-            double* gsum = p.acc + (size_t)o * T * 2;
-            for (int n = lane; n < T; n += 32) {
-                const double2 a = acc[n];
-                if (!(fabs(a.x) < 1e300) || !(fabs(a.y) < 1e300)) flag(p.err, ACUM_DEVERR_NONFINITE, &p.err->nonfinite);
-                if (p.nchunk == 1) {
-                    reinterpret_cast<double2*>(gsum)[n] = a;
-                } else {
-                    atomicAdd(gsum + 2 * n, a.x);
-                    atomicAdd(gsum + 2 * n + 1, a.y);
-                }
+    // flush this block's bins
+    if (obs_ok) {
+        double* gsum = p.acc + (size_t)o * T * 2;
+        for (int n = lane; n < T; n += 32) {
+            const double2 a = acc[n];
+            if (!(fabs(a.x) < 1e300) || !(fabs(a.y) < 1e300)) flag(p.err, ACUM_DEVERR_NONFINITE, &p.err->nonfinite);
+            if (p.nchunk == 1) {
+                reinterpret_cast<double2*>(gsum)[n] = a;
+            } else {
+                atomicAdd(gsum + 2 * n, a.x);
+                atomicAdd(gsum + 2 * n + 1, a.y);
             }
         }
     }
@@ -1190,17 +1116,17 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
     return cudaSuccess;
 }
 
-template <bool F64, int SE>
-static cudaError_t launch_t(const KParams& kp, int items, int threads, size_t smem, cudaStream_t s)
+template <int SE>
+static cudaError_t launch_f64_t(const KParams& kp, int items, int threads, size_t smem, cudaStream_t s)
 {
     static size_t configured = 0;
     if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(tonal_kernel<F64, SE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(tonal_f64_kernel<SE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
-    tonal_kernel<F64, SE><<<items, threads, smem, s>>>(kp);
+    tonal_f64_kernel<SE><<<items, threads, smem, s>>>(kp);
     return cudaGetLastError();
 }
 
@@ -1276,7 +1202,7 @@ cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s)
 {
     KParams kp;
     fill_kparams(r, kp);
-    if (r.precision == ACUM_PLAIN_FP64) return launch_t<true, kSE64>(kp, r.t.items, 32 * r.t.W, r.t.smem, s);
+    if (r.precision == ACUM_PLAIN_FP64) return launch_f64_t<kSE64>(kp, r.t.items, 32 * r.t.W, r.t.smem, s);
     const int threads = 32 * (r.t.W / kOPW);
     if (mixed_lean()) {
         if (r.t.SE == 2) return launch_mixed_t<2, true>(kp, r.t.items, threads, r.t.smem, s);
