@@ -318,6 +318,7 @@ int acum_ctx::ensure_prep(bool need64, bool need32, bool need_fields)
     a.nW = nW;
     a.a0 = in.a0;
     a.rho = in.rhoRef;
+    for (int c = 0; c < 3; ++c) a.vinf[c] = der.vinf[c];
     a.pscale = 0.5 * in.rhoRef * (in.Mref * in.Mref) * (in.a0 * in.a0);
     a.cfd = in.CFDscale;
     a.dTau = der.dTau;
@@ -677,6 +678,7 @@ int find_pth(const S* rObs, const S* tObs, S* pT, S* pL, S* pA, const S* Xham, c
     a.nW = nW;
     a.a0 = a0;
     a.rho = rhoRef;
+    for (int k = 0; k < 3; ++k) a.vinf[k] = (double)hv[k];
     if (f64) {
         CK(nullptr, c->d_rec64.ensure(nrec));
         CK(nullptr, cudaMemsetAsync(c->d_rec64.p, 0, nrec * 8, st));

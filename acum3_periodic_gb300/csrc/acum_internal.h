@@ -17,7 +17,8 @@ namespace acum {
 //   g1: Mx, My, Mz, M2        (M     = V / a0,  M2 = |V|^2 / a0^2)
 //   g2: Mdx, Mdy, Mdz, ATD    (Md    = Vdot / a0, ATD = D1 * rho0 * (V.n) * a0 * ds)
 //   g3: Lx, Ly, Lz, Lm        (L     = P n,  Lm = L.V / a0)
-//   g4: Ldx, Ldy, Ldz, 0      (Ldot  = Pdot n + P ndot)
+//   g4: Ldx, Ldy, Ldz, xv     (Ldot  = Pdot n + P ndot, xv = x.vInf for the anchored
+//                              retarded time of the mixed form)
 // In HBM the records are tiled [element][window][group][32 steps][4]: a (element,
 // 32-step window) tile is contiguous (2560 B in FP32, 5120 B in FP64), which is what one
 // bulk (TMA) copy moves into shared memory.
@@ -59,6 +60,7 @@ struct PrepArgs {
     const int* e_count;    // device: E_i per surface
     int E, Epad, T, nW;
     double a0, rho, pscale, cfd, dTau;
+    double vinf[3];
     int periodic, lowpass;
     double gauss[13];
     float* ser;            // scratch [E][8][T] float
@@ -81,6 +83,7 @@ struct AosArgs {
     const long long* proff;
     int E, Epad, T, nW;
     double a0, rho;
+    double vinf[3];
     double* rec64;
     float* rec32;
 };

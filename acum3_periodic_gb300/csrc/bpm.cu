@@ -16,9 +16,10 @@
 //  bb_spec_kernel    per (section, step, band), FP32: the spectral amplitudes A of the six
 //      sub-model components (TBL-TE suction/pressure/separation, LBL-VS, TEB-VS, tip).
 //  bb_obs_kernel     per (observer, section, step, band): D from the observer geometry
-//      (once per (observer, section, step), shared by all bands), then the energies
-//      max(D*A, 1e-10) (the reference's -100 dB clip) summed over sections and steps in
-//      FP32 partial sums folded into FP64.
+//      (once per (observer, section, step), shared by all bands through shared memory),
+//      then the energies max(D*A, 1e-10) (the reference's -100 dB clip) summed over
+//      sections and steps in FP32 partial sums folded into FP64; lane = observer, so
+//      each amplitude is read once per warp as a shared-memory broadcast.
 //  bb_final_kernel   the energy means over steps and the band sum, in FP64 dB
 //      (bb_core.cu:563-583).
 //
@@ -511,131 +512,153 @@ __global__ void bb_spec_kernel(const float* __restrict__ sc, const double* __res
     o[1] = make_float4(At, Av, q[27], 0.f);
 }
 
-// Observer contraction.  Block = OB observers x all bands; thread = (band, group of OG
-// observers).  Per tile of TS (section, step) items: first the directivity factors D of
-// every (observer, item) into shared memory, then the band energies.
-constexpr int kOB = 32, kOG = 4, kTS = 128;
-constexpr int kBpmThreads = kBands * (kOB / kOG);  // 336
+// Observer contraction.  Block = 32 observers (lane = observer) x 7 warps of 6 bands.
+// Per tile of kTI (section, step) items: the amplitudes of all 42 bands (contiguous in
+// `amp`, 1344 B per item) are copied into shared memory, and the directivity factors D
+// of the block's 32 observers for the kTI items are computed once into shared memory;
+// then each lane adds, for its observer and its warp's 6 bands, the clipped energies of
+// every item.  The amplitude reads are warp-uniform (one shared-memory broadcast per
+// band and item), the D reads conflict-free.  FP32 partial sums over at most 1024 items
+// are folded into FP64 sums private to the block's (observer tile, item range):
+// part[split][band][component][observer], reduced over the splits by bb_final_kernel.
+constexpr int kObsLanes = 32;
+constexpr int kBandsPerWarp = 3;
+constexpr int kBandWarps = kBands / kBandsPerWarp;  // 14
+constexpr int kBpmThreads = 32 * kBandWarps;        // 448
+constexpr int kTI = 16;                             // items per tile
+constexpr int kFoldTiles = 64;                      // 1024 items per FP32 partial
+static_assert(kBands % kBandsPerWarp == 0, "band split");
 
-__global__ void __launch_bounds__(kBpmThreads) bb_obs_kernel(const float* __restrict__ geo,
-                                                             const float* __restrict__ amp,
-                                                             const float* __restrict__ obs, int O, long long nst,
-                                                             long long per_split, float vx, float vy, float vz,
-                                                             float a0, int aa_mode, double* __restrict__ sums,
-                                                             int atomic)
+__device__ __forceinline__ float2 bb_directivity(const float* __restrict__ geo, const float* __restrict__ obs, int o,
+                                                 float vx, float vy, float vz, float aa, float iaMv)
 {
-    __shared__ float2 sD[kOB][kTS];
-    const int o0 = blockIdx.x * kOB;
+    const float4* g = reinterpret_cast<const float4*>(geo);
+    const float4 g0 = g[0], g1 = g[1], g2 = g[2], g3 = g[3];
+    float rx = obs[3 * o] - g0.x, ry = obs[3 * o + 1] - g0.y, rz = obs[3 * o + 2] - g0.z;
+    // convected emission time (bb_core.cu:515-520)
+    const float bb = rx * vx + ry * vy + rz * vz;
+    const float cc = rx * rx + ry * ry + rz * rz;
+    const float tau = (-bb + sqrtf(bb * bb + aa * cc)) * iaMv;
+    rx -= vx * tau;
+    ry -= vy * tau;
+    rz -= vz * tau;
+    const float r2 = rx * rx + ry * ry + rz * rz;
+    // frame rows: chord (g0.w, g1.x, g1.y), span (g1.z, g1.w, g2.x), normal (g2.y, g2.z, g2.w)
+    const float p0 = rx * g0.w + ry * g1.x + rz * g1.y;
+    const float p1 = rx * g1.z + ry * g1.w + rz * g2.x;
+    const float p2 = rx * g2.y + ry * g2.z + rz * g2.w;
+    const float cx = fabsf(p0) * rsqrtf(r2);                // cos(theta)
+    const float cy = fabsf(p1) * rsqrtf(p1 * p1 + p2 * p2);  // cos(phi)
+    // sin^2(theta/2), sin^2(theta), sin^2(phi) without the acos; a zero angle is replaced
+    // by 1e-10 as the reference does (bb_core.cu:525-530)
+    const float sh2 = cx >= 1.f ? 2.5e-21f : 0.5f * (1.f - cx);
+    const float sth2 = cx >= 1.f ? 1e-20f : (1.f - cx) * (1.f + cx);
+    const float sp2 = cy >= 1.f ? 1e-20f : (1.f - cy) * (1.f + cy);
+    // directivities d_h, d_l (bb_core.cu:620-624) over r^2
+    const float M = g3.x, Mc = g3.y;
+    const float q1 = 1.f + M * cx, q2 = 1.f + (M - Mc) * cx;
+    const float Dh = __fdividef(2.f * sh2 * sp2, q1 * q2 * q2 * r2);
+    const float Dl = __fdividef(sth2 * sp2, q1 * q1 * q1 * q1 * r2);
+    return make_float2(Dh, g3.z != 0.f ? Dl : Dh);
+}
+
+__global__ void __launch_bounds__(kBpmThreads, 2) bb_obs_kernel(const float* __restrict__ geo,
+                                                                const float* __restrict__ amp,
+                                                                const float* __restrict__ obs, int O, long long nst,
+                                                                long long per_split, float vx, float vy, float vz,
+                                                                float a0, int aa_mode, double* __restrict__ part)
+{
+    __shared__ __align__(16) float4 sA[kTI * kBands * 2];
+    __shared__ float2 sD[kTI][kObsLanes];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int o0 = blockIdx.x * kObsLanes;
+    const int o = o0 + lane;
     const long long st_begin = (long long)blockIdx.y * per_split;
     const long long st_end = min(nst, st_begin + per_split);
-    const int fb = threadIdx.x % kBands, og = threadIdx.x / kBands;
     const float aMv = a0 * a0 - (vx * vx + vy * vy + vz * vz);
     const float aa = aa_mode == 1 ? 0.f : aMv;
-    float acc[kOG][6];
-    double tot[kOG][6];
+    const float iaMv = 1.0f / aMv;
+    const float4* amp4 = reinterpret_cast<const float4*>(amp);
+    double* mine = part + (size_t)blockIdx.y * kBands * 6 * O;  // [band][component][observer]
+    float acc[kBandsPerWarp][6];
 #pragma unroll
-    for (int q = 0; q < kOG; ++q)
+    for (int b = 0; b < kBandsPerWarp; ++b)
 #pragma unroll
-        for (int c = 0; c < 6; ++c) {
-            acc[q][c] = 0.f;
-            tot[q][c] = 0.0;
-        }
-    int tiles = 0;
-    for (long long t0 = st_begin; t0 < st_end; t0 += kTS) {
-        const int n = (int)min((long long)kTS, st_end - t0);
-        __syncthreads();
-        // directivity / r^2 per (observer, item) (bb_core.cu:515-530 and 620-624)
-        for (int pidx = threadIdx.x; pidx < kOB * kTS; pidx += blockDim.x) {
-            const int ol = pidx / kTS, it = pidx % kTS;
-            const int o = o0 + ol;
-            float2 D = make_float2(0.f, 0.f);
-            if (o < O && it < n) {
-                const float4* g = reinterpret_cast<const float4*>(geo + (t0 + it) * kGeo);
-                const float4 g0 = g[0], g1 = g[1], g2 = g[2], g3 = g[3];
-                float rx = obs[3 * o] - g0.x, ry = obs[3 * o + 1] - g0.y, rz = obs[3 * o + 2] - g0.z;
-                const float bb = rx * vx + ry * vy + rz * vz;
-                const float cc = rx * rx + ry * ry + rz * rz;
-                const float tau = (-bb + sqrtf(bb * bb + aa * cc)) / aMv;
-                rx -= vx * tau;
-                ry -= vy * tau;
-                rz -= vz * tau;
-                const float r2 = rx * rx + ry * ry + rz * rz;
-                const float rpn = sqrtf(r2);
-                // frame rows: chord (g0.w, g1.x, g1.y), span (g1.z, g1.w, g2.x), normal (g2.y, g2.z, g2.w)
-                const float p0 = rx * g0.w + ry * g1.x + rz * g1.y;
-                const float p1 = rx * g1.z + ry * g1.w + rz * g2.x;
-                const float p2 = rx * g2.y + ry * g2.z + rz * g2.w;
-                const float re = sqrtf(p1 * p1 + p2 * p2);
-                const float cx = fabsf(p0 / rpn);  // cos(theta)
-                const float cy = fabsf(p1) / re;   // cos(phi)
-                // sin^2(theta/2), sin^2(theta), sin^2(phi) without the acos; a zero angle is
-                // replaced by 1e-10 as the reference does
-                const float sh2 = cx >= 1.f ? 2.5e-21f : 0.5f * (1.f - cx);
-                const float sth2 = cx >= 1.f ? 1e-20f : (1.f - cx) * (1.f + cx);
-                const float sp2 = cy >= 1.f ? 1e-20f : (1.f - cy) * (1.f + cy);
-                const float M = g3.x, Mc = g3.y;
-                const float q1 = 1.f + M * cx, q2 = 1.f + (M - Mc) * cx;
-                const float dh = 2.f * sh2 * sp2 / (q1 * q2 * q2);
-                const float dl = sth2 * sp2 / (q1 * q1 * q1 * q1);
-                const float Dh = dh / r2;
-                D = make_float2(Dh, g3.z != 0.f ? dl / r2 : Dh);
-            }
-            sD[ol][it] = D;
-        }
-        __syncthreads();
-        for (int it = 0; it < n; ++it) {
-            const float4* a = reinterpret_cast<const float4*>(amp + ((t0 + it) * kBands + fb) * kAmp);
-            const float4 A0 = a[0], A1 = a[1];
+        for (int c = 0; c < 6; ++c) acc[b][c] = 0.f;
+    auto fold = [&]() {
+        if (o < O) {
+            // addresses formed here, not hoisted out of the item loop (36 live pointers
+            // would cost more registers than the accumulators)
+            size_t stride = (size_t)O;
+            asm volatile("" : "+l"(stride));
+            double* q = mine + (size_t)warp * kBandsPerWarp * 6 * stride + o;
 #pragma unroll
-            for (int q = 0; q < kOG; ++q) {
-                const float2 D = sD[og * kOG + q][it];
-                acc[q][0] += fmaxf(D.x * A0.x, 1e-10f);   // TBL-TE pressure side
-                acc[q][1] += fmaxf(D.x * A0.y, 1e-10f);   // TBL-TE suction side
-                acc[q][2] += fmaxf(D.y * A0.z, 1e-10f);   // separation
-                acc[q][3] = fmaf(D.x, A0.w, acc[q][3]);   // LBL-VS
-                acc[q][4] = fmaf(D.x, A1.x, acc[q][4]);   // TEB-VS
-                if (A1.y != 0.f) acc[q][5] += A1.y * fmaxf(D.x * A1.z, 2.2204460492503131e-16f);  // tip
-            }
-        }
-        if (++tiles == 8) {
-            // fold the FP32 partial sums into FP64 every 8 tiles (1024 items)
-#pragma unroll
-            for (int q = 0; q < kOG; ++q)
+            for (int b = 0; b < kBandsPerWarp; ++b)
 #pragma unroll
                 for (int c = 0; c < 6; ++c) {
-                    tot[q][c] += (double)acc[q][c];
-                    acc[q][c] = 0.f;
+                    *q += (double)acc[b][c];
+                    q += stride;
                 }
+        }
+#pragma unroll
+        for (int b = 0; b < kBandsPerWarp; ++b)
+#pragma unroll
+            for (int c = 0; c < 6; ++c) acc[b][c] = 0.f;
+    };
+    int tiles = 0;
+    for (long long t0 = st_begin; t0 < st_end; t0 += kTI) {
+        const int n = (int)min((long long)kTI, st_end - t0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < n * kBands * 2; i += blockDim.x) sA[i] = amp4[t0 * kBands * 2 + i];
+#pragma unroll 1
+        for (int pidx = threadIdx.x; pidx < kTI * kObsLanes; pidx += blockDim.x) {
+            const int it = pidx / kObsLanes, ol = pidx % kObsLanes;
+            float2 D = make_float2(0.f, 0.f);
+            if (it < n && o0 + ol < O) D = bb_directivity(geo + (t0 + it) * kGeo, obs, o0 + ol, vx, vy, vz, aa, iaMv);
+            sD[it][ol] = D;
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int it = 0; it < n; ++it) {
+            const float2 D = sD[it][lane];
+#pragma unroll
+            for (int b = 0; b < kBandsPerWarp; ++b) {
+                const int band = warp * kBandsPerWarp + b;
+                const float4 A0 = sA[(it * kBands + band) * 2], A1 = sA[(it * kBands + band) * 2 + 1];
+                acc[b][0] += fmaxf(D.x * A0.x, 1e-10f);  // TBL-TE pressure side
+                acc[b][1] += fmaxf(D.x * A0.y, 1e-10f);  // TBL-TE suction side
+                acc[b][2] += fmaxf(D.y * A0.z, 1e-10f);  // separation
+                acc[b][3] = fmaf(D.x, A0.w, acc[b][3]);  // LBL-VS
+                acc[b][4] = fmaf(D.x, A1.x, acc[b][4]);  // TEB-VS
+                if (A1.y != 0.f) acc[b][5] += A1.y * fmaxf(D.x * A1.z, 2.2204460492503131e-16f);  // tip
+            }
+        }
+        if (++tiles == kFoldTiles) {
+            fold();
             tiles = 0;
         }
     }
-#pragma unroll
-    for (int q = 0; q < kOG; ++q) {
-        const int o = o0 + og * kOG + q;
-        if (o >= O) continue;
-        double* s = sums + ((size_t)o * kBands + fb) * 6;
-#pragma unroll
-        for (int c = 0; c < 6; ++c) {
-            const double v = tot[q][c] + (double)acc[q][c];
-            if (atomic) atomicAdd(s + c, v);
-            else s[c] = v;
-        }
-    }
+    fold();
 }
 
 // Energy mean over steps and band sum in dB (bb_core.cu:563-583); the component sums
 // of the clipped energies become the seven levels.  Components of `sums`: TBL pressure,
 // suction, separation, LBL, TEB, tip; of BBspl: total, separation, suction, pressure,
 // LBL, TEB, tip.
-__global__ void bb_final_kernel(const double* __restrict__ sums, int O, int T, const double* __restrict__ seed_spl,
-                                const double* __restrict__ seed_oas, double* __restrict__ spl,
-                                double* __restrict__ oaspl)
+__global__ void bb_final_kernel(const double* __restrict__ part, int nsplit, int O, int T,
+                                const double* __restrict__ seed_spl, const double* __restrict__ seed_oas,
+                                double* __restrict__ spl, double* __restrict__ oaspl)
 {
     const int o = blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= O) return;
     double oas = pow(10.0, seed_oas[o] / 10.0);
     for (int f = 0; f < kBands; ++f) {
-        const double* s = sums + ((size_t)o * kBands + f) * 6;
+        double s[6];
+        for (int c = 0; c < 6; ++c) {
+            double v = 0.0;
+            for (int k = 0; k < nsplit; ++k) v += part[(((size_t)k * kBands + f) * 6 + c) * O + o];
+            s[c] = v;
+        }
         // the -100 dB seed of every (observer, step, band, component) contributes T * 1e-10
         const double floor_t = T * 1e-10;
         const double comp[7] = {s[0] + s[1] + s[2] + s[3] + s[4] + s[5], s[2], s[1], s[0], s[3], s[4], s[5]};
@@ -743,8 +766,7 @@ static int bpm_run(acum_ctx* ctx, int aa_mode, const double* seed_spl_h, const d
     const long long nst = (long long)s->S * T;
     cudaStream_t st = ctx->stream;
     cudaError_t e;
-    if ((e = s->sums.ensure((size_t)O * kBands * 6)) != cudaSuccess ||
-        (e = s->spl.ensure((size_t)O * kBands * 7)) != cudaSuccess || (e = s->oaspl.ensure(O)) != cudaSuccess ||
+    if ((e = s->spl.ensure((size_t)O * kBands * 7)) != cudaSuccess || (e = s->oaspl.ensure(O)) != cudaSuccess ||
         (e = s->seed_spl.ensure((size_t)O * kBands * 7)) != cudaSuccess || (e = s->seed_oas.ensure(O)) != cudaSuccess)
         return cuda_fail(ctx, e, "bpm alloc");
     std::vector<double> sspl((size_t)O * kBands * 7, -100.0), soas(O, -100.0);
@@ -777,18 +799,32 @@ static int bpm_run(acum_ctx* ctx, int aa_mode, const double* seed_spl_h, const d
     bb_pos_kernel<<<nb, 128, 0, st>>>(d);
     bb_prep_kernel<<<nb, 128, 0, st>>>(d);
     bb_spec_kernel<<<(int)((nst * kBands + 255) / 256), 256, 0, st>>>(s->sc.p, s->ff.p, s->amp.p, nst);
-    const int oblocks = (O + kOB - 1) / kOB;
-    int split = std::max(1, (4 * ctx->num_sms + oblocks - 1) / oblocks);
-    split = (int)std::min<long long>(split, (nst + kTS - 1) / kTS);
-    const long long per_split = ((nst + split - 1) / split + kTS - 1) / kTS * kTS;
+    // item ranges: with 2 resident blocks per SM, the number of splits (up to 16 blocks
+    // per SM in all) with the smallest wave-quantisation loss
+    const int oblocks = (O + kObsLanes - 1) / kObsLanes;
+    const int slots = 2 * ctx->num_sms;
+    int split = 1;
+    double best = 1e30;
+    const int maxs = (int)std::max<long long>(1, std::min<long long>((8 * slots + oblocks - 1) / oblocks,
+                                                                      (nst + kTI - 1) / kTI));
+    for (int k = 1; k <= maxs; ++k) {
+        const double waves = (double)oblocks * k / slots;
+        const double cost = std::ceil(waves) / waves + 0.01 * k;
+        if (cost < best) {
+            best = cost;
+            split = k;
+        }
+    }
+    const long long per_split = ((nst + split - 1) / split + kTI - 1) / kTI * kTI;
     split = (int)((nst + per_split - 1) / per_split);
-    if (split > 1) cudaMemsetAsync(s->sums.p, 0, (size_t)O * kBands * 6 * 8, st);
+    if ((e = s->sums.ensure((size_t)split * kBands * 6 * O)) != cudaSuccess) return cuda_fail(ctx, e, "bpm alloc");
+    cudaMemsetAsync(s->sums.p, 0, (size_t)split * kBands * 6 * O * 8, st);
     dim3 grid(oblocks, split);
     bb_obs_kernel<<<grid, kBpmThreads, 0, st>>>(s->geo.p, s->amp.p, ctx->d_obs32.p, O, nst, per_split,
                                                 (float)d.vinf[0], (float)d.vinf[1], (float)d.vinf[2], (float)d.a0,
-                                                aa_mode, s->sums.p, split > 1);
-    bb_final_kernel<<<(O + 127) / 128, 128, 0, st>>>(s->sums.p, O, T, s->seed_spl.p, s->seed_oas.p, s->spl.p,
-                                                     s->oaspl.p);
+                                                aa_mode, s->sums.p);
+    bb_final_kernel<<<(O + 127) / 128, 128, 0, st>>>(s->sums.p, split, O, T, s->seed_spl.p, s->seed_oas.p,
+                                                     s->spl.p, s->oaspl.p);
     cudaEventRecord(ctx->ev[EV_BPM1], st);
     ctx->launches += 5;
     ctx->bpm_timed = true;

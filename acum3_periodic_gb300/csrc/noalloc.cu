@@ -51,7 +51,8 @@ __global__ void noalloc_records_kernel(const float* __restrict__ X, const float*
                                        const int* __restrict__ E, const int* __restrict__ XPtr,
                                        const int* __restrict__ NPtr, const int* __restrict__ VPtr,
                                        const int* __restrict__ PRPtr, int nSurf, int Etot, int T, int nW, double a0,
-                                       double rho, float* __restrict__ rec)
+                                       double rho, double vx_inf, double vy_inf, double vz_inf,
+                                       float* __restrict__ rec)
 {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long long)Etot * T) return;
@@ -77,7 +78,7 @@ __global__ void noalloc_records_kernel(const float* __restrict__ X, const float*
     r[11] = D1 * rho * (vx * nx + vy * ny + vz * nz) * a0 * ds;
     r[12] = L[0]; r[13] = L[1]; r[14] = L[2]; r[15] = (L[0] * vx + L[1] * vy + L[2] * vz) * ia0;
     r[16] = Pd * nx + P * (double)n[3]; r[17] = Pd * ny + P * (double)n[4]; r[18] = Pd * nz + P * (double)n[5];
-    r[19] = 0.0;
+    r[19] = (double)x[0] * vx_inf + (double)x[1] * vy_inf + (double)x[2] * vz_inf;
     const int w = t / kWin, lane = t % kWin;
     const size_t tile = ((size_t)e * nW + w) * (kGroups * kWin * 4);
     for (int q = 0; q < kGroups; ++q)
@@ -159,7 +160,7 @@ extern "C" int acum_find_pressure_time_history_noalloc(const float* rObs, const 
     const long long n = Et * nTime;
     noalloc_records_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(Xham, Nham, Vham, PRham, E, XPtr, NPtr, VPtr,
                                                                    PRPtr, nSurf, (int)Et, nTime, nW, a0, rhoRef,
-                                                                   rec);
+                                                                   (double)hv[0], (double)hv[1], (double)hv[2], rec);
     int sms = 0, optin = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);

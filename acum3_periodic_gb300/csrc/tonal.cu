@@ -238,7 +238,8 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
         }
         rec[12] = L[0]; rec[13] = L[1]; rec[14] = L[2];
         rec[15] = (L[0] * v[0] + L[1] * v[1] + L[2] * v[2]) * ia0;
-        rec[16] = Ld[0]; rec[17] = Ld[1]; rec[18] = Ld[2]; rec[19] = 0.0;
+        rec[16] = Ld[0]; rec[17] = Ld[1]; rec[18] = Ld[2];
+        rec[19] = x[0] * a.vinf[0] + x[1] * a.vinf[1] + x[2] * a.vinf[2];
         const int w = t / kWin, lane = t % kWin;
         const size_t tile = ((size_t)e * a.nW + w) * (kGroups * kWin * 4);
         for (int q = 0; q < kGroups; ++q) {
@@ -296,7 +297,7 @@ __global__ void aos_record_kernel(AosArgs a)
         rec[16 + c] = Pd * n[c] + Pt * nd[c];
     }
     rec[15] = (rec[12] * v[0] + rec[13] * v[1] + rec[14] * v[2]) * ia0;
-    rec[19] = 0.0;
+    rec[19] = x[0] * a.vinf[0] + x[1] * a.vinf[1] + x[2] * a.vinf[2];
     const int w = t / kWin, lane = t % kWin;
     const size_t tile = ((size_t)e * a.nW + w) * (kGroups * kWin * 4);
     for (int q = 0; q < kGroups; ++q) {
@@ -747,16 +748,50 @@ struct MixedShared {
 constexpr float kRound = 12582912.0f;  // 1.5 * 2^23
 constexpr int kRoundBits = 0x4B400000;
 
+// Per-observer constants of the anchored retarded time.  The anchor is the retarded time
+// t0 from the origin to the observer, solved once per observer in FP64; each sample then
+// solves for t = t0 + dt from the difference of the two retarded-time quadratics,
+//     alpha dt^2 + 2 b dt - num = 0,   b = s0 + (d - D0).v,
+//     num = |d|^2 - |D0|^2 - 2 t0 (d - D0).v,   d - D0 = -src,   |d|^2 - |D0|^2 = -src.(d + D0)
+// (D0 = observer, s0 = alpha t0 + D0.v), whose terms are all of the size of the source
+// offset from the origin rather than of the observer distance: dt, and with it the
+// observer time t0 * oM/dPsi + dt * oM/dPsi (the first part split exactly into an
+// integer and a fraction in FP64), carries FP32 rounding relative to dt only.
+struct Anchor {
+    float t0, t2, s0, kf;  // t0, 2 t0, alpha t0 + D0.v, frac(t0 * oM / dPsi)
+    int ki;                // round(t0 * oM / dPsi)
+};
+
+__device__ __forceinline__ Anchor make_anchor(const KParams& p, float ox, float oy, float oz)
+{
+    const double x = ox, y = oy, z = oz;
+    const double b0 = x * p.vx + y * p.vy + z * p.vz;
+    const double c0 = x * x + y * y + z * z;
+    const double s0 = sqrt(b0 * b0 + p.alpha * c0);
+    const double t0 = c0 / (s0 + b0);  // = (s0 - b0) / alpha without the cancellation
+    const double K = t0 * (p.oM / p.dPsi);
+    const double Kr = rint(K);
+    Anchor a;
+    a.t0 = (float)t0;
+    a.t2 = (float)(2.0 * t0);
+    a.s0 = (float)s0;
+    a.kf = (float)(K - Kr);
+    a.ki = (int)Kr;
+    return a;
+}
+
 __device__ __forceinline__ SmpF sample_mixed_lean(const float4& g0, const float4& g1, const float4& g2,
                                                   const float4& g3, const float4& g4, float ox, float oy, float oz,
-                                                  const KParams& p, int tau, DeviceErr* err)
+                                                  const Anchor& an, const KParams& p, int tau, DeviceErr* err)
 {
     const float dx = ox - g0.x, dy = oy - g0.y, dz = oz - g0.z;
-    const float c = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    const float beta = fmaf(dx, p.vxf, fmaf(dy, p.vyf, dz * p.vzf));
-    const float q2 = fmaf(beta, beta, p.alphaf * c);
-    const float s = q2 * rsqrtf(q2);
-    const float tr = (s - beta) * p.ialphaf;
+    // anchored retarded time (g4.w = src.v)
+    const float cc = -fmaf(g0.x, dx + ox, fmaf(g0.y, dy + oy, g0.z * (dz + oz)));
+    const float num = fmaf(an.t2, g4.w, cc);
+    const float bp = an.s0 - g4.w;
+    const float q = fmaf(bp, bp, p.alphaf * num);
+    const float dt = __fdividef(num, bp + q * rsqrtf(q));
+    const float tr = an.t0 + dt;
     const float rx = fmaf(-p.vxf, tr, dx), ry = fmaf(-p.vyf, tr, dy), rz = fmaf(-p.vzf, tr, dz);
     const float r = p.a0f * tr;
     const float ir = __fdividef(1.0f, r);
@@ -771,13 +806,12 @@ __device__ __forceinline__ SmpF sample_mixed_lean(const float4& g0, const float4
     SmpF o;
     o.pt = g2.w * base * G * K;
     o.pl = g0.w * base * fmaf(Lr * G, K, fmaf(qa, Lr - g3.w, Ldr));
-    // observer time in bins: tau + tr * (oM / dPsi) = k + f, the product kept as a float pair
-    const float ph = tr * p.kbhi;
-    const float pe = fmaf(tr, p.kbhi, -ph) + tr * p.kblo;
-    if (!(ph < 4.0e6f)) flag(err, ACUM_DEVERR_ORDER, &err->order);  // outside the rounding's range
-    const float t = __fadd_rn(ph, kRound);
-    o.k = tau + (__float_as_int(t) - kRoundBits);
-    o.f = (ph - __fsub_rn(t, kRound)) + pe;
+    // observer time in bins: tau + round(t0 oM/dPsi) + x, x = frac(t0 oM/dPsi) + dt oM/dPsi
+    const float x = fmaf(dt, p.kbhi, an.kf);
+    if (!(fabsf(x) < 4.0e6f)) flag(err, ACUM_DEVERR_ORDER, &err->order);  // outside the rounding's range
+    const float t = __fadd_rn(x, kRound);
+    o.k = tau + an.ki + (__float_as_int(t) - kRoundBits);
+    o.f = x - __fsub_rn(t, kRound);
     return o;
 }
 
@@ -862,6 +896,7 @@ __device__ __forceinline__ void mixed_item(const KParams& p, int ot, int e0, int
     float ox[OPW], oy[OPW], oz[OPW];
     bool oks[OPW];
     float2* acc[OPW];
+    Anchor anc[OPW];
 #pragma unroll
     for (int q = 0; q < OPW; ++q) {
         const int o = ot * W + warp * OPW + q;
@@ -871,6 +906,7 @@ __device__ __forceinline__ void mixed_item(const KParams& p, int ot, int e0, int
         oy[q] = p.obs32[3 * oc + 1];
         oz[q] = p.obs32[3 * oc + 2];
         acc[q] = acc_all + (size_t)(warp * OPW + q) * T;
+        if (LEAN) anc[q] = make_anchor(p, ox[q], oy[q], oz[q]);
     }
     SmpF carry[OPW][SE], first[OPW][SE];
     const float invT = p.invTf;
@@ -900,8 +936,8 @@ __device__ __forceinline__ void mixed_item(const KParams& p, int ot, int e0, int
 #pragma unroll
             for (int q = 0; q < OPW; ++q) {
                 if (LEAN)
-                    cur[q][j] = sample_mixed_lean(gg[0], gg[1], gg[2], gg[3], gg[4], ox[q], oy[q], oz[q], p, tau,
-                                                  p.err);
+                    cur[q][j] = sample_mixed_lean(gg[0], gg[1], gg[2], gg[3], gg[4], ox[q], oy[q], oz[q], anc[q], p,
+                                                  tau, p.err);
                 else
                     cur[q][j] = sample_mixed(gg[0], gg[1], gg[2], gg[3], gg[4], ox[q], oy[q], oz[q], p, tau);
             }
@@ -1089,12 +1125,14 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
     t.NS = NS;
     t.smem = tonal_smem(W, T, NS, SE, rb);
     const int obs_tiles = (r.g.O + W - 1) / W;
-    const int per_sm = std::max(1, (int)((228 * 1024) / (t.smem + 1024)));
+    // resident blocks per SM: shared memory, and registers (~128 per thread)
+    const int per_sm = std::max(1, std::min((int)((228 * 1024) / (t.smem + 1024)), 65536 / (128 * 32 * (W / opw))));
     const int slots = num_sms * per_sm;
     const int groups = r.g.Epad / SE;
-    const int ips = items_per_sm > 0 ? items_per_sm : 4;
-    // number of element chunks: enough work items to fill the machine; among the
-    // candidates prefer the one with the smallest wave-quantisation loss
+    const int ips = items_per_sm > 0 ? items_per_sm : 64;
+    // number of element chunks: among 1 .. ips work items per slot, the one with the
+    // smallest wave-quantisation loss (a small charge per extra chunk for its prologue
+    // and its flush of the bins)
     int best = 1;
     double best_cost = 1e30;
     const int maxc = std::max(1, std::min(groups, std::max(1, (ips * slots + obs_tiles - 1) / obs_tiles)));
