@@ -44,6 +44,7 @@ struct AdjDev {
     const void* obs;  // [O][3]
     const void* g;    // [O][T]
     double a0, alpha, ialpha, vx, vy, vz, dTau, oM, dPsi, kb;
+    unsigned tmod;    // ceil(2^32 / T)
     double* cot;      // [E][T][19] FP64
 };
 
@@ -51,6 +52,24 @@ template <typename R>
 struct V3 {
     R x, y, z;
 };
+
+// reciprocal and square root: IEEE in FP64, the fast hardware forms in FP32 (the FP32
+// adjoint is compared with the FP64 one, not with the reference)
+__device__ __forceinline__ double rcp_(double x) { return 1.0 / x; }
+__device__ __forceinline__ float rcp_(float x) { return __fdividef(1.0f, x); }
+__device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+__device__ __forceinline__ float sqrt_(float x) { return x * rsqrtf(x); }
+
+// floor(t / dPsi): the FP64 form divides as the forward does; the FP32 form multiplies
+__device__ __forceinline__ int bin_floor(double t, double dPsi, double) { return (int)floor(t / dPsi); }
+__device__ __forceinline__ int bin_floor(float t, float, float idPsi) { return (int)floorf(t * idPsi); }
+
+// n mod T for 0 <= n < 2^24 by multiply-high with m = ceil(2^32 / T)
+__device__ __forceinline__ int wrap_T(int n, int T, unsigned m)
+{
+    int r = n - (int)__umulhi((unsigned)n, m) * T;
+    return r < 0 ? r + T : r;
+}
 
 // forward integrand with the intermediates the reverse pass needs
 template <typename R>
@@ -79,18 +98,18 @@ __device__ __forceinline__ Fwd<R> forward(const R* f, R ox, R oy, R oz, const Ad
     a.dz = oz - f[2];
     a.c = a.dx * a.dx + a.dy * a.dy + a.dz * a.dz;
     a.beta = a.dx * vx + a.dy * vy + a.dz * vz;
-    a.s = sqrt(a.beta * a.beta + (R)p.alpha * a.c);
+    a.s = sqrt_(a.beta * a.beta + (R)p.alpha * a.c);
     a.tr = (a.s - a.beta) * (R)p.ialpha;
     a.rx = a.dx - vx * a.tr;
     a.ry = a.dy - vy * a.tr;
     a.rz = a.dz - vz * a.tr;
     const R r = a0 * a.tr;
-    a.ir = (R)1 / r;
+    a.ir = rcp_(r);
     a.Mr = (f[4] * a.rx + f[5] * a.ry + f[6] * a.rz) * a.ir;
     a.Mdr = (f[8] * a.rx + f[9] * a.ry + f[10] * a.rz) * a.ir;
     a.Lr = (f[12] * a.rx + f[13] * a.ry + f[14] * a.rz) * a.ir;
     a.Ldr = (f[16] * a.rx + f[17] * a.ry + f[18] * a.rz) * a.ir;
-    a.G = (R)1 / ((R)1 - a.Mr);
+    a.G = rcp_((R)1 - a.Mr);
     a.qa = a0 * a.ir;
     a.K = a.Mdr + a.qa * (a.Mr - f[7]);
     a.base = a.ir * a.G * a.G;
@@ -137,6 +156,7 @@ __device__ __forceinline__ void reverse(const R* f, const Fwd<R>& a, R pb, R tb,
     Mrb += Gb * a.G * a.G;
     // the four projections X.r_hat = (X . rv) ir
     R rvx = 0, rvy = 0, rvz = 0;
+    const R r_len = a0 * a.tr;
     auto proj = [&](int i0, R sb, R val) {
         acc[i0] += sb * a.ir * a.rx;
         acc[i0 + 1] += sb * a.ir * a.ry;
@@ -144,7 +164,7 @@ __device__ __forceinline__ void reverse(const R* f, const Fwd<R>& a, R pb, R tb,
         rvx += sb * a.ir * f[i0];
         rvy += sb * a.ir * f[i0 + 1];
         rvz += sb * a.ir * f[i0 + 2];
-        irb += sb * val / a.ir;  // (X . rv) = val / ir
+        irb += sb * val * r_len;  // (X . rv) = val / ir
     };
     proj(4, Mrb, a.Mr);
     proj(8, Mdrb, a.Mdr);
@@ -158,7 +178,7 @@ __device__ __forceinline__ void reverse(const R* f, const Fwd<R>& a, R pb, R tb,
     // tr = (s - beta) / alpha,  s = sqrt(beta^2 + alpha c)
     const R sb = trb * (R)p.ialpha;
     R betab = -trb * (R)p.ialpha;
-    const R q2b = sb / ((R)2 * a.s);
+    const R q2b = sb * rcp_((R)2 * a.s);
     betab += q2b * (R)2 * a.beta;
     const R cb = q2b * (R)p.alpha;
     dxb += betab * vx + cb * (R)2 * a.dx;
@@ -178,7 +198,7 @@ __global__ void __launch_bounds__(128) adjoint_kernel(AdjDev p)
     if (warp_g >= p.E * p.nWa) return;  // warp-uniform
     const int e = warp_g / p.nWa, w = warp_g % p.nWa;
     const int tau = kAdjStride * w - 1 + lane;  // unwrapped step of this lane's sample
-    const int step = ((tau % p.T) + p.T) % p.T;
+    const int step = tau < 0 ? tau + p.T : (tau >= p.T ? tau - p.T : tau);
     const bool owner = lane >= 1 && lane <= kAdjStride && tau >= 0 && tau < p.T;
     R f[20];
     load_rec<R>(reinterpret_cast<const R*>(p.rec), p.nW, e, step, f);
@@ -187,7 +207,7 @@ __global__ void __launch_bounds__(128) adjoint_kernel(AdjDev p)
     for (int k = 0; k < kCot; ++k) acc[k] = 0;
     const R* obs = reinterpret_cast<const R*>(p.obs);
     const R* gg = reinterpret_cast<const R*>(p.g);
-    const R dPsi = (R)p.dPsi;
+    const R dPsi = (R)p.dPsi, idPsi = (R)(1.0 / p.dPsi);
     for (int o = 0; o < p.O; ++o) {
         const Fwd<R> a = forward<R>(f, obs[3 * o], obs[3 * o + 1], obs[3 * o + 2], p, tau);
         const R pc = a.pt + a.pl;
@@ -196,12 +216,15 @@ __global__ void __launch_bounds__(128) adjoint_kernel(AdjDev p)
         // interval (t(tau-1), t(tau)] of this lane: bins n with tp < n dPsi <= t
         R rp = 0, lp = 0, rt = 0, lt = 0;
         if (lane >= 1 && a.t > tp) {
-            const int n0 = (int)floor(tp / dPsi) + 1, n1 = (int)floor(a.t / dPsi);
-            const R inv = (R)1 / (a.t - tp);
+            // the bin bounds as the forward forms them: floor(t / dPsi)
+            const int n0 = bin_floor(tp, dPsi, idPsi) + 1, n1 = bin_floor(a.t, dPsi, idPsi);
+            const R inv = rcp_(a.t - tp);
             const R dp = pc - pp;
             const R* grow = gg + (size_t)o * p.T;
+            int idx = n0 >= 0 ? wrap_T(n0, p.T, p.tmod) : ((n0 % p.T) + p.T) % p.T;
             for (int n = n0; n <= n1 && n - n0 < 4; ++n) {
-                const R g = grow[((n % p.T) + p.T) % p.T];
+                const R g = grow[idx];
+                if (++idx == p.T) idx = 0;
                 const R wgt = ((R)n * dPsi - tp) * inv;
                 rp += g * wgt;
                 lp += g * ((R)1 - wgt);
@@ -461,6 +484,7 @@ extern "C" int acum_tonal_adjoint(acum_ctx* ctx, int precision, const double* dJ
     p.dTau = ctx->der.dTau;
     p.oM = ctx->der.oM;
     p.dPsi = ctx->der.dPsi;
+    p.tmod = (unsigned)((0x100000000ull + (unsigned long long)ctx->T - 1) / (unsigned long long)ctx->T);
     CKA(s->cot.ensure((size_t)E * T * kCot));
     p.cot = s->cot.p;
     const long long warps = E * p.nWa;
