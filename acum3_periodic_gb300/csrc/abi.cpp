@@ -219,6 +219,31 @@ extern "C" int acum_update_surfaces(acum_ctx* ctx, const float* raw, int raw_on_
     return ACUM_OK;
 }
 
+extern "C" int acum_read_deck_sizes(const char* dir, long long* out)
+{
+    if (!dir || !out) return fail(nullptr, ACUM_ERR_INVALID, "acum_read_deck_sizes: null argument");
+    std::string d(dir), err;
+    acum_inputs in;
+    int ns = 0, nob = 0;
+    std::vector<float> obs, raw;
+    std::vector<int> ne;
+    if (!read_inputs(d, in, ns, &err)) return fail(nullptr, ACUM_ERR_IO, err);
+    BBDeck bb;
+    if (in.BB_noise == 1 && !read_bb(d, ns, in.nTime, bb, &err)) return fail(nullptr, ACUM_ERR_IO, err);
+    if (!read_observers(d, obs, nob, &err)) return fail(nullptr, ACUM_ERR_IO, err);
+    if (!read_surfaces(d, ns, in.nTime, ne, raw, &err)) return fail(nullptr, ACUM_ERR_IO, err);
+    long long E = 0, bbs = 0;
+    for (int x : ne) E += x;
+    for (int n : bb.nsect) bbs += n;
+    out[0] = ns;
+    out[1] = in.nTime;
+    out[2] = nob;
+    out[3] = E;
+    out[4] = in.BB_noise == 1 ? bbs : 0;
+    out[5] = in.BB_noise == 1 ? 1 : 0;
+    return ACUM_OK;
+}
+
 extern "C" int acum_load_deck(acum_ctx* ctx, const char* dir)
 {
     if (!ctx || !dir) return fail(ctx, ACUM_ERR_INVALID, "acum_load_deck: null argument");

@@ -71,6 +71,7 @@ SIGNATURES = {
     "acum_surfaces_device_ptr": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "acum_mark_surfaces_changed": (C.c_int, [C.c_void_p]),
     "acum_sync": (C.c_int, [C.c_void_p]),
+    "acum_read_deck_sizes": (C.c_int, [C.c_char_p, C.POINTER(C.c_longlong)]),
     "acum_last_plan": (C.c_int, [C.c_void_p, _IP]),
     "acum_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "acum_bpm": (C.c_int, [C.c_void_p, C.c_int, _DP, _DP]),

@@ -102,6 +102,9 @@ typedef struct {
 int acum_set_bb(acum_ctx* ctx, const acum_bb_desc* bb);
 
 /* sizes: out[0]=nSurf, [1]=nTime, [2]=nObs, [3]=elements, [4]=BB sections, [5]=BB_noise */
+/* Parses and validates a deck directory on the host only (no device needed): the same
+ * readers and checks as acum_load_deck.  out[6] as acum_get_sizes. */
+int acum_read_deck_sizes(const char* dir, long long* out);
 int acum_get_sizes(const acum_ctx* ctx, long long* out);
 
 /* Uploads what is not on the device yet and runs preprocess_imper's steps on the GPU
