@@ -198,6 +198,7 @@ int acum_ctx::upload_deck_common(const acum_inputs& inp, int nob, const float* o
 extern "C" int acum_set_deck(acum_ctx* ctx, const acum_inputs* in, int nobs, const float* obs_file, int nsurf,
                              const int* nelem, const float* raw, int raw_on_device)
 {
+    acum::NvtxRange nvtx_range_("acum_set_deck");
     if (!ctx || !in || !obs_file || !nelem || !raw) return fail(ctx, ACUM_ERR_INVALID, "acum_set_deck: null argument");
     int rc = ctx->upload_deck_common(*in, nobs, obs_file, nsurf, nelem);
     if (rc) return rc;
@@ -221,6 +222,7 @@ extern "C" int acum_update_surfaces(acum_ctx* ctx, const float* raw, int raw_on_
 
 extern "C" int acum_read_deck_sizes(const char* dir, long long* out)
 {
+    acum::NvtxRange nvtx_range_("acum_read_deck_sizes");
     if (!dir || !out) return fail(nullptr, ACUM_ERR_INVALID, "acum_read_deck_sizes: null argument");
     std::string d(dir), err;
     acum_inputs in;
@@ -246,6 +248,7 @@ extern "C" int acum_read_deck_sizes(const char* dir, long long* out)
 
 extern "C" int acum_load_deck(acum_ctx* ctx, const char* dir)
 {
+    acum::NvtxRange nvtx_range_("acum_load_deck");
     if (!ctx || !dir) return fail(ctx, ACUM_ERR_INVALID, "acum_load_deck: null argument");
     std::string d(dir), err;
     acum_inputs in;
@@ -365,6 +368,7 @@ int acum_ctx::ensure_prep(bool need64, bool need32, bool need_fields)
 
 extern "C" int acum_preprocess(acum_ctx* ctx)
 {
+    acum::NvtxRange nvtx_range_("acum_preprocess");
     if (!ctx) return ACUM_ERR_INVALID;
     if (!ctx->have_deck) return fail(ctx, ACUM_ERR_STATE, "no deck");
     ctx->begin_run();
@@ -452,6 +456,7 @@ int acum_ctx::finish_run()
 
 extern "C" int acum_tonal_device(acum_ctx* ctx, int precision, double* d_pT, double* d_pL, double* d_pA)
 {
+    acum::NvtxRange nvtx_range_("acum_tonal_device");
     if (!ctx) return ACUM_ERR_INVALID;
     if (!ctx->have_deck) return fail(ctx, ACUM_ERR_STATE, "no deck");
     ctx->begin_run();
@@ -497,6 +502,7 @@ extern "C" int acum_sync(acum_ctx* ctx)
 
 extern "C" int acum_tonal(acum_ctx* ctx, int precision, double* pT, double* pL, double* pA)
 {
+    acum::NvtxRange nvtx_range_("acum_tonal");
     if (!ctx) return ACUM_ERR_INVALID;
     if (!ctx->have_deck) return fail(ctx, ACUM_ERR_STATE, "no deck");
     DeviceGuard g(ctx->device);
@@ -521,6 +527,7 @@ extern "C" int acum_tonal(acum_ctx* ctx, int precision, double* pT, double* pL, 
 
 extern "C" int acum_tonal_from_host(acum_ctx* ctx, int precision, const float* raw, double* pA_host)
 {
+    acum::NvtxRange nvtx_range_("acum_tonal_from_host");
     if (!ctx || !raw || !pA_host) return fail(ctx, ACUM_ERR_INVALID, "acum_tonal_from_host: null argument");
     if (!ctx->have_deck) return fail(ctx, ACUM_ERR_STATE, "no deck");
     DeviceGuard g(ctx->device);
@@ -580,6 +587,7 @@ extern "C" int acum_last_timing(const acum_ctx* ctx, int which, double* ms, long
 
 extern "C" int acum_write_outputs(acum_ctx* ctx, const char* dir)
 {
+    acum::NvtxRange nvtx_range_("acum_write_outputs");
     if (!ctx || !dir) return ACUM_ERR_INVALID;
     std::string err;
     if (ctx->have_tonal) {
@@ -772,6 +780,7 @@ extern "C" int acum_find_pressure_time_history(const float* rObs, const float* t
                                                float dPsi, float dTau, float a0, float rhoRef, const float* vInf,
                                                float oM, void* stream)
 {
+    acum::NvtxRange nvtx_range_("acum_find_pressure_time_history");
     return find_pth<float>(rObs, tObs, pT, pL, pA, Xham, Nham, Vham, PRham, nSurf, XPtr, NPtr, VPtr, PRPtr, E, nObs,
                            nTime, dPsi, dTau, a0, rhoRef, vInf, oM, stream);
 }
@@ -783,6 +792,7 @@ extern "C" int acum_find_pressure_time_history_f64(const double* rObs, const dou
                                                    int nObs, int nTime, double dPsi, double dTau, double a0,
                                                    double rhoRef, const double* vInf, double oM, void* stream)
 {
+    acum::NvtxRange nvtx_range_("acum_find_pressure_time_history_f64");
     return find_pth<double>(rObs, tObs, pT, pL, pA, Xham, Nham, Vham, PRham, nSurf, XPtr, NPtr, VPtr, PRPtr, E, nObs,
                             nTime, dPsi, dTau, a0, rhoRef, vInf, oM, stream);
 }
@@ -792,6 +802,7 @@ extern "C" int acum_preprocess_imper(float* Xham, float* Nham, float* Vham, floa
                                      float dTau, float a0, float rhoRef, float Mref, float CFDscale, int periodic,
                                      int lowpass)
 {
+    acum::NvtxRange nvtx_range_("acum_preprocess_imper");
     if (!Xham || !Nham || !Vham || !PRham || !XPtr || !NPtr || !VPtr || !PRPtr || !E || nSurf <= 0 || nTime < 4)
         return fail(nullptr, ACUM_ERR_INVALID, "preprocess_imper: bad argument");
     int dev = 0;

@@ -434,6 +434,7 @@ using namespace acum;
 extern "C" int acum_tonal_adjoint(acum_ctx* ctx, int precision, const double* dJ_dpA, double* J, double* g_cp,
                                   double* g_x, double* g_n)
 {
+    acum::NvtxRange nvtx_range_("acum_tonal_adjoint");
     if (!ctx) return ACUM_ERR_INVALID;
     if (!ctx->have_deck) return fail(ctx, ACUM_ERR_STATE, "no deck");
     if (precision != ACUM_PLAIN_FP64 && precision != ACUM_MIXED) return fail(ctx, ACUM_ERR_INVALID, "precision");

@@ -284,6 +284,7 @@ extern "C" const char* acum_batch_last_error(const acum_batch* b) { return b ? b
 extern "C" int acum_batch_add(acum_batch* b, const acum_inputs* in, int nobs, const float* obs_file, int nsurf,
                               const int* nelem, const float* raw, int* case_id)
 {
+    acum::NvtxRange nvtx_range_("acum_batch_add");
     if (!b || !in || !obs_file || !nelem || !raw) return bfail(b, ACUM_ERR_INVALID, "acum_batch_add: null argument");
     if (nsurf <= 0 || nobs <= 0 || in->nTime < 6) return bfail(b, ACUM_ERR_INVALID, "acum_batch_add: bad sizes");
     long long E = 0;
@@ -337,12 +338,14 @@ extern "C" int acum_batch_count(const acum_batch* b, int* ncase)
 
 extern "C" int acum_batch_prepare(acum_batch* b)
 {
+    acum::NvtxRange nvtx_range_("acum_batch_prepare");
     if (!b) return ACUM_ERR_INVALID;
     return plan(b);
 }
 
 extern "C" int acum_batch_run(acum_batch* b, int precision, int mode)
 {
+    acum::NvtxRange nvtx_range_("acum_batch_run");
     if (!b) return ACUM_ERR_INVALID;
     if (precision != ACUM_MIXED) return bfail(b, ACUM_ERR_UNSUPPORTED, "batched runs are mixed precision only");
     if (mode < 0 || mode > 2) return bfail(b, ACUM_ERR_INVALID, "mode must be 0, 1 or 2");
@@ -452,6 +455,7 @@ extern "C" int acum_batch_get_tile(const acum_batch* b, int* obs_per_block, int*
 
 extern "C" int acum_batch_autotune(acum_batch* b, int sample_stride, double* best_ms)
 {
+    acum::NvtxRange nvtx_range_("acum_batch_autotune");
     if (!b) return ACUM_ERR_INVALID;
     if (b->cases.empty()) return bfail(b, ACUM_ERR_STATE, "the batch has no cases");
     if (sample_stride < 1) return bfail(b, ACUM_ERR_INVALID, "sample_stride must be >= 1");

@@ -846,6 +846,7 @@ using namespace acum;
 
 extern "C" int acum_set_bb(acum_ctx* ctx, const acum_bb_desc* b)
 {
+    acum::NvtxRange nvtx_range_("acum_set_bb");
     if (!ctx || !b) return fail(ctx, ACUM_ERR_INVALID, "acum_set_bb: null argument");
     if (!ctx->have_deck) return fail(ctx, ACUM_ERR_STATE, "acum_set_bb: set the tonal deck first");
     if (b->nsurf <= 0 || b->nsurf > ctx->nsurf)
@@ -905,6 +906,7 @@ extern "C" int acum_set_bb(acum_ctx* ctx, const acum_bb_desc* b)
 
 extern "C" int acum_bpm(acum_ctx* ctx, int aa_mode, double* BBspl, double* BBoaspl)
 {
+    acum::NvtxRange nvtx_range_("acum_bpm");
     if (!ctx) return ACUM_ERR_INVALID;
     ctx->begin_run();
     return bpm_run(ctx, aa_mode, nullptr, nullptr, BBspl, BBoaspl);
@@ -920,6 +922,7 @@ extern "C" int acum_find_bb_noise(int nSurf_BB, int nObs, int nTime, float dTau,
                                   int t_del, const float* vInf, const float* rObs, const float* tObs, int nf2,
                                   const float* ff, float a0, float* BBspl, float* BBoaspl)
 {
+    acum::NvtxRange nvtx_range_("acum_find_bb_noise");
     (void)tObs;
     if (nSurf_BB <= 0 || nObs <= 0 || nTime < 6 || !span || !omega || !ccw || !psi_offset || !trip || !rotate ||
         !translate || !xsPtr || !dsPtr || !nsect || !xyzcR || !bbdata || !nsect_t || !nmach_t || !naoa_t || !nre_t ||

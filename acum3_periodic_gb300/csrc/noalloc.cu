@@ -100,6 +100,7 @@ extern "C" int acum_find_pressure_time_history_noalloc(const float* rObs, const 
                                                        float dPsi, float dTau, float a0, float rhoRef,
                                                        const float* vInf, float oM, void* stream)
 {
+    acum::NvtxRange nvtx_range_("acum_find_pressure_time_history_noalloc");
     (void)tObs;
     auto bad = [](int code, const char* m) {
         snprintf(g_na_msg, sizeof g_na_msg, "%s", m);
