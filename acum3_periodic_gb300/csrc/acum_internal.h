@@ -44,6 +44,7 @@ struct TonalTile {
     int chunk;  // elements per work item (multiple of SE)
     int nchunk;
     int items;
+    int grid;         // blocks launched (the mixed kernel strides over the items)
     int flush_elems;  // mixed: elements summed in FP32 before the FP64 flush
     int opw;          // observers per warp
     size_t smem;
@@ -128,6 +129,7 @@ constexpr int kBatchNS = 4;
 // dynamic shared memory of the persistent kernel for W observers per block, elements per
 // stage SE and the longest case's nTime
 size_t batch_smem(int W, int SE, int Tmax);
+int batch_blocks_per_sm(int W, int SE, int Tmax);
 cudaError_t launch_tonal_batch(const KParams* d_cases, const BatchItem* d_items, int nitems, int* d_counter, int W,
                                int SE, int Tmax, int grid, cudaStream_t s);
 // acc [O][T][2] of every case -> pA [T][O] (overwrite)

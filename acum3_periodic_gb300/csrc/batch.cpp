@@ -103,7 +103,7 @@ TonalRun case_run(const acum_batch* b, const acum_ctx* c, double* acc)
     r.t.W = b->W;
     r.t.SE = b->SE;
     r.t.NS = kBatchNS;
-    r.t.flush_elems = 64;
+    r.t.flush_elems = 128;
     r.t.opw = 1;
     r.t.chunk = c->Epad;
     r.t.nchunk = 1;
@@ -133,12 +133,18 @@ void build_items(const acum_batch* b, int W, int SE, int ips, std::vector<BatchI
         const int groups = c->Epad / SE;
         const double per_tile = (double)W * c->Epad * c->T;
         int nchunk = (int)std::ceil(per_tile / std::max(target, 1.0));
+        // element chunks of at most ~16 MB of records, so that the items of one chunk,
+        // which run close together in time, share it in L2
+        const size_t per_elem = (size_t)c->nW * kGroups * kWin * 4 * sizeof(float);
+        const int max_groups = std::max(1, (int)(((size_t)16 << 20) / per_elem) / SE);
+        nchunk = std::max(nchunk, (groups + max_groups - 1) / max_groups);
         nchunk = std::max(1, std::min(nchunk, groups));
         const int gpc = (groups + nchunk - 1) / nchunk;
-        for (int ot = 0; ot < tiles; ++ot) {
-            const int wobs = std::min(W, c->nobs - ot * W);
-            for (int g0 = 0; g0 < groups; g0 += gpc) {
-                const int e0 = g0 * SE, e1 = std::min(groups, g0 + gpc) * SE;
+        // chunk-major: equal-cost items of a case stay in this order after the sort
+        for (int g0 = 0; g0 < groups; g0 += gpc) {
+            const int e0 = g0 * SE, e1 = std::min(groups, g0 + gpc) * SE;
+            for (int ot = 0; ot < tiles; ++ot) {
+                const int wobs = std::min(W, c->nobs - ot * W);
                 v.push_back({(double)wobs * (e1 - e0) * c->T, BatchItem{(int)ci, ot, e0, e1}});
             }
         }
@@ -453,66 +459,154 @@ extern "C" int acum_batch_get_tile(const acum_batch* b, int* obs_per_block, int*
     return ACUM_OK;
 }
 
-extern "C" int acum_batch_autotune(acum_batch* b, int sample_stride, double* best_ms)
+namespace {
+
+// A probe work list: items of `chunk` elements (every observer tile of every case), every
+// k-th of them so that about `target` items remain.  Returns the evaluations it holds.
+double probe_items(const acum_batch* b, int W, int SE, int chunk, long target, std::vector<BatchItem>& out)
+{
+    std::vector<BatchItem> all;
+    std::vector<double> cost;
+    for (size_t ci = 0; ci < b->cases.size(); ++ci) {
+        const acum_ctx* c = b->cases[ci];
+        const int tiles = (c->nobs + W - 1) / W;
+        for (int e0 = 0; e0 < c->Epad; e0 += chunk)
+            for (int ot = 0; ot < tiles; ++ot) {
+                const int e1 = std::min(c->Epad, e0 + chunk) / SE * SE;
+                if (e1 <= e0) continue;
+                all.push_back(BatchItem{(int)ci, ot, e0, e1});
+                cost.push_back((double)std::min(W, c->nobs - ot * W) * (e1 - e0) * c->T);
+            }
+    }
+    const size_t k = std::max<size_t>(1, all.size() / (size_t)std::max<long>(1, target));
+    out.clear();
+    double ev = 0;
+    for (size_t i = 0; i < all.size(); i += k) {
+        out.push_back(all[i]);
+        ev += cost[i];
+    }
+    return ev;
+}
+
+// device time of one persistent launch over `items` (the second of two launches)
+int time_items(acum_batch* b, DBuf<BatchItem>& d, const std::vector<BatchItem>& items, double* ms)
+{
+    BK(b, d.ensure(items.size()));
+    BK(b, cudaMemcpy(d.p, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice));
+    float f = 0;
+    for (int rep = 0; rep < 2; ++rep) {
+        BK(b, cudaEventRecord(b->ev0, b->stream));
+        int rc = enqueue_persistent(b, d.p, (int)items.size(), false);
+        if (rc) return rc;
+        BK(b, cudaEventRecord(b->ev1, b->stream));
+        BK(b, cudaStreamSynchronize(b->stream));
+        BK(b, cudaEventElapsedTime(&f, b->ev0, b->ev1));
+    }
+    *ms = f;
+    return check_err(b);
+}
+
+// Greedy list scheduling of the work list (largest first) on `slots` blocks that each
+// take the next item when they finish one: the predicted makespan in ms.
+double makespan(const acum_batch* b, const std::vector<BatchItem>& items, int W, int slots, double ms_per_eval,
+                double ms_per_item)
+{
+    std::vector<double> heap(slots, 0.0);  // min-heap of block finish times
+    auto cmp = [](double x, double y) { return x > y; };
+    std::make_heap(heap.begin(), heap.end(), cmp);
+    double end = 0;
+    for (const BatchItem& it : items) {
+        const acum_ctx* c = b->cases[it.c];
+        const double ev = (double)std::min(W, c->nobs - it.ot * W) * (it.e1 - it.e0) * c->T;
+        std::pop_heap(heap.begin(), heap.end(), cmp);
+        const double t = heap.back() + ms_per_item + ev * ms_per_eval;
+        heap.back() = t;
+        std::push_heap(heap.begin(), heap.end(), cmp);
+        end = std::max(end, t);
+    }
+    return end;
+}
+
+}  // namespace
+
+extern "C" int acum_batch_autotune(acum_batch* b, int probe_per_sm, double* best_ms)
 {
     acum::NvtxRange nvtx_range_("acum_batch_autotune");
     if (!b) return ACUM_ERR_INVALID;
     if (b->cases.empty()) return bfail(b, ACUM_ERR_STATE, "the batch has no cases");
-    if (sample_stride < 1) return bfail(b, ACUM_ERR_INVALID, "sample_stride must be >= 1");
+    if (probe_per_sm < 0) return bfail(b, ACUM_ERR_INVALID, "probe_per_sm must be >= 0");
+    const int per_sm = probe_per_sm > 0 ? probe_per_sm : 8;
     DeviceGuard g(b->device);
     b->Tmax = 0;
     for (const acum_ctx* c : b->cases) b->Tmax = std::max(b->Tmax, c->T);
-    const int Ws[] = {8, 12, 16}, SEs[] = {2, 4}, IPS[] = {4, 8, 16};
-    double best = 1e300;
-    int bw = b->W, bse = b->SE, bips = b->ips;
-    DBuf<BatchItem> d_sample;
+    const long target = (long)per_sm * b->num_sms;
+    // 1. kernel throughput of every (observers per block, elements per stage): one
+    //    persistent launch over a spread of 32-element items from all cases
+    const int Ws[] = {8, 12, 16}, SEs[] = {2, 4};
+    double best_rate = 0;
+    int bw = b->W, bse = b->SE;
+    DBuf<BatchItem> d_probe;
+    std::vector<BatchItem> probe;
     for (int W : Ws)
         for (int SE : SEs) {
             if (!shape_fits(b, W, SE)) continue;
-            for (int ips : IPS) {
-                b->W = W;
-                b->SE = SE;
-                b->ips = ips;
-                int rc = plan(b);
-                if (rc) return rc;
-                std::vector<BatchItem> s;
-                double frac_num = 0, frac_den = 0;
-                for (size_t k = 0; k < b->items.size(); ++k) {
-                    const BatchItem& it = b->items[k];
-                    const double cost = (double)(it.e1 - it.e0) * b->cases[it.c]->T;
-                    frac_den += cost;
-                    if (k % sample_stride == 0) {
-                        s.push_back(it);
-                        frac_num += cost;
-                    }
-                }
-                BK(b, d_sample.ensure(s.size()));
-                BK(b, cudaMemcpy(d_sample.p, s.data(), s.size() * sizeof(BatchItem), cudaMemcpyHostToDevice));
-                float ms = 0;
-                for (int rep = 0; rep < 2; ++rep) {  // the first launch warms up
-                    BK(b, cudaEventRecord(b->ev0, b->stream));
-                    rc = enqueue_persistent(b, d_sample.p, (int)s.size(), false);
-                    if (rc) return rc;
-                    BK(b, cudaEventRecord(b->ev1, b->stream));
-                    BK(b, cudaStreamSynchronize(b->stream));
-                    BK(b, cudaEventElapsedTime(&ms, b->ev0, b->ev1));
-                }
-                rc = check_err(b);
-                if (rc) return rc;
-                const double est = ms * (frac_den / std::max(frac_num, 1.0));
-                if (est < best) {
-                    best = est;
-                    bw = W;
-                    bse = SE;
-                    bips = ips;
-                }
+            b->W = W;
+            b->SE = SE;
+            int rc = plan(b);
+            if (rc) return rc;
+            const double ev = probe_items(b, W, SE, 32, target, probe);
+            double ms = 0;
+            rc = time_items(b, d_probe, probe, &ms);
+            if (rc) return rc;
+            const double rate = ev / std::max(ms, 1e-6);
+            if (rate > best_rate) {
+                best_rate = rate;
+                bw = W;
+                bse = SE;
             }
         }
-    d_sample.release();
+    // 2. for the fastest shape, the per-item and per-evaluation costs from two probes of
+    //    different item sizes, then items per SM by the predicted makespan of the
+    //    largest-first dynamic schedule
     b->W = bw;
     b->SE = bse;
-    b->ips = bips;
     int rc = plan(b);
+    if (rc) return rc;
+    double ev1 = probe_items(b, bw, bse, 32, target, probe), ms1 = 0;
+    const double n1 = (double)probe.size();
+    rc = time_items(b, d_probe, probe, &ms1);
+    if (rc) return rc;
+    double ev2 = probe_items(b, bw, bse, 128, target, probe), ms2 = 0;
+    const double n2 = (double)probe.size();
+    rc = time_items(b, d_probe, probe, &ms2);
+    if (rc) return rc;
+    d_probe.release();
+    const int slots = b->num_sms * batch_blocks_per_sm(bw, bse, b->Tmax);
+    // ms = (n ov + ev c) / slots for a launch whose items spread over all slots
+    double c_ev = 0, ov = 0;
+    const double det = n1 * ev2 - n2 * ev1;
+    if (std::fabs(det) > 0) {
+        ov = (ms1 * ev2 - ms2 * ev1) / det * slots;
+        c_ev = (n1 * ms2 - n2 * ms1) / det * slots;
+    }
+    if (!(c_ev > 0) || !(ov >= 0)) {  // noisy probes: per-evaluation cost only
+        c_ev = ms2 * slots / std::max(ev2, 1.0);
+        ov = 0;
+    }
+    double best = 1e300;
+    int bips = b->ips;
+    for (int ips : {4, 8, 16, 32}) {
+        b->ips = ips;
+        std::vector<BatchItem> items;
+        build_items(b, bw, bse, ips, items);
+        const double t = makespan(b, items, bw, slots, c_ev, ov);
+        if (t < best) {
+            best = t;
+            bips = ips;
+        }
+    }
+    b->ips = bips;
+    rc = plan(b);
     if (rc) return rc;
     b->have_result = false;
     if (best_ms) *best_ms = best;

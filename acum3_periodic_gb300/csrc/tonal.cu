@@ -336,49 +336,6 @@ struct SmpD {
     double pt, pl;
 };
 
-// Farassat-1A integrand with U = V and the normal-velocity rates forced to 0
-// (core.cu:93-154), rearranged around K = Mdot_r + (a0/r)(Mr - M^2):
-//   pThick = ATD/r * G^3 * K
-//   pLoad  = dsD/r * G^2 * (Ldot_r + (a0/r)(L_r - L_M) + L_r G K),  G = 1/(1-Mr)
-// where the records carry D1 = 1/(4 pi a0) inside ATD and dsD.
-__device__ __forceinline__ SmpF sample_mixed(const float4& g0, const float4& g1, const float4& g2, const float4& g3,
-                                             const float4& g4, float ox, float oy, float oz, const KParams& p,
-                                             int tau)
-{
-    const float dx = ox - g0.x, dy = oy - g0.y, dz = oz - g0.z;
-    const float c = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    const float beta = fmaf(dx, p.vxf, fmaf(dy, p.vyf, dz * p.vzf));
-    // retarded time: positive root of (|v|^2 - a0^2) t^2 - 2 beta t + c = 0 (core.cu:261-279)
-    const float q2 = fmaf(beta, beta, p.alphaf * c);
-    const float s = q2 * rsqrtf(q2);
-    const float tr = (s - beta) * p.ialphaf;
-    const float rx = fmaf(-p.vxf, tr, dx), ry = fmaf(-p.vyf, tr, dy), rz = fmaf(-p.vzf, tr, dz);
-    const float r = p.a0f * tr;
-    const float ir = __fdividef(1.0f, r);
-    const float Mr = fmaf(g1.x, rx, fmaf(g1.y, ry, g1.z * rz)) * ir;
-    const float Mdr = fmaf(g2.x, rx, fmaf(g2.y, ry, g2.z * rz)) * ir;
-    const float Lr = fmaf(g3.x, rx, fmaf(g3.y, ry, g3.z * rz)) * ir;
-    const float Ldr = fmaf(g4.x, rx, fmaf(g4.y, ry, g4.z * rz)) * ir;
-    const float G = __fdividef(1.0f, 1.0f - Mr);
-    const float qa = p.a0f * ir;
-    const float K = fmaf(qa, Mr - g1.w, Mdr);
-    const float base = ir * G * G;
-    SmpF o;
-    o.pt = g2.w * base * G * K;
-    o.pl = g0.w * base * fmaf(Lr * G, K, fmaf(qa, Lr - g3.w, Ldr));
-    // observer time in bins: tau + tr * (oM / dPsi), the product kept as a float pair
-    const float ph = tr * p.kbhi;
-    const float pe = fmaf(tr, p.kbhi, -ph) + tr * p.kblo;
-    const float n0 = floorf(ph);
-    float f = (ph - n0) + pe;
-    int k = tau + (int)n0;
-    if (f >= 1.0f) { f -= 1.0f; k += 1; }
-    else if (f < 0.0f) { f += 1.0f; k -= 1; }
-    o.k = k;
-    o.f = f;
-    return o;
-}
-
 __device__ __forceinline__ SmpD sample_f64(const dbl4& g0, const dbl4& g1, const dbl4& g2, const dbl4& g3,
                                            const dbl4& g4, double ox, double oy, double oz, const KParams& p, int tau)
 {
@@ -405,15 +362,6 @@ __device__ __forceinline__ SmpD sample_f64(const dbl4& g0, const dbl4& g1, const
     o.t = (tau * p.dTau + tr) * p.oM;
     o.nb = (int)floor(o.t / p.dPsi);
     return o;
-}
-
-__device__ __forceinline__ int wrap_bin(int n, int T, float invT)
-{
-    int q = __float2int_rz((float)n * invT);
-    int r = n - q * T;
-    if (r < 0) r += T;
-    else if (r >= T) r -= T;
-    return r;
 }
 
 __device__ __forceinline__ void deposit_f64(double2* acc, int T, const KParams& p, const SmpD& a, const SmpD& b,
@@ -665,98 +613,36 @@ __global__ void __launch_bounds__(512, 1) tonal_f64_kernel(const KParams p)
     }
 }
 
-// ----------------------------------------------------------- mixed kernel v2
+// ------------------------------------------------------------------ mixed form
 //
-// The mixed form's kernel.  Each warp serves OPW observers, so a record loaded from
-// shared memory feeds OPW evaluations, and each lane carries OPW x SE independent
-// samples per stage (instruction-level parallelism in place of more warps).  The left
-// neighbour of lane l's sample comes from one rotating shuffle (lane l-1); lane 0 keeps
-// what it received in the previous window (the previous window's lane 31), and the first
-// sample of an element stays in lane 0 for the periodic wrap at its end.
+// One warp per observer; lane = source step of a 32-step window; each lane carries SE
+// independent samples per stage (one per element of the stage).  The left neighbour of
+// lane l's sample comes from one rotating shuffle (lane l-1); lane 0 keeps what it
+// received in the previous window (the previous window's lane 31), and the first sample
+// of an element stays in lane 0 for the periodic wrap at its end.
 
-// RMW of one bin of a warp's observer row
-__device__ __forceinline__ void add_bin(float2* acc, int idx, float w, float pt, float dT, float pl, float dL)
-{
-    float2 v = acc[idx];
-    v.x += fmaf(w, dT, pt);
-    v.y += fmaf(w, dL, pl);
-    acc[idx] = v;
-}
+// Farassat-1A integrand with U = V and the normal-velocity rates forced to 0
+// (core.cu:93-154), rearranged around K = Mdot_r + (a0/r)(Mr - M^2):
+//   pThick = ATD/r * G^3 * K
+//   pLoad  = dsD/r * G^2 * (Ldot_r + (a0/r)(L_r - L_M) + L_r G K),  G = 1/(1-Mr)
+// where the records carry D1 = 1/(4 pi a0) inside ATD and dsD.
+//
+// Retarded time.  Per observer, the retarded time t0 from the origin is solved once in
+// FP64; each sample then solves for t = t0 + dt from the difference of the two retarded-
+// time quadratics (core.cu:261-279 form: alpha t^2 + 2 beta t - |d|^2 = 0),
+//     alpha dt^2 + 2 b dt - num = 0,   b = s0 + (d - D0).v,
+//     num = |d|^2 - |D0|^2 - 2 t0 (d - D0).v,   d - D0 = -x,   |d|^2 - |D0|^2 = -x.(d + D0)
+// (D0 = observer, x = source, s0 = alpha t0 + D0.v, x.v carried in the records), whose
+// terms are all of the size of the source's offset from the origin rather than of the
+// observer distance.  The observer time in bins, tau + t0 oM/dPsi + dt oM/dPsi, keeps the
+// first part split exactly (FP64) into an integer and a fraction, so FP32 rounding
+// applies to dt only.  The integer part of the remainder is rounded to nearest by the
+// 1.5 * 2^23 addition (exact for |x| < 2^22, checked), leaving a fraction in [-0.5, 0.5];
+// bin indices are reduced modulo T by a multiply-high with m = ceil(2^32 / T).
 
-// bins in (u(a), u(b) + kshift]; cnt <= 2 whenever |Mr| < 1, handled without a loop
-__device__ __forceinline__ void deposit_v2(float2* acc, int T, float invT, const SmpF& a, const SmpF& b, int kshift,
-                                           bool active, DeviceErr* err)
-{
-    const int cnt = b.k + kshift - a.k;
-    const float du = (float)cnt + (b.f - a.f);
-    const bool fast = active && cnt >= 1 && cnt <= 2 && du > 0.0f;
-    if (fast) {
-        const float inv = __fdividef(1.0f, du);
-        const float dT = b.pt - a.pt, dL = b.pl - a.pl;
-        int idx = wrap_bin(a.k + 1, T, invT);
-        const float w1 = (1.0f - a.f) * inv;
-        add_bin(acc, idx, w1, a.pt, dT, a.pl, dL);
-        if (cnt == 2) {
-            if (++idx == T) idx = 0;
-            add_bin(acc, idx, w1 + inv, a.pt, dT, a.pl, dL);
-        }
-    } else if (active && !(cnt == 0 && du > 0.0f)) {
-        // more than two bins in one step (a step faster than the bin rate: |Mr| > 1) or a
-        // decreasing / non-finite observer time
-        if (cnt > 2 && cnt <= T && du > 0.0f) {
-            const float inv = __fdividef(1.0f, du);
-            const float dT = b.pt - a.pt, dL = b.pl - a.pl;
-            int idx = wrap_bin(a.k + 1, T, invT);
-            for (int m = 1; m <= cnt; ++m) {
-                add_bin(acc, idx, ((float)m - a.f) * inv, a.pt, dT, a.pl, dL);
-                if (++idx == T) idx = 0;
-            }
-        } else {
-            flag(err, ACUM_DEVERR_ORDER, &err->order);
-        }
-    }
-}
-
-__device__ __forceinline__ SmpF shfl_idx(const SmpF& v, int src)
-{
-    SmpF o;
-    o.k = __shfl_sync(0xffffffffu, v.k, src);
-    o.f = __shfl_sync(0xffffffffu, v.f, src);
-    o.pt = __shfl_sync(0xffffffffu, v.pt, src);
-    o.pl = __shfl_sync(0xffffffffu, v.pl, src);
-    return o;
-}
-
-// Block-wide shared state of the mixed kernels besides the dynamic shared memory.
-struct MixedShared {
-    int abort;
-    int release[kMaxStages];
-    int last[kMaxStages];
-};
-
-// One work item of the mixed form: observers [ot*W, ot*W + W) and elements [e0, e1)
-// (a multiple of SE) of the case `p`.  The dynamic shared memory holds the warps' FP32
-// bin rows (W x acc_T float2, laid out for the item's T) followed by the NS-stage ring;
-// `stage_off` is where the ring starts (fixed for a launch).  `gbase` counts the stages
-// the block has consumed before this item, so consecutive items of a persistent block
-// continue the mbarrier phases of the same ring.  On entry every slot is free and all
-// bin rows are zero; on return (without abort) the same holds again.
-// Lean forms of the observer time and the deposit: the integer part of the observer time
-// is rounded to nearest by the 1.5 * 2^23 addition (exact for |x| < 2^22, checked), so the
-// fraction lies in [-0.5, 0.5]; the bin index is reduced modulo T by a multiply-high with
-// m = ceil(2^32 / T).  Both stay on the FMA and integer pipes.
 constexpr float kRound = 12582912.0f;  // 1.5 * 2^23
 constexpr int kRoundBits = 0x4B400000;
 
-// Per-observer constants of the anchored retarded time.  The anchor is the retarded time
-// t0 from the origin to the observer, solved once per observer in FP64; each sample then
-// solves for t = t0 + dt from the difference of the two retarded-time quadratics,
-//     alpha dt^2 + 2 b dt - num = 0,   b = s0 + (d - D0).v,
-//     num = |d|^2 - |D0|^2 - 2 t0 (d - D0).v,   d - D0 = -src,   |d|^2 - |D0|^2 = -src.(d + D0)
-// (D0 = observer, s0 = alpha t0 + D0.v), whose terms are all of the size of the source
-// offset from the origin rather than of the observer distance: dt, and with it the
-// observer time t0 * oM/dPsi + dt * oM/dPsi (the first part split exactly into an
-// integer and a fraction in FP64), carries FP32 rounding relative to dt only.
 struct Anchor {
     float t0, t2, s0, kf;  // t0, 2 t0, alpha t0 + D0.v, frac(t0 * oM / dPsi)
     int ki;                // round(t0 * oM / dPsi)
@@ -780,12 +666,12 @@ __device__ __forceinline__ Anchor make_anchor(const KParams& p, float ox, float 
     return a;
 }
 
-__device__ __forceinline__ SmpF sample_mixed_lean(const float4& g0, const float4& g1, const float4& g2,
-                                                  const float4& g3, const float4& g4, float ox, float oy, float oz,
-                                                  const Anchor& an, const KParams& p, int tau, DeviceErr* err)
+__device__ __forceinline__ SmpF sample_mixed(const float4& g0, const float4& g1, const float4& g2, const float4& g3,
+                                             const float4& g4, float ox, float oy, float oz, const Anchor& an,
+                                             const KParams& p, int tau, DeviceErr* err)
 {
     const float dx = ox - g0.x, dy = oy - g0.y, dz = oz - g0.z;
-    // anchored retarded time (g4.w = src.v)
+    // anchored retarded time (g4.w = x.v)
     const float cc = -fmaf(g0.x, dx + ox, fmaf(g0.y, dy + oy, g0.z * (dz + oz)));
     const float num = fmaf(an.t2, g4.w, cc);
     const float bp = an.s0 - g4.w;
@@ -827,9 +713,20 @@ __device__ __forceinline__ float small_int_to_float(int v)
     return __int_as_float(v + kRoundBits) - kRound;  // exact for |v| < 2^22
 }
 
-// bins n with u(a) < n <= u(b) + kshift, u = k + f with f in [-0.5, 0.5]
-__device__ __forceinline__ void deposit_lean(float2* acc, int T, unsigned tm, const SmpF& a, const SmpF& b,
-                                             int kshift, bool active, DeviceErr* err)
+// RMW of one bin of a warp's observer row
+__device__ __forceinline__ void add_bin(float2* acc, int idx, float w, float pt, float dT, float pl, float dL)
+{
+    float2 v = acc[idx];
+    v.x += fmaf(w, dT, pt);
+    v.y += fmaf(w, dL, pl);
+    acc[idx] = v;
+}
+
+// bins n with u(a) < n <= u(b) + kshift, u = k + f with f in [-0.5, 0.5], the value
+// interpolated between the two samples.  For |Mr| < 1 an interval holds at most 2 bins
+// (u(b) - u(a) = 1 - Mr < 2): the first bin is unrolled and the second conditional.
+__device__ __forceinline__ void deposit(float2* acc, int T, unsigned tm, const SmpF& a, const SmpF& b, int kshift,
+                                        bool active, DeviceErr* err)
 {
     const int dk = b.k + kshift - a.k;
     const bool a_up = a.f >= 0.0f;  // floor(u(a)) = k(a) - 1 + a_up
@@ -847,6 +744,7 @@ __device__ __forceinline__ void deposit_lean(float2* acc, int T, unsigned tm, co
             add_bin(acc, idx, w1 + inv, a.pt, dT, a.pl, dL);
         }
     } else if (active && !(cnt == 0 && du > 0.0f)) {
+        // more than two bins in one step (|Mr| > 1) or a decreasing / non-finite time
         if (cnt > 2 && cnt <= T && du > 0.0f) {
             const float inv = __fdividef(1.0f, du);
             const float dT = b.pt - a.pt, dL = b.pl - a.pl;
@@ -862,14 +760,38 @@ __device__ __forceinline__ void deposit_lean(float2* acc, int T, unsigned tm, co
     }
 }
 
-template <int OPW, int SE, bool LEAN>
+__device__ __forceinline__ SmpF shfl_idx(const SmpF& v, int src)
+{
+    SmpF o;
+    o.k = __shfl_sync(0xffffffffu, v.k, src);
+    o.f = __shfl_sync(0xffffffffu, v.f, src);
+    o.pt = __shfl_sync(0xffffffffu, v.pt, src);
+    o.pl = __shfl_sync(0xffffffffu, v.pl, src);
+    return o;
+}
+
+// Block-wide shared state of the mixed kernels besides the dynamic shared memory.
+struct MixedShared {
+    int abort;
+    int release[kMaxStages];
+    int last[kMaxStages];
+};
+
+// One work item of the mixed form: observers [ot*W, ot*W + W) and elements [e0, e1)
+// (a multiple of SE) of the deck `p`.  The dynamic shared memory holds the warps' FP32
+// bin rows (W x T float2, laid out for the item's T) followed by the NS-stage ring;
+// `stage_off` is where the ring starts (fixed for a launch).  `gbase` counts the stages
+// the block has consumed before this item, so consecutive items of a block continue the
+// mbarrier phases of the same ring.  On entry every slot is free and all bin rows are
+// zero; on return (without abort) the same holds again.
+template <int SE>
 __device__ __forceinline__ void mixed_item(const KParams& p, int ot, int e0, int e1, unsigned char* smem,
                                            size_t stage_off, MixedShared& sh, unsigned& gbase)
 {
     constexpr int kTile = kGroups * kWin * 4;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nwarps = blockDim.x >> 5;
-    const int W = p.W;  // observers per block = nwarps * OPW
+    const int W = p.W;  // observers per block = warps
     const int T = p.T, NS = p.NS, nW = p.nW;
     float2* acc_all = reinterpret_cast<float2*>(smem);
     float* stages = reinterpret_cast<float*>(smem + stage_off);
@@ -893,23 +815,13 @@ __device__ __forceinline__ void mixed_item(const KParams& p, int ot, int e0, int
     if (threadIdx.x == 0)
         for (int i = 0; i < NS && i < N; ++i) issue(i);
 
-    float ox[OPW], oy[OPW], oz[OPW];
-    bool oks[OPW];
-    float2* acc[OPW];
-    Anchor anc[OPW];
-#pragma unroll
-    for (int q = 0; q < OPW; ++q) {
-        const int o = ot * W + warp * OPW + q;
-        oks[q] = o < p.O;
-        const int oc = oks[q] ? o : 0;
-        ox[q] = p.obs32[3 * oc];
-        oy[q] = p.obs32[3 * oc + 1];
-        oz[q] = p.obs32[3 * oc + 2];
-        acc[q] = acc_all + (size_t)(warp * OPW + q) * T;
-        if (LEAN) anc[q] = make_anchor(p, ox[q], oy[q], oz[q]);
-    }
-    SmpF carry[OPW][SE], first[OPW][SE];
-    const float invT = p.invTf;
+    const int o = ot * W + warp;
+    const bool ok_obs = o < p.O;
+    const int oc = ok_obs ? o : 0;
+    const float ox = p.obs32[3 * oc], oy = p.obs32[3 * oc + 1], oz = p.obs32[3 * oc + 2];
+    float2* acc = acc_all + (size_t)warp * T;
+    const Anchor anc = make_anchor(p, ox, oy, oz);
+    SmpF carry[SE], first[SE];
 
     int s = (int)(g0 % (unsigned)NS), w = 0, g = 0, since_flush = 0;
     uint32_t par = (g0 / (unsigned)NS) & 1u;
@@ -926,52 +838,34 @@ __device__ __forceinline__ void mixed_item(const KParams& p, int ot, int e0, int
         const int tau = w * kWin + lane;
         const bool valid = tau < T;
         const float* st = stages + (size_t)s * SE * kTile;
-        SmpF cur[OPW][SE];
+        SmpF cur[SE];
 #pragma unroll
         for (int j = 0; j < SE; ++j) {
             const float* tl = st + (size_t)j * kTile + lane * 4;
             float4 gg[kGroups];
 #pragma unroll
             for (int q = 0; q < kGroups; ++q) gg[q] = *reinterpret_cast<const float4*>(tl + q * kWin * 4);
-#pragma unroll
-            for (int q = 0; q < OPW; ++q) {
-                if (LEAN)
-                    cur[q][j] = sample_mixed_lean(gg[0], gg[1], gg[2], gg[3], gg[4], ox[q], oy[q], oz[q], anc[q], p,
-                                                  tau, p.err);
-                else
-                    cur[q][j] = sample_mixed(gg[0], gg[1], gg[2], gg[3], gg[4], ox[q], oy[q], oz[q], p, tau);
-            }
+            cur[j] = sample_mixed(gg[0], gg[1], gg[2], gg[3], gg[4], ox, oy, oz, anc, p, tau, p.err);
         }
         const bool first_win = w == 0, last_win = w == nW - 1;
         const int rot_src = (lane + 31) & 31;
 #pragma unroll
-        for (int q = 0; q < OPW; ++q) {
-#pragma unroll
-            for (int j = 0; j < SE; ++j) {
-                const SmpF rot = shfl_idx(cur[q][j], rot_src);
-                const SmpF prev = lane == 0 ? carry[q][j] : rot;
-                const bool act = oks[q] && valid && !(first_win && lane == 0);
-                if (LEAN) deposit_lean(acc[q], T, p.tmod, prev, cur[q][j], 0, act, p.err);
-                else deposit_v2(acc[q], T, invT, prev, cur[q][j], 0, act, p.err);
-                carry[q][j] = rot;
-                if (first_win && lane == 0) first[q][j] = cur[q][j];
-                if (last_win) {
-                    // the periodic wrap: (t(T-1), t(0) + period] (core.cu:173-194)
-                    const SmpF lastS = shfl_idx(cur[q][j], min(31, T - 1 - w * kWin));
-                    if (lane == 0) {
-                        if (LEAN) deposit_lean(acc[q], T, p.tmod, lastS, first[q][j], T, oks[q], p.err);
-                        else deposit_v2(acc[q], T, invT, lastS, first[q][j], T, oks[q], p.err);
-                    }
-                }
+        for (int j = 0; j < SE; ++j) {
+            const SmpF rot = shfl_idx(cur[j], rot_src);
+            const SmpF prev = lane == 0 ? carry[j] : rot;
+            deposit(acc, T, p.tmod, prev, cur[j], 0, ok_obs && valid && !(first_win && lane == 0), p.err);
+            carry[j] = rot;
+            if (first_win && lane == 0) first[j] = cur[j];
+            if (last_win) {
+                // the periodic wrap: (t(T-1), t(0) + period] (core.cu:173-194)
+                const SmpF lastS = shfl_idx(cur[j], min(31, T - 1 - w * kWin));
+                if (lane == 0) deposit(acc, T, p.tmod, lastS, first[j], T, ok_obs, p.err);
             }
         }
         // FP32 partial sums cover at most `flush_groups` element groups before they are
         // added to the FP64 sums in global memory
         if (last_win && (++since_flush == p.flush_groups || g == ngroups - 1)) {
-#pragma unroll
-            for (int q = 0; q < OPW; ++q)
-                if (oks[q])
-                    flush_bins(acc[q], p.acc + (size_t)(ot * W + warp * OPW + q) * T * 2, T, lane, false, p.err);
+            if (ok_obs) flush_bins(acc, p.acc + (size_t)o * T * 2, T, lane, false, p.err);
             since_flush = 0;
         }
         // release the slot; the last warp to finish with it refills it with stage i + NS
@@ -1024,29 +918,37 @@ __device__ __forceinline__ void mixed_drain(unsigned char* smem, size_t stage_of
     __syncthreads();
 }
 
-template <int OPW, int SE, bool LEAN>
-__global__ void __launch_bounds__(OPW == 1 ? 512 : 256, 1) tonal_mixed_kernel(const KParams p)
+// Single deck: block b takes the items b, b + grid, b + 2 grid, ... of the list ordered
+// element chunk first (item = chunk * obs_tiles + observer tile), so that the blocks
+// running at any time share one chunk of records in L2 and each record is read from
+// HBM about once per launch.
+template <int SE>
+__global__ void __launch_bounds__(512, 1) tonal_mixed_kernel(const KParams p)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ MixedShared sh;
     const size_t stage_off = acc_region_bytes(p.W, p.T, 8);
     mixed_init(smem, stage_off, p.NS, SE, sh);
-    const int item = blockIdx.x;
-    const int ot = item % p.obs_tiles, ec = item / p.obs_tiles;
-    const int e0 = ec * p.chunk;
-    const int e1 = min(e0 + p.chunk, p.Epad);
     unsigned gbase = 0;
-    mixed_item<OPW, SE, LEAN>(p, ot, e0, e1, smem, stage_off, sh, gbase);
-    __syncthreads();
-    if (sh.abort) mixed_drain(smem, stage_off, p.NS, SE, sh);
+    const int nitems = p.obs_tiles * p.nchunk;
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const int ot = item % p.obs_tiles, ec = item / p.obs_tiles;
+        const int e0 = ec * p.chunk;
+        const int e1 = min(e0 + p.chunk, p.Epad);
+        mixed_item<SE>(p, ot, e0, e1, smem, stage_off, sh, gbase);
+        __syncthreads();
+        if (sh.abort) {
+            mixed_drain(smem, stage_off, p.NS, SE, sh);
+            break;
+        }
+    }
 }
 
-// Persistent form over many cases: one block per SM takes work items from a shared
-// counter (largest first, as the host sorts them) until none are left.  Item k is
-// (case, observer tile, first element, end element); the case's constants are copied
-// into shared memory at the start of each item.
-
-template <int SE, bool LEAN>
+// Many decks: one block per SM (as many as fit) takes work items from a shared counter
+// (largest first, as the host sorts them) until none are left.  Item k is (case,
+// observer tile, first element, end element); the case's constants are copied into
+// shared memory at the start of each item.
+template <int SE>
 __global__ void __launch_bounds__(512, 1)
     tonal_batch_kernel(const KParams* __restrict__ cases, const BatchItem* __restrict__ items, int nitems,
                        int* counter, int NS, size_t stage_off)
@@ -1069,7 +971,7 @@ __global__ void __launch_bounds__(512, 1)
         for (int k = threadIdx.x; k < kWords; k += blockDim.x)
             reinterpret_cast<int*>(&sp)[k] = reinterpret_cast<const int*>(cases + it.c)[k];
         __syncthreads();
-        mixed_item<1, SE, LEAN>(sp, it.ot, it.e0, it.e1, smem, stage_off, sh, gbase);
+        mixed_item<SE>(sp, it.ot, it.e0, it.e1, smem, stage_off, sh, gbase);
         __syncthreads();
         if (sh.abort) {
             mixed_drain(smem, stage_off, NS, SE, sh);
@@ -1079,7 +981,6 @@ __global__ void __launch_bounds__(512, 1)
 }
 
 constexpr int kSE32 = 4;
-constexpr int kOPW = 1;
 static_assert(kMaxStages >= 4, "stage bookkeeping");
 constexpr int kSE64 = 2;
 
@@ -1095,7 +996,7 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
     const int rb = f64 ? 8 : 4;
     // mixed: elements per stage 2 or 4 (default 4); FP64: 2
     const int SE = f64 ? kSE64 : (SE_req == 2 ? 2 : kSE32);
-    const int opw = f64 ? 1 : kOPW;
+    const int opw = 1;
     r.t.opw = opw;
     const int T = r.g.T;
     int W = W_req > 0 ? W_req : 16;
@@ -1119,7 +1020,7 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
         while (NS < kMaxStages && tonal_smem(W, T, NS + 1, SE, rb) <= budget && per_sm_at(NS + 1) >= resident) ++NS;
     }
     TonalTile& t = r.t;
-    t.flush_elems = f64 ? 1 << 30 : 64;
+    t.flush_elems = 1 << 30;
     t.W = W;
     t.SE = SE;
     t.NS = NS;
@@ -1129,10 +1030,29 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
     const int per_sm = std::max(1, std::min((int)((228 * 1024) / (t.smem + 1024)), 65536 / (128 * 32 * (W / opw))));
     const int slots = num_sms * per_sm;
     const int groups = r.g.Epad / SE;
+    if (!f64) {
+        // Mixed: element chunks whose FP32 records (nW x 2560 B per element) take about
+        // 16 MB, so that the blocks running at one time (which work on one chunk) find the
+        // chunk in L2 and each record is read from HBM about once per launch; smaller if
+        // needed to give every slot `items_per_sm` items (default 8).  The FP32 bin rows
+        // are flushed every 128 elements.
+        const size_t per_elem = (size_t)r.g.nW * kGroups * kWin * 4 * sizeof(float);
+        long chunk = (long)std::max<size_t>((size_t)SE, ((size_t)16 << 20) / per_elem);
+        const int ips = items_per_sm > 0 ? items_per_sm : 8;
+        const long want = std::max<long>(1, ((long)ips * slots + obs_tiles - 1) / obs_tiles);
+        chunk = std::min(chunk, ((long)r.g.Epad + want - 1) / want);
+        chunk = std::max<long>(SE, chunk / SE * SE);
+        t.chunk = (int)chunk;
+        t.nchunk = (int)(((long)r.g.Epad + chunk - 1) / chunk);
+        t.items = obs_tiles * t.nchunk;
+        t.grid = std::min(t.items, slots);
+        t.flush_elems = 128;
+        return cudaSuccess;
+    }
     const int ips = items_per_sm > 0 ? items_per_sm : 64;
-    // number of element chunks: among 1 .. ips work items per slot, the one with the
-    // smallest wave-quantisation loss (a small charge per extra chunk for its prologue
-    // and its flush of the bins)
+    // FP64: number of element chunks among 1 .. ips work items per slot with the smallest
+    // wave-quantisation loss (a small charge per extra chunk for its prologue and its
+    // flush of the bins); one block per item
     int best = 1;
     double best_cost = 1e30;
     const int maxc = std::max(1, std::min(groups, std::max(1, (ips * slots + obs_tiles - 1) / obs_tiles)));
@@ -1151,6 +1071,7 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
     t.chunk = gpc * SE;
     t.nchunk = (groups + gpc - 1) / gpc;
     t.items = obs_tiles * t.nchunk;
+    t.grid = t.items;
     return cudaSuccess;
 }
 
@@ -1168,29 +1089,18 @@ static cudaError_t launch_f64_t(const KParams& kp, int items, int threads, size_
     return cudaGetLastError();
 }
 
-template <int SE, bool LEAN>
-static cudaError_t launch_mixed_t(const KParams& kp, int items, int threads, size_t smem, cudaStream_t s)
+template <int SE>
+static cudaError_t launch_mixed_t(const KParams& kp, int grid, int threads, size_t smem, cudaStream_t s)
 {
     static size_t configured = 0;
     if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(tonal_mixed_kernel<kOPW, SE, LEAN>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(tonal_mixed_kernel<SE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
-    tonal_mixed_kernel<kOPW, SE, LEAN><<<items, threads, smem, s>>>(kp);
+    tonal_mixed_kernel<SE><<<grid, threads, smem, s>>>(kp);
     return cudaGetLastError();
-}
-
-// the mixed kernel's form: lean (integer-pipe observer time and bin wrap) unless
-// ACUM_MIXED_FORM=classic selects the float-modulo form (kept for comparison)
-static bool mixed_lean()
-{
-    static const int v = [] {
-        const char* e = getenv("ACUM_MIXED_FORM");
-        return (e && strcmp(e, "classic") == 0) ? 0 : 1;
-    }();
-    return v != 0;
 }
 
 void fill_kparams(const TonalRun& r, KParams& kp)
@@ -1241,13 +1151,8 @@ cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s)
     KParams kp;
     fill_kparams(r, kp);
     if (r.precision == ACUM_PLAIN_FP64) return launch_f64_t<kSE64>(kp, r.t.items, 32 * r.t.W, r.t.smem, s);
-    const int threads = 32 * (r.t.W / kOPW);
-    if (mixed_lean()) {
-        if (r.t.SE == 2) return launch_mixed_t<2, true>(kp, r.t.items, threads, r.t.smem, s);
-        return launch_mixed_t<kSE32, true>(kp, r.t.items, threads, r.t.smem, s);
-    }
-    if (r.t.SE == 2) return launch_mixed_t<2, false>(kp, r.t.items, threads, r.t.smem, s);
-    return launch_mixed_t<kSE32, false>(kp, r.t.items, threads, r.t.smem, s);
+    if (r.t.SE == 2) return launch_mixed_t<2>(kp, r.t.grid, 32 * r.t.W, r.t.smem, s);
+    return launch_mixed_t<kSE32>(kp, r.t.grid, 32 * r.t.W, r.t.smem, s);
 }
 
 size_t batch_smem(int W, int SE, int Tmax)
@@ -1256,27 +1161,35 @@ size_t batch_smem(int W, int SE, int Tmax)
            (size_t)kBatchNS * 8;
 }
 
-template <int SE, bool LEAN>
+template <int SE>
 static cudaError_t launch_batch_t(const KParams* d_cases, const BatchItem* d_items, int nitems, int* d_counter, int W,
                                   int Tmax, int grid, cudaStream_t s)
 {
     static size_t configured = 0;
     const size_t smem = batch_smem(W, SE, Tmax);
     if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(tonal_batch_kernel<SE, LEAN>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(tonal_batch_kernel<SE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
     // as many resident blocks per SM as shared memory and registers allow
     int per_sm = 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<SE, LEAN>, 32 * W, smem) !=
-            cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<SE>, 32 * W, smem) != cudaSuccess ||
         per_sm < 1)
         per_sm = 1;
-    tonal_batch_kernel<SE, LEAN><<<grid * per_sm, 32 * W, smem, s>>>(d_cases, d_items, nitems, d_counter, kBatchNS,
-                                                                     acc_region_bytes(W, Tmax, 8));
+    tonal_batch_kernel<SE><<<grid * per_sm, 32 * W, smem, s>>>(d_cases, d_items, nitems, d_counter, kBatchNS,
+                                                               acc_region_bytes(W, Tmax, 8));
     return cudaGetLastError();
+}
+
+int batch_blocks_per_sm(int W, int SE, int Tmax)
+{
+    int per_sm = 1;
+    const size_t smem = batch_smem(W, SE, Tmax);
+    cudaError_t e = SE == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<2>, 32 * W, smem)
+                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<4>, 32 * W, smem);
+    return (e == cudaSuccess && per_sm > 0) ? per_sm : 1;
 }
 
 // grid = SMs; the launch puts as many blocks on each SM as fit
@@ -1284,13 +1197,8 @@ cudaError_t launch_tonal_batch(const KParams* d_cases, const BatchItem* d_items,
                                int SE, int Tmax, int grid, cudaStream_t s)
 {
     if (W < 1 || W > 16 || grid < 1) return cudaErrorInvalidValue;
-    const bool lean = mixed_lean();
-    if (SE == 2)
-        return lean ? launch_batch_t<2, true>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s)
-                    : launch_batch_t<2, false>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s);
-    if (SE == 4)
-        return lean ? launch_batch_t<4, true>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s)
-                    : launch_batch_t<4, false>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s);
+    if (SE == 2) return launch_batch_t<2>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s);
+    if (SE == 4) return launch_batch_t<4>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s);
     return cudaErrorInvalidValue;
 }
 

@@ -373,15 +373,18 @@ class Batch:
         self._ck(self.L.acum_batch_get_tile(self.h, C.byref(a), C.byref(b), C.byref(c)))
         return a.value, b.value, c.value
 
-    def autotune(self, sample_stride: int = 16) -> float:
+    def autotune(self, probe_per_sm: int = 0) -> float:
+        """Picks the tile shape; returns the predicted batch time in ms."""
         ms = C.c_double()
-        self._ck(self.L.acum_batch_autotune(self.h, sample_stride, C.byref(ms)))
+        self._ck(self.L.acum_batch_autotune(self.h, probe_per_sm, C.byref(ms)))
         return ms.value
 
     def run(self, mode: int = 2, precision: int = MIXED):
         self._ck(self.L.acum_batch_run(self.h, precision, mode))
 
     def result(self, case: int) -> np.ndarray:
+        if not 0 <= case < len(self.shapes):
+            raise AcumError(-1, "bad case index %d" % case)
         T, O, _ = self.shapes[case]
         out = np.empty((T, O), np.float64)
         self._ck(self.L.acum_batch_result(self.h, case, _p(out)))

@@ -225,7 +225,7 @@ def batch_leg(native, device, steps=1, inflight=6):
     evals = np.array([e for (_, _, e) in b.shapes], np.float64)
     total = float(evals.sum())
     t0 = time.perf_counter()
-    est_ms = b.autotune(sample_stride=32)
+    est_ms = b.autotune()
     tune_s = time.perf_counter() - t0
     tile = b.tile()
     res = {"workload": "workload 4: 64 rotor cases, one persistent launch (CUDA graph) vs one launch per case",

@@ -280,12 +280,15 @@ int acum_batch_case_timing(const acum_batch* b, int case_id, double* ms);
 /* obs_per_block 1..16, elems_per_stage 2 or 4, items_per_sm >= 1 (0 keeps a value). */
 int acum_batch_set_tile(acum_batch* b, int obs_per_block, int elems_per_stage, int items_per_sm);
 int acum_batch_get_tile(const acum_batch* b, int* obs_per_block, int* elems_per_stage, int* items_per_sm);
-/* Times the persistent launch for each candidate tile shape on a sample of its work
- * items (every `sample_stride`-th, largest first; 1 = all), keeps the fastest and
- * returns its estimated full-batch time in *best_ms.  Candidates: obs_per_block in
- * {8, 12, 16} x elems_per_stage in {2, 4} x items_per_sm in {4, 8, 16}, skipping shapes
- * whose shared memory does not fit. */
-int acum_batch_autotune(acum_batch* b, int sample_stride, double* best_ms);
+/* Chooses the tile shape.  (1) For every observers-per-block in {8, 12, 16} x elements-per-
+ * stage in {2, 4} whose shared memory fits, one persistent launch over a probe of
+ * 32-element work items spread over all cases (about probe_per_sm items per SM; 0 = 8)
+ * gives the kernel's throughput; the fastest shape is kept.  (2) Two probes of that shape
+ * with 32- and 128-element items give its cost per work item and per evaluation, from
+ * which the largest-first dynamic schedule of the real work list is simulated for
+ * items_per_sm in {4, 8, 16, 32}; the shortest predicted makespan is kept and returned in
+ * *best_ms. */
+int acum_batch_autotune(acum_batch* b, int probe_per_sm, double* best_ms);
 
 #ifdef __cplusplus
 }

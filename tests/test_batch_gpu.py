@@ -115,9 +115,9 @@ def test_tile_shapes_agree(batch, singles, W, SE, ips):
 
 def test_autotune(batch, singles):
     b, decks = batch
-    est = b.autotune(sample_stride=2)
+    est = b.autotune()
     W, SE, ips = b.tile()
-    assert W in (8, 12, 16) and SE in (2, 4) and ips in (4, 8, 16)
+    assert W in (8, 12, 16) and SE in (2, 4) and ips in (4, 8, 16, 32)
     assert est > 0
     b.run(mode=2)
     for i in range(len(decks)):
