@@ -36,6 +36,7 @@
 
 #include "acum_internal.h"
 #include "ctx.h"
+#include "ptx.h"
 
 namespace acum {
 
@@ -512,25 +513,39 @@ __global__ void bb_spec_kernel(const float* __restrict__ sc, const double* __res
     o[1] = make_float4(At, Av, q[27], 0.f);
 }
 
-// Observer contraction.  Block = 32 observers (lane = observer) x 7 warps of 6 bands.
-// Per tile of kTI (section, step) items: the amplitudes of all 42 bands (contiguous in
-// `amp`, 1344 B per item) are copied into shared memory, and the directivity factors D
-// of the block's 32 observers for the kTI items are computed once into shared memory;
-// then each lane adds, for its observer and its warp's 6 bands, the clipped energies of
-// every item.  The amplitude reads are warp-uniform (one shared-memory broadcast per
-// band and item), the D reads conflict-free.  FP32 partial sums over at most 1024 items
-// are folded into FP64 sums private to the block's (observer tile, item range):
+// Observer contraction.  Block = 64 observers (lane l serves observers l and l + 32) x
+// 14 warps of 3 bands.  Per tile of kTI (section, step) items, the amplitudes of all 42
+// bands (contiguous in `amp`, 1344 B per item) and the items' geometry records arrive in
+// shared memory by one bulk copy into a double buffer (the next tile's copy runs while
+// this one is consumed); the directivity factors D of the block's observers for the
+// tile are computed once into shared memory; then each lane adds, for its two observers
+// and its warp's 3 bands, the clipped energies of every item.  The amplitude reads are
+// warp-uniform (one shared-memory broadcast per band and item, shared by two
+// observers), the D reads conflict-free.  FP32 partial sums over at most 1024 items are
+// folded into FP64 sums private to the block's (observer tile, item range):
 // part[split][band][component][observer], reduced over the splits by bb_final_kernel.
-constexpr int kObsLanes = 32;
+constexpr int kObsPerLane = 2;
+constexpr int kObsBlock = 32 * kObsPerLane;         // 64
 constexpr int kBandsPerWarp = 3;
 constexpr int kBandWarps = kBands / kBandsPerWarp;  // 14
 constexpr int kBpmThreads = 32 * kBandWarps;        // 448
 constexpr int kTI = 16;                             // items per tile
 constexpr int kFoldTiles = 64;                      // 1024 items per FP32 partial
+constexpr int kAmpItemBytes = kBands * kAmp * 4;    // 1344
+constexpr int kGeoItemBytes = kGeo * 4;             // 64
 static_assert(kBands % kBandsPerWarp == 0, "band split");
+static_assert(kAmpItemBytes % 16 == 0 && kGeoItemBytes % 16 == 0, "bulk copy granularity");
 
-__device__ __forceinline__ float2 bb_directivity(const float* __restrict__ geo, const float* __restrict__ obs, int o,
-                                                 float vx, float vy, float vz, float aa, float iaMv)
+// dynamic shared memory of bb_obs_kernel: 2 x (amplitude tile + geometry tile), the D
+// tile, the block's observers, 2 mbarriers
+constexpr size_t kObsSmemA = (size_t)kTI * kAmpItemBytes;
+constexpr size_t kObsSmemG = (size_t)kTI * kGeoItemBytes;
+constexpr size_t kObsSmemBuf = kObsSmemA + kObsSmemG;
+constexpr size_t kObsSmemD = (size_t)kTI * kObsBlock * sizeof(float2);
+constexpr size_t kObsSmem = 2 * kObsSmemBuf + kObsSmemD + kObsBlock * 3 * sizeof(float) + 2 * sizeof(uint64_t);
+
+__device__ __forceinline__ float2 bb_directivity(const float* geo, const float* obs, int o, float vx, float vy,
+                                                 float vz, float aa, float iaMv)
 {
     const float4* g = reinterpret_cast<const float4*>(geo);
     const float4 g0 = g[0], g1 = g[1], g2 = g[2], g3 = g[3];
@@ -562,81 +577,137 @@ __device__ __forceinline__ float2 bb_directivity(const float* __restrict__ geo, 
     return make_float2(Dh, g3.z != 0.f ? Dl : Dh);
 }
 
-__global__ void __launch_bounds__(kBpmThreads, 2) bb_obs_kernel(const float* __restrict__ geo,
+__global__ void __launch_bounds__(kBpmThreads, 1) bb_obs_kernel(const float* __restrict__ geo,
                                                                 const float* __restrict__ amp,
                                                                 const float* __restrict__ obs, int O, long long nst,
                                                                 long long per_split, float vx, float vy, float vz,
-                                                                float a0, int aa_mode, double* __restrict__ part)
+                                                                float a0, int aa_mode, double* __restrict__ part,
+                                                                DeviceErr* err)
 {
-    __shared__ __align__(16) float4 sA[kTI * kBands * 2];
-    __shared__ float2 sD[kTI][kObsLanes];
+    extern __shared__ __align__(128) unsigned char sm[];
+    float2* sD = reinterpret_cast<float2*>(sm + 2 * kObsSmemBuf);  // [kTI][kObsBlock]
+    float* sObs = reinterpret_cast<float*>(sm + 2 * kObsSmemBuf + kObsSmemD);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + 2 * kObsSmemBuf + kObsSmemD + kObsBlock * 3 * sizeof(float));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int o0 = blockIdx.x * kObsLanes;
-    const int o = o0 + lane;
+    const int o0 = blockIdx.x * kObsBlock;
     const long long st_begin = (long long)blockIdx.y * per_split;
     const long long st_end = min(nst, st_begin + per_split);
+    const int ntiles = st_end > st_begin ? (int)((st_end - st_begin + kTI - 1) / kTI) : 0;
     const float aMv = a0 * a0 - (vx * vx + vy * vy + vz * vz);
     const float aa = aa_mode == 1 ? 0.f : aMv;
     const float iaMv = 1.0f / aMv;
-    const float4* amp4 = reinterpret_cast<const float4*>(amp);
     double* mine = part + (size_t)blockIdx.y * kBands * 6 * O;  // [band][component][observer]
-    float acc[kBandsPerWarp][6];
+
+    for (int i = threadIdx.x; i < kObsBlock * 3; i += blockDim.x) {
+        const int o = o0 + i / 3;
+        sObs[i] = o < O ? obs[3 * o0 + i] : 0.f;
+    }
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    // tile j -> buffer j & 1: amplitudes then geometry of its items
+    auto issue = [&](int j) {
+        const long long t0 = st_begin + (long long)j * kTI;
+        const int n = (int)min((long long)kTI, st_end - t0);
+        unsigned char* buf = sm + (size_t)(j & 1) * kObsSmemBuf;
+        mbar_expect_tx(&bars[j & 1], (uint32_t)(n * (kAmpItemBytes + kGeoItemBytes)));
+        bulk_g2s(buf, amp + t0 * kBands * kAmp, (uint32_t)(n * kAmpItemBytes), &bars[j & 1]);
+        bulk_g2s(buf + kObsSmemA, geo + t0 * kGeo, (uint32_t)(n * kGeoItemBytes), &bars[j & 1]);
+    };
+    if (threadIdx.x == 0)
+        for (int j = 0; j < 2 && j < ntiles; ++j) issue(j);
+
+    float acc[kObsPerLane][kBandsPerWarp][6];
 #pragma unroll
-    for (int b = 0; b < kBandsPerWarp; ++b)
-#pragma unroll
-        for (int c = 0; c < 6; ++c) acc[b][c] = 0.f;
-    auto fold = [&]() {
-        if (o < O) {
-            // addresses formed here, not hoisted out of the item loop (36 live pointers
-            // would cost more registers than the accumulators)
-            size_t stride = (size_t)O;
-            asm volatile("" : "+l"(stride));
-            double* q = mine + (size_t)warp * kBandsPerWarp * 6 * stride + o;
-#pragma unroll
-            for (int b = 0; b < kBandsPerWarp; ++b)
-#pragma unroll
-                for (int c = 0; c < 6; ++c) {
-                    *q += (double)acc[b][c];
-                    q += stride;
-                }
-        }
+    for (int q = 0; q < kObsPerLane; ++q)
 #pragma unroll
         for (int b = 0; b < kBandsPerWarp; ++b)
 #pragma unroll
-            for (int c = 0; c < 6; ++c) acc[b][c] = 0.f;
+            for (int c = 0; c < 6; ++c) acc[q][b][c] = 0.f;
+    auto fold = [&]() {
+#pragma unroll
+        for (int q = 0; q < kObsPerLane; ++q) {
+            const int o = o0 + q * 32 + lane;
+            if (o < O) {
+                // addresses formed here, not hoisted out of the item loop
+                size_t stride = (size_t)O;
+                asm volatile("" : "+l"(stride));
+                double* p = mine + (size_t)warp * kBandsPerWarp * 6 * stride + o;
+#pragma unroll
+                for (int b = 0; b < kBandsPerWarp; ++b)
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) {
+                        *p += (double)acc[q][b][c];
+                        p += stride;
+                    }
+            }
+#pragma unroll
+            for (int b = 0; b < kBandsPerWarp; ++b)
+#pragma unroll
+                for (int c = 0; c < 6; ++c) acc[q][b][c] = 0.f;
+        }
     };
+    int aborted_at = -1;
     int tiles = 0;
-    for (long long t0 = st_begin; t0 < st_end; t0 += kTI) {
+    for (int j = 0; j < ntiles; ++j) {
+        const long long t0 = st_begin + (long long)j * kTI;
         const int n = (int)min((long long)kTI, st_end - t0);
-        __syncthreads();
-        for (int i = threadIdx.x; i < n * kBands * 2; i += blockDim.x) sA[i] = amp4[t0 * kBands * 2 + i];
+        const unsigned char* buf = sm + (size_t)(j & 1) * kObsSmemBuf;
+        const bool ok = mbar_wait_bounded(&bars[j & 1], (uint32_t)((j >> 1) & 1));
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) flag(err, ACUM_DEVERR_TIMEOUT, &err->timeout);
+            aborted_at = j;
+            break;
+        }
+        const float4* sA = reinterpret_cast<const float4*>(buf);
+        const float* sG = reinterpret_cast<const float*>(buf + kObsSmemA);
+        // D of every (item, observer) of the tile (bb_core.cu:515-530, 620-624)
 #pragma unroll 1
-        for (int pidx = threadIdx.x; pidx < kTI * kObsLanes; pidx += blockDim.x) {
-            const int it = pidx / kObsLanes, ol = pidx % kObsLanes;
+        for (int pidx = threadIdx.x; pidx < kTI * kObsBlock; pidx += blockDim.x) {
+            const int it = pidx / kObsBlock, ol = pidx % kObsBlock;
             float2 D = make_float2(0.f, 0.f);
-            if (it < n && o0 + ol < O) D = bb_directivity(geo + (t0 + it) * kGeo, obs, o0 + ol, vx, vy, vz, aa, iaMv);
-            sD[it][ol] = D;
+            if (it < n && o0 + ol < O) D = bb_directivity(sG + it * kGeo, sObs, ol, vx, vy, vz, aa, iaMv);
+            sD[it * kObsBlock + ol] = D;
         }
         __syncthreads();
 #pragma unroll 1
         for (int it = 0; it < n; ++it) {
-            const float2 D = sD[it][lane];
+            const float2 D0 = sD[it * kObsBlock + lane], D1 = sD[it * kObsBlock + 32 + lane];
 #pragma unroll
             for (int b = 0; b < kBandsPerWarp; ++b) {
                 const int band = warp * kBandsPerWarp + b;
                 const float4 A0 = sA[(it * kBands + band) * 2], A1 = sA[(it * kBands + band) * 2 + 1];
-                acc[b][0] += fmaxf(D.x * A0.x, 1e-10f);  // TBL-TE pressure side
-                acc[b][1] += fmaxf(D.x * A0.y, 1e-10f);  // TBL-TE suction side
-                acc[b][2] += fmaxf(D.y * A0.z, 1e-10f);  // separation
-                acc[b][3] = fmaf(D.x, A0.w, acc[b][3]);  // LBL-VS
-                acc[b][4] = fmaf(D.x, A1.x, acc[b][4]);  // TEB-VS
-                if (A1.y != 0.f) acc[b][5] += A1.y * fmaxf(D.x * A1.z, 2.2204460492503131e-16f);  // tip
+#pragma unroll
+                for (int q = 0; q < kObsPerLane; ++q) {
+                    const float2 D = q == 0 ? D0 : D1;
+                    acc[q][b][0] += fmaxf(D.x * A0.x, 1e-10f);  // TBL-TE pressure side
+                    acc[q][b][1] += fmaxf(D.x * A0.y, 1e-10f);  // TBL-TE suction side
+                    acc[q][b][2] += fmaxf(D.y * A0.z, 1e-10f);  // separation
+                    acc[q][b][3] = fmaf(D.x, A0.w, acc[q][b][3]);  // LBL-VS
+                    acc[q][b][4] = fmaf(D.x, A1.x, acc[q][b][4]);  // TEB-VS
+                    if (A1.y != 0.f) acc[q][b][5] += A1.y * fmaxf(D.x * A1.z, 2.2204460492503131e-16f);  // tip
+                }
             }
         }
+        // every thread is done with this buffer and the D tile: refill with tile j + 2
+        __syncthreads();
+        if (threadIdx.x == 0 && j + 2 < ntiles) issue(j + 2);
         if (++tiles == kFoldTiles) {
             fold();
             tiles = 0;
         }
+    }
+    if (aborted_at >= 0) {
+        // wait (bounded) for the copies still in flight (tiles j and j + 1) before the
+        // block exits
+        if (threadIdx.x == 0)
+            for (int j = aborted_at; j < ntiles && j < aborted_at + 2; ++j)
+                (void)mbar_wait_bounded(&bars[j & 1], (uint32_t)((j >> 1) & 1));
+        __syncthreads();
+        return;
     }
     fold();
 }
@@ -799,10 +870,21 @@ static int bpm_run(acum_ctx* ctx, int aa_mode, const double* seed_spl_h, const d
     bb_pos_kernel<<<nb, 128, 0, st>>>(d);
     bb_prep_kernel<<<nb, 128, 0, st>>>(d);
     bb_spec_kernel<<<(int)((nst * kBands + 255) / 256), 256, 0, st>>>(s->sc.p, s->ff.p, s->amp.p, nst);
-    // item ranges: with 2 resident blocks per SM, the number of splits (up to 16 blocks
-    // per SM in all) with the smallest wave-quantisation loss
-    const int oblocks = (O + kObsLanes - 1) / kObsLanes;
-    const int slots = 2 * ctx->num_sms;
+    // item ranges: the number of splits (up to 8 waves of resident blocks) with the
+    // smallest wave-quantisation loss
+    const int oblocks = (O + kObsBlock - 1) / kObsBlock;
+    static bool configured = false;
+    if (!configured) {
+        if ((e = cudaFuncSetAttribute(bb_obs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kObsSmem)) !=
+            cudaSuccess)
+            return cuda_fail(ctx, e, "bpm configure");
+        configured = true;
+    }
+    int per_sm = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bb_obs_kernel, kBpmThreads, kObsSmem) != cudaSuccess ||
+        per_sm < 1)
+        per_sm = 1;
+    const int slots = per_sm * ctx->num_sms;
     int split = 1;
     double best = 1e30;
     const int maxs = (int)std::max<long long>(1, std::min<long long>((8 * slots + oblocks - 1) / oblocks,
@@ -820,9 +902,9 @@ static int bpm_run(acum_ctx* ctx, int aa_mode, const double* seed_spl_h, const d
     if ((e = s->sums.ensure((size_t)split * kBands * 6 * O)) != cudaSuccess) return cuda_fail(ctx, e, "bpm alloc");
     cudaMemsetAsync(s->sums.p, 0, (size_t)split * kBands * 6 * O * 8, st);
     dim3 grid(oblocks, split);
-    bb_obs_kernel<<<grid, kBpmThreads, 0, st>>>(s->geo.p, s->amp.p, ctx->d_obs32.p, O, nst, per_split,
-                                                (float)d.vinf[0], (float)d.vinf[1], (float)d.vinf[2], (float)d.a0,
-                                                aa_mode, s->sums.p);
+    bb_obs_kernel<<<grid, kBpmThreads, kObsSmem, st>>>(s->geo.p, s->amp.p, ctx->d_obs32.p, O, nst, per_split,
+                                                       (float)d.vinf[0], (float)d.vinf[1], (float)d.vinf[2],
+                                                       (float)d.a0, aa_mode, s->sums.p, ctx->d_err.p);
     bb_final_kernel<<<(O + 127) / 128, 128, 0, st>>>(s->sums.p, split, O, T, s->seed_spl.p, s->seed_oas.p,
                                                      s->spl.p, s->oaspl.p);
     cudaEventRecord(ctx->ev[EV_BPM1], st);
@@ -834,6 +916,15 @@ static int bpm_run(acum_ctx* ctx, int aa_mode, const double* seed_spl_h, const d
     cudaMemcpyAsync(ctx->h_spl.data(), s->spl.p, ctx->h_spl.size() * 8, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(ctx->h_oaspl.data(), s->oaspl.p, O * 8, cudaMemcpyDeviceToHost, st);
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(ctx, e, "bpm run");
+    {
+        DeviceErr h;
+        if ((e = cudaMemcpy(&h, ctx->d_err.p, sizeof(h), cudaMemcpyDeviceToHost)) != cudaSuccess)
+            return cuda_fail(ctx, e, "bpm error word");
+        if (h.bits & ACUM_DEVERR_TIMEOUT) {
+            cudaMemset(ctx->d_err.p, 0, sizeof(DeviceErr));
+            return fail(ctx, ACUM_ERR_TIMEOUT, "a bounded shared-memory pipeline wait ran out; results are incomplete");
+        }
+    }
     if (spl_h) memcpy(spl_h, ctx->h_spl.data(), ctx->h_spl.size() * 8);
     if (oas_h) memcpy(oas_h, ctx->h_oaspl.data(), O * 8);
     ctx->have_bpm = true;

@@ -1,0 +1,74 @@
+// ptx.h -- device helpers shared by the kernels: mbarrier operations (every wait
+// bounded), the bulk (TMA) global -> shared copy, and the device error word.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "acum_internal.h"
+
+namespace acum {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Every wait on a barrier is bounded: after kMaxSpin polls the wait gives up, records
+// ACUM_DEVERR_TIMEOUT and the kernel unwinds instead of hanging.
+constexpr long kMaxSpin = 1L << 24;
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity)
+{
+    for (long it = 0; it < kMaxSpin; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// bulk TMA copy global -> shared, completion signalled on `bar` (bytes % 16 == 0,
+// both addresses 16-byte aligned)
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void flag(DeviceErr* e, unsigned bit, unsigned* counter)
+{
+    atomicOr(&e->bits, bit);
+    atomicAdd(counter, 1u);
+}
+
+}  // namespace acum
