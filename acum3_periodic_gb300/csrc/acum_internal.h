@@ -45,6 +45,7 @@ struct TonalTile {
     int nchunk;
     int items;
     int grid;         // blocks launched (the mixed kernel strides over the items)
+    int tile_group;   // mixed: observer tiles per group of the item order
     int flush_elems;  // mixed: elements summed in FP32 before the FP64 flush
     int opw;          // observers per warp
     size_t smem;
@@ -114,7 +115,7 @@ struct KParams {
     unsigned tmod;  // ceil(2^32 / T): bin index modulo T by multiply-high
     // FP64 constants
     double a0, alpha, ialpha, vx, vy, vz, dTau, oM, dPsi, lpi;
-    int W, NS, chunk, nchunk, obs_tiles, flush_groups;
+    int W, NS, chunk, nchunk, obs_tiles, flush_groups, tile_group;
     double* acc;
     DeviceErr* err;
 };

@@ -724,7 +724,7 @@ struct MixedShared {
 // mbarrier phases of the same ring.  On entry every slot is free and all bin rows are
 // zero; on return (without abort) the same holds again.
 template <int SE>
-__device__ __forceinline__ void mixed_item(const KParams& p, int ot, int e0, int e1, unsigned char* smem,
+__device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot, int e0, int e1, unsigned char* smem,
                                            size_t stage_off, MixedShared& sh, unsigned& gbase)
 {
     constexpr int kTile = kGroups * kWin * 4;
@@ -857,10 +857,11 @@ __device__ __forceinline__ void mixed_drain(unsigned char* smem, size_t stage_of
     __syncthreads();
 }
 
-// Single deck: block b takes the items b, b + grid, b + 2 grid, ... of the list ordered
-// element chunk first (item = chunk * obs_tiles + observer tile), so that the blocks
-// running at any time share one chunk of records in L2 and each record is read from
-// HBM about once per launch.
+// Single deck: block b takes the items b, b + grid, b + 2 grid, ... of a list ordered by
+// observer-tile group, then element chunk, then tile within the group.  The blocks
+// running at any time therefore share one chunk of records in L2 (each record is read
+// from HBM once per group), and the FP64 sums they add into belong to one group of
+// tiles, small enough to stay in L2 beside the records.
 template <int SE>
 __global__ void __launch_bounds__(512, 1) tonal_mixed_kernel(const KParams p)
 {
@@ -870,8 +871,12 @@ __global__ void __launch_bounds__(512, 1) tonal_mixed_kernel(const KParams p)
     mixed_init(smem, stage_off, p.NS, SE, sh);
     unsigned gbase = 0;
     const int nitems = p.obs_tiles * p.nchunk;
+    const int G = p.tile_group, per_group = G * p.nchunk;
+    const int last_g = (p.obs_tiles - 1) / G, last_n = p.obs_tiles - last_g * G;
     for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
-        const int ot = item % p.obs_tiles, ec = item / p.obs_tiles;
+        const int g = item / per_group, r = item - g * per_group;
+        const int gn = g == last_g ? last_n : G;
+        const int ec = r / gn, ot = g * G + (r - ec * gn);
         const int e0 = ec * p.chunk;
         const int e1 = min(e0 + p.chunk, p.Epad);
         mixed_item<SE>(p, ot, e0, e1, smem, stage_off, sh, gbase);
@@ -984,6 +989,11 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
         t.chunk = (int)chunk;
         t.nchunk = (int)(((long)r.g.Epad + chunk - 1) / chunk);
         t.items = obs_tiles * t.nchunk;
+        // observer tiles per group: their FP64 sums (W x T x 16 B per tile) within ~48 MB
+        int G = (int)std::max<size_t>(1, ((size_t)48 << 20) / ((size_t)W * r.g.T * 16));
+        G = std::min(G, obs_tiles);
+        const int ngroups = (obs_tiles + G - 1) / G;
+        t.tile_group = (obs_tiles + ngroups - 1) / ngroups;
         t.grid = std::min(t.items, slots);
         t.flush_elems = 128;
         return cudaSuccess;
@@ -1011,6 +1021,7 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
     t.nchunk = (groups + gpc - 1) / gpc;
     t.items = obs_tiles * t.nchunk;
     t.grid = t.items;
+    t.tile_group = obs_tiles;
     return cudaSuccess;
 }
 
@@ -1080,6 +1091,7 @@ void fill_kparams(const TonalRun& r, KParams& kp)
     kp.chunk = r.t.chunk;
     kp.nchunk = r.t.nchunk;
     kp.obs_tiles = (g.O + r.t.W - 1) / r.t.W;
+    kp.tile_group = r.t.tile_group > 0 ? r.t.tile_group : kp.obs_tiles;
     kp.flush_groups = std::max(1, r.t.flush_elems / r.t.SE);
     kp.acc = r.acc;
     kp.err = r.err;
