@@ -19,12 +19,24 @@ namespace acum {
 //   g3: Lx, Ly, Lz, Lm        (L     = P n,  Lm = L.V / a0)
 //   g4: Ldx, Ldy, Ldz, xv     (Ldot  = Pdot n + P ndot, xv = x.vInf for the anchored
 //                              retarded time of the mixed form)
-// In HBM the records are tiled [element][window][group][32 steps][4]: a (element,
-// 32-step window) tile is contiguous (2560 B in FP32, 5120 B in FP64), which is what one
-// bulk (TMA) copy moves into shared memory.
+// In HBM the FP64 records are tiled [element][window][group][32 steps][4]: an (element,
+// 32-step window) tile is contiguous (5120 B), which is what one bulk (TMA) copy moves
+// into shared memory.  The FP32 records interleave pairs of elements so that the mixed
+// kernel reads the two elements' values of a field as one register pair (the operand of
+// a packed FP32 instruction): [element pair][window][group][half][32 steps][4], half 0 =
+// (f0 of e, f0 of e+1, f1 of e, f1 of e+1), half 1 = the same for fields 2 and 3; an
+// (element pair, window) tile is 5120 B.
 constexpr int kGroups = 5;
 constexpr int kWin = 32;
 constexpr int kFields = 18;  // x,y,z,ds, n(3), ndot(3), V(3), Vdot(3), P, Pdot
+
+// float offset of field c (0..3) of group q of element e at step t in the FP32 records
+__host__ __device__ __forceinline__ size_t rec32_offset(int e, int nW, int t, int q, int c)
+{
+    const int w = t / kWin, lane = t % kWin;
+    return ((((size_t)(e >> 1) * nW + w) * kGroups + q) * 2 + (c >> 1)) * (kWin * 4) + (size_t)lane * 4 +
+           (size_t)((c & 1) * 2 + (e & 1));
+}
 
 struct DeviceErr {
     unsigned int bits;
@@ -67,7 +79,7 @@ struct PrepArgs {
     double gauss[13];
     float* ser;            // scratch [E][8][T] float
     double* rec64;         // [Epad][nW][5][32][4] or null
-    float* rec32;          // [Epad][nW][5][32][4] or null
+    float* rec32;          // pair-interleaved FP32 records (rec32_offset) or null
     double* fields;        // optional [E][T][18]
 };
 cudaError_t launch_prep(const PrepArgs& a, cudaStream_t s);

@@ -22,7 +22,7 @@
 //     scalings -> dJ/dCp, dJ/dx, dJ/dn in file coordinates.
 //
 // Records as the forward builds them (tonal.cu):
-//   g0 = x, y, z, dsD   g1 = M(3), M2   g2 = Md(3), ATD   g3 = L(3), Lm   g4 = Ld(3), 0
+//   g0 = x, y, z, dsD   g1 = M(3), M2   g2 = Md(3), ATD   g3 = L(3), Lm   g4 = Ld(3), x.vInf
 #include <cuda_runtime.h>
 #include <math.h>
 #include <string.h>
@@ -77,15 +77,25 @@ struct Fwd {
     R dx, dy, dz, c, beta, s, tr, rx, ry, rz, ir, Mr, Mdr, Lr, Ldr, G, qa, K, base, Y, pt, pl, t;
 };
 
-template <typename R>
-__device__ __forceinline__ void load_rec(const R* rec, int nW, int e, int step, R* f)
+// the 20 record fields of (element, step): FP64 tiles [element][window][group][32][4],
+// FP32 tiles of element pairs (rec32_offset)
+__device__ __forceinline__ void load_rec(const double* rec, int nW, int e, int step, double* f)
 {
-    const R* tile = rec + ((size_t)e * nW + step / kWin) * (kGroups * kWin * 4);
+    const double* tile = rec + ((size_t)e * nW + step / kWin) * (kGroups * kWin * 4);
     const int lane = step % kWin;
 #pragma unroll
     for (int q = 0; q < kGroups; ++q)
 #pragma unroll
         for (int c = 0; c < 4; ++c) f[4 * q + c] = tile[((size_t)q * kWin + lane) * 4 + c];
+}
+
+__device__ __forceinline__ void load_rec(const float* rec, int nW, int e, int step, float* f)
+{
+    const float* base = rec + rec32_offset(e, nW, step, 0, 0);
+#pragma unroll
+    for (int q = 0; q < kGroups; ++q)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) f[4 * q + c] = base[rec32_offset(0, 1, 0, q, c)];
 }
 
 template <typename R>
@@ -201,7 +211,7 @@ __global__ void __launch_bounds__(128) adjoint_kernel(AdjDev p)
     const int step = tau < 0 ? tau + p.T : (tau >= p.T ? tau - p.T : tau);
     const bool owner = lane >= 1 && lane <= kAdjStride && tau >= 0 && tau < p.T;
     R f[20];
-    load_rec<R>(reinterpret_cast<const R*>(p.rec), p.nW, e, step, f);
+    load_rec(reinterpret_cast<const R*>(p.rec), p.nW, e, step, f);
     R acc[kCot];
 #pragma unroll
     for (int k = 0; k < kCot; ++k) acc[k] = 0;

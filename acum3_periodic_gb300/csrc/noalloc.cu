@@ -79,11 +79,9 @@ __global__ void noalloc_records_kernel(const float* __restrict__ X, const float*
     r[12] = L[0]; r[13] = L[1]; r[14] = L[2]; r[15] = (L[0] * vx + L[1] * vy + L[2] * vz) * ia0;
     r[16] = Pd * nx + P * (double)n[3]; r[17] = Pd * ny + P * (double)n[4]; r[18] = Pd * nz + P * (double)n[5];
     r[19] = (double)x[0] * vx_inf + (double)x[1] * vy_inf + (double)x[2] * vz_inf;
-    const int w = t / kWin, lane = t % kWin;
-    const size_t tile = ((size_t)e * nW + w) * (kGroups * kWin * 4);
+    float* r32 = rec + rec32_offset(e, nW, t, 0, 0);
     for (int q = 0; q < kGroups; ++q)
-        *reinterpret_cast<float4*>(rec + tile + ((size_t)q * kWin + lane) * 4) =
-            make_float4((float)r[4 * q], (float)r[4 * q + 1], (float)r[4 * q + 2], (float)r[4 * q + 3]);
+        for (int c = 0; c < 4; ++c) r32[rec32_offset(0, 1, 0, q, c)] = (float)r[4 * q + c];
 }
 
 }  // namespace acum

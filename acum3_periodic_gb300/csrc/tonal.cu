@@ -188,10 +188,11 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
                 d[0] = make_double2(rec[4 * q], rec[4 * q + 1]);
                 d[1] = make_double2(rec[4 * q + 2], rec[4 * q + 3]);
             }
-            if (a.rec32) {
-                *reinterpret_cast<float4*>(a.rec32 + off) =
-                    make_float4((float)rec[4 * q], (float)rec[4 * q + 1], (float)rec[4 * q + 2], (float)rec[4 * q + 3]);
-            }
+        }
+        if (a.rec32) {
+            float* r32 = a.rec32 + rec32_offset(e, a.nW, t, 0, 0);
+            for (int q = 0; q < kGroups; ++q)
+                for (int c = 0; c < 4; ++c) r32[rec32_offset(0, 1, 0, q, c)] = (float)rec[4 * q + c];
         }
     }
 }
@@ -246,9 +247,11 @@ __global__ void aos_record_kernel(AosArgs a)
             d[0] = make_double2(rec[4 * q], rec[4 * q + 1]);
             d[1] = make_double2(rec[4 * q + 2], rec[4 * q + 3]);
         }
-        if (a.rec32)
-            *reinterpret_cast<float4*>(a.rec32 + off) =
-                make_float4((float)rec[4 * q], (float)rec[4 * q + 1], (float)rec[4 * q + 2], (float)rec[4 * q + 3]);
+    }
+    if (a.rec32) {
+        float* r32 = a.rec32 + rec32_offset(e, a.nW, t, 0, 0);
+        for (int q = 0; q < kGroups; ++q)
+            for (int c = 0; c < 4; ++c) r32[rec32_offset(0, 1, 0, q, c)] = (float)rec[4 * q + c];
     }
 }
 
@@ -263,9 +266,9 @@ cudaError_t launch_aos_records(const AosArgs& a, cudaStream_t s)
 
 // ------------------------------------------------------------- tonal kernel
 
-struct SmpF {
-    int k;      // integer part of the observer time in bins (unwrapped)
-    float f;    // fraction in [0, 1)
+struct __align__(16) SmpF {
+    int k;      // observer time in bins (unwrapped) = k + f
+    float f;    // in [-0.5, 0.5]
     float pt, pl;
 };
 
@@ -605,39 +608,73 @@ __device__ __forceinline__ Anchor make_anchor(const KParams& p, float ox, float 
     return a;
 }
 
-__device__ __forceinline__ SmpF sample_mixed(const float4& g0, const float4& g1, const float4& g2, const float4& g3,
-                                             const float4& g4, float ox, float oy, float oz, const Anchor& an,
-                                             const KParams& p, int tau, DeviceErr* err)
+// packed FP32 (two lanes of an f32x2 register pair, one per element of a pair)
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+__device__ __forceinline__ float2 rcp2(float2 a) { return make_float2(__fdividef(1.0f, a.x), __fdividef(1.0f, a.y)); }
+
+// One field group of an element pair as read from the FP32 records: x = both elements'
+// field 0, y = field 1, z = field 2, w = field 3.
+struct G2 {
+    float2 x, y, z, w;
+};
+
+__device__ __forceinline__ G2 load_g2(const float* half0)
 {
-    const float dx = ox - g0.x, dy = oy - g0.y, dz = oz - g0.z;
-    // anchored retarded time (g4.w = x.v)
-    const float cc = -fmaf(g0.x, dx + ox, fmaf(g0.y, dy + oy, g0.z * (dz + oz)));
-    const float num = fmaf(an.t2, g4.w, cc);
-    const float bp = an.s0 - g4.w;
-    const float q = fmaf(bp, bp, p.alphaf * num);
-    const float dt = __fdividef(num, bp + q * rsqrtf(q));
-    const float tr = an.t0 + dt;
-    const float rx = fmaf(-p.vxf, tr, dx), ry = fmaf(-p.vyf, tr, dy), rz = fmaf(-p.vzf, tr, dz);
-    const float r = p.a0f * tr;
-    const float ir = __fdividef(1.0f, r);
-    const float Mr = fmaf(g1.x, rx, fmaf(g1.y, ry, g1.z * rz)) * ir;
-    const float Mdr = fmaf(g2.x, rx, fmaf(g2.y, ry, g2.z * rz)) * ir;
-    const float Lr = fmaf(g3.x, rx, fmaf(g3.y, ry, g3.z * rz)) * ir;
-    const float Ldr = fmaf(g4.x, rx, fmaf(g4.y, ry, g4.z * rz)) * ir;
-    const float G = __fdividef(1.0f, 1.0f - Mr);
-    const float qa = p.a0f * ir;
-    const float K = fmaf(qa, Mr - g1.w, Mdr);
-    const float base = ir * G * G;
-    SmpF o;
-    o.pt = g2.w * base * G * K;
-    o.pl = g0.w * base * fmaf(Lr * G, K, fmaf(qa, Lr - g3.w, Ldr));
+    const float4 lo = *reinterpret_cast<const float4*>(half0);
+    const float4 hi = *reinterpret_cast<const float4*>(half0 + kWin * 4);
+    G2 g;
+    g.x = make_float2(lo.x, lo.y);
+    g.y = make_float2(lo.z, lo.w);
+    g.z = make_float2(hi.x, hi.y);
+    g.w = make_float2(hi.z, hi.w);
+    return g;
+}
+
+// The samples of one step of an element pair, in packed FP32 (see the comment above for
+// the integrand and the anchored retarded time).  g[q] = group q of the pair's records.
+__device__ __forceinline__ void sample_mixed2(const G2* g, float ox, float oy, float oz, const Anchor& an,
+                                              const KParams& p, int tau, DeviceErr* err, SmpF& oa, SmpF& ob)
+{
+    const float2 OX = f2(ox), OY = f2(oy), OZ = f2(oz);
+    const float2 dx = sub2(OX, g[0].x), dy = sub2(OY, g[0].y), dz = sub2(OZ, g[0].z);
+    // anchored retarded time (g4.w = x.v): -num = x.(d + D0) - 2 t0 x.v
+    const float2 S = fma2(g[0].x, add2(dx, OX), fma2(g[0].y, add2(dy, OY), mul2(g[0].z, add2(dz, OZ))));
+    const float2 nnum = fma2(f2(-an.t2), g[4].w, S);
+    const float2 bp = sub2(f2(an.s0), g[4].w);
+    const float2 q = fma2(f2(-p.alphaf), nnum, mul2(bp, bp));
+    const float2 den = fma2(q, make_float2(rsqrtf(q.x), rsqrtf(q.y)), bp);
+    const float2 dt = mul2(nnum, make_float2(__fdividef(-1.0f, den.x), __fdividef(-1.0f, den.y)));
+    const float2 tr = add2(f2(an.t0), dt);
+    const float2 rx = fma2(f2(-p.vxf), tr, dx), ry = fma2(f2(-p.vyf), tr, dy), rz = fma2(f2(-p.vzf), tr, dz);
+    const float2 ir = rcp2(mul2(f2(p.a0f), tr));
+    const float2 Mr = mul2(fma2(g[1].x, rx, fma2(g[1].y, ry, mul2(g[1].z, rz))), ir);
+    const float2 Mdr = mul2(fma2(g[2].x, rx, fma2(g[2].y, ry, mul2(g[2].z, rz))), ir);
+    const float2 Lr = mul2(fma2(g[3].x, rx, fma2(g[3].y, ry, mul2(g[3].z, rz))), ir);
+    const float2 Ldr = mul2(fma2(g[4].x, rx, fma2(g[4].y, ry, mul2(g[4].z, rz))), ir);
+    const float2 G = rcp2(sub2(f2(1.0f), Mr));
+    const float2 qa = mul2(f2(p.a0f), ir);
+    const float2 K = fma2(qa, sub2(Mr, g[1].w), Mdr);
+    const float2 base = mul2(mul2(ir, G), G);
+    const float2 pt = mul2(mul2(g[2].w, base), mul2(G, K));
+    const float2 pl = mul2(mul2(g[0].w, base), fma2(mul2(Lr, G), K, fma2(qa, sub2(Lr, g[3].w), Ldr)));
     // observer time in bins: tau + round(t0 oM/dPsi) + x, x = frac(t0 oM/dPsi) + dt oM/dPsi
-    const float x = fmaf(dt, p.kbhi, an.kf);
-    if (!(fabsf(x) < 4.0e6f)) flag(err, ACUM_DEVERR_ORDER, &err->order);  // outside the rounding's range
-    const float t = __fadd_rn(x, kRound);
-    o.k = tau + an.ki + (__float_as_int(t) - kRoundBits);
-    o.f = x - __fsub_rn(t, kRound);
-    return o;
+    const float2 x = fma2(dt, f2(p.kbhi), f2(an.kf));
+    if (!(fabsf(x.x) < 4.0e6f) || !(fabsf(x.y) < 4.0e6f)) flag(err, ACUM_DEVERR_ORDER, &err->order);
+    const float2 t = add2(x, f2(kRound));
+    const float2 fr = sub2(x, add2(t, f2(-kRound)));
+    const int kb = tau + an.ki - kRoundBits;
+    oa.k = kb + __float_as_int(t.x);
+    ob.k = kb + __float_as_int(t.y);
+    oa.f = fr.x;
+    ob.f = fr.y;
+    oa.pt = pt.x;
+    ob.pt = pt.y;
+    oa.pl = pl.x;
+    ob.pl = pl.y;
 }
 
 __device__ __forceinline__ int mod_T(int n, int T, unsigned m)
@@ -710,7 +747,9 @@ __device__ __forceinline__ SmpF shfl_idx(const SmpF& v, int src)
 }
 
 // Block-wide shared state of the mixed kernels besides the dynamic shared memory.
-struct MixedShared {
+struct __align__(16) MixedShared {
+    SmpF carry[16][2][4];  // per warp: left neighbour of lane 0, double-buffered by window parity
+    SmpF first[16][4];     // per warp: first sample of each element of the stage (periodic wrap)
     int abort;
     int release[kMaxStages];
     int last[kMaxStages];
@@ -739,16 +778,18 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
     const int N = ngroups * nW;
     const unsigned g0 = gbase;
 
+    // stage = SE / 2 element-pair tiles of one window (2 kTile floats each)
     const float* rec = reinterpret_cast<const float*>(p.rec);
-    const uint32_t tile_bytes = kTile * sizeof(float);
+    const uint32_t pair_bytes = 2 * kTile * sizeof(float);
     auto issue = [&](int i) {
         const unsigned gi = g0 + (unsigned)i;
         const int s = (int)(gi % (unsigned)NS), g = i / nW, w = i % nW;
         sh.last[s] = (int)gi;
-        mbar_expect_tx(&bars[s], tile_bytes * SE);
-        for (int j = 0; j < SE; ++j) {
-            const int e = e0 + g * SE + j;
-            bulk_g2s(stages + ((size_t)s * SE + j) * kTile, rec + ((size_t)e * nW + w) * kTile, tile_bytes, &bars[s]);
+        mbar_expect_tx(&bars[s], pair_bytes * (SE / 2));
+        for (int jp = 0; jp < SE / 2; ++jp) {
+            const int pr = (e0 + g * SE) / 2 + jp;
+            bulk_g2s(stages + ((size_t)s * SE + 2 * jp) * kTile, rec + ((size_t)pr * nW + w) * (2 * kTile), pair_bytes,
+                     &bars[s]);
         }
     };
     if (threadIdx.x == 0)
@@ -760,7 +801,6 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
     const float ox = p.obs32[3 * oc], oy = p.obs32[3 * oc + 1], oz = p.obs32[3 * oc + 2];
     float2* acc = acc_all + (size_t)warp * T;
     const Anchor anc = make_anchor(p, ox, oy, oz);
-    SmpF carry[SE], first[SE];
 
     int s = (int)(g0 % (unsigned)NS), w = 0, g = 0, since_flush = 0;
     uint32_t par = (g0 / (unsigned)NS) & 1u;
@@ -779,26 +819,28 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
         const float* st = stages + (size_t)s * SE * kTile;
         SmpF cur[SE];
 #pragma unroll
-        for (int j = 0; j < SE; ++j) {
-            const float* tl = st + (size_t)j * kTile + lane * 4;
-            float4 gg[kGroups];
+        for (int jp = 0; jp < SE / 2; ++jp) {
+            const float* tl = st + (size_t)(2 * jp) * kTile + lane * 4;
+            G2 gg[kGroups];
 #pragma unroll
-            for (int q = 0; q < kGroups; ++q) gg[q] = *reinterpret_cast<const float4*>(tl + q * kWin * 4);
-            cur[j] = sample_mixed(gg[0], gg[1], gg[2], gg[3], gg[4], ox, oy, oz, anc, p, tau, p.err);
+            for (int q = 0; q < kGroups; ++q) gg[q] = load_g2(tl + q * 2 * kWin * 4);
+            sample_mixed2(gg, ox, oy, oz, anc, p, tau, p.err, cur[2 * jp], cur[2 * jp + 1]);
         }
         const bool first_win = w == 0, last_win = w == nW - 1;
         const int rot_src = (lane + 31) & 31;
 #pragma unroll
         for (int j = 0; j < SE; ++j) {
-            const SmpF rot = shfl_idx(cur[j], rot_src);
-            const SmpF prev = lane == 0 ? carry[j] : rot;
+            // the left neighbour: lane l - 1, or for lane 0 the previous window's lane 31
+            // (kept in shared memory, double-buffered by window parity)
+            SmpF prev = shfl_idx(cur[j], rot_src);
+            if (lane == 0) prev = sh.carry[warp][w & 1][j];
             deposit(acc, T, p.tmod, prev, cur[j], 0, ok_obs && valid && !(first_win && lane == 0), p.err);
-            carry[j] = rot;
-            if (first_win && lane == 0) first[j] = cur[j];
+            if (lane == 31) sh.carry[warp][(w + 1) & 1][j] = cur[j];
+            if (first_win && lane == 0) sh.first[warp][j] = cur[j];
             if (last_win) {
                 // the periodic wrap: (t(T-1), t(0) + period] (core.cu:173-194)
                 const SmpF lastS = shfl_idx(cur[j], min(31, T - 1 - w * kWin));
-                if (lane == 0) deposit(acc, T, p.tmod, lastS, first[j], T, ok_obs, p.err);
+                if (lane == 0) deposit(acc, T, p.tmod, lastS, sh.first[warp][j], T, ok_obs, p.err);
             }
         }
         // FP32 partial sums cover at most `flush_groups` element groups before they are
@@ -945,8 +987,8 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
     const int T = r.g.T;
     int W = W_req > 0 ? W_req : 16;
     W = std::min(W, 16);
-    // keep 1 KB of the per-block limit for the kernel's static shared memory
-    const size_t budget = smem_optin - 1024;
+    // keep 4 KB of the per-block limit for the kernels' static shared memory
+    const size_t budget = smem_optin - 4096;
     while (W > opw && tonal_smem(W, T, 4, SE, rb) > budget) W -= opw;
     if (tonal_smem(W, T, 4, SE, rb) > budget) return cudaErrorInvalidValue;
     if (W_req <= 0) {
@@ -976,12 +1018,14 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
     const int groups = r.g.Epad / SE;
     if (!f64) {
         // Mixed: element chunks whose FP32 records (nW x 2560 B per element) take about
-        // 16 MB, so that the blocks running at one time (which work on one chunk) find the
-        // chunk in L2 and each record is read from HBM about once per launch; smaller if
-        // needed to give every slot `items_per_sm` items (default 8).  The FP32 bin rows
-        // are flushed every 128 elements.
+        // 32 MB, so that the blocks running at one time (which work on one chunk) find the
+        // chunk in L2 and each record is read from HBM a few times per launch at most;
+        // smaller if needed to give every slot `items_per_sm` items (default 8).  The FP32
+        // bin rows are flushed to the FP64 sums once per item (at most 512 elements):
+        // larger chunks would re-read records, smaller ones would add FP64 flush traffic.
         const size_t per_elem = (size_t)r.g.nW * kGroups * kWin * 4 * sizeof(float);
-        long chunk = (long)std::max<size_t>((size_t)SE, ((size_t)16 << 20) / per_elem);
+        long chunk = (long)std::max<size_t>((size_t)SE, ((size_t)32 << 20) / per_elem);
+        chunk = std::min<long>(chunk, 512);
         const int ips = items_per_sm > 0 ? items_per_sm : 8;
         const long want = std::max<long>(1, ((long)ips * slots + obs_tiles - 1) / obs_tiles);
         chunk = std::min(chunk, ((long)r.g.Epad + want - 1) / want);
@@ -989,13 +1033,11 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
         t.chunk = (int)chunk;
         t.nchunk = (int)(((long)r.g.Epad + chunk - 1) / chunk);
         t.items = obs_tiles * t.nchunk;
-        // observer tiles per group: their FP64 sums (W x T x 16 B per tile) within ~48 MB
-        int G = (int)std::max<size_t>(1, ((size_t)48 << 20) / ((size_t)W * r.g.T * 16));
-        G = std::min(G, obs_tiles);
-        const int ngroups = (obs_tiles + G - 1) / G;
-        t.tile_group = (obs_tiles + ngroups - 1) / ngroups;
+        // one group of all observer tiles: grouping them so that their FP64 sums stay in
+        // L2 re-reads the records once per group and measured no faster
+        t.tile_group = obs_tiles;
         t.grid = std::min(t.items, slots);
-        t.flush_elems = 128;
+        t.flush_elems = t.chunk;
         return cudaSuccess;
     }
     const int ips = items_per_sm > 0 ? items_per_sm : 64;
