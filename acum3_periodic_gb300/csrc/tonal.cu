@@ -689,13 +689,10 @@ __device__ __forceinline__ float small_int_to_float(int v)
     return __int_as_float(v + kRoundBits) - kRound;  // exact for |v| < 2^22
 }
 
-// RMW of one bin of a warp's observer row
-__device__ __forceinline__ void add_bin(float2* acc, int idx, float w, float pt, float dT, float pl, float dL)
+// RMW of one bin of a warp's observer row: (pT, pL) += p(a) + w (p(b) - p(a)), packed
+__device__ __forceinline__ void add_bin(float2* acc, int idx, float w, float2 pa, float2 dp)
 {
-    float2 v = acc[idx];
-    v.x += fmaf(w, dT, pt);
-    v.y += fmaf(w, dL, pl);
-    acc[idx] = v;
+    acc[idx] = fma2(f2(w), dp, add2(acc[idx], pa));
 }
 
 // bins n with u(a) < n <= u(b) + kshift, u = k + f with f in [-0.5, 0.5], the value
@@ -711,23 +708,23 @@ __device__ __forceinline__ void deposit(float2* acc, int T, unsigned tm, const S
     const bool fast = active && cnt >= 1 && cnt <= 2 && du > 0.0f;
     if (fast) {
         const float inv = __fdividef(1.0f, du);
-        const float dT = b.pt - a.pt, dL = b.pl - a.pl;
+        const float2 pa = make_float2(a.pt, a.pl), dp = sub2(make_float2(b.pt, b.pl), pa);
         int idx = mod_T(a.k + (a_up ? 1 : 0), T, tm);
         const float w1 = ((a_up ? 1.0f : 0.0f) - a.f) * inv;
-        add_bin(acc, idx, w1, a.pt, dT, a.pl, dL);
+        add_bin(acc, idx, w1, pa, dp);
         if (cnt == 2) {
             if (++idx == T) idx = 0;
-            add_bin(acc, idx, w1 + inv, a.pt, dT, a.pl, dL);
+            add_bin(acc, idx, w1 + inv, pa, dp);
         }
     } else if (active && !(cnt == 0 && du > 0.0f)) {
         // more than two bins in one step (|Mr| > 1) or a decreasing / non-finite time
         if (cnt > 2 && cnt <= T && du > 0.0f) {
             const float inv = __fdividef(1.0f, du);
-            const float dT = b.pt - a.pt, dL = b.pl - a.pl;
+            const float2 pa = make_float2(a.pt, a.pl), dp = sub2(make_float2(b.pt, b.pl), pa);
             int idx = mod_T(a.k + (a_up ? 1 : 0), T, tm);
             const float f0 = (a_up ? 1.0f : 0.0f) - a.f;
             for (int m = 0; m < cnt; ++m) {
-                add_bin(acc, idx, (f0 + (float)m) * inv, a.pt, dT, a.pl, dL);
+                add_bin(acc, idx, (f0 + (float)m) * inv, pa, dp);
                 if (++idx == T) idx = 0;
             }
         } else {
