@@ -38,6 +38,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "elem·obs·step evals/s: mixed vs FP64 at ≤0.05 dB OASPL; adjoint/fwd ratio"
 ALG_FLOPS_PER_EVAL = 102  # FP ops per tonal evaluation (integrand + observer time + deposits)
+# DRAM bytes (read + write) of one workload-2 launch of the mixed kernel, measured with ncu
+# (one pass: dram__bytes_read.sum + dram__bytes_write.sum); mostly the FP64 flushes of the
+# FP32 bin rows, the records themselves being read about once
+TONAL_TRAFFIC_BYTES = 33.86e9
 WORKLOAD = "workload 2: 4-blade rotor, 32000 elements, 1440 steps/rev, 4096 observers, tonal mixed precision"
 
 
@@ -399,7 +403,9 @@ def main():
         "kernels_ms_per_step": {"preprocess": float(np.mean(prep_ms)), "tonal_mixed": kms,
                                 "finalize": float(np.mean(fin_ms))},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": achieved / fp32_peak, "traffic": None,
+                     "frac": achieved / fp32_peak, "traffic": TONAL_TRAFFIC_BYTES,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one full-size "
+                                       "launch of this kernel (bytes per launch; algorithmic: %d)" % rec_bytes,
                      "peak_source": "measured FP32 FMA throughput of this GPU (acum_measure_peak); "
                                     "MEASURED_PEAKS.json holds no CUDA-core FP32 peak",
                      "algorithmic_flops_per_eval": ALG_FLOPS_PER_EVAL,
