@@ -1,8 +1,10 @@
 // probe.cu -- measures the FP32 and FP64 FMA throughput of the device (the CUDA-core
-// peaks the tonal kernels are compute-bound against), with CUDA events.
+// peaks the tonal kernels are compute-bound against), with CUDA events; and a self-test
+// of the bounded barrier wait that every pipelined kernel uses.
 #include <cuda_runtime.h>
 
 #include "acum_internal.h"
+#include "ptx.h"
 
 namespace {
 
@@ -46,7 +48,54 @@ cudaError_t measure(int sms, int iters, double* tflops)
     return cudaGetLastError();
 }
 
+// One block waits on an mbarrier whose phase is completed (arrive = 1) or never completed
+// (arrive = 0) with the bounded wait of the kernels; reports whether it gave up and how
+// long it waited.
+__global__ void wait_selftest_kernel(unsigned long long limit_ns, int arrive, int* timed_out,
+                                     unsigned long long* waited_ns)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        acum::mbar_init(&bar, 1);
+        acum::mbar_fence_init();
+    }
+    __syncthreads();
+    if (arrive && threadIdx.x == 0) acum::mbar_arrive(&bar);
+    __syncthreads();
+    const unsigned long long t0 = acum::global_ns();
+    const bool ok = acum::mbar_wait_bounded(&bar, 0u, limit_ns);
+    const unsigned long long dt = acum::global_ns() - t0;
+    if (threadIdx.x == 0) {
+        *timed_out = ok ? 0 : 1;
+        *waited_ns = dt;
+    }
+}
+
 }  // namespace
+
+extern "C" int acum_selftest_wait(int device, double limit_s, int arrive, int* timed_out, double* waited_s)
+{
+    if (!timed_out || !waited_s || !(limit_s > 0.0) || limit_s > 10.0) return ACUM_ERR_INVALID;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    if (cudaSetDevice(device) != cudaSuccess) return ACUM_ERR_CUDA;
+    int* d_to = nullptr;
+    unsigned long long* d_ns = nullptr;
+    cudaError_t e = cudaMalloc(&d_to, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&d_ns, sizeof(unsigned long long));
+    if (e == cudaSuccess) {
+        wait_selftest_kernel<<<1, 32>>>((unsigned long long)(limit_s * 1e9), arrive ? 1 : 0, d_to, d_ns);
+        e = cudaDeviceSynchronize();
+    }
+    unsigned long long ns = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(timed_out, d_to, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&ns, d_ns, sizeof(ns), cudaMemcpyDeviceToHost);
+    if (d_to) cudaFree(d_to);
+    if (d_ns) cudaFree(d_ns);
+    cudaSetDevice(prev);
+    *waited_s = ns * 1e-9;
+    return e == cudaSuccess ? ACUM_OK : ACUM_ERR_CUDA;
+}
 
 extern "C" int acum_measure_peak(int device, int which, double* tflops)
 {

@@ -43,15 +43,35 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
     return ok != 0;
 }
 
-// Every wait on a barrier is bounded: after kMaxSpin polls the wait gives up, records
-// ACUM_DEVERR_TIMEOUT and the kernel unwinds instead of hanging.
-constexpr long kMaxSpin = 1L << 24;
+// Every wait on a barrier is bounded in time: it gives up after limit_ns of the global
+// timer (2 s by default; kMaxSpin polls should the timer not advance), and the caller
+// records ACUM_DEVERR_TIMEOUT and unwinds instead of hanging.  A wait whose first poll
+// succeeds (the common case) reads no timer.
+constexpr unsigned long long kWaitLimitNs = 2000000000ull;
+constexpr long kMaxSpin = 1L << 26;
 
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity)
+__device__ __forceinline__ unsigned long long global_ns()
 {
-    for (long it = 0; it < kMaxSpin; ++it)
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+                                                  unsigned long long limit_ns = kWaitLimitNs)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    for (long it = 0; it < kMaxSpin; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 255) == 255 && global_ns() - t0 > limit_ns) return false;
+    }
     return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 // bulk TMA copy global -> shared, completion signalled on `bar` (bytes % 16 == 0,

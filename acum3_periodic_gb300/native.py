@@ -71,6 +71,7 @@ SIGNATURES = {
     "acum_surfaces_device_ptr": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "acum_mark_surfaces_changed": (C.c_int, [C.c_void_p]),
     "acum_sync": (C.c_int, [C.c_void_p]),
+    "acum_selftest_wait": (C.c_int, [C.c_int, C.c_double, C.c_int, _IP, _DP]),
     "acum_read_deck_sizes": (C.c_int, [C.c_char_p, C.POINTER(C.c_longlong)]),
     "acum_last_plan": (C.c_int, [C.c_void_p, _IP]),
     "acum_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
@@ -399,6 +400,15 @@ class Batch:
         ms = C.c_double()
         self._ck(self.L.acum_batch_case_timing(self.h, case, C.byref(ms)))
         return ms.value
+
+
+def selftest_wait(device: int, limit_s: float, arrive: bool):
+    """(timed_out, waited_s) of one bounded barrier wait on the device."""
+    to, ws = C.c_int(), C.c_double()
+    rc = lib().acum_selftest_wait(device, limit_s, 1 if arrive else 0, C.byref(to), C.byref(ws))
+    if rc != 0:
+        raise AcumError(rc, "acum_selftest_wait failed")
+    return bool(to.value), ws.value
 
 
 class PinnedBuffer:

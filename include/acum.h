@@ -173,6 +173,13 @@ int acum_set_tile(acum_ctx* ctx, int obs_per_block, int elems_per_stage, int ite
  * [2] pipeline stages, [3] elements per work item, [4] element chunks, [5] work items. */
 int acum_last_plan(const acum_ctx* ctx, int* out);
 
+/* Self-test of the bounded wait that every pipelined kernel uses on its barriers: one
+ * block waits on a barrier that is completed (arrive = 1) or never completed (arrive = 0)
+ * and gives up after limit_s (0 < limit_s <= 10); *timed_out = 1 if it gave up, *waited_s
+ * the device time it waited.  The kernels themselves give up after 2 s, record
+ * ACUM_DEVERR_TIMEOUT and return; the context stays usable. */
+int acum_selftest_wait(int device, double limit_s, int arrive, int* timed_out, double* waited_s);
+
 /* Measured FMA throughput of `device` in TFLOP/s: which = 0 FP32, 1 FP64 (a short
  * FMA-chain kernel timed with CUDA events; the CUDA-core peaks of the roofline). */
 int acum_measure_peak(int device, int which, double* tflops);
