@@ -18,8 +18,9 @@
 //  bb_obs_kernel     per (observer, section, step, band): D from the observer geometry
 //      (once per (observer, section, step), shared by all bands through shared memory),
 //      then the energies max(D*A, 1e-10) (the reference's -100 dB clip) summed over
-//      sections and steps in FP32 partial sums folded into FP64; lane = observer, so
-//      each amplitude is read once per warp as a shared-memory broadcast.
+//      sections and steps in FP32 partial sums folded into FP64; lane = observer and
+//      warp = band pair, so each amplitude is read once per warp as a shared-memory
+//      broadcast and one packed FP32 instruction covers both bands.
 //  bb_final_kernel   the energy means over steps and the band sum, in FP64 dB
 //      (bb_core.cu:563-583).
 //
@@ -508,40 +509,43 @@ __global__ void bb_spec_kernel(const float* __restrict__ sc, const double* __res
         const float lg = log10f(f * q[25] / q[26]) + 0.3f;
         Av = exp10f((126.0f - 30.5f * (lg * lg)) * 0.1f);
     }
-    float4* o = reinterpret_cast<float4*>(amp + id * kAmp);
-    o[0] = make_float4(Ap, As, Aa, Al);
-    o[1] = make_float4(At, Av, q[27], 0.f);
+    // band pairs interleaved: [item][band / 2][field][band % 2] (the operand pairs of the
+    // packed contraction in bb_obs_kernel)
+    float* o = amp + st * (kBands * kAmp) + (size_t)(fb >> 1) * (2 * kAmp) + (fb & 1);
+    const float v[kAmp] = {Ap, As, Aa, Al, At, Av, q[27], 0.f};
+#pragma unroll
+    for (int c = 0; c < kAmp; ++c) o[2 * c] = v[c];
 }
 
 // Observer contraction.  Block = 64 observers (lane l serves observers l and l + 32) x
-// 14 warps of 3 bands.  Per tile of kTI (section, step) items, the amplitudes of all 42
-// bands (contiguous in `amp`, 1344 B per item) and the items' geometry records arrive in
-// shared memory by one bulk copy into a double buffer (the next tile's copy runs while
-// this one is consumed); the directivity factors D of the block's observers for the
-// tile are computed once into shared memory; then each lane adds, for its two observers
-// and its warp's 3 bands, the clipped energies of every item.  The amplitude reads are
-// warp-uniform (one shared-memory broadcast per band and item, shared by two
-// observers), the D reads conflict-free.  FP32 partial sums over at most 1024 items are
-// folded into FP64 sums private to the block's (observer tile, item range):
+// 21 warps, one per pair of bands.  Per tile of kTI (section, step) items, the amplitudes
+// of all 42 bands (contiguous in `amp`, 1344 B per item, band pairs interleaved) and the
+// items' geometry records arrive in shared memory by one bulk copy into a double buffer
+// (the next tile's copy runs while this one is consumed); the directivity factors D of the
+// block's observers for the tile are computed once into shared memory (each stored twice,
+// as the operand pair of a packed instruction); then each lane adds, for its two
+// observers and its warp's two bands, the clipped energies of every item in packed FP32
+// (one f32x2 operation covers both bands).  The amplitude reads are warp-uniform (shared-
+// memory broadcasts), the D reads conflict-free.  FP32 partial sums over at most 1024
+// items are folded into FP64 sums private to the block's (observer tile, item range):
 // part[split][band][component][observer], reduced over the splits by bb_final_kernel.
 constexpr int kObsPerLane = 2;
-constexpr int kObsBlock = 32 * kObsPerLane;         // 64
-constexpr int kBandsPerWarp = 3;
-constexpr int kBandWarps = kBands / kBandsPerWarp;  // 14
-constexpr int kBpmThreads = 32 * kBandWarps;        // 448
-constexpr int kTI = 16;                             // items per tile
-constexpr int kFoldTiles = 64;                      // 1024 items per FP32 partial
-constexpr int kAmpItemBytes = kBands * kAmp * 4;    // 1344
-constexpr int kGeoItemBytes = kGeo * 4;             // 64
-static_assert(kBands % kBandsPerWarp == 0, "band split");
+constexpr int kObsBlock = 32 * kObsPerLane;  // 64
+constexpr int kPairWarps = kBands / 2;       // 21
+constexpr int kBpmThreads = 32 * kPairWarps; // 672
+constexpr int kTI = 16;                      // items per tile
+constexpr int kFoldTiles = 64;               // 1024 items per FP32 partial
+constexpr int kAmpItemBytes = kBands * kAmp * 4;  // 1344
+constexpr int kGeoItemBytes = kGeo * 4;           // 64
+static_assert(kBands % 2 == 0, "band pairs");
 static_assert(kAmpItemBytes % 16 == 0 && kGeoItemBytes % 16 == 0, "bulk copy granularity");
 
 // dynamic shared memory of bb_obs_kernel: 2 x (amplitude tile + geometry tile), the D
-// tile, the block's observers, 2 mbarriers
+// tile (float4 (Dh, Dh, Dl, Dl) per item and observer), the block's observers, 2 mbarriers
 constexpr size_t kObsSmemA = (size_t)kTI * kAmpItemBytes;
 constexpr size_t kObsSmemG = (size_t)kTI * kGeoItemBytes;
 constexpr size_t kObsSmemBuf = kObsSmemA + kObsSmemG;
-constexpr size_t kObsSmemD = (size_t)kTI * kObsBlock * sizeof(float2);
+constexpr size_t kObsSmemD = (size_t)kTI * kObsBlock * sizeof(float4);
 constexpr size_t kObsSmem = 2 * kObsSmemBuf + kObsSmemD + kObsBlock * 3 * sizeof(float) + 2 * sizeof(uint64_t);
 
 __device__ __forceinline__ float2 bb_directivity(const float* geo, const float* obs, int o, float vx, float vy,
@@ -577,6 +581,8 @@ __device__ __forceinline__ float2 bb_directivity(const float* geo, const float* 
     return make_float2(Dh, g3.z != 0.f ? Dl : Dh);
 }
 
+__device__ __forceinline__ float2 clip2(float2 v, float lo) { return make_float2(fmaxf(v.x, lo), fmaxf(v.y, lo)); }
+
 __global__ void __launch_bounds__(kBpmThreads, 1) bb_obs_kernel(const float* __restrict__ geo,
                                                                 const float* __restrict__ amp,
                                                                 const float* __restrict__ obs, int O, long long nst,
@@ -585,10 +591,10 @@ __global__ void __launch_bounds__(kBpmThreads, 1) bb_obs_kernel(const float* __r
                                                                 DeviceErr* err)
 {
     extern __shared__ __align__(128) unsigned char sm[];
-    float2* sD = reinterpret_cast<float2*>(sm + 2 * kObsSmemBuf);  // [kTI][kObsBlock]
+    float4* sD = reinterpret_cast<float4*>(sm + 2 * kObsSmemBuf);  // [kTI][kObsBlock]
     float* sObs = reinterpret_cast<float*>(sm + 2 * kObsSmemBuf + kObsSmemD);
     uint64_t* bars = reinterpret_cast<uint64_t*>(sm + 2 * kObsSmemBuf + kObsSmemD + kObsBlock * 3 * sizeof(float));
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;  // warp = band pair
     const int o0 = blockIdx.x * kObsBlock;
     const long long st_begin = (long long)blockIdx.y * per_split;
     const long long st_end = min(nst, st_begin + per_split);
@@ -620,13 +626,11 @@ __global__ void __launch_bounds__(kBpmThreads, 1) bb_obs_kernel(const float* __r
     if (threadIdx.x == 0)
         for (int j = 0; j < 2 && j < ntiles; ++j) issue(j);
 
-    float acc[kObsPerLane][kBandsPerWarp][6];
+    float2 acc[kObsPerLane][6];  // (band 2 warp, band 2 warp + 1)
 #pragma unroll
     for (int q = 0; q < kObsPerLane; ++q)
 #pragma unroll
-        for (int b = 0; b < kBandsPerWarp; ++b)
-#pragma unroll
-            for (int c = 0; c < 6; ++c) acc[q][b][c] = 0.f;
+        for (int c = 0; c < 6; ++c) acc[q][c] = make_float2(0.f, 0.f);
     auto fold = [&]() {
 #pragma unroll
         for (int q = 0; q < kObsPerLane; ++q) {
@@ -635,19 +639,16 @@ __global__ void __launch_bounds__(kBpmThreads, 1) bb_obs_kernel(const float* __r
                 // addresses formed here, not hoisted out of the item loop
                 size_t stride = (size_t)O;
                 asm volatile("" : "+l"(stride));
-                double* p = mine + (size_t)warp * kBandsPerWarp * 6 * stride + o;
+                double* p0 = mine + (size_t)(2 * warp) * 6 * stride + o;  // band 2 warp
+                double* p1 = p0 + 6 * stride;                             // band 2 warp + 1
 #pragma unroll
-                for (int b = 0; b < kBandsPerWarp; ++b)
-#pragma unroll
-                    for (int c = 0; c < 6; ++c) {
-                        *p += (double)acc[q][b][c];
-                        p += stride;
-                    }
+                for (int c = 0; c < 6; ++c) {
+                    p0[c * stride] += (double)acc[q][c].x;
+                    p1[c * stride] += (double)acc[q][c].y;
+                }
             }
 #pragma unroll
-            for (int b = 0; b < kBandsPerWarp; ++b)
-#pragma unroll
-                for (int c = 0; c < 6; ++c) acc[q][b][c] = 0.f;
+            for (int c = 0; c < 6; ++c) acc[q][c] = make_float2(0.f, 0.f);
         }
     };
     int aborted_at = -1;
@@ -670,26 +671,29 @@ __global__ void __launch_bounds__(kBpmThreads, 1) bb_obs_kernel(const float* __r
             const int it = pidx / kObsBlock, ol = pidx % kObsBlock;
             float2 D = make_float2(0.f, 0.f);
             if (it < n && o0 + ol < O) D = bb_directivity(sG + it * kGeo, sObs, ol, vx, vy, vz, aa, iaMv);
-            sD[it * kObsBlock + ol] = D;
+            sD[it * kObsBlock + ol] = make_float4(D.x, D.x, D.y, D.y);
         }
         __syncthreads();
 #pragma unroll 1
         for (int it = 0; it < n; ++it) {
-            const float2 D0 = sD[it * kObsBlock + lane], D1 = sD[it * kObsBlock + 32 + lane];
+            // the warp's band pair: fields (Ap, As), (Aa, Al), (At, Av), (gtip, -) of both bands
+            const float4* a = sA + (it * kPairWarps + warp) * 4;
+            const float4 a0v = a[0], a1v = a[1], a2v = a[2], a3v = a[3];
+            const float2 Ap = make_float2(a0v.x, a0v.y), As = make_float2(a0v.z, a0v.w);
+            const float2 Aa = make_float2(a1v.x, a1v.y), Al = make_float2(a1v.z, a1v.w);
+            const float2 At = make_float2(a2v.x, a2v.y), Av = make_float2(a2v.z, a2v.w);
+            const float2 Ag = make_float2(a3v.x, a3v.y);
+            const bool tip = Av.x != 0.f || Av.y != 0.f;
 #pragma unroll
-            for (int b = 0; b < kBandsPerWarp; ++b) {
-                const int band = warp * kBandsPerWarp + b;
-                const float4 A0 = sA[(it * kBands + band) * 2], A1 = sA[(it * kBands + band) * 2 + 1];
-#pragma unroll
-                for (int q = 0; q < kObsPerLane; ++q) {
-                    const float2 D = q == 0 ? D0 : D1;
-                    acc[q][b][0] += fmaxf(D.x * A0.x, 1e-10f);  // TBL-TE pressure side
-                    acc[q][b][1] += fmaxf(D.x * A0.y, 1e-10f);  // TBL-TE suction side
-                    acc[q][b][2] += fmaxf(D.y * A0.z, 1e-10f);  // separation
-                    acc[q][b][3] = fmaf(D.x, A0.w, acc[q][b][3]);  // LBL-VS
-                    acc[q][b][4] = fmaf(D.x, A1.x, acc[q][b][4]);  // TEB-VS
-                    if (A1.y != 0.f) acc[q][b][5] += A1.y * fmaxf(D.x * A1.z, 2.2204460492503131e-16f);  // tip
-                }
+            for (int q = 0; q < kObsPerLane; ++q) {
+                const float4 D = sD[it * kObsBlock + q * 32 + lane];
+                const float2 Dh = make_float2(D.x, D.y), Dl = make_float2(D.z, D.w);
+                acc[q][0] = add2(acc[q][0], clip2(mul2(Dh, Ap), 1e-10f));  // TBL-TE pressure side
+                acc[q][1] = add2(acc[q][1], clip2(mul2(Dh, As), 1e-10f));  // TBL-TE suction side
+                acc[q][2] = add2(acc[q][2], clip2(mul2(Dl, Aa), 1e-10f));  // separation
+                acc[q][3] = fma2(Dh, Al, acc[q][3]);                       // LBL-VS
+                acc[q][4] = fma2(Dh, At, acc[q][4]);                       // TEB-VS
+                if (tip) acc[q][5] = fma2(Av, clip2(mul2(Dh, Ag), 2.2204460492503131e-16f), acc[q][5]);  // tip
             }
         }
         // every thread is done with this buffer and the D tile: refill with tile j + 2

@@ -1,5 +1,5 @@
 // ptx.h -- device helpers shared by the kernels: mbarrier operations (every wait
-// bounded), the bulk (TMA) global -> shared copy, and the device error word.
+// bounded), the bulk (TMA) global -> shared copy, the device error word, packed FP32.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -90,5 +90,13 @@ __device__ __forceinline__ void flag(DeviceErr* e, unsigned bit, unsigned* count
     atomicOr(&e->bits, bit);
     atomicAdd(counter, 1u);
 }
+
+// packed FP32: two values in an f32x2 register pair, one instruction (sm_100 and later)
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+__device__ __forceinline__ float2 rcp2(float2 a) { return make_float2(__fdividef(1.0f, a.x), __fdividef(1.0f, a.y)); }
 
 }  // namespace acum

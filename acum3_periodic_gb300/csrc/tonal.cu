@@ -608,14 +608,6 @@ __device__ __forceinline__ Anchor make_anchor(const KParams& p, float ox, float 
     return a;
 }
 
-// packed FP32 (two lanes of an f32x2 register pair, one per element of a pair)
-__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
-__device__ __forceinline__ float2 rcp2(float2 a) { return make_float2(__fdividef(1.0f, a.x), __fdividef(1.0f, a.y)); }
-
 // One field group of an element pair as read from the FP32 records: x = both elements'
 // field 0, y = field 1, z = field 2, w = field 3.
 struct G2 {
