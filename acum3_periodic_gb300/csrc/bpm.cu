@@ -533,8 +533,8 @@ constexpr int kObsPerLane = 2;
 constexpr int kObsBlock = 32 * kObsPerLane;  // 64
 constexpr int kPairWarps = kBands / 2;       // 21
 constexpr int kBpmThreads = 32 * kPairWarps; // 672
-constexpr int kTI = 16;                      // items per tile
-constexpr int kFoldTiles = 64;               // 1024 items per FP32 partial
+constexpr int kTI = 32;                      // items per tile
+constexpr int kFoldTiles = 32;               // 1024 items per FP32 partial
 constexpr int kAmpItemBytes = kBands * kAmp * 4;  // 1344
 constexpr int kGeoItemBytes = kGeo * 4;           // 64
 static_assert(kBands % 2 == 0, "band pairs");
