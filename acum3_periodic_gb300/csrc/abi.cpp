@@ -303,7 +303,7 @@ extern "C" int acum_set_tile(acum_ctx* ctx, int obs_per_block, int elems_per_sta
 {
     if (!ctx) return ACUM_ERR_INVALID;
     if (obs_per_block < 0 || obs_per_block > 16 || items_per_sm < 0 || items_per_sm > 64 ||
-        (elems_per_stage != 0 && elems_per_stage != 2 && elems_per_stage != 4))
+        (elems_per_stage != 0 && elems_per_stage != 2 && elems_per_stage != 4 && elems_per_stage != 8))
         return fail(ctx, ACUM_ERR_INVALID, "acum_set_tile: out of range");
     ctx->tile_W = obs_per_block;
     ctx->tile_SE = elems_per_stage;

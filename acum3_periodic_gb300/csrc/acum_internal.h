@@ -143,6 +143,7 @@ constexpr int kBatchNS = 4;
 // stage SE and the longest case's nTime
 size_t batch_smem(int W, int SE, int Tmax);
 int batch_blocks_per_sm(int W, int SE, int Tmax);
+size_t batch_static_smem(int SE);  // static shared memory to keep beside batch_smem
 cudaError_t launch_tonal_batch(const KParams* d_cases, const BatchItem* d_items, int nitems, int* d_counter, int W,
                                int SE, int Tmax, int grid, cudaStream_t s);
 // acc [O][T][2] of every case -> pA [T][O] (overwrite)

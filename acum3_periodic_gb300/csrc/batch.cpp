@@ -156,8 +156,7 @@ void build_items(const acum_batch* b, int W, int SE, int ips, std::vector<BatchI
 
 bool shape_fits(const acum_batch* b, int W, int SE)
 {
-    // keep 4 KB of the per-block limit for the kernel's static shared memory
-    return batch_smem(W, SE, b->Tmax) + 4096 <= b->smem_optin;
+    return batch_smem(W, SE, b->Tmax) + batch_static_smem(SE) <= b->smem_optin;
 }
 
 int plan(acum_batch* b)

@@ -736,9 +736,10 @@ __device__ __forceinline__ SmpF shfl_idx(const SmpF& v, int src)
 }
 
 // Block-wide shared state of the mixed kernels besides the dynamic shared memory.
+template <int SE>
 struct __align__(16) MixedShared {
-    SmpF carry[16][2][4];  // per warp: left neighbour of lane 0, double-buffered by window parity
-    SmpF first[16][4];     // per warp: first sample of each element of the stage (periodic wrap)
+    SmpF carry[16][2][SE];  // per warp: left neighbour of lane 0, double-buffered by window parity
+    SmpF first[16][SE];     // per warp: first sample of each element of the stage (periodic wrap)
     int abort;
     int release[kMaxStages];
     int last[kMaxStages];
@@ -753,7 +754,7 @@ struct __align__(16) MixedShared {
 // zero; on return (without abort) the same holds again.
 template <int SE>
 __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot, int e0, int e1, unsigned char* smem,
-                                           size_t stage_off, MixedShared& sh, unsigned& gbase)
+                                           size_t stage_off, MixedShared<SE>& sh, unsigned& gbase)
 {
     constexpr int kTile = kGroups * kWin * 4;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -859,7 +860,8 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
     gbase = g0 + (unsigned)N;
 }
 
-__device__ __forceinline__ void mixed_init(unsigned char* smem, size_t stage_off, int NS, int SE, MixedShared& sh)
+template <int SE>
+__device__ __forceinline__ void mixed_init(unsigned char* smem, size_t stage_off, int NS, MixedShared<SE>& sh)
 {
     constexpr int kTile = kGroups * kWin * 4;
     float2* acc_all = reinterpret_cast<float2*>(smem);
@@ -878,7 +880,8 @@ __device__ __forceinline__ void mixed_init(unsigned char* smem, size_t stage_off
 }
 
 // After an abort: wait (bounded) for the copies still in flight before the block exits.
-__device__ __forceinline__ void mixed_drain(unsigned char* smem, size_t stage_off, int NS, int SE, MixedShared& sh)
+template <int SE>
+__device__ __forceinline__ void mixed_drain(unsigned char* smem, size_t stage_off, int NS, MixedShared<SE>& sh)
 {
     constexpr int kTile = kGroups * kWin * 4;
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + stage_off + (size_t)NS * SE * kTile * sizeof(float));
@@ -897,9 +900,9 @@ template <int SE>
 __global__ void __launch_bounds__(512, 1) tonal_mixed_kernel(const KParams p)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ MixedShared sh;
+    __shared__ MixedShared<SE> sh;
     const size_t stage_off = acc_region_bytes(p.W, p.T, 8);
-    mixed_init(smem, stage_off, p.NS, SE, sh);
+    mixed_init<SE>(smem, stage_off, p.NS, sh);
     unsigned gbase = 0;
     const int nitems = p.obs_tiles * p.nchunk;
     const int G = p.tile_group, per_group = G * p.nchunk;
@@ -913,7 +916,7 @@ __global__ void __launch_bounds__(512, 1) tonal_mixed_kernel(const KParams p)
         mixed_item<SE>(p, ot, e0, e1, smem, stage_off, sh, gbase);
         __syncthreads();
         if (sh.abort) {
-            mixed_drain(smem, stage_off, p.NS, SE, sh);
+            mixed_drain<SE>(smem, stage_off, p.NS, sh);
             break;
         }
     }
@@ -929,10 +932,10 @@ __global__ void __launch_bounds__(512, 1)
                        int* counter, int NS, size_t stage_off)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ MixedShared sh;
+    __shared__ MixedShared<SE> sh;
     __shared__ __align__(16) KParams sp;
     __shared__ BatchItem s_it;
-    mixed_init(smem, stage_off, NS, SE, sh);
+    mixed_init<SE>(smem, stage_off, NS, sh);
     unsigned gbase = 0;
     for (;;) {
         if (threadIdx.x == 0) {
@@ -949,7 +952,7 @@ __global__ void __launch_bounds__(512, 1)
         mixed_item<SE>(sp, it.ot, it.e0, it.e1, smem, stage_off, sh, gbase);
         __syncthreads();
         if (sh.abort) {
-            mixed_drain(smem, stage_off, NS, SE, sh);
+            mixed_drain<SE>(smem, stage_off, NS, sh);
             break;
         }
     }
@@ -957,7 +960,17 @@ __global__ void __launch_bounds__(512, 1)
 
 constexpr int kSE32 = 4;
 static_assert(kMaxStages >= 4, "stage bookkeeping");
+static_assert(sizeof(SmpF) == 16, "sample record");
 constexpr int kSE64 = 2;
+
+// static shared memory of the mixed kernels (MixedShared<SE> and, in the batched form,
+// the case's constants and the current item), rounded up
+static size_t mixed_static_smem(int SE)
+{
+    return (size_t)16 * 3 * SE * sizeof(SmpF) + 256;
+}
+
+size_t batch_static_smem(int SE) { return mixed_static_smem(SE) + 512; }
 
 static size_t tonal_smem(int W, int T, int NS, int SE, int real_bytes)
 {
@@ -970,16 +983,18 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
     const bool f64 = r.precision == ACUM_PLAIN_FP64;
     const int rb = f64 ? 8 : 4;
     // mixed: elements per stage 2 or 4 (default 4); FP64: 2
-    const int SE = f64 ? kSE64 : (SE_req == 2 ? 2 : kSE32);
+    // mixed: elements per stage 2, 4 (default) or 8; a stage of 8 needs only 2 ring stages
+    const int SE = f64 ? kSE64 : ((SE_req == 2 || SE_req == 8) ? SE_req : kSE32);
+    const int NSmin = SE == 8 ? 2 : 4;
     const int opw = 1;
     r.t.opw = opw;
     const int T = r.g.T;
     int W = W_req > 0 ? W_req : 16;
     W = std::min(W, 16);
-    // keep 4 KB of the per-block limit for the kernels' static shared memory
-    const size_t budget = smem_optin - 4096;
-    while (W > opw && tonal_smem(W, T, 4, SE, rb) > budget) W -= opw;
-    if (tonal_smem(W, T, 4, SE, rb) > budget) return cudaErrorInvalidValue;
+    // keep room in the per-block limit for the kernels' static shared memory
+    const size_t budget = smem_optin - (f64 ? 1024 : mixed_static_smem(SE));
+    while (W > opw && tonal_smem(W, T, NSmin, SE, rb) > budget) W -= opw;
+    if (tonal_smem(W, T, NSmin, SE, rb) > budget) return cudaErrorInvalidValue;
     if (W_req <= 0) {
         // do not spread few observers over many idle warps
         W = std::max(opw, std::min(W, (r.g.O + opw - 1) / opw * opw));
@@ -988,10 +1003,10 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
     // mixed: as many ring stages (4..8) as the shared memory left over by the bins holds,
     // without lowering the blocks per SM (registers, ~128 per thread, allow 65536 / (128 *
     // 32 W) blocks of W warps)
-    int NS = 4;
+    int NS = NSmin;
     if (!f64) {
         const auto per_sm_at = [&](int ns) { return (int)((228 * 1024) / (tonal_smem(W, T, ns, SE, rb) + 1024)); };
-        const int resident = std::max(1, std::min(per_sm_at(4), 65536 / (128 * 32 * (W / opw))));
+        const int resident = std::max(1, std::min(per_sm_at(NSmin), 65536 / (128 * 32 * (W / opw))));
         while (NS < kMaxStages && tonal_smem(W, T, NS + 1, SE, rb) <= budget && per_sm_at(NS + 1) >= resident) ++NS;
     }
     TonalTile& t = r.t;
@@ -1134,6 +1149,7 @@ cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s)
     fill_kparams(r, kp);
     if (r.precision == ACUM_PLAIN_FP64) return launch_f64_t<kSE64>(kp, r.t.items, 32 * r.t.W, r.t.smem, s);
     if (r.t.SE == 2) return launch_mixed_t<2>(kp, r.t.grid, 32 * r.t.W, r.t.smem, s);
+    if (r.t.SE == 8) return launch_mixed_t<8>(kp, r.t.grid, 32 * r.t.W, r.t.smem, s);
     return launch_mixed_t<kSE32>(kp, r.t.grid, 32 * r.t.W, r.t.smem, s);
 }
 

@@ -167,7 +167,7 @@ int acum_device_error_word(acum_ctx* ctx, uint32_t* out, int reset);
 int acum_last_timing(const acum_ctx* ctx, int which, double* ms, long long* launches);
 
 /* Tile shape of the tonal kernels (0 = let the library choose): observers per block
- * (1..16), elements per pipeline stage (mixed form: 2 or 4) and work items per SM. */
+ * (1..16), elements per pipeline stage (mixed form: 2, 4 or 8) and work items per SM. */
 int acum_set_tile(acum_ctx* ctx, int obs_per_block, int elems_per_stage, int items_per_sm);
 /* The plan of the last tonal run: out[0] observers per block, [1] elements per stage,
  * [2] pipeline stages, [3] elements per work item, [4] element chunks, [5] work items. */
