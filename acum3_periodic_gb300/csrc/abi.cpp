@@ -67,6 +67,8 @@ using namespace acum;
 void acum_ctx::release_all()
 {
     d_raw.release();
+    d_raw_alt.release();
+    raw_cur = nullptr;
     d_obs64.release();
     d_obs32.release();
     d_esurf.release();
@@ -122,6 +124,11 @@ extern "C" int acum_destroy(acum_ctx* ctx)
         ctx->release_all();
         for (int i = 0; i < kNumEvents; ++i) cudaEventDestroy(ctx->ev[i]);
         if (ctx->owns_stream) cudaStreamDestroy(ctx->stream);
+        if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+        for (int k = 0; k < 2; ++k) {
+            if (ctx->ev_copied[k]) cudaEventDestroy(ctx->ev_copied[k]);
+            if (ctx->ev_free[k]) cudaEventDestroy(ctx->ev_free[k]);
+        }
     }
     delete ctx;
     return ACUM_OK;
@@ -334,7 +341,7 @@ int acum_ctx::ensure_prep(bool need64, bool need32, bool need_fields)
     if (need_fields) CK(this, d_fields.ensure((size_t)E * T * kFields));
     PrepArgs a;
     memset(&a, 0, sizeof(a));
-    a.raw = d_raw.p;
+    a.raw = raw_cur ? raw_cur : d_raw.p;
     a.nsurf = nsurf;
     a.raw_off = d_rawoff.p;
     a.e_surf = d_esurf.p;
@@ -497,6 +504,45 @@ extern "C" int acum_sync(acum_ctx* ctx)
     if (!ctx) return ACUM_ERR_INVALID;
     DeviceGuard g(ctx->device);
     CK(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ctx->copy_stream) CK(ctx, cudaStreamSynchronize(ctx->copy_stream));
+    return ctx->finish_run();
+}
+
+extern "C" int acum_tonal_from_host_async(acum_ctx* ctx, int precision, const float* raw, double* pA_host)
+{
+    acum::NvtxRange nvtx_range_("acum_tonal_from_host_async");
+    if (!ctx || !raw || !pA_host) return fail(ctx, ACUM_ERR_INVALID, "acum_tonal_from_host_async: null argument");
+    if (!ctx->have_deck) return fail(ctx, ACUM_ERR_STATE, "no deck");
+    DeviceGuard g(ctx->device);
+    if (!ctx->copy_stream) {
+        CK(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; ++k) {
+            CK(ctx, cudaEventCreateWithFlags(&ctx->ev_copied[k], cudaEventDisableTiming));
+            CK(ctx, cudaEventCreateWithFlags(&ctx->ev_free[k], cudaEventDisableTiming));
+            CK(ctx, cudaEventRecord(ctx->ev_free[k], ctx->stream));
+        }
+    }
+    CK(ctx, ctx->d_raw_alt.ensure(ctx->raw_floats));
+    const int b = ctx->async_next;
+    ctx->async_next ^= 1;
+    float* buf = b == 0 ? ctx->d_raw.p : ctx->d_raw_alt.p;
+    const size_t n = (size_t)ctx->T * ctx->nobs;
+    CK(ctx, ctx->d_out.ensure(3 * n));
+    // the copy of this call's rows waits only for the run that last read the same buffer,
+    // so it overlaps the previous call's compute
+    CK(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_free[b], 0));
+    CK(ctx, cudaMemcpyAsync(buf, raw, ctx->raw_floats * 4, cudaMemcpyHostToDevice, ctx->copy_stream));
+    CK(ctx, cudaEventRecord(ctx->ev_copied[b], ctx->copy_stream));
+    CK(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_copied[b], 0));
+    ctx->begin_run();
+    ctx->raw_cur = buf;
+    ctx->invalidate();
+    int rc = ctx->run_tonal(precision, nullptr, nullptr, ctx->d_out.p + 2 * n);
+    ctx->raw_cur = nullptr;
+    ctx->invalidate();  // the records now hold this buffer's rows, not d_raw's
+    if (rc) return rc;
+    CK(ctx, cudaEventRecord(ctx->ev_free[b], ctx->stream));
+    CK(ctx, cudaMemcpyAsync(pA_host, ctx->d_out.p + 2 * n, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
     return ACUM_OK;
 }
 

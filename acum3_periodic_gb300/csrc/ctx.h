@@ -97,6 +97,13 @@ struct acum_ctx {
 
     // device buffers
     acum::DBuf<float> d_raw;
+    // pipelined runs from host rows (acum_tonal_from_host_async): a second row buffer,
+    // a copy stream and per-buffer events; raw_cur is the buffer the preprocessing reads
+    acum::DBuf<float> d_raw_alt;
+    float* raw_cur = nullptr;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
+    int async_next = 0;
     acum::DBuf<double> d_obs64;
     acum::DBuf<float> d_obs32;
     acum::DBuf<int> d_esurf, d_elocal, d_ecount;

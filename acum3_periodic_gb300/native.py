@@ -71,6 +71,7 @@ SIGNATURES = {
     "acum_surfaces_device_ptr": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "acum_mark_surfaces_changed": (C.c_int, [C.c_void_p]),
     "acum_sync": (C.c_int, [C.c_void_p]),
+    "acum_tonal_from_host_async": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "acum_selftest_wait": (C.c_int, [C.c_int, C.c_double, C.c_int, _IP, _DP]),
     "acum_read_deck_sizes": (C.c_int, [C.c_char_p, C.POINTER(C.c_longlong)]),
     "acum_last_plan": (C.c_int, [C.c_void_p, _IP]),
@@ -254,6 +255,9 @@ class Context:
 
     def tonal_from_host(self, precision: int, raw_ptr: int, pA_ptr: int):
         self._ck(self.L.acum_tonal_from_host(self.h, precision, C.c_void_p(raw_ptr), C.c_void_p(pA_ptr)))
+
+    def tonal_from_host_async(self, precision: int, raw_ptr: int, pA_ptr: int):
+        self._ck(self.L.acum_tonal_from_host_async(self.h, precision, C.c_void_p(raw_ptr), C.c_void_p(pA_ptr)))
 
     def tonal_device(self, precision: int, pT_ptr: int, pL_ptr: int, pA_ptr: int):
         self._ck(self.L.acum_tonal_device(self.h, precision, C.c_void_p(pT_ptr), C.c_void_p(pL_ptr),

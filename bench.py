@@ -353,12 +353,14 @@ def main():
     pin_pA = native.PinnedBuffer((deck.nTime, deck.nObs), np.float64)
     ctx.tonal_from_host(native.MIXED, pin_raw.ptr, pin_pA.ptr)
     barrier(dist)
+    # one synchronous call for the copy share of a call, then the timed steps pipelined
+    # (each step's rows copied while the previous step solves; every copy in the region)
+    ctx.tonal_from_host(native.MIXED, pin_raw.ptr, pin_pA.ptr)
+    call, prep_, kern_, fin_ = (ctx.timing(w)[0] for w in (5, 1, 0, 2))
     timer.start()
-    e2e_parts = []
     for _ in range(args.steps):
-        ctx.tonal_from_host(native.MIXED, pin_raw.ptr, pin_pA.ptr)
-        call, prep_, kern_, fin_ = (ctx.timing(w)[0] for w in (5, 1, 0, 2))
-        e2e_parts.append((call, prep_, kern_, fin_))
+        ctx.tonal_from_host_async(native.MIXED, pin_raw.ptr, pin_pA.ptr)
+    ctx.sync()
     e2e_elapsed = max_over_ranks(dist, timer.stop())
     barrier(dist)
     e2e_value = replica_throughput(ws, evals, args.steps, e2e_elapsed)
@@ -401,8 +403,8 @@ def main():
                    "precision": "mixed", "l2": "inputs larger than L2 (1.47 GB rows, 3.7 GB records per step)",
                    "parallelism": "replicas" if ws > 1 else "1 GPU"},
         "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": int(raw.nbytes),
-                "call_ms": float(np.median([q[0] for q in e2e_parts])),
-                "copies_ms": float(np.median([q[0] - q[1] - q[2] - q[3] for q in e2e_parts])),
+                "api": "acum_tonal_from_host_async (pinned rows in, pA out; copies overlap the previous step)",
+                "synchronous_call_ms": call, "synchronous_copies_ms": call - prep_ - kern_ - fin_,
                 "d2h_bytes_per_step": int(deck.nTime * deck.nObs * 8)},
         "gpu_launches": int(launches),
         "kernels_ms_per_step": {"preprocess": float(np.mean(prep_ms)), "tonal_mixed": kms,
