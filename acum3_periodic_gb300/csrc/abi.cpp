@@ -522,10 +522,10 @@ extern "C" int acum_tonal_from_host_async(acum_ctx* ctx, int precision, const fl
             CK(ctx, cudaEventRecord(ctx->ev_free[k], ctx->stream));
         }
     }
-    CK(ctx, ctx->d_raw_alt.ensure(ctx->raw_floats));
+    CK(ctx, ctx->d_raw_alt.ensure(2 * ctx->raw_floats));
     const int b = ctx->async_next;
     ctx->async_next ^= 1;
-    float* buf = b == 0 ? ctx->d_raw.p : ctx->d_raw_alt.p;
+    float* buf = ctx->d_raw_alt.p + (size_t)b * ctx->raw_floats;
     const size_t n = (size_t)ctx->T * ctx->nobs;
     CK(ctx, ctx->d_out.ensure(3 * n));
     // the copy of this call's rows waits only for the run that last read the same buffer,

@@ -97,8 +97,9 @@ struct acum_ctx {
 
     // device buffers
     acum::DBuf<float> d_raw;
-    // pipelined runs from host rows (acum_tonal_from_host_async): a second row buffer,
-    // a copy stream and per-buffer events; raw_cur is the buffer the preprocessing reads
+    // pipelined runs from host rows (acum_tonal_from_host_async): two row buffers of
+    // their own, a copy stream and per-buffer events; raw_cur is the buffer the
+    // preprocessing reads (null: d_raw)
     acum::DBuf<float> d_raw_alt;
     float* raw_cur = nullptr;
     cudaStream_t copy_stream = nullptr;

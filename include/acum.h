@@ -139,10 +139,11 @@ int acum_mark_surfaces_changed(acum_ctx* ctx);
 int acum_sync(acum_ctx* ctx);
 /* acum_tonal_from_host without waiting: the host rows (acum_set_deck layout, pinned
  * memory for the copy to overlap) are copied into one of two device row buffers on a copy
- * stream while the previous call's solve runs, then preprocessed and solved; pA
+ * stream while the previous call's solve runs (two buffers besides the context's own
+ * rows), then preprocessed and solved; pA
  * [nTime][nObs] is written to pA_host when the solve ends.  Returns at once; acum_sync
- * waits.  raw and pA_host must stay valid until then.  Leaves the rows last set by
- * acum_set_deck / acum_update_surfaces in place (acum_tonal runs on those). */
+ * waits.  raw and pA_host must stay valid until then.  The context's own rows (the last
+ * acum_set_deck / acum_update_surfaces) stay in place; acum_tonal runs on those. */
 int acum_tonal_from_host_async(acum_ctx* ctx, int precision, const float* raw, double* pA_host);
 /* The context's CUDA stream (a cudaStream_t), on which every run of the context is
  * issued; a caller may record events on it or order its own work after it. */
