@@ -163,7 +163,7 @@ int acum_ctx::upload_deck_common(const acum_inputs& inp, int nob, const float* o
     raw_floats = (size_t)off;
     T = in.nTime;
     nW = (T + kWin - 1) / kWin;
-    Epad = (int)((E + 3) / 4 * 4);
+    Epad = (int)((E + 7) / 8 * 8);  // a multiple of every elements-per-stage
     // observers: rObs = obs.dat * OBSscale (io.cu:123-128)
     obs_file_h.assign(obs_file, obs_file + 3 * (size_t)nob);
     std::vector<double> o64(3 * (size_t)nob);
@@ -733,7 +733,7 @@ int find_pth(const S* rObs, const S* tObs, S* pT, S* pL, S* pA, const S* Xham, c
             po[k] = hP[i] + (long long)j * nTime * 2;
         }
     const int nW = (nTime + kWin - 1) / kWin;
-    const int Epad = (int)((E + 3) / 4 * 4);
+    const int Epad = (int)((E + 7) / 8 * 8);
     CK(nullptr, c->d_off.ensure(4 * (size_t)E));
     CK(nullptr, cudaMemcpyAsync(c->d_off.p, xo.data(), E * 8, cudaMemcpyHostToDevice, st));
     CK(nullptr, cudaMemcpyAsync(c->d_off.p + E, no.data(), E * 8, cudaMemcpyHostToDevice, st));

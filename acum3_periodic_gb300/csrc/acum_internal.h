@@ -138,7 +138,8 @@ void fill_kparams(const TonalRun& r, KParams& kp);
 struct BatchItem {
     int c, ot, e0, e1;
 };
-constexpr int kBatchNS = 4;
+// ring stages of the batched kernel: 4, or 2 for stages of 8 elements
+constexpr int batch_stages(int SE) { return SE == 8 ? 2 : 4; }
 // dynamic shared memory of the persistent kernel for W observers per block, elements per
 // stage SE and the longest case's nTime
 size_t batch_smem(int W, int SE, int Tmax);

@@ -30,7 +30,7 @@ struct acum_batch {
     std::vector<acum_ctx*> cases;
 
     // tile shape and plan
-    int W = 16, SE = 4, ips = 8;
+    int W = 16, SE = 8, ips = 8;
     bool planned = false;
     int Tmax = 0;
     int nitems = 0;
@@ -102,7 +102,7 @@ TonalRun case_run(const acum_batch* b, const acum_ctx* c, double* acc)
     r.precision = ACUM_MIXED;
     r.t.W = b->W;
     r.t.SE = b->SE;
-    r.t.NS = kBatchNS;
+    r.t.NS = batch_stages(b->SE);
     r.t.flush_elems = 128;
     r.t.opw = 1;
     r.t.chunk = c->Epad;
@@ -301,7 +301,7 @@ extern "C" int acum_batch_add(acum_batch* b, const acum_inputs* in, int nobs, co
     DeviceGuard g(b->device);
     // what the case holds while it is added (rows + records) and afterwards (records,
     // sums, results), against the device's free memory with 1 GiB to spare
-    const long long T = in->nTime, nW = (T + kWin - 1) / kWin, Epad = (E + 3) / 4 * 4;
+    const long long T = in->nTime, nW = (T + kWin - 1) / kWin, Epad = (E + 7) / 8 * 8;
     const double rows = (double)E * T * 8 * 4, recs = (double)Epad * nW * kGroups * kWin * 4 * 4;
     const double sums = (double)nobs * T * 8 * 3;
     size_t free_b = 0, total_b = 0;
@@ -439,8 +439,8 @@ extern "C" int acum_batch_set_tile(acum_batch* b, int obs_per_block, int elems_p
 {
     if (!b) return ACUM_ERR_INVALID;
     if (obs_per_block < 0 || obs_per_block > 16 || items_per_sm < 0 ||
-        (elems_per_stage != 0 && elems_per_stage != 2 && elems_per_stage != 4))
-        return bfail(b, ACUM_ERR_INVALID, "acum_batch_set_tile: obs_per_block 1..16, elems_per_stage 2 or 4");
+        (elems_per_stage != 0 && elems_per_stage != 2 && elems_per_stage != 4 && elems_per_stage != 8))
+        return bfail(b, ACUM_ERR_INVALID, "acum_batch_set_tile: obs_per_block 1..16, elems_per_stage 2, 4 or 8");
     if (obs_per_block) b->W = obs_per_block;
     if (elems_per_stage) b->SE = elems_per_stage;
     if (items_per_sm) b->ips = items_per_sm;
@@ -541,7 +541,7 @@ extern "C" int acum_batch_autotune(acum_batch* b, int probe_per_sm, double* best
     const long target = (long)per_sm * b->num_sms;
     // 1. kernel throughput of every (observers per block, elements per stage): one
     //    persistent launch over a spread of 32-element items from all cases
-    const int Ws[] = {8, 12, 16}, SEs[] = {2, 4};
+    const int Ws[] = {8, 12, 16}, SEs[] = {2, 4, 8};
     double best_rate = 0;
     int bw = b->W, bse = b->SE;
     DBuf<BatchItem> d_probe;

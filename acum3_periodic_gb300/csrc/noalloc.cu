@@ -140,7 +140,7 @@ extern "C" int acum_find_pressure_time_history_noalloc(const float* rObs, const 
     }
     if (Et <= 0) return bad(ACUM_ERR_INVALID, "findPressureTimeHistory_noalloc: no elements");
     const int nW = (nTime + kWin - 1) / kWin;
-    const long long Epad = (Et + 3) / 4 * 4;
+    const long long Epad = (Et + 7) / 8 * 8;
     const size_t rec_bytes = (size_t)Epad * nW * kGroups * kWin * 4 * sizeof(float);
     const size_t acc_off = (rec_bytes + 255) / 256 * 256;
     const size_t acc_bytes = (size_t)nObs * nTime * 2 * sizeof(double);

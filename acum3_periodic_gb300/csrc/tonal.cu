@@ -983,8 +983,9 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
     const bool f64 = r.precision == ACUM_PLAIN_FP64;
     const int rb = f64 ? 8 : 4;
     // mixed: elements per stage 2 or 4 (default 4); FP64: 2
-    // mixed: elements per stage 2, 4 (default) or 8; a stage of 8 needs only 2 ring stages
-    const int SE = f64 ? kSE64 : ((SE_req == 2 || SE_req == 8) ? SE_req : kSE32);
+    // mixed: elements per stage 2, 4 or 8 (default: the most samples in flight per lane);
+    // a stage of 8 needs only 2 ring stages
+    const int SE = f64 ? kSE64 : ((SE_req == 2 || SE_req == 4) ? SE_req : 8);
     const int NSmin = SE == 8 ? 2 : 4;
     const int opw = 1;
     r.t.opw = opw;
@@ -1155,8 +1156,8 @@ cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s)
 
 size_t batch_smem(int W, int SE, int Tmax)
 {
-    return acc_region_bytes(W, Tmax, 8) + (size_t)kBatchNS * SE * kGroups * kWin * 4 * sizeof(float) +
-           (size_t)kBatchNS * 8;
+    const int NS = batch_stages(SE);
+    return acc_region_bytes(W, Tmax, 8) + (size_t)NS * SE * kGroups * kWin * 4 * sizeof(float) + (size_t)NS * 8;
 }
 
 template <int SE>
@@ -1176,7 +1177,7 @@ static cudaError_t launch_batch_t(const KParams* d_cases, const BatchItem* d_ite
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<SE>, 32 * W, smem) != cudaSuccess ||
         per_sm < 1)
         per_sm = 1;
-    tonal_batch_kernel<SE><<<grid * per_sm, 32 * W, smem, s>>>(d_cases, d_items, nitems, d_counter, kBatchNS,
+    tonal_batch_kernel<SE><<<grid * per_sm, 32 * W, smem, s>>>(d_cases, d_items, nitems, d_counter, batch_stages(SE),
                                                                acc_region_bytes(W, Tmax, 8));
     return cudaGetLastError();
 }
@@ -1185,8 +1186,9 @@ int batch_blocks_per_sm(int W, int SE, int Tmax)
 {
     int per_sm = 1;
     const size_t smem = batch_smem(W, SE, Tmax);
-    cudaError_t e = SE == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<2>, 32 * W, smem)
-                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<4>, 32 * W, smem);
+    cudaError_t e = SE == 2   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<2>, 32 * W, smem)
+                    : SE == 8 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<8>, 32 * W, smem)
+                              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<4>, 32 * W, smem);
     return (e == cudaSuccess && per_sm > 0) ? per_sm : 1;
 }
 
@@ -1197,6 +1199,7 @@ cudaError_t launch_tonal_batch(const KParams* d_cases, const BatchItem* d_items,
     if (W < 1 || W > 16 || grid < 1) return cudaErrorInvalidValue;
     if (SE == 2) return launch_batch_t<2>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s);
     if (SE == 4) return launch_batch_t<4>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s);
+    if (SE == 8) return launch_batch_t<8>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s);
     return cudaErrorInvalidValue;
 }
 

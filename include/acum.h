@@ -293,11 +293,11 @@ int acum_batch_result(acum_batch* b, int case_id, double* pA);
 int acum_batch_timing(const acum_batch* b, double* ms, long long* launches);
 /* Device time of one case's tonal kernel in the last mode-1 run. */
 int acum_batch_case_timing(const acum_batch* b, int case_id, double* ms);
-/* obs_per_block 1..16, elems_per_stage 2 or 4, items_per_sm >= 1 (0 keeps a value). */
+/* obs_per_block 1..16, elems_per_stage 2, 4 or 8, items_per_sm >= 1 (0 keeps a value). */
 int acum_batch_set_tile(acum_batch* b, int obs_per_block, int elems_per_stage, int items_per_sm);
 int acum_batch_get_tile(const acum_batch* b, int* obs_per_block, int* elems_per_stage, int* items_per_sm);
 /* Chooses the tile shape.  (1) For every observers-per-block in {8, 12, 16} x elements-per-
- * stage in {2, 4} whose shared memory fits, one persistent launch over a probe of
+ * stage in {2, 4, 8} whose shared memory fits, one persistent launch over a probe of
  * 32-element work items spread over all cases (about probe_per_sm items per SM; 0 = 8)
  * gives the kernel's throughput; the fastest shape is kept.  (2) Two probes of that shape
  * with 32- and 128-element items give its cost per work item and per evaluation, from

@@ -103,7 +103,7 @@ def test_against_fp64_oracle(batch):
         assert per_bin_rms(got, ref).max() < BIN_RMS
 
 
-@pytest.mark.parametrize("W,SE,ips", [(8, 2, 4), (12, 4, 16), (16, 2, 8), (5, 4, 1)])
+@pytest.mark.parametrize("W,SE,ips", [(8, 2, 4), (12, 4, 16), (16, 2, 8), (5, 4, 1), (16, 8, 8), (7, 8, 2)])
 def test_tile_shapes_agree(batch, singles, W, SE, ips):
     b, decks = batch
     b.set_tile(W, SE, ips)
@@ -117,7 +117,7 @@ def test_autotune(batch, singles):
     b, decks = batch
     est = b.autotune()
     W, SE, ips = b.tile()
-    assert W in (8, 12, 16) and SE in (2, 4) and ips in (4, 8, 16, 32)
+    assert W in (8, 12, 16) and SE in (2, 4, 8) and ips in (4, 8, 16, 32)
     assert est > 0
     b.run(mode=2)
     for i in range(len(decks)):
