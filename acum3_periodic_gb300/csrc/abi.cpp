@@ -253,6 +253,21 @@ extern "C" int acum_read_deck_sizes(const char* dir, long long* out)
     return ACUM_OK;
 }
 
+extern "C" int acum_write_surface_cache(const char* dir)
+{
+    acum::NvtxRange nvtx_range_("acum_write_surface_cache");
+    if (!dir) return fail(nullptr, ACUM_ERR_INVALID, "acum_write_surface_cache: null argument");
+    std::string d(dir), err;
+    acum_inputs in;
+    int ns = 0;
+    std::vector<float> raw;
+    std::vector<int> ne;
+    if (!read_inputs(d, in, ns, &err)) return fail(nullptr, ACUM_ERR_IO, err);
+    if (!read_surfaces(d, ns, in.nTime, ne, raw, &err)) return fail(nullptr, ACUM_ERR_IO, err);
+    if (!write_surface_cache(d, ns, in.nTime, ne, raw, &err)) return fail(nullptr, ACUM_ERR_IO, err);
+    return ACUM_OK;
+}
+
 extern "C" int acum_load_deck(acum_ctx* ctx, const char* dir)
 {
     acum::NvtxRange nvtx_range_("acum_load_deck");

@@ -5,7 +5,9 @@
 // rows are stored as float, as read_surf stores them.  Large surface files are parsed in
 // parallel over line-aligned chunks.
 #include <math.h>
+#include <stdint.h>
 #include <stdio.h>
+#include <sys/stat.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -217,10 +219,92 @@ bool read_observers(const std::string& dir, std::vector<float>& obs, int& nobs, 
     return true;
 }
 
+// Binary cache of the surface rows (surfaces/surfaces.acumbin): the float rows exactly as
+// read from the text files, with the size and modification time of each text file, so a
+// later load skips the text parse when none of them changed.
+namespace {
+const char kCacheMagic[8] = {'A', 'C', 'U', 'M', 'S', 'R', 'F', '1'};
+
+struct FileStamp {
+    int64_t size, mtime_ns;
+};
+
+bool stamp_of(const std::string& fn, FileStamp& st)
+{
+    struct stat sb;
+    if (stat(fn.c_str(), &sb) != 0) return false;
+    st.size = (int64_t)sb.st_size;
+    st.mtime_ns = (int64_t)sb.st_mtim.tv_sec * 1000000000LL + (int64_t)sb.st_mtim.tv_nsec;
+    return true;
+}
+
+std::string surface_file(const std::string& dir, int i)
+{
+    return dir + "/surfaces/surface_" + std::to_string(i + 1) + ".dat";
+}
+
+std::string cache_file(const std::string& dir) { return dir + "/surfaces/surfaces.acumbin"; }
+
+// rows from the cache if it exists and matches every text file; false otherwise
+bool read_surface_cache(const std::string& dir, int nsurf, int ntime, std::vector<int>& nelem,
+                        std::vector<float>& raw)
+{
+    FILE* f = fopen(cache_file(dir).c_str(), "rb");
+    if (!f) return false;
+    bool ok = false;
+    char magic[8];
+    int32_t ns = 0, nt = 0;
+    if (fread(magic, 1, 8, f) == 8 && memcmp(magic, kCacheMagic, 8) == 0 && fread(&ns, 4, 1, f) == 1 &&
+        fread(&nt, 4, 1, f) == 1 && ns == nsurf && nt == ntime) {
+        std::vector<int32_t> ne(ns);
+        std::vector<FileStamp> st(ns);
+        ok = fread(ne.data(), 4, ns, f) == (size_t)ns && fread(st.data(), sizeof(FileStamp), ns, f) == (size_t)ns;
+        size_t total = 0;
+        for (int i = 0; ok && i < ns; ++i) {
+            FileStamp now;
+            ok = ne[i] >= 0 && stamp_of(surface_file(dir, i), now) && now.size == st[i].size &&
+                 now.mtime_ns == st[i].mtime_ns;
+            total += (size_t)ntime * ne[i] * 8;
+        }
+        if (ok) {
+            raw.assign(total, 0.f);
+            ok = fread(raw.data(), 4, total, f) == total;
+            if (ok) nelem.assign(ne.begin(), ne.end());
+        }
+    }
+    fclose(f);
+    if (!ok) raw.clear();
+    return ok;
+}
+}  // namespace
+
+bool write_surface_cache(const std::string& dir, int nsurf, int ntime, const std::vector<int>& nelem,
+                         const std::vector<float>& raw, std::string* err)
+{
+    std::vector<FileStamp> st(nsurf);
+    for (int i = 0; i < nsurf; ++i)
+        if (!stamp_of(surface_file(dir, i), st[i])) return set_err(err, "Unable to stat " + surface_file(dir, i));
+    const std::string tmp = cache_file(dir) + ".tmp";
+    FILE* f = fopen(tmp.c_str(), "wb");
+    if (!f) return set_err(err, "Unable to write " + tmp);
+    const int32_t ns = nsurf, nt = ntime;
+    std::vector<int32_t> ne(nelem.begin(), nelem.end());
+    bool ok = fwrite(kCacheMagic, 1, 8, f) == 8 && fwrite(&ns, 4, 1, f) == 1 && fwrite(&nt, 4, 1, f) == 1 &&
+              fwrite(ne.data(), 4, ns, f) == (size_t)ns && fwrite(st.data(), sizeof(FileStamp), ns, f) == (size_t)ns &&
+              fwrite(raw.data(), 4, raw.size(), f) == raw.size();
+    ok = (fclose(f) == 0) && ok;
+    if (!ok || rename(tmp.c_str(), cache_file(dir).c_str()) != 0) {
+        remove(tmp.c_str());
+        return set_err(err, "Unable to write " + cache_file(dir));
+    }
+    return true;
+}
+
 // io.cu:206-333 (impermeable rows: x y z Cp A nx ny nz)
 bool read_surfaces(const std::string& dir, int nsurf, int ntime, std::vector<int>& nelem, std::vector<float>& raw,
                    std::string* err)
 {
+    if (read_surface_cache(dir, nsurf, ntime, nelem, raw)) return true;
     nelem.assign(nsurf, 0);
     std::vector<std::string> bufs(nsurf);
     size_t total = 0;

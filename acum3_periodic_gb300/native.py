@@ -74,6 +74,7 @@ SIGNATURES = {
     "acum_tonal_from_host_async": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "acum_selftest_wait": (C.c_int, [C.c_int, C.c_double, C.c_int, _IP, _DP]),
     "acum_read_deck_sizes": (C.c_int, [C.c_char_p, C.POINTER(C.c_longlong)]),
+    "acum_write_surface_cache": (C.c_int, [C.c_char_p]),
     "acum_last_plan": (C.c_int, [C.c_void_p, _IP]),
     "acum_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "acum_bpm": (C.c_int, [C.c_void_p, C.c_int, _DP, _DP]),

@@ -102,6 +102,13 @@ typedef struct {
 int acum_set_bb(acum_ctx* ctx, const acum_bb_desc* bb);
 
 /* sizes: out[0]=nSurf, [1]=nTime, [2]=nObs, [3]=elements, [4]=BB sections, [5]=BB_noise */
+/* Writes surfaces/surfaces.acumbin in a deck directory: the surface rows as read from the
+ * text files (io.cu:206-333), with the size and modification time of each text file.
+ * acum_load_deck and acum_read_deck_sizes then read the rows from it instead of parsing
+ * the text while no text file has changed; a stale or foreign cache is ignored.  Host
+ * only.  (No reference counterpart.) */
+int acum_write_surface_cache(const char* dir);
+
 /* Parses and validates a deck directory on the host only (no device needed): the same
  * readers and checks as acum_load_deck.  out[6] as acum_get_sizes. */
 int acum_read_deck_sizes(const char* dir, long long* out);

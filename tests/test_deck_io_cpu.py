@@ -122,3 +122,33 @@ def test_missing_broadband_files(bb_deck, tmp_path):
     shutil.copytree(bb_deck[1], p2)
     os.remove(p2 / "input_BB")
     assert sizes(p2)[0] == IO_ERR
+
+
+def write_cache(path):
+    from acum3_periodic_gb300 import native
+    return native.lib().acum_write_surface_cache(os.fsencode(str(path)))
+
+
+def test_surface_cache_used_and_refreshed(tonal_deck, tmp_path):
+    d, src = tonal_deck
+    p = copy_of(src, tmp_path)
+    assert write_cache(p) == 0
+    assert os.path.exists(p / "surfaces" / "surfaces.acumbin")
+    rc, s, _ = sizes(p)
+    assert rc == 0 and s == [d.nSurf, d.nTime, d.nObs, d.E, 0, 0]
+    # a changed text file makes the cache stale: the text is parsed (and here found short)
+    fn = p / "surfaces" / "surface_1.dat"
+    lines = open(fn).read().splitlines()
+    with open(fn, "w") as f:
+        f.write("\n".join(lines[:-3]) + "\n")
+    rc, _, msg = sizes(p)
+    assert rc == IO_ERR and "surface_1" in msg
+
+
+def test_foreign_surface_cache_ignored(tonal_deck, tmp_path):
+    d, src = tonal_deck
+    p = copy_of(src, tmp_path)
+    with open(p / "surfaces" / "surfaces.acumbin", "wb") as f:
+        f.write(b"not a cache" * 10)
+    rc, s, _ = sizes(p)
+    assert rc == 0 and s == [d.nSurf, d.nTime, d.nObs, d.E, 0, 0]

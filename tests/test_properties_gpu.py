@@ -154,3 +154,16 @@ def test_pipelined_host_runs_match_synchronous(ctx):
     assert per_bin_rms(again, base).max() < 1e-12
     for b in rows + outs:
         b.close()
+
+
+def test_deck_from_surface_cache_is_identical(ctx, tmp_path):
+    from acum3_periodic_gb300 import native
+    from acum3_periodic_gb300.deck import write_deck
+    d = synth.config_deck(0, scale=dict(n_span=6, n_chord_side=4, ntime=48, nobs=8))
+    write_deck(d, str(tmp_path))
+    ctx.load_deck(str(tmp_path))
+    _, _, text = ctx.tonal(native.PLAIN_FP64)
+    assert native.lib().acum_write_surface_cache(str(tmp_path).encode()) == 0
+    ctx.load_deck(str(tmp_path))
+    _, _, cached = ctx.tonal(native.PLAIN_FP64)
+    assert np.array_equal(text, cached)
