@@ -125,6 +125,7 @@ struct KParams {
     // mixed constants
     float a0f, alphaf, ialphaf, vxf, vyf, vzf, kbhi, kblo, invTf;
     unsigned tmod;  // ceil(2^32 / T): bin index modulo T by multiply-high
+    int toff;       // a multiple of T >= 2^23, added to bin indices before the modulo
     // FP64 constants
     double a0, alpha, ialpha, vx, vy, vz, dTau, oM, dPsi, lpi;
     int W, NS, chunk, nchunk, obs_tiles, flush_groups, tile_group;

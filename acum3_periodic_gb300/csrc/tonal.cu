@@ -604,7 +604,7 @@ __device__ __forceinline__ Anchor make_anchor(const KParams& p, float ox, float 
     a.t2 = (float)(2.0 * t0);
     a.s0 = (float)s0;
     a.kf = (float)(K - Kr);
-    a.ki = (int)Kr;
+    a.ki = (int)(Kr - floor(Kr / p.T) * p.T);  // bins wrap with period T: keep the index small
     return a;
 }
 
@@ -629,7 +629,7 @@ __device__ __forceinline__ G2 load_g2(const float* half0)
 // The samples of one step of an element pair, in packed FP32 (see the comment above for
 // the integrand and the anchored retarded time).  g[q] = group q of the pair's records.
 __device__ __forceinline__ void sample_mixed2(const G2* g, float ox, float oy, float oz, const Anchor& an,
-                                              const KParams& p, int tau, DeviceErr* err, SmpF& oa, SmpF& ob)
+                                              const KParams& p, int tau, unsigned& bad, SmpF& oa, SmpF& ob)
 {
     const float2 OX = f2(ox), OY = f2(oy), OZ = f2(oz);
     const float2 dx = sub2(OX, g[0].x), dy = sub2(OY, g[0].y), dz = sub2(OZ, g[0].z);
@@ -655,7 +655,7 @@ __device__ __forceinline__ void sample_mixed2(const G2* g, float ox, float oy, f
     const float2 pl = mul2(mul2(g[0].w, base), fma2(mul2(Lr, G), K, fma2(qa, sub2(Lr, g[3].w), Ldr)));
     // observer time in bins: tau + round(t0 oM/dPsi) + x, x = frac(t0 oM/dPsi) + dt oM/dPsi
     const float2 x = fma2(dt, f2(p.kbhi), f2(an.kf));
-    if (!(fabsf(x.x) < 4.0e6f) || !(fabsf(x.y) < 4.0e6f)) flag(err, ACUM_DEVERR_ORDER, &err->order);
+    bad |= (!(fabsf(x.x) < 4.0e6f) || !(fabsf(x.y) < 4.0e6f)) ? 1u : 0u;  // outside the rounding's range
     const float2 t = add2(x, f2(kRound));
     const float2 fr = sub2(x, add2(t, f2(-kRound)));
     const int kb = tau + an.ki - kRoundBits;
@@ -671,7 +671,7 @@ __device__ __forceinline__ void sample_mixed2(const G2* g, float ox, float oy, f
 
 __device__ __forceinline__ int mod_T(int n, int T, unsigned m)
 {
-    // 0 <= n < 2^24: the multiply-high quotient is floor(n / T) or one more
+    // 0 <= n < 2^25: the multiply-high quotient is floor(n / T) or one more
     int r = n - (int)__umulhi((unsigned)n, m) * T;
     return r < 0 ? r + T : r;
 }
@@ -689,38 +689,38 @@ __device__ __forceinline__ void add_bin(float2* acc, int idx, float w, float2 pa
 
 // bins n with u(a) < n <= u(b) + kshift, u = k + f with f in [-0.5, 0.5], the value
 // interpolated between the two samples.  For |Mr| < 1 an interval holds at most 2 bins
-// (u(b) - u(a) = 1 - Mr < 2): the first bin is unrolled and the second conditional.
-__device__ __forceinline__ void deposit(float2* acc, int T, unsigned tm, const SmpF& a, const SmpF& b, int kshift,
-                                        bool active, DeviceErr* err)
+// (u(b) - u(a) = 1 - Mr < 2).  Both are written by every lane without a branch: a lane
+// with fewer bins, or none, adds into the row's scratch slot acc[T] instead, which is
+// never read.  The bins of the lanes of a warp are disjoint (observer time increases
+// with the step), so only the scratch slot is written by more than one lane.  Intervals
+// of more than two bins (|Mr| >= 1) add the rest in a loop; a decreasing or non-finite
+// observer time, or a bin index outside the range of the modulo (an observer more than
+// ~2^23 bins away), sets `bad` and deposits nothing.  `toff` is a multiple of T of at
+// least 2^23 that keeps the bin index non-negative for the modulo.
+__device__ __forceinline__ void deposit(float2* acc, int T, unsigned tm, int toff, const SmpF& a, const SmpF& b,
+                                        int kshift, bool active, unsigned& bad)
 {
     const int dk = b.k + kshift - a.k;
     const bool a_up = a.f >= 0.0f;  // floor(u(a)) = k(a) - 1 + a_up
     const int cnt = dk + (b.f < 0.0f ? 0 : 1) - (a_up ? 1 : 0);
     const float du = small_int_to_float(dk) + (b.f - a.f);
-    const bool fast = active && cnt >= 1 && cnt <= 2 && du > 0.0f;
-    if (fast) {
-        const float inv = __fdividef(1.0f, du);
-        const float2 pa = make_float2(a.pt, a.pl), dp = sub2(make_float2(b.pt, b.pl), pa);
-        int idx = mod_T(a.k + (a_up ? 1 : 0), T, tm);
-        const float w1 = ((a_up ? 1.0f : 0.0f) - a.f) * inv;
-        add_bin(acc, idx, w1, pa, dp);
-        if (cnt == 2) {
-            if (++idx == T) idx = 0;
-            add_bin(acc, idx, w1 + inv, pa, dp);
-        }
-    } else if (active && !(cnt == 0 && du > 0.0f)) {
-        // more than two bins in one step (|Mr| > 1) or a decreasing / non-finite time
-        if (cnt > 2 && cnt <= T && du > 0.0f) {
-            const float inv = __fdividef(1.0f, du);
-            const float2 pa = make_float2(a.pt, a.pl), dp = sub2(make_float2(b.pt, b.pl), pa);
-            int idx = mod_T(a.k + (a_up ? 1 : 0), T, tm);
-            const float f0 = (a_up ? 1.0f : 0.0f) - a.f;
-            for (int m = 0; m < cnt; ++m) {
-                add_bin(acc, idx, (f0 + (float)m) * inv, pa, dp);
-                if (++idx == T) idx = 0;
-            }
-        } else {
-            flag(err, ACUM_DEVERR_ORDER, &err->order);
+    const int n = a.k + (a_up ? 1 : 0) + toff;
+    const bool ok = du > 0.0f && cnt >= 0 && cnt <= T && n >= 0 && n < (1 << 25);
+    bad |= (active && !ok) ? 1u : 0u;
+    const bool one = active && ok && cnt >= 1, two = one && cnt >= 2;
+    const float inv = __fdividef(1.0f, ok ? du : 1.0f);
+    const float2 pa = make_float2(a.pt, a.pl), dp = sub2(make_float2(b.pt, b.pl), pa);
+    const int idx = mod_T(one ? n : 0, T, tm);
+    const int idx2 = idx + 1 == T ? 0 : idx + 1;
+    const float w1 = ((a_up ? 1.0f : 0.0f) - a.f) * inv;
+    const int i1 = one ? idx : T, i2 = two ? idx2 : T;
+    acc[i1] = add2(acc[i1], fma2(f2(w1), dp, pa));
+    acc[i2] = add2(acc[i2], fma2(f2(w1 + inv), dp, pa));
+    if (one && cnt > 2) {
+        int i = idx2;
+        for (int m = 2; m < cnt; ++m) {
+            if (++i == T) i = 0;
+            acc[i] = add2(acc[i], fma2(f2(w1 + (float)m * inv), dp, pa));
         }
     }
 }
@@ -789,8 +789,9 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
     const bool ok_obs = o < p.O;
     const int oc = ok_obs ? o : 0;
     const float ox = p.obs32[3 * oc], oy = p.obs32[3 * oc + 1], oz = p.obs32[3 * oc + 2];
-    float2* acc = acc_all + (size_t)warp * T;
+    float2* acc = acc_all + (size_t)warp * (T + 1);  // T bins + the scratch slot
     const Anchor anc = make_anchor(p, ox, oy, oz);
+    unsigned bad = 0;
 
     int s = (int)(g0 % (unsigned)NS), w = 0, g = 0, since_flush = 0;
     uint32_t par = (g0 / (unsigned)NS) & 1u;
@@ -814,7 +815,7 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
             G2 gg[kGroups];
 #pragma unroll
             for (int q = 0; q < kGroups; ++q) gg[q] = load_g2(tl + q * 2 * kWin * 4);
-            sample_mixed2(gg, ox, oy, oz, anc, p, tau, p.err, cur[2 * jp], cur[2 * jp + 1]);
+            sample_mixed2(gg, ox, oy, oz, anc, p, tau, bad, cur[2 * jp], cur[2 * jp + 1]);
         }
         const bool first_win = w == 0, last_win = w == nW - 1;
         const int rot_src = (lane + 31) & 31;
@@ -824,13 +825,13 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
             // (kept in shared memory, double-buffered by window parity)
             SmpF prev = shfl_idx(cur[j], rot_src);
             if (lane == 0) prev = sh.carry[warp][w & 1][j];
-            deposit(acc, T, p.tmod, prev, cur[j], 0, ok_obs && valid && !(first_win && lane == 0), p.err);
+            deposit(acc, T, p.tmod, p.toff, prev, cur[j], 0, ok_obs && valid && !(first_win && lane == 0), bad);
             if (lane == 31) sh.carry[warp][(w + 1) & 1][j] = cur[j];
             if (first_win && lane == 0) sh.first[warp][j] = cur[j];
             if (last_win) {
                 // the periodic wrap: (t(T-1), t(0) + period] (core.cu:173-194)
                 const SmpF lastS = shfl_idx(cur[j], min(31, T - 1 - w * kWin));
-                if (lane == 0) deposit(acc, T, p.tmod, lastS, sh.first[warp][j], T, ok_obs, p.err);
+                if (lane == 0) deposit(acc, T, p.tmod, p.toff, lastS, sh.first[warp][j], T, ok_obs, bad);
             }
         }
         // FP32 partial sums cover at most `flush_groups` element groups before they are
@@ -857,6 +858,11 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
             ++g;
         }
     }
+    // the scratch slot holds whatever the lanes without a bin added; the next item's rows
+    // (of another length in a batch) may cover it
+    __syncwarp();
+    if (lane == 0) acc[T] = make_float2(0.f, 0.f);
+    if (__any_sync(0xffffffffu, bad != 0) && lane == 0) flag(p.err, ACUM_DEVERR_ORDER, &p.err->order);
     gbase = g0 + (unsigned)N;
 }
 
@@ -901,7 +907,7 @@ __global__ void __launch_bounds__(512, 1) tonal_mixed_kernel(const KParams p)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ MixedShared<SE> sh;
-    const size_t stage_off = acc_region_bytes(p.W, p.T, 8);
+    const size_t stage_off = acc_region_bytes(p.W, p.T + 1, 8);
     mixed_init<SE>(smem, stage_off, p.NS, sh);
     unsigned gbase = 0;
     const int nitems = p.obs_tiles * p.nchunk;
@@ -974,8 +980,9 @@ size_t batch_static_smem(int SE) { return mixed_static_smem(SE) + 512; }
 
 static size_t tonal_smem(int W, int T, int NS, int SE, int real_bytes)
 {
-    const int acc_bytes = real_bytes == 8 ? 16 : 8;  // double2 or float2 per bin
-    return acc_region_bytes(W, T, acc_bytes) + (size_t)NS * SE * kGroups * kWin * 4 * real_bytes + (size_t)NS * 8;
+    // FP64: double2 per bin; mixed: float2 per bin plus one scratch slot per row
+    const size_t acc = real_bytes == 8 ? acc_region_bytes(W, T, 16) : acc_region_bytes(W, T + 1, 8);
+    return acc + (size_t)NS * SE * kGroups * kWin * 4 * real_bytes + (size_t)NS * 8;
 }
 
 cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int num_sms, size_t smem_optin)
@@ -1133,6 +1140,7 @@ void fill_kparams(const TonalRun& r, KParams& kp)
     kp.kblo = (float)(kb - (double)kp.kbhi);
     kp.invTf = 1.0f / (float)g.T;
     kp.tmod = (unsigned)((0x100000000ull + (unsigned long long)g.T - 1) / (unsigned long long)g.T);
+    kp.toff = (int)(((1 << 23) + g.T - 1) / g.T * g.T);
     kp.W = r.t.W;
     kp.NS = r.t.NS;
     kp.chunk = r.t.chunk;
@@ -1157,7 +1165,8 @@ cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s)
 size_t batch_smem(int W, int SE, int Tmax)
 {
     const int NS = batch_stages(SE);
-    return acc_region_bytes(W, Tmax, 8) + (size_t)NS * SE * kGroups * kWin * 4 * sizeof(float) + (size_t)NS * 8;
+    return acc_region_bytes(W, Tmax + 1, 8) + (size_t)NS * SE * kGroups * kWin * 4 * sizeof(float) +
+           (size_t)NS * 8;
 }
 
 template <int SE>
@@ -1178,7 +1187,7 @@ static cudaError_t launch_batch_t(const KParams* d_cases, const BatchItem* d_ite
         per_sm < 1)
         per_sm = 1;
     tonal_batch_kernel<SE><<<grid * per_sm, 32 * W, smem, s>>>(d_cases, d_items, nitems, d_counter, batch_stages(SE),
-                                                               acc_region_bytes(W, Tmax, 8));
+                                                               acc_region_bytes(W, Tmax + 1, 8));
     return cudaGetLastError();
 }
 
