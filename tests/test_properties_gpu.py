@@ -162,8 +162,12 @@ def test_deck_from_surface_cache_is_identical(ctx, tmp_path):
     d = synth.config_deck(0, scale=dict(n_span=6, n_chord_side=4, ntime=48, nobs=8))
     write_deck(d, str(tmp_path))
     ctx.load_deck(str(tmp_path))
+    f_text = ctx.fields()
     _, _, text = ctx.tonal(native.PLAIN_FP64)
     assert native.lib().acum_write_surface_cache(str(tmp_path).encode()) == 0
     ctx.load_deck(str(tmp_path))
+    # the preprocessed fields are a deterministic function of the rows: bit for bit
+    assert np.array_equal(f_text, ctx.fields())
     _, _, cached = ctx.tonal(native.PLAIN_FP64)
-    assert np.array_equal(text, cached)
+    # the FP64 bin sums are formed by atomics in a run-dependent order: equal to rounding
+    assert np.max(np.abs(cached - text)) <= 1e-12 * np.max(np.abs(text))
