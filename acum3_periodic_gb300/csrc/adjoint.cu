@@ -32,6 +32,7 @@
 
 #include "acum_internal.h"
 #include "ctx.h"
+#include "ptx.h"
 
 namespace acum {
 
@@ -56,9 +57,9 @@ struct V3 {
 // reciprocal and square root: IEEE in FP64, the fast hardware forms in FP32 (the FP32
 // adjoint is compared with the FP64 one, not with the reference)
 __device__ __forceinline__ double rcp_(double x) { return 1.0 / x; }
-__device__ __forceinline__ float rcp_(float x) { return __fdividef(1.0f, x); }
+__device__ __forceinline__ float rcp_(float x) { return rcp_ftz(x); }
 __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
-__device__ __forceinline__ float sqrt_(float x) { return x * rsqrtf(x); }
+__device__ __forceinline__ float sqrt_(float x) { return x * rsqrt_ftz(x); }
 
 // floor(t / dPsi): the FP64 form divides as the forward does; the FP32 form multiplies
 __device__ __forceinline__ int bin_floor(double t, double dPsi, double) { return (int)floor(t / dPsi); }

@@ -267,8 +267,8 @@ cudaError_t launch_aos_records(const AosArgs& a, cudaStream_t s)
 // ------------------------------------------------------------- tonal kernel
 
 struct __align__(16) SmpF {
-    int k;      // observer time in bins (unwrapped) = k + f
-    float f;    // in [-0.5, 0.5]
+    int k;      // observer time in bins u = k + f: k = floor(u)
+    float f;    // u - k in [0, 1] (NaN: the observer time is out of range)
     float pt, pl;
 };
 
@@ -379,13 +379,18 @@ __host__ __device__ __forceinline__ size_t acc_region_bytes(int W, int T, int ac
     return ((size_t)W * T * acc_bytes + 127) / 128 * 128;
 }
 
-// Adds a warp's bins to the global FP64 sums [obs][bin][2] and clears them.  `direct`
+// Adds a warp's bins (and its overflow slot, into bin 0) to the global FP64 sums
+// [obs][bin][2] and clears them.  `direct`
 // stores instead of adding (the block is the only writer of these sums).
 __device__ __forceinline__ void flush_bins(float2* acc, double* g, int T, int lane, bool direct, DeviceErr* err)
 {
     __syncwarp();
     for (int n = lane; n < T; n += 32) {
-        const float2 v = acc[n];
+        float2 v = acc[n];
+        if (n == 0) {  // the overflow slot: bin 0 of the next period
+            v = add2(v, acc[T]);
+            acc[T] = make_float2(0.f, 0.f);
+        }
         if (!(fabsf(v.x) < 3.0e38f) || !(fabsf(v.y) < 3.0e38f)) flag(err, ACUM_DEVERR_NONFINITE, &err->nonfinite);
         if (direct) {
             reinterpret_cast<double2*>(g)[n] = make_double2((double)v.x, (double)v.y);
@@ -578,8 +583,8 @@ __global__ void __launch_bounds__(512, 1) tonal_f64_kernel(const KParams p)
 // terms are all of the size of the source's offset from the origin rather than of the
 // observer distance.  The observer time in bins, tau + t0 oM/dPsi + dt oM/dPsi, keeps the
 // first part split exactly (FP64) into an integer and a fraction, so FP32 rounding
-// applies to dt only.  The integer part of the remainder is rounded to nearest by the
-// 1.5 * 2^23 addition (exact for |x| < 2^22, checked), leaving a fraction in [-0.5, 0.5];
+// applies to dt only.  The floor of the remainder x comes from adding 1.5 * 2^23 rounded
+// towards minus infinity (exact for |x| < 2^22, checked), leaving a fraction in [0, 1];
 // bin indices are reduced modulo T by a multiply-high with m = ceil(2^32 / T).
 
 constexpr float kRound = 12582912.0f;  // 1.5 * 2^23
@@ -629,7 +634,7 @@ __device__ __forceinline__ G2 load_g2(const float* half0)
 // The samples of one step of an element pair, in packed FP32 (see the comment above for
 // the integrand and the anchored retarded time).  g[q] = group q of the pair's records.
 __device__ __forceinline__ void sample_mixed2(const G2* g, float ox, float oy, float oz, const Anchor& an,
-                                              const KParams& p, int tau, unsigned& bad, SmpF& oa, SmpF& ob)
+                                              const KParams& p, int tau, SmpF& oa, SmpF& ob)
 {
     const float2 OX = f2(ox), OY = f2(oy), OZ = f2(oz);
     const float2 dx = sub2(OX, g[0].x), dy = sub2(OY, g[0].y), dz = sub2(OZ, g[0].z);
@@ -638,8 +643,8 @@ __device__ __forceinline__ void sample_mixed2(const G2* g, float ox, float oy, f
     const float2 nnum = fma2(f2(-an.t2), g[4].w, S);
     const float2 bp = sub2(f2(an.s0), g[4].w);
     const float2 q = fma2(f2(-p.alphaf), nnum, mul2(bp, bp));
-    const float2 den = fma2(q, make_float2(rsqrtf(q.x), rsqrtf(q.y)), bp);
-    const float2 dt = mul2(nnum, make_float2(__fdividef(-1.0f, den.x), __fdividef(-1.0f, den.y)));
+    const float2 den = fma2(q, make_float2(rsqrt_ftz(q.x), rsqrt_ftz(q.y)), bp);
+    const float2 dt = mul2(nnum, make_float2(-rcp_ftz(den.x), -rcp_ftz(den.y)));
     const float2 tr = add2(f2(an.t0), dt);
     const float2 rx = fma2(f2(-p.vxf), tr, dx), ry = fma2(f2(-p.vyf), tr, dy), rz = fma2(f2(-p.vzf), tr, dz);
     const float2 ir = rcp2(mul2(f2(p.a0f), tr));
@@ -653,16 +658,17 @@ __device__ __forceinline__ void sample_mixed2(const G2* g, float ox, float oy, f
     const float2 base = mul2(mul2(ir, G), G);
     const float2 pt = mul2(mul2(g[2].w, base), mul2(G, K));
     const float2 pl = mul2(mul2(g[0].w, base), fma2(mul2(Lr, G), K, fma2(qa, sub2(Lr, g[3].w), Ldr)));
-    // observer time in bins: tau + round(t0 oM/dPsi) + x, x = frac(t0 oM/dPsi) + dt oM/dPsi
+    // observer time in bins: tau + round(t0 oM/dPsi) + x, x = frac(t0 oM/dPsi) + dt oM/dPsi;
+    // outside the floor's range (or not finite) the fraction is NaN, which the deposit
+    // rejects (and reports) whatever the integer part holds
     const float2 x = fma2(dt, f2(p.kbhi), f2(an.kf));
-    bad |= (!(fabsf(x.x) < 4.0e6f) || !(fabsf(x.y) < 4.0e6f)) ? 1u : 0u;  // outside the rounding's range
-    const float2 t = add2(x, f2(kRound));
+    const float2 t = __fadd2_rd(x, f2(kRound));
     const float2 fr = sub2(x, add2(t, f2(-kRound)));
     const int kb = tau + an.ki - kRoundBits;
     oa.k = kb + __float_as_int(t.x);
     ob.k = kb + __float_as_int(t.y);
-    oa.f = fr.x;
-    ob.f = fr.y;
+    oa.f = fabsf(x.x) < 4.0e6f ? fr.x : __int_as_float(0x7fc00000);
+    ob.f = fabsf(x.y) < 4.0e6f ? fr.y : __int_as_float(0x7fc00000);
     oa.pt = pt.x;
     ob.pt = pt.y;
     oa.pl = pl.x;
@@ -687,40 +693,45 @@ __device__ __forceinline__ void add_bin(float2* acc, int idx, float w, float2 pa
     acc[idx] = fma2(f2(w), dp, add2(acc[idx], pa));
 }
 
-// bins n with u(a) < n <= u(b) + kshift, u = k + f with f in [-0.5, 0.5], the value
+// A warp's observer row: T bins, then an overflow slot (index T, bin 0 of the next
+// period, added into bin 0 when the row is flushed) and a scratch slot (index T + 1,
+// never read).
+//
+// Bins n with u(a) < n <= u(b) + kshift: n = k(a) + 1 ... k(b) + kshift, the value
 // interpolated between the two samples.  For |Mr| < 1 an interval holds at most 2 bins
-// (u(b) - u(a) = 1 - Mr < 2).  Both are written by every lane without a branch: a lane
-// with fewer bins, or none, adds into the row's scratch slot acc[T] instead, which is
-// never read.  The bins of the lanes of a warp are disjoint (observer time increases
-// with the step), so only the scratch slot is written by more than one lane.  Intervals
-// of more than two bins (|Mr| >= 1) add the rest in a loop; a decreasing or non-finite
-// observer time, or a bin index outside the range of the modulo (an observer more than
-// ~2^23 bins away), sets `bad` and deposits nothing.  `toff` is a multiple of T of at
-// least 2^23 that keeps the bin index non-negative for the modulo.
+// (u(b) - u(a) = 1 - Mr < 2).  Both are written by every lane without a branch: the
+// first at the first bin modulo T, the second at the slot after it (which may be the
+// overflow slot); a lane with fewer bins adds into the scratch slot instead.  The bins of
+// the lanes of a warp are disjoint (observer time increases with the step), so only the
+// scratch slot is written by more than one lane.  Intervals of more than two bins
+// (|Mr| >= 1) add the rest in a loop; a decreasing or non-finite observer time (or an
+// interval of more than T bins) sets `bad` and deposits nothing.  `toff` is a multiple of
+// T of at least 2^23 that keeps the bin index non-negative for the modulo (|k| < 2^22
+// plus twice the period).
 __device__ __forceinline__ void deposit(float2* acc, int T, unsigned tm, int toff, const SmpF& a, const SmpF& b,
                                         int kshift, bool active, unsigned& bad)
 {
-    const int dk = b.k + kshift - a.k;
-    const bool a_up = a.f >= 0.0f;  // floor(u(a)) = k(a) - 1 + a_up
-    const int cnt = dk + (b.f < 0.0f ? 0 : 1) - (a_up ? 1 : 0);
-    const float du = small_int_to_float(dk) + (b.f - a.f);
-    const int n = a.k + (a_up ? 1 : 0) + toff;
-    const bool ok = du > 0.0f && cnt >= 0 && cnt <= T && n >= 0 && n < (1 << 25);
+    const int cnt = b.k + kshift - a.k;
+    const float du = small_int_to_float(cnt) + (b.f - a.f);
+    const bool ok = du > 0.0f;  // false for NaN
     bad |= (active && !ok) ? 1u : 0u;
     const bool one = active && ok && cnt >= 1, two = one && cnt >= 2;
-    const float inv = __fdividef(1.0f, ok ? du : 1.0f);
+    const float inv = rcp_ftz(ok ? du : 1.0f);
     const float2 pa = make_float2(a.pt, a.pl), dp = sub2(make_float2(b.pt, b.pl), pa);
-    const int idx = mod_T(one ? n : 0, T, tm);
-    const int idx2 = idx + 1 == T ? 0 : idx + 1;
-    const float w1 = ((a_up ? 1.0f : 0.0f) - a.f) * inv;
-    const int i1 = one ? idx : T, i2 = two ? idx2 : T;
+    const int idx = mod_T(one ? a.k + 1 + toff : 0, T, tm);
+    const float w1 = (1.0f - a.f) * inv;
+    const int i1 = one ? idx : T + 1, i2 = two ? idx + 1 : T + 1;
     acc[i1] = add2(acc[i1], fma2(f2(w1), dp, pa));
     acc[i2] = add2(acc[i2], fma2(f2(w1 + inv), dp, pa));
     if (one && cnt > 2) {
-        int i = idx2;
-        for (int m = 2; m < cnt; ++m) {
-            if (++i == T) i = 0;
-            acc[i] = add2(acc[i], fma2(f2(w1 + (float)m * inv), dp, pa));
+        if (cnt > T) {
+            bad = 1u;
+        } else {
+            int i = idx + 1;
+            for (int m = 2; m < cnt; ++m) {
+                if (++i >= T) i -= T;
+                acc[i] = add2(acc[i], fma2(f2(w1 + (float)m * inv), dp, pa));
+            }
         }
     }
 }
@@ -789,7 +800,7 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
     const bool ok_obs = o < p.O;
     const int oc = ok_obs ? o : 0;
     const float ox = p.obs32[3 * oc], oy = p.obs32[3 * oc + 1], oz = p.obs32[3 * oc + 2];
-    float2* acc = acc_all + (size_t)warp * (T + 1);  // T bins + the scratch slot
+    float2* acc = acc_all + (size_t)warp * (T + 2);  // T bins, the overflow and the scratch slot
     const Anchor anc = make_anchor(p, ox, oy, oz);
     unsigned bad = 0;
 
@@ -815,7 +826,7 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
             G2 gg[kGroups];
 #pragma unroll
             for (int q = 0; q < kGroups; ++q) gg[q] = load_g2(tl + q * 2 * kWin * 4);
-            sample_mixed2(gg, ox, oy, oz, anc, p, tau, bad, cur[2 * jp], cur[2 * jp + 1]);
+            sample_mixed2(gg, ox, oy, oz, anc, p, tau, cur[2 * jp], cur[2 * jp + 1]);
         }
         const bool first_win = w == 0, last_win = w == nW - 1;
         const int rot_src = (lane + 31) & 31;
@@ -861,7 +872,7 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
     // the scratch slot holds whatever the lanes without a bin added; the next item's rows
     // (of another length in a batch) may cover it
     __syncwarp();
-    if (lane == 0) acc[T] = make_float2(0.f, 0.f);
+    if (lane == 0) acc[T + 1] = make_float2(0.f, 0.f);
     if (__any_sync(0xffffffffu, bad != 0) && lane == 0) flag(p.err, ACUM_DEVERR_ORDER, &p.err->order);
     gbase = g0 + (unsigned)N;
 }
@@ -907,7 +918,7 @@ __global__ void __launch_bounds__(512, 1) tonal_mixed_kernel(const KParams p)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ MixedShared<SE> sh;
-    const size_t stage_off = acc_region_bytes(p.W, p.T + 1, 8);
+    const size_t stage_off = acc_region_bytes(p.W, p.T + 2, 8);
     mixed_init<SE>(smem, stage_off, p.NS, sh);
     unsigned gbase = 0;
     const int nitems = p.obs_tiles * p.nchunk;
@@ -980,8 +991,8 @@ size_t batch_static_smem(int SE) { return mixed_static_smem(SE) + 512; }
 
 static size_t tonal_smem(int W, int T, int NS, int SE, int real_bytes)
 {
-    // FP64: double2 per bin; mixed: float2 per bin plus one scratch slot per row
-    const size_t acc = real_bytes == 8 ? acc_region_bytes(W, T, 16) : acc_region_bytes(W, T + 1, 8);
+    // FP64: double2 per bin; mixed: float2 per bin plus the overflow and scratch slots per row
+    const size_t acc = real_bytes == 8 ? acc_region_bytes(W, T, 16) : acc_region_bytes(W, T + 2, 8);
     return acc + (size_t)NS * SE * kGroups * kWin * 4 * real_bytes + (size_t)NS * 8;
 }
 
@@ -1165,7 +1176,7 @@ cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s)
 size_t batch_smem(int W, int SE, int Tmax)
 {
     const int NS = batch_stages(SE);
-    return acc_region_bytes(W, Tmax + 1, 8) + (size_t)NS * SE * kGroups * kWin * 4 * sizeof(float) +
+    return acc_region_bytes(W, Tmax + 2, 8) + (size_t)NS * SE * kGroups * kWin * 4 * sizeof(float) +
            (size_t)NS * 8;
 }
 
@@ -1187,7 +1198,7 @@ static cudaError_t launch_batch_t(const KParams* d_cases, const BatchItem* d_ite
         per_sm < 1)
         per_sm = 1;
     tonal_batch_kernel<SE><<<grid * per_sm, 32 * W, smem, s>>>(d_cases, d_items, nitems, d_counter, batch_stages(SE),
-                                                               acc_region_bytes(W, Tmax + 1, 8));
+                                                               acc_region_bytes(W, Tmax + 2, 8));
     return cudaGetLastError();
 }
 
