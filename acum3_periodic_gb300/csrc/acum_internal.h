@@ -41,6 +41,9 @@ __host__ __device__ __forceinline__ size_t rec32_offset(int e, int nW, int t, in
 struct DeviceErr {
     unsigned int bits;
     unsigned int disc, order, nonfinite, timeout;
+    // work-list counters of the persistent tonal kernel: the next item to take and the
+    // blocks done; the last block of a launch sets both back to zero
+    int item_next, item_done;
 };
 
 struct TonalGeom {

@@ -908,23 +908,30 @@ __device__ __forceinline__ void mixed_drain(unsigned char* smem, size_t stage_of
     __syncthreads();
 }
 
-// Single deck: block b takes the items b, b + grid, b + 2 grid, ... of a list ordered by
-// observer-tile group, then element chunk, then tile within the group.  The blocks
-// running at any time therefore share one chunk of records in L2 (each record is read
-// from HBM once per group), and the FP64 sums they add into belong to one group of
-// tiles, small enough to stay in L2 beside the records.
+// Single deck: the blocks take the items of a list ordered by observer-tile group, then
+// element chunk, then tile within the group, one at a time from a counter in global
+// memory.  The blocks running at any time therefore share one or two chunks of records
+// in L2 (each record is read from HBM about once per group), and the FP64 sums they add
+// into belong to one group of tiles.
 template <int SE>
 __global__ void __launch_bounds__(512, 1) tonal_mixed_kernel(const KParams p)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ MixedShared<SE> sh;
+    __shared__ int s_item;
     const size_t stage_off = acc_region_bytes(p.W, p.T + 2, 8);
     mixed_init<SE>(smem, stage_off, p.NS, sh);
     unsigned gbase = 0;
     const int nitems = p.obs_tiles * p.nchunk;
     const int G = p.tile_group, per_group = G * p.nchunk;
     const int last_g = (p.obs_tiles - 1) / G, last_n = p.obs_tiles - last_g * G;
-    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+    for (;;) {
+        // items are taken in order from a shared counter, so that the blocks stay within
+        // about one item of each other and share one or two chunks of records in L2
+        if (threadIdx.x == 0) s_item = atomicAdd(&p.err->item_next, 1);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= nitems) break;
         const int g = item / per_group, r = item - g * per_group;
         const int gn = g == last_g ? last_n : G;
         const int ec = r / gn, ot = g * G + (r - ec * gn);
@@ -935,6 +942,13 @@ __global__ void __launch_bounds__(512, 1) tonal_mixed_kernel(const KParams p)
         if (sh.abort) {
             mixed_drain<SE>(smem, stage_off, p.NS, sh);
             break;
+        }
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&p.err->item_done, 1) == (int)gridDim.x - 1) {
+            atomicExch(&p.err->item_next, 0);
+            atomicExch(&p.err->item_done, 0);
         }
     }
 }
@@ -980,14 +994,42 @@ static_assert(kMaxStages >= 4, "stage bookkeeping");
 static_assert(sizeof(SmpF) == 16, "sample record");
 constexpr int kSE64 = 2;
 
-// static shared memory of the mixed kernels (MixedShared<SE> and, in the batched form,
-// the case's constants and the current item), rounded up
-static size_t mixed_static_smem(int SE)
+// static shared memory of a kernel as compiled (MixedShared<SE> and, in the batched form,
+// the case's constants and the current item); an estimate if the query fails
+template <typename K>
+static size_t static_smem_of(K kernel, size_t estimate)
 {
-    return (size_t)16 * 3 * SE * sizeof(SmpF) + 256;
+    cudaFuncAttributes a;
+    if (cudaFuncGetAttributes(&a, kernel) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return estimate;
+    }
+    return a.sharedSizeBytes;
 }
 
-size_t batch_static_smem(int SE) { return mixed_static_smem(SE) + 512; }
+static size_t mixed_static_smem(int SE)
+{
+    static size_t v[9] = {};
+    if (SE != 2 && SE != 4 && SE != 8) SE = 8;
+    if (!v[SE]) {
+        const size_t est = (size_t)16 * 3 * SE * sizeof(SmpF) + 256;
+        v[SE] = SE == 2 ? static_smem_of(tonal_mixed_kernel<2>, est)
+                        : SE == 4 ? static_smem_of(tonal_mixed_kernel<4>, est) : static_smem_of(tonal_mixed_kernel<8>, est);
+    }
+    return v[SE];
+}
+
+size_t batch_static_smem(int SE)
+{
+    static size_t v[9] = {};
+    if (SE != 2 && SE != 4 && SE != 8) SE = 8;
+    if (!v[SE]) {
+        const size_t est = (size_t)16 * 3 * SE * sizeof(SmpF) + 768;
+        v[SE] = SE == 2 ? static_smem_of(tonal_batch_kernel<2>, est)
+                        : SE == 4 ? static_smem_of(tonal_batch_kernel<4>, est) : static_smem_of(tonal_batch_kernel<8>, est);
+    }
+    return v[SE];
+}
 
 static size_t tonal_smem(int W, int T, int NS, int SE, int real_bytes)
 {
