@@ -116,7 +116,8 @@ struct TonalRun {
     DeviceErr* err;
     int precision;
 };
-cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int num_sms, size_t smem_optin);
+cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int num_sms, size_t smem_optin,
+                       int opw_req = 0);
 cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s);
 
 // Constants of one tonal launch (one case), as the kernels read them.

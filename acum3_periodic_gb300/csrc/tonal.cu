@@ -747,30 +747,31 @@ __device__ __forceinline__ SmpF shfl_idx(const SmpF& v, int src)
 }
 
 // Block-wide shared state of the mixed kernels besides the dynamic shared memory.
-template <int SE>
+template <int SE, int OPW>
 struct __align__(16) MixedShared {
-    SmpF carry[16][2][SE];  // per warp: left neighbour of lane 0, double-buffered by window parity
-    SmpF first[16][SE];     // per warp: first sample of each element of the stage (periodic wrap)
+    SmpF carry[16 / OPW][2][OPW][SE];  // per warp and observer: left neighbour of lane 0, by window parity
+    SmpF first[16 / OPW][OPW][SE];     // per warp and observer: first sample of each element (periodic wrap)
     int abort;
     int release[kMaxStages];
     int last[kMaxStages];
 };
 
 // One work item of the mixed form: observers [ot*W, ot*W + W) and elements [e0, e1)
-// (a multiple of SE) of the deck `p`.  The dynamic shared memory holds the warps' FP32
-// bin rows (W x T float2, laid out for the item's T) followed by the NS-stage ring;
+// (a multiple of SE) of the deck `p`; each warp evaluates OPW observers on the records it
+// loads once.  The dynamic shared memory holds the FP32 bin rows (W rows of T + 2 float2,
+// laid out for the item's T) followed by the NS-stage ring;
 // `stage_off` is where the ring starts (fixed for a launch).  `gbase` counts the stages
 // the block has consumed before this item, so consecutive items of a block continue the
 // mbarrier phases of the same ring.  On entry every slot is free and all bin rows are
 // zero; on return (without abort) the same holds again.
-template <int SE>
+template <int SE, int OPW>
 __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot, int e0, int e1, unsigned char* smem,
-                                           size_t stage_off, MixedShared<SE>& sh, unsigned& gbase)
+                                           size_t stage_off, MixedShared<SE, OPW>& sh, unsigned& gbase)
 {
     constexpr int kTile = kGroups * kWin * 4;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nwarps = blockDim.x >> 5;
-    const int W = p.W;  // observers per block = warps
+    const int W = p.W;  // observers per block = OPW x warps
     const int T = p.T, NS = p.NS, nW = p.nW;
     float2* acc_all = reinterpret_cast<float2*>(smem);
     float* stages = reinterpret_cast<float*>(smem + stage_off);
@@ -796,12 +797,22 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
     if (threadIdx.x == 0)
         for (int i = 0; i < NS && i < N; ++i) issue(i);
 
-    const int o = ot * W + warp;
-    const bool ok_obs = o < p.O;
-    const int oc = ok_obs ? o : 0;
-    const float ox = p.obs32[3 * oc], oy = p.obs32[3 * oc + 1], oz = p.obs32[3 * oc + 2];
-    float2* acc = acc_all + (size_t)warp * (T + 2);  // T bins, the overflow and the scratch slot
-    const Anchor anc = make_anchor(p, ox, oy, oz);
+    int o[OPW];
+    bool ok_obs[OPW];
+    float ox[OPW], oy[OPW], oz[OPW];
+    float2* acc[OPW];
+    Anchor anc[OPW];
+#pragma unroll
+    for (int q = 0; q < OPW; ++q) {
+        o[q] = ot * W + warp * OPW + q;
+        ok_obs[q] = o[q] < p.O;
+        const int oc = ok_obs[q] ? o[q] : 0;
+        ox[q] = p.obs32[3 * oc];
+        oy[q] = p.obs32[3 * oc + 1];
+        oz[q] = p.obs32[3 * oc + 2];
+        acc[q] = acc_all + (size_t)(warp * OPW + q) * (T + 2);  // T bins, the overflow and the scratch slot
+        anc[q] = make_anchor(p, ox[q], oy[q], oz[q]);
+    }
     unsigned bad = 0;
 
     int s = (int)(g0 % (unsigned)NS), w = 0, g = 0, since_flush = 0;
@@ -819,36 +830,44 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
         const int tau = w * kWin + lane;
         const bool valid = tau < T;
         const float* st = stages + (size_t)s * SE * kTile;
-        SmpF cur[SE];
+        SmpF cur[OPW][SE];
 #pragma unroll
         for (int jp = 0; jp < SE / 2; ++jp) {
             const float* tl = st + (size_t)(2 * jp) * kTile + lane * 4;
             G2 gg[kGroups];
 #pragma unroll
             for (int q = 0; q < kGroups; ++q) gg[q] = load_g2(tl + q * 2 * kWin * 4);
-            sample_mixed2(gg, ox, oy, oz, anc, p, tau, cur[2 * jp], cur[2 * jp + 1]);
+#pragma unroll
+            for (int q = 0; q < OPW; ++q)
+                sample_mixed2(gg, ox[q], oy[q], oz[q], anc[q], p, tau, cur[q][2 * jp], cur[q][2 * jp + 1]);
         }
         const bool first_win = w == 0, last_win = w == nW - 1;
         const int rot_src = (lane + 31) & 31;
 #pragma unroll
-        for (int j = 0; j < SE; ++j) {
-            // the left neighbour: lane l - 1, or for lane 0 the previous window's lane 31
-            // (kept in shared memory, double-buffered by window parity)
-            SmpF prev = shfl_idx(cur[j], rot_src);
-            if (lane == 0) prev = sh.carry[warp][w & 1][j];
-            deposit(acc, T, p.tmod, p.toff, prev, cur[j], 0, ok_obs && valid && !(first_win && lane == 0), bad);
-            if (lane == 31) sh.carry[warp][(w + 1) & 1][j] = cur[j];
-            if (first_win && lane == 0) sh.first[warp][j] = cur[j];
-            if (last_win) {
-                // the periodic wrap: (t(T-1), t(0) + period] (core.cu:173-194)
-                const SmpF lastS = shfl_idx(cur[j], min(31, T - 1 - w * kWin));
-                if (lane == 0) deposit(acc, T, p.tmod, p.toff, lastS, sh.first[warp][j], T, ok_obs, bad);
+        for (int q = 0; q < OPW; ++q) {
+#pragma unroll
+            for (int j = 0; j < SE; ++j) {
+                // the left neighbour: lane l - 1, or for lane 0 the previous window's lane
+                // 31 (kept in shared memory, double-buffered by window parity)
+                SmpF prev = shfl_idx(cur[q][j], rot_src);
+                if (lane == 0) prev = sh.carry[warp][w & 1][q][j];
+                deposit(acc[q], T, p.tmod, p.toff, prev, cur[q][j], 0,
+                        ok_obs[q] && valid && !(first_win && lane == 0), bad);
+                if (lane == 31) sh.carry[warp][(w + 1) & 1][q][j] = cur[q][j];
+                if (first_win && lane == 0) sh.first[warp][q][j] = cur[q][j];
+                if (last_win) {
+                    // the periodic wrap: (t(T-1), t(0) + period] (core.cu:173-194)
+                    const SmpF lastS = shfl_idx(cur[q][j], min(31, T - 1 - w * kWin));
+                    if (lane == 0) deposit(acc[q], T, p.tmod, p.toff, lastS, sh.first[warp][q][j], T, ok_obs[q], bad);
+                }
             }
         }
         // FP32 partial sums cover at most `flush_groups` element groups before they are
         // added to the FP64 sums in global memory
         if (last_win && (++since_flush == p.flush_groups || g == ngroups - 1)) {
-            if (ok_obs) flush_bins(acc, p.acc + (size_t)o * T * 2, T, lane, false, p.err);
+#pragma unroll
+            for (int q = 0; q < OPW; ++q)
+                if (ok_obs[q]) flush_bins(acc[q], p.acc + (size_t)o[q] * T * 2, T, lane, false, p.err);
             since_flush = 0;
         }
         // release the slot; the last warp to finish with it refills it with stage i + NS
@@ -872,13 +891,15 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
     // the scratch slot holds whatever the lanes without a bin added; the next item's rows
     // (of another length in a batch) may cover it
     __syncwarp();
-    if (lane == 0) acc[T + 1] = make_float2(0.f, 0.f);
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < OPW; ++q) acc[q][T + 1] = make_float2(0.f, 0.f);
     if (__any_sync(0xffffffffu, bad != 0) && lane == 0) flag(p.err, ACUM_DEVERR_ORDER, &p.err->order);
     gbase = g0 + (unsigned)N;
 }
 
-template <int SE>
-__device__ __forceinline__ void mixed_init(unsigned char* smem, size_t stage_off, int NS, MixedShared<SE>& sh)
+template <int SE, int OPW>
+__device__ __forceinline__ void mixed_init(unsigned char* smem, size_t stage_off, int NS, MixedShared<SE, OPW>& sh)
 {
     constexpr int kTile = kGroups * kWin * 4;
     float2* acc_all = reinterpret_cast<float2*>(smem);
@@ -897,8 +918,8 @@ __device__ __forceinline__ void mixed_init(unsigned char* smem, size_t stage_off
 }
 
 // After an abort: wait (bounded) for the copies still in flight before the block exits.
-template <int SE>
-__device__ __forceinline__ void mixed_drain(unsigned char* smem, size_t stage_off, int NS, MixedShared<SE>& sh)
+template <int SE, int OPW>
+__device__ __forceinline__ void mixed_drain(unsigned char* smem, size_t stage_off, int NS, MixedShared<SE, OPW>& sh)
 {
     constexpr int kTile = kGroups * kWin * 4;
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + stage_off + (size_t)NS * SE * kTile * sizeof(float));
@@ -913,14 +934,14 @@ __device__ __forceinline__ void mixed_drain(unsigned char* smem, size_t stage_of
 // memory.  The blocks running at any time therefore share one or two chunks of records
 // in L2 (each record is read from HBM about once per group), and the FP64 sums they add
 // into belong to one group of tiles.
-template <int SE>
-__global__ void __launch_bounds__(512, 1) tonal_mixed_kernel(const KParams p)
+template <int SE, int OPW>
+__global__ void __launch_bounds__(512 / OPW, 1) tonal_mixed_kernel(const KParams p)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ MixedShared<SE> sh;
+    __shared__ MixedShared<SE, OPW> sh;
     __shared__ int s_item;
     const size_t stage_off = acc_region_bytes(p.W, p.T + 2, 8);
-    mixed_init<SE>(smem, stage_off, p.NS, sh);
+    mixed_init<SE, OPW>(smem, stage_off, p.NS, sh);
     unsigned gbase = 0;
     const int nitems = p.obs_tiles * p.nchunk;
     const int G = p.tile_group, per_group = G * p.nchunk;
@@ -937,10 +958,10 @@ __global__ void __launch_bounds__(512, 1) tonal_mixed_kernel(const KParams p)
         const int ec = r / gn, ot = g * G + (r - ec * gn);
         const int e0 = ec * p.chunk;
         const int e1 = min(e0 + p.chunk, p.Epad);
-        mixed_item<SE>(p, ot, e0, e1, smem, stage_off, sh, gbase);
+        mixed_item<SE, OPW>(p, ot, e0, e1, smem, stage_off, sh, gbase);
         __syncthreads();
         if (sh.abort) {
-            mixed_drain<SE>(smem, stage_off, p.NS, sh);
+            mixed_drain<SE, OPW>(smem, stage_off, p.NS, sh);
             break;
         }
     }
@@ -963,10 +984,10 @@ __global__ void __launch_bounds__(512, 1)
                        int* counter, int NS, size_t stage_off)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ MixedShared<SE> sh;
+    __shared__ MixedShared<SE, 1> sh;
     __shared__ __align__(16) KParams sp;
     __shared__ BatchItem s_it;
-    mixed_init<SE>(smem, stage_off, NS, sh);
+    mixed_init<SE, 1>(smem, stage_off, NS, sh);
     unsigned gbase = 0;
     for (;;) {
         if (threadIdx.x == 0) {
@@ -980,16 +1001,18 @@ __global__ void __launch_bounds__(512, 1)
         for (int k = threadIdx.x; k < kWords; k += blockDim.x)
             reinterpret_cast<int*>(&sp)[k] = reinterpret_cast<const int*>(cases + it.c)[k];
         __syncthreads();
-        mixed_item<SE>(sp, it.ot, it.e0, it.e1, smem, stage_off, sh, gbase);
+        mixed_item<SE, 1>(sp, it.ot, it.e0, it.e1, smem, stage_off, sh, gbase);
         __syncthreads();
         if (sh.abort) {
-            mixed_drain<SE>(smem, stage_off, NS, sh);
+            mixed_drain<SE, 1>(smem, stage_off, NS, sh);
             break;
         }
     }
 }
 
 constexpr int kSE32 = 4;
+constexpr int kMixedSE = 8;   // samples in flight per lane of the mixed kernel (SE x OPW)
+constexpr int kMixedOPW = 1;  // observers per warp of the mixed kernel
 static_assert(kMaxStages >= 4, "stage bookkeeping");
 static_assert(sizeof(SmpF) == 16, "sample record");
 constexpr int kSE64 = 2;
@@ -1007,16 +1030,24 @@ static size_t static_smem_of(K kernel, size_t estimate)
     return a.sharedSizeBytes;
 }
 
-static size_t mixed_static_smem(int SE)
+static size_t mixed_static_smem(int SE, int opw)
 {
-    static size_t v[9] = {};
+    static size_t v[3][9] = {};
     if (SE != 2 && SE != 4 && SE != 8) SE = 8;
-    if (!v[SE]) {
+    if (opw != 2) opw = 1;
+    size_t& x = v[opw][SE];
+    if (!x) {
         const size_t est = (size_t)16 * 3 * SE * sizeof(SmpF) + 256;
-        v[SE] = SE == 2 ? static_smem_of(tonal_mixed_kernel<2>, est)
-                        : SE == 4 ? static_smem_of(tonal_mixed_kernel<4>, est) : static_smem_of(tonal_mixed_kernel<8>, est);
+        if (opw == 2)
+            x = SE == 2   ? static_smem_of(tonal_mixed_kernel<2, 2>, est)
+                : SE == 4 ? static_smem_of(tonal_mixed_kernel<4, 2>, est)
+                          : static_smem_of(tonal_mixed_kernel<8, 2>, est);
+        else
+            x = SE == 2   ? static_smem_of(tonal_mixed_kernel<2, 1>, est)
+                : SE == 4 ? static_smem_of(tonal_mixed_kernel<4, 1>, est)
+                          : static_smem_of(tonal_mixed_kernel<8, 1>, est);
     }
-    return v[SE];
+    return x;
 }
 
 size_t batch_static_smem(int SE)
@@ -1038,22 +1069,29 @@ static size_t tonal_smem(int W, int T, int NS, int SE, int real_bytes)
     return acc + (size_t)NS * SE * kGroups * kWin * 4 * real_bytes + (size_t)NS * 8;
 }
 
-cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int num_sms, size_t smem_optin)
+cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int num_sms, size_t smem_optin,
+                       int opw_req)
 {
     const bool f64 = r.precision == ACUM_PLAIN_FP64;
     const int rb = f64 ? 8 : 4;
-    // mixed: elements per stage 2 or 4 (default 4); FP64: 2
-    // mixed: elements per stage 2, 4 or 8 (default: the most samples in flight per lane);
-    // a stage of 8 needs only 2 ring stages
-    const int SE = f64 ? kSE64 : ((SE_req == 2 || SE_req == 4) ? SE_req : 8);
+    // FP64: elements per stage 2, one observer per warp.  Mixed: elements per stage 2, 4
+    // or 8 and observers per warp 1 or 2 (default: kMixedSE / kMixedOPW elements of
+    // kMixedOPW observers).  A stage of 8 needs only 2 ring stages.
+    int SE = kSE64, opw = 1;
+    if (!f64) {
+        opw = (opw_req == 1 || opw_req == 2) ? opw_req : kMixedOPW;
+        SE = (SE_req == 2 || SE_req == 4 || SE_req == 8) ? SE_req : kMixedSE / opw;
+
+    }
     const int NSmin = SE == 8 ? 2 : 4;
-    const int opw = 1;
     r.t.opw = opw;
     const int T = r.g.T;
+    // at most 16 observers per block: 16 warps of one, or 8 of two (the register limit of
+    // the two-observer form's 256 threads)
     int W = W_req > 0 ? W_req : 16;
     W = std::min(W, 16);
     // keep room in the per-block limit for the kernels' static shared memory
-    const size_t budget = smem_optin - (f64 ? 1024 : mixed_static_smem(SE));
+    const size_t budget = smem_optin - (f64 ? 1024 : mixed_static_smem(SE, opw));
     while (W > opw && tonal_smem(W, T, NSmin, SE, rb) > budget) W -= opw;
     if (tonal_smem(W, T, NSmin, SE, rb) > budget) return cudaErrorInvalidValue;
     if (W_req <= 0) {
@@ -1146,17 +1184,17 @@ static cudaError_t launch_f64_t(const KParams& kp, int items, int threads, size_
     return cudaGetLastError();
 }
 
-template <int SE>
+template <int SE, int OPW>
 static cudaError_t launch_mixed_t(const KParams& kp, int grid, int threads, size_t smem, cudaStream_t s)
 {
     static size_t configured = 0;
     if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(tonal_mixed_kernel<SE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(tonal_mixed_kernel<SE, OPW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
-    tonal_mixed_kernel<SE><<<grid, threads, smem, s>>>(kp);
+    tonal_mixed_kernel<SE, OPW><<<grid, threads, smem, s>>>(kp);
     return cudaGetLastError();
 }
 
@@ -1210,9 +1248,15 @@ cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s)
     KParams kp;
     fill_kparams(r, kp);
     if (r.precision == ACUM_PLAIN_FP64) return launch_f64_t<kSE64>(kp, r.t.items, 32 * r.t.W, r.t.smem, s);
-    if (r.t.SE == 2) return launch_mixed_t<2>(kp, r.t.grid, 32 * r.t.W, r.t.smem, s);
-    if (r.t.SE == 8) return launch_mixed_t<8>(kp, r.t.grid, 32 * r.t.W, r.t.smem, s);
-    return launch_mixed_t<kSE32>(kp, r.t.grid, 32 * r.t.W, r.t.smem, s);
+    const int threads = 32 * (r.t.W / r.t.opw);
+    if (r.t.opw == 2) {
+        if (r.t.SE == 2) return launch_mixed_t<2, 2>(kp, r.t.grid, threads, r.t.smem, s);
+        if (r.t.SE == 4) return launch_mixed_t<4, 2>(kp, r.t.grid, threads, r.t.smem, s);
+        return launch_mixed_t<8, 2>(kp, r.t.grid, threads, r.t.smem, s);
+    }
+    if (r.t.SE == 2) return launch_mixed_t<2, 1>(kp, r.t.grid, threads, r.t.smem, s);
+    if (r.t.SE == 8) return launch_mixed_t<8, 1>(kp, r.t.grid, threads, r.t.smem, s);
+    return launch_mixed_t<4, 1>(kp, r.t.grid, threads, r.t.smem, s);
 }
 
 size_t batch_smem(int W, int SE, int Tmax)

@@ -83,6 +83,7 @@ SIGNATURES = {
     "acum_device_error_word": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.c_int]),
     "acum_last_timing": (C.c_int, [C.c_void_p, C.c_int, _DP, C.POINTER(C.c_longlong)]),
     "acum_set_tile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "acum_set_obs_per_warp": (C.c_int, [C.c_void_p, C.c_int]),
     "acum_measure_peak": (C.c_int, [C.c_int, C.c_int, _DP]),
     "acum_host_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t]),
     "acum_host_free": (C.c_int, [C.c_void_p]),
@@ -295,13 +296,15 @@ class Context:
     def write_outputs(self, path: str):
         self._ck(self.L.acum_write_outputs(self.h, os.fsencode(path)))
 
-    def set_tile(self, obs_per_block=0, elems_per_stage=0, items_per_sm=0):
+    def set_tile(self, obs_per_block=0, elems_per_stage=0, items_per_sm=0, obs_per_warp=0):
         self._ck(self.L.acum_set_tile(self.h, obs_per_block, elems_per_stage, items_per_sm))
+        self._ck(self.L.acum_set_obs_per_warp(self.h, obs_per_warp))
 
     def last_plan(self) -> dict:
-        v = (C.c_int * 6)()
+        v = (C.c_int * 7)()
         self._ck(self.L.acum_last_plan(self.h, v))
-        keys = ("obs_per_block", "elems_per_stage", "stages", "elems_per_item", "element_chunks", "work_items")
+        keys = ("obs_per_block", "elems_per_stage", "stages", "elems_per_item", "element_chunks", "work_items",
+                "obs_per_warp")
         return dict(zip(keys, (int(x) for x in v)))
 
     def timing(self, which: int):

@@ -185,8 +185,12 @@ int acum_last_timing(const acum_ctx* ctx, int which, double* ms, long long* laun
 /* Tile shape of the tonal kernels (0 = let the library choose): observers per block
  * (1..16), elements per pipeline stage (mixed form: 2, 4 or 8) and work items per SM. */
 int acum_set_tile(acum_ctx* ctx, int obs_per_block, int elems_per_stage, int items_per_sm);
-/* The plan of the last tonal run: out[0] observers per block, [1] elements per stage,
- * [2] pipeline stages, [3] elements per work item, [4] element chunks, [5] work items. */
+/* Observers evaluated per warp of the mixed tonal kernel on the records it loads once:
+ * 1 or 2 (0 = let the library choose). */
+int acum_set_obs_per_warp(acum_ctx* ctx, int obs_per_warp);
+/* The plan of the last tonal run (out holds 7 ints): out[0] observers per block,
+ * [1] elements per stage, [2] pipeline stages, [3] elements per work item, [4] element
+ * chunks, [5] work items, [6] observers per warp. */
 int acum_last_plan(const acum_ctx* ctx, int* out);
 
 /* Self-test of the bounded wait that every pipelined kernel uses on its barriers: one
