@@ -128,6 +128,9 @@ struct KParams {
     const double* obs64;
     // mixed constants
     float a0f, alphaf, ialphaf, vxf, vyf, vzf, kbhi, kblo, invTf;
+    // the same as pairs (both halves equal), the operands of the packed FP32 instructions:
+    // -alpha, -vInf, a0, oM / dPsi
+    float2 nalpha2, nvx2, nvy2, nvz2, a02, kb2;
     unsigned tmod;  // ceil(2^32 / T): bin index modulo T by multiply-high
     int toff;       // a multiple of T >= 2^23, added to bin indices before the modulo
     // FP64 constants

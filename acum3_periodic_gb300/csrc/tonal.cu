@@ -642,18 +642,18 @@ __device__ __forceinline__ void sample_mixed2(const G2* g, float ox, float oy, f
     const float2 S = fma2(g[0].x, add2(dx, OX), fma2(g[0].y, add2(dy, OY), mul2(g[0].z, add2(dz, OZ))));
     const float2 nnum = fma2(f2(-an.t2), g[4].w, S);
     const float2 bp = sub2(f2(an.s0), g[4].w);
-    const float2 q = fma2(f2(-p.alphaf), nnum, mul2(bp, bp));
+    const float2 q = fma2(p.nalpha2, nnum, mul2(bp, bp));
     const float2 den = fma2(q, make_float2(rsqrt_ftz(q.x), rsqrt_ftz(q.y)), bp);
     const float2 dt = mul2(nnum, make_float2(-rcp_ftz(den.x), -rcp_ftz(den.y)));
     const float2 tr = add2(f2(an.t0), dt);
-    const float2 rx = fma2(f2(-p.vxf), tr, dx), ry = fma2(f2(-p.vyf), tr, dy), rz = fma2(f2(-p.vzf), tr, dz);
-    const float2 ir = rcp2(mul2(f2(p.a0f), tr));
+    const float2 rx = fma2(p.nvx2, tr, dx), ry = fma2(p.nvy2, tr, dy), rz = fma2(p.nvz2, tr, dz);
+    const float2 ir = rcp2(mul2(p.a02, tr));
     const float2 Mr = mul2(fma2(g[1].x, rx, fma2(g[1].y, ry, mul2(g[1].z, rz))), ir);
     const float2 Mdr = mul2(fma2(g[2].x, rx, fma2(g[2].y, ry, mul2(g[2].z, rz))), ir);
     const float2 Lr = mul2(fma2(g[3].x, rx, fma2(g[3].y, ry, mul2(g[3].z, rz))), ir);
     const float2 Ldr = mul2(fma2(g[4].x, rx, fma2(g[4].y, ry, mul2(g[4].z, rz))), ir);
     const float2 G = rcp2(sub2(f2(1.0f), Mr));
-    const float2 qa = mul2(f2(p.a0f), ir);
+    const float2 qa = mul2(p.a02, ir);
     const float2 K = fma2(qa, sub2(Mr, g[1].w), Mdr);
     const float2 base = mul2(mul2(ir, G), G);
     const float2 pt = mul2(mul2(g[2].w, base), mul2(G, K));
@@ -661,7 +661,7 @@ __device__ __forceinline__ void sample_mixed2(const G2* g, float ox, float oy, f
     // observer time in bins: tau + round(t0 oM/dPsi) + x, x = frac(t0 oM/dPsi) + dt oM/dPsi;
     // outside the floor's range (or not finite) the fraction is NaN, which the deposit
     // rejects (and reports) whatever the integer part holds
-    const float2 x = fma2(dt, f2(p.kbhi), f2(an.kf));
+    const float2 x = fma2(dt, p.kb2, f2(an.kf));
     const float2 t = __fadd2_rd(x, f2(kRound));
     const float2 fr = sub2(x, add2(t, f2(-kRound)));
     const int kb = tau + an.ki - kRoundBits;
@@ -1230,6 +1230,12 @@ void fill_kparams(const TonalRun& r, KParams& kp)
     kp.kbhi = (float)kb;
     kp.kblo = (float)(kb - (double)kp.kbhi);
     kp.invTf = 1.0f / (float)g.T;
+    kp.nalpha2 = make_float2(-kp.alphaf, -kp.alphaf);
+    kp.nvx2 = make_float2(-kp.vxf, -kp.vxf);
+    kp.nvy2 = make_float2(-kp.vyf, -kp.vyf);
+    kp.nvz2 = make_float2(-kp.vzf, -kp.vzf);
+    kp.a02 = make_float2(kp.a0f, kp.a0f);
+    kp.kb2 = make_float2(kp.kbhi, kp.kbhi);
     kp.tmod = (unsigned)((0x100000000ull + (unsigned long long)g.T - 1) / (unsigned long long)g.T);
     kp.toff = (int)(((1 << 23) + g.T - 1) / g.T * g.T);
     kp.W = r.t.W;
