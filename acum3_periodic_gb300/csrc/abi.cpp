@@ -352,15 +352,19 @@ int acum_ctx::ensure_prep(bool need64, bool need32, bool need_fields)
     if (!d_raw.p) return fail(this, ACUM_ERR_STATE, "the surface rows were released after preprocessing");
     if (T > 4096) return fail(this, ACUM_ERR_UNSUPPORTED, "nTime above 4096 is not supported by the preprocessing");
     const size_t nrec = (size_t)Epad * nW * kGroups * kWin * 4;
+    const long long layout[4] = {(long long)E, (long long)Epad, (long long)nW, (long long)T};
+    const auto same = [&](const long long* l) { return std::equal(l, l + 4, layout); };
     if (do64) {
-        bool fresh = d_rec64.n < nrec;
+        const bool clear = d_rec64.n < nrec || !same(rec64_layout);
         CK(this, d_rec64.ensure(nrec));
-        if (fresh) CK(this, cudaMemsetAsync(d_rec64.p, 0, nrec * 8, stream));
+        if (clear) CK(this, cudaMemsetAsync(d_rec64.p, 0, nrec * 8, stream));
+        std::copy(layout, layout + 4, rec64_layout);
     }
     if (do32) {
-        bool fresh = d_rec32.n < nrec;
+        const bool clear = d_rec32.n < nrec || !same(rec32_layout);
         CK(this, d_rec32.ensure(nrec));
-        if (fresh) CK(this, cudaMemsetAsync(d_rec32.p, 0, nrec * 4, stream));
+        if (clear) CK(this, cudaMemsetAsync(d_rec32.p, 0, nrec * 4, stream));
+        std::copy(layout, layout + 4, rec32_layout);
     }
     if (need_fields) CK(this, d_fields.ensure((size_t)E * T * kFields));
     PrepArgs a;

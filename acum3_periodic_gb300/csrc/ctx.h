@@ -113,6 +113,10 @@ struct acum_ctx {
     acum::DBuf<float> d_rec32;
     acum::DBuf<acum::DeviceErr> d_err;
     bool rec64_ok = false, rec32_ok = false;
+    // layout (E, Epad, nW, T) the record buffers were last written for: the preprocessing
+    // writes the real elements and steps only, so a buffer whose padding may hold records
+    // of another layout is cleared first
+    long long rec64_layout[4] = {-1, -1, -1, -1}, rec32_layout[4] = {-1, -1, -1, -1};
 
     // results kept for acum_write_outputs
     std::vector<double> h_out, h_spl, h_oaspl;

@@ -191,3 +191,20 @@ def test_mixed_tile_shapes_against_oracle(ctx, W, SE, opw):
     assert per_bin_rms(mA, oA).max() < MIXED_RMS_TOL
     assert np.abs(oaspl_db(mA) - oaspl_db(oA)).max() < OASPL_TOL_DB
     assert ctx.error_word(reset=True) == 0
+
+
+def test_decks_in_sequence_on_one_context(ctx):
+    """Decks of falling and rising sizes set one after the other on one context: each
+    result matches the oracle, so nothing of a previous deck (its records in the padding
+    of a reused buffer, its plan) reaches the next."""
+    from acum3_periodic_gb300 import native
+    for T, nobs, ns in [(96, 29, 7), (64, 29, 7), (45, 13, 7), (75, 29, 5), (45, 29, 7), (90, 29, 7)]:
+        d = synth.config_deck(0, replicate=35, scale=dict(n_span=ns, n_chord_side=5, ntime=T, nobs=nobs))
+        oT, oL, oA, bad = O.tonal(d)
+        assert bad == 0
+        ctx.set_deck(d, bb=False)
+        _, _, pA = ctx.tonal(native.PLAIN_FP64)
+        assert per_bin_rel(pA, oA).max() < F64_TOL, T
+        _, _, mA = ctx.tonal(native.MIXED)
+        assert per_bin_rms(mA, oA).max() < MIXED_RMS_TOL, T
+        assert ctx.error_word(reset=True) == 0
