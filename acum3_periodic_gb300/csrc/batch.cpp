@@ -133,10 +133,10 @@ void build_items(const acum_batch* b, int W, int SE, int ips, std::vector<BatchI
         const int groups = c->Epad / SE;
         const double per_tile = (double)W * c->Epad * c->T;
         int nchunk = (int)std::ceil(per_tile / std::max(target, 1.0));
-        // element chunks of at most ~16 MB of records, so that the items of one chunk,
-        // which run close together in time, share it in L2
+        // element chunks of at most ~32 MB of records (as the single-deck plan), so that
+        // the items of one chunk, which run close together in time, share it in L2
         const size_t per_elem = (size_t)c->nW * kGroups * kWin * 4 * sizeof(float);
-        const int max_groups = std::max(1, (int)(((size_t)16 << 20) / per_elem) / SE);
+        const int max_groups = std::max(1, (int)(((size_t)32 << 20) / per_elem) / SE);
         nchunk = std::max(nchunk, (groups + max_groups - 1) / max_groups);
         nchunk = std::max(1, std::min(nchunk, groups));
         const int gpc = (groups + nchunk - 1) / nchunk;

@@ -1010,7 +1010,6 @@ __global__ void __launch_bounds__(512, 1)
     }
 }
 
-constexpr int kSE32 = 4;
 constexpr int kMixedSE = 8;   // samples in flight per lane of the mixed kernel (SE x OPW)
 constexpr int kMixedOPW = 1;  // observers per warp of the mixed kernel
 static_assert(kMaxStages >= 4, "stage bookkeeping");
