@@ -592,7 +592,7 @@ constexpr int kRoundBits = 0x4B400000;
 
 struct Anchor {
     float t0, t2, s0, kf;  // t0, 2 t0, alpha t0 + D0.v, frac(t0 * oM / dPsi)
-    int ki;                // round(t0 * oM / dPsi)
+    int ki;                // round(t0 * oM / dPsi) modulo T, plus p.toff
 };
 
 __device__ __forceinline__ Anchor make_anchor(const KParams& p, float ox, float oy, float oz)
@@ -609,7 +609,9 @@ __device__ __forceinline__ Anchor make_anchor(const KParams& p, float ox, float 
     a.t2 = (float)(2.0 * t0);
     a.s0 = (float)s0;
     a.kf = (float)(K - Kr);
-    a.ki = (int)(Kr - floor(Kr / p.T) * p.T);  // bins wrap with period T: keep the index small
+    // bins wrap with period T: the index is kept small, plus the offset p.toff (a multiple
+    // of T of at least 2^23) that keeps it non-negative for the modulo
+    a.ki = (int)(Kr - floor(Kr / p.T) * p.T) + p.toff;
     return a;
 }
 
@@ -703,36 +705,48 @@ __device__ __forceinline__ void add_bin(float2* acc, int idx, float w, float2 pa
 // first at the first bin modulo T, the second at the slot after it (which may be the
 // overflow slot); a lane with fewer bins adds into the scratch slot instead.  The bins of
 // the lanes of a warp are disjoint (observer time increases with the step), so only the
-// scratch slot is written by more than one lane.  Intervals of more than two bins
-// (|Mr| >= 1) add the rest in a loop; a decreasing or non-finite observer time (or an
-// interval of more than T bins) sets `bad` and deposits nothing.  `toff` is a multiple of
-// T of at least 2^23 that keeps the bin index non-negative for the modulo (|k| < 2^22
-// plus twice the period).
-__device__ __forceinline__ void deposit(float2* acc, int T, unsigned tm, int toff, const SmpF& a, const SmpF& b,
-                                        int kshift, bool active, unsigned& bad)
+// scratch slot is written by more than one lane.  A decreasing or non-finite observer
+// time sets `bad` and deposits nothing.  Intervals of more than two bins (|Mr| >= 1) set
+// `more`: the caller then adds their other bins with deposit_rest.  The integer parts k
+// carry a multiple of T of at least 2^23 (the anchor's), which keeps the bin index
+// non-negative for the modulo.
+__device__ __forceinline__ void deposit(float2* acc, int T, unsigned tm, const SmpF& a, const SmpF& b, int kshift,
+                                        bool active, unsigned& bad, bool& more)
 {
     const int cnt = b.k + kshift - a.k;
     const float du = small_int_to_float(cnt) + (b.f - a.f);
     const bool ok = du > 0.0f;  // false for NaN
     bad |= (active && !ok) ? 1u : 0u;
     const bool one = active && ok && cnt >= 1, two = one && cnt >= 2;
+    more |= two && cnt > 2;
     const float inv = rcp_ftz(ok ? du : 1.0f);
     const float2 pa = make_float2(a.pt, a.pl), dp = sub2(make_float2(b.pt, b.pl), pa);
-    const int idx = mod_T(one ? a.k + 1 + toff : 0, T, tm);
+    const int idx = mod_T(a.k + 1, T, tm);  // used only when `one`
     const float w1 = (1.0f - a.f) * inv;
     const int i1 = one ? idx : T + 1, i2 = two ? idx + 1 : T + 1;
     acc[i1] = add2(acc[i1], fma2(f2(w1), dp, pa));
     acc[i2] = add2(acc[i2], fma2(f2(w1 + inv), dp, pa));
-    if (one && cnt > 2) {
-        if (cnt > T) {
-            bad = 1u;
-        } else {
-            int i = idx + 1;
-            for (int m = 2; m < cnt; ++m) {
-                if (++i >= T) i -= T;
-                acc[i] = add2(acc[i], fma2(f2(w1 + (float)m * inv), dp, pa));
-            }
-        }
+}
+
+// The bins after the first two of an interval that holds more (see deposit); an interval
+// of more than T bins sets `bad` instead.
+__device__ __forceinline__ void deposit_rest(float2* acc, int T, unsigned tm, const SmpF& a, const SmpF& b,
+                                             int kshift, bool active, unsigned& bad)
+{
+    const int cnt = b.k + kshift - a.k;
+    const float du = small_int_to_float(cnt) + (b.f - a.f);
+    if (!(active && du > 0.0f && cnt > 2)) return;
+    if (cnt > T) {
+        bad = 1u;
+        return;
+    }
+    const float inv = rcp_ftz(du);
+    const float2 pa = make_float2(a.pt, a.pl), dp = sub2(make_float2(b.pt, b.pl), pa);
+    const float w1 = (1.0f - a.f) * inv;
+    int i = mod_T(a.k + 1, T, tm);
+    for (int m = 1; m < cnt; ++m) {
+        if (++i >= T) i -= T;
+        if (m >= 2) acc[i] = add2(acc[i], fma2(f2(w1 + (float)m * inv), dp, pa));
     }
 }
 
@@ -814,6 +828,7 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
         anc[q] = make_anchor(p, ox[q], oy[q], oz[q]);
     }
     unsigned bad = 0;
+    bool more = false;
 
     int s = (int)(g0 % (unsigned)NS), w = 0, g = 0, since_flush = 0;
     uint32_t par = (g0 / (unsigned)NS) & 1u;
@@ -851,16 +866,34 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
                 // 31 (kept in shared memory, double-buffered by window parity)
                 SmpF prev = shfl_idx(cur[q][j], rot_src);
                 if (lane == 0) prev = sh.carry[warp][w & 1][q][j];
-                deposit(acc[q], T, p.tmod, p.toff, prev, cur[q][j], 0,
-                        ok_obs[q] && valid && !(first_win && lane == 0), bad);
+                deposit(acc[q], T, p.tmod, prev, cur[q][j], 0, ok_obs[q] && valid && !(first_win && lane == 0), bad,
+                        more);
                 if (lane == 31) sh.carry[warp][(w + 1) & 1][q][j] = cur[q][j];
                 if (first_win && lane == 0) sh.first[warp][q][j] = cur[q][j];
                 if (last_win) {
                     // the periodic wrap: (t(T-1), t(0) + period] (core.cu:173-194)
                     const SmpF lastS = shfl_idx(cur[q][j], min(31, T - 1 - w * kWin));
-                    if (lane == 0) deposit(acc[q], T, p.tmod, p.toff, lastS, sh.first[warp][q][j], T, ok_obs[q], bad);
+                    if (lane == 0) {
+                        bool wrap_more = false;
+                        deposit(acc[q], T, p.tmod, lastS, sh.first[warp][q][j], T, ok_obs[q], bad, wrap_more);
+                        if (wrap_more) deposit_rest(acc[q], T, p.tmod, lastS, sh.first[warp][q][j], T, ok_obs[q], bad);
+                    }
                 }
             }
+        }
+        // intervals of more than two bins (|Mr| >= 1): their other bins, for the whole warp
+        if (__any_sync(0xffffffffu, more)) {
+#pragma unroll
+            for (int q = 0; q < OPW; ++q) {
+#pragma unroll
+                for (int j = 0; j < SE; ++j) {
+                    SmpF prev = shfl_idx(cur[q][j], rot_src);
+                    if (lane == 0) prev = sh.carry[warp][w & 1][q][j];
+                    deposit_rest(acc[q], T, p.tmod, prev, cur[q][j], 0,
+                                 ok_obs[q] && valid && !(first_win && lane == 0), bad);
+                }
+            }
+            more = false;
         }
         // FP32 partial sums cover at most `flush_groups` element groups before they are
         // added to the FP64 sums in global memory

@@ -208,3 +208,21 @@ def test_decks_in_sequence_on_one_context(ctx):
         _, _, mA = ctx.tonal(native.MIXED)
         assert per_bin_rms(mA, oA).max() < MIXED_RMS_TOL, T
         assert ctx.error_word(reset=True) == 0
+
+
+def test_supersonic_intervals_of_three_bins(ctx):
+    """A rotor at tip Mach 0.95 in a Mach 0.45 stream: the observer time advances by up
+    to 2.5 bins per step on one side (intervals of three bins, the mixed kernel's
+    per-stage extra pass) and runs backwards on the other (skipped, reported as
+    ACUM_DEVERR_ORDER by both forms).  The two forms deposit the same intervals."""
+    from acum3_periodic_gb300 import native
+    d = synth.config_deck(0, replicate=36, scale=dict(n_span=6, n_chord_side=4, ntime=72, nobs=16,
+                                                       tip_mach=0.95, minf=0.45))
+    ctx.set_deck(d, bb=False)
+    ctx.error_word(reset=True)
+    _, _, ref = ctx.tonal(native.PLAIN_FP64)
+    assert ctx.error_word(reset=True) & native.DEVERR_ORDER
+    _, _, got = ctx.tonal(native.MIXED)
+    assert ctx.error_word(reset=True) & native.DEVERR_ORDER
+    assert np.all(np.isfinite(got))
+    assert per_bin_rms(got, ref).max() < 1e-3
