@@ -210,11 +210,32 @@ def test_decks_in_sequence_on_one_context(ctx):
         assert ctx.error_word(reset=True) == 0
 
 
+def _observer_time_bins(d, fields):
+    """u[o, e, tau]: observer time in bins of every sample (FP64, the retarded-time root
+    of core.cu:261-279 and the observer time of core.cu:156)."""
+    der = d.derived()
+    x = fields[:, :, 0:3]
+    v = np.asarray(der["vInf"], np.float64)
+    a0 = float(der["a0"])
+    alpha = a0 * a0 - v @ v
+    out = []
+    for o in d.observers().astype(np.float64):
+        dd = o[None, None, :] - x
+        c = np.sum(dd * dd, -1)
+        beta = dd @ v
+        tr = (np.sqrt(beta * beta + alpha * c) - beta) / alpha
+        out.append((np.arange(d.nTime)[None, :] * float(der["dTau"]) + tr) * float(der["oM"]) / float(der["dPsi"]))
+    return np.array(out)
+
+
 def test_supersonic_intervals_of_three_bins(ctx):
     """A rotor at tip Mach 0.95 in a Mach 0.45 stream: the observer time advances by up
     to 2.5 bins per step on one side (intervals of three bins, the mixed kernel's
-    per-stage extra pass) and runs backwards on the other (skipped, reported as
-    ACUM_DEVERR_ORDER by both forms).  The two forms deposit the same intervals."""
+    per-stage extra pass) and runs backwards on the other (skipped and reported as
+    ACUM_DEVERR_ORDER by both forms).  Near the Doppler singularity (1 - Mr -> 0) the
+    integrand is unbounded and the two precisions part, so the forms are compared on the
+    bins that no interval of less than 0.5 bins per step (or its neighbours) reaches;
+    those bins include the three-bin intervals."""
     from acum3_periodic_gb300 import native
     d = synth.config_deck(0, replicate=36, scale=dict(n_span=6, n_chord_side=4, ntime=72, nobs=16,
                                                        tip_mach=0.95, minf=0.45))
@@ -225,4 +246,20 @@ def test_supersonic_intervals_of_three_bins(ctx):
     _, _, got = ctx.tonal(native.MIXED)
     assert ctx.error_word(reset=True) & native.DEVERR_ORDER
     assert np.all(np.isfinite(got))
-    assert per_bin_rms(got, ref).max() < 1e-3
+    T = d.nTime
+    u = _observer_time_bins(d, ctx.fields())                      # [O][E][T]
+    ub = np.concatenate([u[:, :, -1:] - T, u], axis=2)             # interval k: (ub[k], ub[k+1]]
+    du = np.diff(ub, axis=2)                                       # [O][E][T]
+    near = du < 0.5
+    near = near | np.roll(near, 1, axis=2) | np.roll(near, -1, axis=2)
+    masked = np.zeros((T, d.nObs), bool)
+    three = np.zeros((T, d.nObs), bool)
+    for o, e, k in zip(*np.nonzero(near)):
+        lo, hi = sorted((ub[o, e, k], ub[o, e, k + 1]))
+        masked[np.arange(int(np.floor(lo)) - 1, int(np.ceil(hi)) + 2) % T, o] = True
+    for o, e, k in zip(*np.nonzero(du > 2.0)):
+        three[np.arange(int(np.floor(ub[o, e, k])) + 1, int(np.floor(ub[o, e, k + 1])) + 1) % T, o] = True
+    keep = ~masked
+    assert (keep & three).sum() >= 20
+    rms = np.sqrt(np.mean(ref ** 2, axis=0, keepdims=True))
+    assert np.max(np.abs(got - ref)[keep] / np.broadcast_to(rms, ref.shape)[keep]) < 1e-4
