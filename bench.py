@@ -209,14 +209,30 @@ def batch_leg(native, device, steps=1, inflight=6):
     steps, 64-2048 observers) resident on the GPU and solved in mixed precision (a) by one
     persistent launch replayed from a CUDA graph, tile shape from the autotuner, and (b) by
     one launch per case.  Decks are generated on host threads (a bounded number in flight)
-    and added one by one; only their records stay on the device."""
+    and added one by one; only their records stay on the device.  The same comparison on
+    64 small cases (the same draws capped at 10 x 2 x 8 panels per blade, 360 steps and
+    128 observers), where one case fills a few SMs only, is in `small_cases`."""
+    from acum3_periodic_gb300 import synth
+    res = _batch_compare(native, device, lambda c: synth.batch_deck(c), steps, inflight)
+    res["workload"] = "workload 4: 64 rotor cases, one persistent launch (CUDA graph) vs one launch per case"
+    small = dict(n_span=10, n_chord_side=8, ntime=360, nobs=128)
+    sm = _batch_compare(native, device, lambda c: synth.batch_deck(c, shrink=small), max(steps, 3), inflight)
+    sm["workload"] = ("64 small rotor cases (workload 4 draws capped at %d x 2 x %d panels per blade, %d steps, "
+                      "%d observers)" % (small["n_span"], small["n_chord_side"], small["ntime"], small["nobs"]))
+    sm["per_case"].pop("per_case", None)
+    sm["per_case"].pop("per_case_columns", None)
+    res["small_cases"] = sm
+    return res
+
+
+def _batch_compare(native, device, make_deck, steps, inflight):
     from concurrent.futures import ThreadPoolExecutor
     from acum3_periodic_gb300 import synth
     ncase = len(synth.batch_specs())
     b = native.Batch(device)
     t0 = time.perf_counter()
     with ThreadPoolExecutor(inflight) as ex:
-        futs = [ex.submit(synth.batch_deck, c) for c in range(min(inflight, ncase))]
+        futs = [ex.submit(make_deck, c) for c in range(min(inflight, ncase))]
         nxt = len(futs)
         for c in range(ncase):
             d = futs[c].result()
@@ -224,7 +240,7 @@ def batch_leg(native, device, steps=1, inflight=6):
             b.add(d)
             del d
             if nxt < ncase:
-                futs.append(ex.submit(synth.batch_deck, nxt))
+                futs.append(ex.submit(make_deck, nxt))
                 nxt += 1
     gen_s = time.perf_counter() - t0
     evals = np.array([e for (_, _, e) in b.shapes], np.float64)
@@ -233,8 +249,7 @@ def batch_leg(native, device, steps=1, inflight=6):
     est_ms = b.autotune()
     tune_s = time.perf_counter() - t0
     tile = b.tile()
-    res = {"workload": "workload 4: 64 rotor cases, one persistent launch (CUDA graph) vs one launch per case",
-           "cases": ncase, "evals": total, "deck_generation_s": gen_s, "autotune_s": tune_s,
+    res = {"cases": ncase, "evals": total, "deck_generation_s": gen_s, "autotune_s": tune_s,
            "tile": {"obs_per_block": tile[0], "elems_per_stage": tile[1], "items_per_sm": tile[2]},
            "autotune_estimate_ms": est_ms}
     for name, mode in (("persistent_graph", 2), ("per_case", 1)):
