@@ -724,8 +724,11 @@ __device__ __forceinline__ void deposit(float2* acc, int T, unsigned tm, const S
     const int idx = mod_T(a.k + 1, T, tm);  // used only when `one`
     const float w1 = (1.0f - a.f) * inv;
     const int i1 = one ? idx : T + 1, i2 = two ? idx + 1 : T + 1;
-    acc[i1] = add2(acc[i1], fma2(f2(w1), dp, pa));
-    acc[i2] = add2(acc[i2], fma2(f2(w1 + inv), dp, pa));
+    // i1 != i2 unless both are the scratch slot, so both bins are read before either is
+    // written (one shared-memory round trip per sample instead of two in sequence)
+    const float2 v1 = acc[i1], v2 = acc[i2];
+    acc[i1] = add2(v1, fma2(f2(w1), dp, pa));
+    acc[i2] = add2(v2, fma2(f2(w1 + inv), dp, pa));
 }
 
 // The bins after the first two of an interval that holds more (see deposit); an interval
