@@ -319,6 +319,7 @@ extern "C" int acum_last_plan(const acum_ctx* ctx, int* out)
     out[4] = t.nchunk;
     out[5] = t.items;
     out[6] = t.opw;
+    out[7] = t.tm ? 1 : 0;
     return ACUM_OK;
 }
 
@@ -331,6 +332,14 @@ extern "C" int acum_set_tile(acum_ctx* ctx, int obs_per_block, int elems_per_sta
     ctx->tile_W = obs_per_block;
     ctx->tile_SE = elems_per_stage;
     ctx->tile_ips = items_per_sm;
+    return ACUM_OK;
+}
+
+extern "C" int acum_set_tensor_memory(acum_ctx* ctx, int use)
+{
+    if (!ctx) return ACUM_ERR_INVALID;
+    if (use < 0 || use > 2) return fail(ctx, ACUM_ERR_INVALID, "acum_set_tensor_memory: out of range");
+    ctx->tile_tm = use;
     return ACUM_OK;
 }
 
@@ -453,7 +462,7 @@ int acum_ctx::run_tonal(int precision, double* d_pT, double* d_pL, double* d_pA)
     r.g.lpi = T * der.dPsi;
     for (int c = 0; c < 3; ++c) r.g.vinf[c] = der.vinf[c];
     r.precision = precision;
-    CK(this, plan_tonal(r, tile_W, tile_SE, tile_ips, num_sms, smem_optin, tile_opw));
+    CK(this, plan_tonal(r, tile_W, tile_SE, tile_ips, num_sms, smem_optin, tile_opw, tile_tm));
     r.rec = f64 ? (const void*)d_rec64.p : (const void*)d_rec32.p;
     r.obs64 = d_obs64.p;
     r.obs32 = d_obs32.p;

@@ -63,6 +63,7 @@ struct TonalTile {
     int tile_group;   // mixed: observer tiles per group of the item order
     int flush_elems;  // mixed: elements summed in FP32 before the FP64 flush
     int opw;          // observers per warp
+    bool tm;          // mixed: record stages copied into tensor memory and read from there
     size_t smem;
 };
 
@@ -117,7 +118,7 @@ struct TonalRun {
     int precision;
 };
 cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int num_sms, size_t smem_optin,
-                       int opw_req = 0);
+                       int opw_req = 0, int tm_req = 0);
 cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s);
 
 // Constants of one tonal launch (one case), as the kernels read them.

@@ -126,7 +126,7 @@ struct acum_ctx {
     unsigned err_bits = 0;
     long long launches = 0;
     bool prep_timed = false, tonal_timed = false, bpm_timed = false, adj_timed = false, call_timed = false;
-    int tile_W = 0, tile_SE = 0, tile_ips = 0, tile_opw = 0;
+    int tile_W = 0, tile_SE = 0, tile_ips = 0, tile_opw = 0, tile_tm = 0;
     acum::TonalTile last_tile;
     bool have_tonal_plan = false;
 

@@ -115,4 +115,83 @@ __device__ __forceinline__ float rsqrt_ftz(float x)
 }
 __device__ __forceinline__ float2 rcp2(float2 a) { return make_float2(rcp_ftz(a.x), rcp_ftz(a.y)); }
 
+// ---------------------------------------------------------------- tensor memory (TMEM)
+// 128 lanes x 512 columns of 32 bits per SM.  A warp reads the 32-lane quarter (warp id
+// mod 4) of it; an address is (lane << 16) | column.  Allocation and release are made by
+// one whole warp; copies from shared memory are issued by one thread and complete on an
+// mbarrier through tcgen05.commit.
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst_smem)),
+                 "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish()
+{
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tmem_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tmem_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// shared-memory writes of this thread (generic proxy) visible to the tensor copies
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Descriptor of a matrix in shared memory without swizzling: 8-row x 16-byte core
+// matrices, rows 16 bytes apart inside one; `lbo` / `sbo` the byte distances between core
+// matrices along the two dimensions; bits 46-48 hold the fixed value 0b001.
+__device__ __forceinline__ uint64_t smem_desc_plain(const void* p, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((smem_u32(p) & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// 32 rows x 128 bits from shared memory into all four lane quarters (columns taddr ..
+// taddr + 3 of lanes 0-31, 32-63, 64-95, 96-127)
+__device__ __forceinline__ void tmem_cp_32x128b_warpx4(uint32_t taddr, uint64_t desc)
+{
+    asm volatile("tcgen05.cp.cta_group::1.32x128b.warpx4 [%0], %1;" ::"r"(taddr), "l"(desc) : "memory");
+}
+// arrive (once) on `bar` when the tensor copies issued so far by this thread are done
+__device__ __forceinline__ void tmem_commit(uint64_t* bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+// 32 consecutive columns of the warp's 32 lanes: lane l gets columns c .. c + 31 of its row
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[40])
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                   "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                   "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+                   "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                 : "r"(taddr));
+}
+// the next 8 columns into r[32..39]
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[40])
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]),
+                   "=r"(r[39])
+                 : "r"(taddr));
+}
+// waits for this thread's tensor loads; the registers are tied to it so that no use is
+// moved above the wait
+__device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[40])
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                   "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]),
+                   "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]),
+                   "+r"(r[29]), "+r"(r[30]), "+r"(r[31]), "+r"(r[32]), "+r"(r[33]), "+r"(r[34]), "+r"(r[35]),
+                   "+r"(r[36]), "+r"(r[37]), "+r"(r[38]), "+r"(r[39])
+                 :
+                 : "memory");
+}
+
 }  // namespace acum

@@ -768,10 +768,23 @@ template <int SE, int OPW>
 struct __align__(16) MixedShared {
     SmpF carry[16 / OPW][2][OPW][SE];  // per warp and observer: left neighbour of lane 0, by window parity
     SmpF first[16 / OPW][OPW][SE];     // per warp and observer: first sample of each element (periodic wrap)
+    uint64_t tfull[kMaxStages];        // tensor-memory form: a slot's copy into tensor memory is complete
     int abort;
     int release[kMaxStages];
     int last[kMaxStages];
+    int claim[kMaxStages];  // tensor-memory form: warps that reached the slot's stage (the first copies)
+    int copied[kMaxStages];  // tensor-memory form: stage of the slot's last copy, -1 = none
+    uint32_t tmem;           // tensor-memory form: base address of the block's columns
 };
+
+// Tensor-memory form: stage slot s, element pair jp of the stage, occupies the 40 columns
+// from tm_col(s, jp) (10 blocks of 4: group q, half h at 4 (2q + h)).
+template <int SE>
+__device__ __forceinline__ uint32_t tm_col(int s, int jp)
+{
+    return (uint32_t)((s * (SE / 2) + jp) * 40);
+}
+constexpr uint32_t kTmemCols = 512;  // NS x SE / 2 x 40 <= 320 for every stage shape
 
 // One work item of the mixed form: observers [ot*W, ot*W + W) and elements [e0, e1)
 // (a multiple of SE) of the deck `p`; each warp evaluates OPW observers on the records it
@@ -781,7 +794,7 @@ struct __align__(16) MixedShared {
 // the block has consumed before this item, so consecutive items of a block continue the
 // mbarrier phases of the same ring.  On entry every slot is free and all bin rows are
 // zero; on return (without abort) the same holds again.
-template <int SE, int OPW>
+template <int SE, int OPW, bool TM>
 __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot, int e0, int e1, unsigned char* smem,
                                            size_t stage_off, MixedShared<SE, OPW>& sh, unsigned& gbase)
 {
@@ -836,7 +849,30 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
     int s = (int)(g0 % (unsigned)NS), w = 0, g = 0, since_flush = 0;
     uint32_t par = (g0 / (unsigned)NS) & 1u;
     for (int i = 0; i < N; ++i) {
-        const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&bars[s], par));
+        bool ok;
+        if (TM) {
+            // the first warp to reach the stage copies it from shared into tensor memory,
+            // once its bulk copies have landed; every warp then waits for that copy
+            int c = 0;
+            if (lane == 0) c = atomicAdd(&sh.claim[s], 1);
+            c = __shfl_sync(0xffffffffu, c, 0);
+            if (c == 0 && lane == 0) {
+                if (mbar_wait_bounded(&bars[s], par)) {
+                    tmem_fence_after();
+                    const float* st = stages + (size_t)s * SE * kTile;
+                    for (int jp = 0; jp < SE / 2; ++jp)
+                        for (int b = 0; b < 2 * kGroups; ++b)
+                            tmem_cp_32x128b_warpx4(sh.tmem + tm_col<SE>(s, jp) + 4u * b,
+                                                   smem_desc_plain(st + (size_t)(2 * jp) * kTile + b * kWin * 4, 128, 128));
+                    tmem_commit(&sh.tfull[s]);
+                    sh.copied[s] = (int)(g0 + (unsigned)i);
+                }
+            }
+            ok = __all_sync(0xffffffffu, mbar_wait_bounded(&sh.tfull[s], par));
+            tmem_fence_after();
+        } else {
+            ok = __all_sync(0xffffffffu, mbar_wait_bounded(&bars[s], par));
+        }
         if (!ok) {
             if (lane == 0) {
                 sh.abort = 1;
@@ -851,10 +887,25 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
         SmpF cur[OPW][SE];
 #pragma unroll
         for (int jp = 0; jp < SE / 2; ++jp) {
-            const float* tl = st + (size_t)(2 * jp) * kTile + lane * 4;
             G2 gg[kGroups];
+            if (TM) {
+                uint32_t r[40];
+                const uint32_t ta = sh.tmem + ((uint32_t)(32 * (warp & 3)) << 16) + tm_col<SE>(s, jp);
+                tmem_ld32(ta, r);
+                tmem_ld8(ta + 32u, r);
+                tmem_wait_ld(r);
 #pragma unroll
-            for (int q = 0; q < kGroups; ++q) gg[q] = load_g2(tl + q * 2 * kWin * 4);
+                for (int q = 0; q < kGroups; ++q) {
+                    gg[q].x = make_float2(__uint_as_float(r[8 * q]), __uint_as_float(r[8 * q + 1]));
+                    gg[q].y = make_float2(__uint_as_float(r[8 * q + 2]), __uint_as_float(r[8 * q + 3]));
+                    gg[q].z = make_float2(__uint_as_float(r[8 * q + 4]), __uint_as_float(r[8 * q + 5]));
+                    gg[q].w = make_float2(__uint_as_float(r[8 * q + 6]), __uint_as_float(r[8 * q + 7]));
+                }
+            } else {
+                const float* tl = st + (size_t)(2 * jp) * kTile + lane * 4;
+#pragma unroll
+                for (int q = 0; q < kGroups; ++q) gg[q] = load_g2(tl + q * 2 * kWin * 4);
+            }
 #pragma unroll
             for (int q = 0; q < OPW; ++q)
                 sample_mixed2(gg, ox[q], oy[q], oz[q], anc[q], p, tau, cur[q][2 * jp], cur[q][2 * jp + 1]);
@@ -907,11 +958,13 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
             since_flush = 0;
         }
         // release the slot; the last warp to finish with it refills it with stage i + NS
+        if (TM) tmem_fence_before();
         __syncwarp();
         if (lane == 0) {
             __threadfence_block();
             if (atomicAdd(&sh.release[s], 1) == nwarps - 1) {
                 sh.release[s] = 0;
+                if (TM) atomicExch(&sh.claim[s], 0);
                 if (i + NS < N) issue(i + NS);
             }
         }
@@ -944,8 +997,11 @@ __device__ __forceinline__ void mixed_init(unsigned char* smem, size_t stage_off
     if (threadIdx.x == 0) {
         for (int s = 0; s < NS; ++s) {
             mbar_init(&bars[s], 1);
+            mbar_init(&sh.tfull[s], 1);
             sh.release[s] = 0;
             sh.last[s] = -1;
+            sh.claim[s] = 0;
+            sh.copied[s] = -1;
         }
         mbar_fence_init();
         sh.abort = 0;
@@ -960,8 +1016,11 @@ __device__ __forceinline__ void mixed_drain(unsigned char* smem, size_t stage_of
     constexpr int kTile = kGroups * kWin * 4;
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + stage_off + (size_t)NS * SE * kTile * sizeof(float));
     if (threadIdx.x == 0)
-        for (int k = 0; k < NS; ++k)
+        for (int k = 0; k < NS; ++k) {
             if (sh.last[k] >= 0) (void)mbar_wait_bounded(&bars[k], (uint32_t)(((unsigned)sh.last[k] / NS) & 1u));
+            if (sh.copied[k] >= 0)
+                (void)mbar_wait_bounded(&sh.tfull[k], (uint32_t)(((unsigned)sh.copied[k] / NS) & 1u));
+        }
     __syncthreads();
 }
 
@@ -970,14 +1029,20 @@ __device__ __forceinline__ void mixed_drain(unsigned char* smem, size_t stage_of
 // memory.  The blocks running at any time therefore share one or two chunks of records
 // in L2 (each record is read from HBM about once per group), and the FP64 sums they add
 // into belong to one group of tiles.
-template <int SE, int OPW>
+template <int SE, int OPW, bool TM>
 __global__ void __launch_bounds__(512 / OPW, 1) tonal_mixed_kernel(const KParams p)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ MixedShared<SE, OPW> sh;
     __shared__ int s_item;
     const size_t stage_off = acc_region_bytes(p.W, p.T + 2, 8);
+    if (TM && threadIdx.x < 32) {  // one block per SM: the allocation does not wait
+        tmem_alloc(&sh.tmem, kTmemCols);
+        tmem_relinquish();
+        tmem_fence_before();
+    }
     mixed_init<SE, OPW>(smem, stage_off, p.NS, sh);
+    if (TM) tmem_fence_after();
     unsigned gbase = 0;
     const int nitems = p.obs_tiles * p.nchunk;
     const int G = p.tile_group, per_group = G * p.nchunk;
@@ -994,12 +1059,17 @@ __global__ void __launch_bounds__(512 / OPW, 1) tonal_mixed_kernel(const KParams
         const int ec = r / gn, ot = g * G + (r - ec * gn);
         const int e0 = ec * p.chunk;
         const int e1 = min(e0 + p.chunk, p.Epad);
-        mixed_item<SE, OPW>(p, ot, e0, e1, smem, stage_off, sh, gbase);
+        mixed_item<SE, OPW, TM>(p, ot, e0, e1, smem, stage_off, sh, gbase);
         __syncthreads();
         if (sh.abort) {
             mixed_drain<SE, OPW>(smem, stage_off, p.NS, sh);
             break;
         }
+    }
+    if (TM) {
+        tmem_fence_before();
+        __syncthreads();
+        if (threadIdx.x < 32) tmem_dealloc(sh.tmem, kTmemCols);
     }
     if (threadIdx.x == 0) {
         __threadfence();
@@ -1037,7 +1107,7 @@ __global__ void __launch_bounds__(512, 1)
         for (int k = threadIdx.x; k < kWords; k += blockDim.x)
             reinterpret_cast<int*>(&sp)[k] = reinterpret_cast<const int*>(cases + it.c)[k];
         __syncthreads();
-        mixed_item<SE, 1>(sp, it.ot, it.e0, it.e1, smem, stage_off, sh, gbase);
+        mixed_item<SE, 1, false>(sp, it.ot, it.e0, it.e1, smem, stage_off, sh, gbase);
         __syncthreads();
         if (sh.abort) {
             mixed_drain<SE, 1>(smem, stage_off, NS, sh);
@@ -1048,6 +1118,7 @@ __global__ void __launch_bounds__(512, 1)
 
 constexpr int kMixedSE = 8;   // samples in flight per lane of the mixed kernel (SE x OPW)
 constexpr int kMixedOPW = 1;  // observers per warp of the mixed kernel
+constexpr bool kMixedTmem = false;  // record stages read from tensor memory by default
 static_assert(kMaxStages >= 4, "stage bookkeeping");
 static_assert(sizeof(SmpF) == 16, "sample record");
 constexpr int kSE64 = 2;
@@ -1065,22 +1136,27 @@ static size_t static_smem_of(K kernel, size_t estimate)
     return a.sharedSizeBytes;
 }
 
-static size_t mixed_static_smem(int SE, int opw)
+static size_t mixed_static_smem(int SE, int opw, bool tm)
 {
-    static size_t v[3][9] = {};
+    static size_t v[2][3][9] = {};
     if (SE != 2 && SE != 4 && SE != 8) SE = 8;
     if (opw != 2) opw = 1;
-    size_t& x = v[opw][SE];
+    if (opw == 2) tm = false;
+    size_t& x = v[tm ? 1 : 0][opw][SE];
     if (!x) {
-        const size_t est = (size_t)16 * 3 * SE * sizeof(SmpF) + 256;
+        const size_t est = (size_t)16 * 3 * SE * sizeof(SmpF) + 512;
         if (opw == 2)
-            x = SE == 2   ? static_smem_of(tonal_mixed_kernel<2, 2>, est)
-                : SE == 4 ? static_smem_of(tonal_mixed_kernel<4, 2>, est)
-                          : static_smem_of(tonal_mixed_kernel<8, 2>, est);
+            x = SE == 2   ? static_smem_of(tonal_mixed_kernel<2, 2, false>, est)
+                : SE == 4 ? static_smem_of(tonal_mixed_kernel<4, 2, false>, est)
+                          : static_smem_of(tonal_mixed_kernel<8, 2, false>, est);
+        else if (tm)
+            x = SE == 2   ? static_smem_of(tonal_mixed_kernel<2, 1, true>, est)
+                : SE == 4 ? static_smem_of(tonal_mixed_kernel<4, 1, true>, est)
+                          : static_smem_of(tonal_mixed_kernel<8, 1, true>, est);
         else
-            x = SE == 2   ? static_smem_of(tonal_mixed_kernel<2, 1>, est)
-                : SE == 4 ? static_smem_of(tonal_mixed_kernel<4, 1>, est)
-                          : static_smem_of(tonal_mixed_kernel<8, 1>, est);
+            x = SE == 2   ? static_smem_of(tonal_mixed_kernel<2, 1, false>, est)
+                : SE == 4 ? static_smem_of(tonal_mixed_kernel<4, 1, false>, est)
+                          : static_smem_of(tonal_mixed_kernel<8, 1, false>, est);
     }
     return x;
 }
@@ -1105,7 +1181,7 @@ static size_t tonal_smem(int W, int T, int NS, int SE, int real_bytes)
 }
 
 cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int num_sms, size_t smem_optin,
-                       int opw_req)
+                       int opw_req, int tm_req)
 {
     const bool f64 = r.precision == ACUM_PLAIN_FP64;
     const int rb = f64 ? 8 : 4;
@@ -1126,7 +1202,10 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
     int W = W_req > 0 ? W_req : 16;
     W = std::min(W, 16);
     // keep room in the per-block limit for the kernels' static shared memory
-    const size_t budget = smem_optin - (f64 ? 1024 : mixed_static_smem(SE, opw));
+    // tensor-memory record stages: mixed form with one observer per warp only
+    const bool tm = !f64 && opw == 1 && (tm_req == 1 || (tm_req == 0 && kMixedTmem));
+    r.t.tm = tm;
+    const size_t budget = smem_optin - (f64 ? 1024 : mixed_static_smem(SE, opw, tm));
     while (W > opw && tonal_smem(W, T, NSmin, SE, rb) > budget) W -= opw;
     if (tonal_smem(W, T, NSmin, SE, rb) > budget) return cudaErrorInvalidValue;
     if (W_req <= 0) {
@@ -1143,15 +1222,22 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
         const int resident = std::max(1, std::min(per_sm_at(NSmin), 65536 / (128 * 32 * (W / opw))));
         while (NS < kMaxStages && tonal_smem(W, T, NS + 1, SE, rb) <= budget && per_sm_at(NS + 1) >= resident) ++NS;
     }
+    // tensor-memory form: the ring's stages fit in the block's kTmemCols columns, and one
+    // block per SM holds them all
+    if (tm) NS = std::max(1, std::min(NS, (int)kTmemCols / (20 * SE)));
     TonalTile& t = r.t;
     t.flush_elems = 1 << 30;
     t.W = W;
     t.SE = SE;
     t.NS = NS;
     t.smem = tonal_smem(W, T, NS, SE, rb);
+    // more than half of the shared memory keeps a second block off the SM (a second
+    // allocation of the tensor-memory columns would wait for the first block to end)
+    if (tm) t.smem = std::max(t.smem, std::min(budget, smem_optin / 2 + 1024));
     const int obs_tiles = (r.g.O + W - 1) / W;
     // resident blocks per SM: shared memory, and registers (~128 per thread)
-    const int per_sm = std::max(1, std::min((int)((228 * 1024) / (t.smem + 1024)), 65536 / (128 * 32 * (W / opw))));
+    const int per_sm =
+        tm ? 1 : std::max(1, std::min((int)((228 * 1024) / (t.smem + 1024)), 65536 / (128 * 32 * (W / opw))));
     const int slots = num_sms * per_sm;
     const int groups = r.g.Epad / SE;
     if (!f64) {
@@ -1219,17 +1305,17 @@ static cudaError_t launch_f64_t(const KParams& kp, int items, int threads, size_
     return cudaGetLastError();
 }
 
-template <int SE, int OPW>
+template <int SE, int OPW, bool TM>
 static cudaError_t launch_mixed_t(const KParams& kp, int grid, int threads, size_t smem, cudaStream_t s)
 {
     static size_t configured = 0;
     if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(tonal_mixed_kernel<SE, OPW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(tonal_mixed_kernel<SE, OPW, TM>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
-    tonal_mixed_kernel<SE, OPW><<<grid, threads, smem, s>>>(kp);
+    tonal_mixed_kernel<SE, OPW, TM><<<grid, threads, smem, s>>>(kp);
     return cudaGetLastError();
 }
 
@@ -1291,13 +1377,18 @@ cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s)
     if (r.precision == ACUM_PLAIN_FP64) return launch_f64_t<kSE64>(kp, r.t.items, 32 * r.t.W, r.t.smem, s);
     const int threads = 32 * (r.t.W / r.t.opw);
     if (r.t.opw == 2) {
-        if (r.t.SE == 2) return launch_mixed_t<2, 2>(kp, r.t.grid, threads, r.t.smem, s);
-        if (r.t.SE == 4) return launch_mixed_t<4, 2>(kp, r.t.grid, threads, r.t.smem, s);
-        return launch_mixed_t<8, 2>(kp, r.t.grid, threads, r.t.smem, s);
+        if (r.t.SE == 2) return launch_mixed_t<2, 2, false>(kp, r.t.grid, threads, r.t.smem, s);
+        if (r.t.SE == 4) return launch_mixed_t<4, 2, false>(kp, r.t.grid, threads, r.t.smem, s);
+        return launch_mixed_t<8, 2, false>(kp, r.t.grid, threads, r.t.smem, s);
     }
-    if (r.t.SE == 2) return launch_mixed_t<2, 1>(kp, r.t.grid, threads, r.t.smem, s);
-    if (r.t.SE == 8) return launch_mixed_t<8, 1>(kp, r.t.grid, threads, r.t.smem, s);
-    return launch_mixed_t<4, 1>(kp, r.t.grid, threads, r.t.smem, s);
+    if (r.t.tm) {
+        if (r.t.SE == 2) return launch_mixed_t<2, 1, true>(kp, r.t.grid, threads, r.t.smem, s);
+        if (r.t.SE == 8) return launch_mixed_t<8, 1, true>(kp, r.t.grid, threads, r.t.smem, s);
+        return launch_mixed_t<4, 1, true>(kp, r.t.grid, threads, r.t.smem, s);
+    }
+    if (r.t.SE == 2) return launch_mixed_t<2, 1, false>(kp, r.t.grid, threads, r.t.smem, s);
+    if (r.t.SE == 8) return launch_mixed_t<8, 1, false>(kp, r.t.grid, threads, r.t.smem, s);
+    return launch_mixed_t<4, 1, false>(kp, r.t.grid, threads, r.t.smem, s);
 }
 
 size_t batch_smem(int W, int SE, int Tmax)

@@ -73,6 +73,7 @@ SIGNATURES = {
     "acum_sync": (C.c_int, [C.c_void_p]),
     "acum_tonal_from_host_async": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "acum_selftest_wait": (C.c_int, [C.c_int, C.c_double, C.c_int, _IP, _DP]),
+    "acum_selftest_tmem": (C.c_int, [C.c_int, _IP, C.c_void_p]),
     "acum_read_deck_sizes": (C.c_int, [C.c_char_p, C.POINTER(C.c_longlong)]),
     "acum_write_surface_cache": (C.c_int, [C.c_char_p]),
     "acum_last_plan": (C.c_int, [C.c_void_p, _IP]),
@@ -84,6 +85,7 @@ SIGNATURES = {
     "acum_last_timing": (C.c_int, [C.c_void_p, C.c_int, _DP, C.POINTER(C.c_longlong)]),
     "acum_set_tile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "acum_set_obs_per_warp": (C.c_int, [C.c_void_p, C.c_int]),
+    "acum_set_tensor_memory": (C.c_int, [C.c_void_p, C.c_int]),
     "acum_measure_peak": (C.c_int, [C.c_int, C.c_int, _DP]),
     "acum_host_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t]),
     "acum_host_free": (C.c_int, [C.c_void_p]),
@@ -296,15 +298,16 @@ class Context:
     def write_outputs(self, path: str):
         self._ck(self.L.acum_write_outputs(self.h, os.fsencode(path)))
 
-    def set_tile(self, obs_per_block=0, elems_per_stage=0, items_per_sm=0, obs_per_warp=0):
+    def set_tile(self, obs_per_block=0, elems_per_stage=0, items_per_sm=0, obs_per_warp=0, tensor_memory=0):
         self._ck(self.L.acum_set_tile(self.h, obs_per_block, elems_per_stage, items_per_sm))
         self._ck(self.L.acum_set_obs_per_warp(self.h, obs_per_warp))
+        self._ck(self.L.acum_set_tensor_memory(self.h, tensor_memory))
 
     def last_plan(self) -> dict:
-        v = (C.c_int * 7)()
+        v = (C.c_int * 8)()
         self._ck(self.L.acum_last_plan(self.h, v))
         keys = ("obs_per_block", "elems_per_stage", "stages", "elems_per_item", "element_chunks", "work_items",
-                "obs_per_warp")
+                "obs_per_warp", "tensor_memory")
         return dict(zip(keys, (int(x) for x in v)))
 
     def timing(self, which: int):
@@ -417,6 +420,16 @@ def selftest_wait(device: int, limit_s: float, arrive: bool):
     if rc != 0:
         raise AcumError(rc, "acum_selftest_wait failed")
     return bool(to.value), ws.value
+
+
+def selftest_tmem(device: int = 0):
+    """(mismatching words, readback [4][32][40]) of the tensor-memory copy self-test."""
+    mis = C.c_int()
+    rb = np.zeros((4, 32, 40), np.uint32)
+    rc = lib().acum_selftest_tmem(device, C.byref(mis), rb.ctypes.data_as(C.c_void_p))
+    if rc != 0:
+        raise AcumError(rc, "acum_selftest_tmem failed")
+    return mis.value, rb
 
 
 class PinnedBuffer:

@@ -188,9 +188,14 @@ int acum_set_tile(acum_ctx* ctx, int obs_per_block, int elems_per_stage, int ite
 /* Observers evaluated per warp of the mixed tonal kernel on the records it loads once:
  * 1 or 2 (0 = let the library choose). */
 int acum_set_obs_per_warp(acum_ctx* ctx, int obs_per_warp);
-/* The plan of the last tonal run (out holds 7 ints): out[0] observers per block,
+/* Record stages of the mixed tonal kernel (one observer per warp) copied once into tensor
+ * memory and read from there by every warp, instead of read by every warp from shared
+ * memory: 1 = yes, 2 = no, 0 = let the library choose. */
+int acum_set_tensor_memory(acum_ctx* ctx, int use);
+/* The plan of the last tonal run (out holds 8 ints): out[0] observers per block,
  * [1] elements per stage, [2] pipeline stages, [3] elements per work item, [4] element
- * chunks, [5] work items, [6] observers per warp. */
+ * chunks, [5] work items, [6] observers per warp, [7] 1 if the record stages were read
+ * from tensor memory. */
 int acum_last_plan(const acum_ctx* ctx, int* out);
 
 /* Self-test of the bounded wait that every pipelined kernel uses on its barriers: one
@@ -199,6 +204,12 @@ int acum_last_plan(const acum_ctx* ctx, int* out);
  * the device time it waited.  The kernels themselves give up after 2 s, record
  * ACUM_DEVERR_TIMEOUT and return; the context stays usable. */
 int acum_selftest_wait(int device, double limit_s, int arrive, int* timed_out, double* waited_s);
+/* Self-test of the tensor-memory path of the record stages: a known pattern laid out as
+ * one element-pair tile is copied from shared memory into tensor memory and read back by
+ * every warp of a block.  *mismatches = words that differ (0 = pass; -1 = the copy did not
+ * complete within the bounded wait); readback (optional, 4 x 32 x 40 words) = what warps
+ * 0-3 read, lane by lane. */
+int acum_selftest_tmem(int device, int* mismatches, unsigned* readback);
 
 /* Measured FMA throughput of `device` in TFLOP/s: which = 0 FP32, 1 FP64 (a short
  * FMA-chain kernel timed with CUDA events; the CUDA-core peaks of the roofline). */

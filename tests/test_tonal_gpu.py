@@ -170,24 +170,27 @@ def test_timing_and_launch_count(ctx):
     assert ms > 0 and launches >= 3
 
 
-@pytest.mark.parametrize("W,SE,opw", [(16, 8, 1), (16, 4, 1), (16, 2, 1), (7, 8, 1),
-                                      (16, 2, 2), (16, 4, 2), (16, 8, 2), (6, 4, 2)])
-def test_mixed_tile_shapes_against_oracle(ctx, W, SE, opw):
+@pytest.mark.parametrize("W,SE,opw,tm", [(16, 8, 1, 2), (16, 4, 1, 2), (16, 2, 1, 2), (7, 8, 1, 2),
+                                         (16, 2, 2, 2), (16, 4, 2, 2), (16, 8, 2, 2), (6, 4, 2, 2),
+                                         (16, 8, 1, 1), (16, 4, 1, 1), (16, 2, 1, 1), (5, 8, 1, 1)])
+def test_mixed_tile_shapes_against_oracle(ctx, W, SE, opw, tm):
     """Every tile shape of the mixed kernel (observers per block, elements per stage,
-    observers per warp) on a deck whose observers, steps and elements are not multiples
-    of the tile; the plan reports the shape that ran."""
+    observers per warp, record stages in shared or tensor memory) on a deck whose
+    observers, steps and elements are not multiples of the tile; the plan reports the
+    shape that ran."""
     from acum3_periodic_gb300 import native
     d = synth.config_deck(0, replicate=34, scale=dict(n_span=7, n_chord_side=5, ntime=75, nobs=29))
     oT, oL, oA, bad = O.tonal(d)
     assert bad == 0
     ctx.set_deck(d, bb=False)
     try:
-        ctx.set_tile(W, SE, 0, opw)
+        ctx.set_tile(W, SE, 0, opw, tm)
         _, _, mA = ctx.tonal(native.MIXED)
         plan = ctx.last_plan()
     finally:
         ctx.set_tile()
     assert (plan["obs_per_block"], plan["elems_per_stage"], plan["obs_per_warp"]) == (W, SE, opw)
+    assert plan["tensor_memory"] == (1 if tm == 1 else 0)
     assert per_bin_rms(mA, oA).max() < MIXED_RMS_TOL
     assert np.abs(oaspl_db(mA) - oaspl_db(oA)).max() < OASPL_TOL_DB
     assert ctx.error_word(reset=True) == 0
