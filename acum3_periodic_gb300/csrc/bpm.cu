@@ -520,12 +520,13 @@ __global__ void bb_spec_kernel(const float* __restrict__ sc, const double* __res
 // Observer contraction.  Block = 64 observers (lane l serves observers l and l + 32) x
 // 21 warps, one per pair of bands.  Per tile of kTI (section, step) items, the amplitudes
 // of all 42 bands (contiguous in `amp`, 1344 B per item, band pairs interleaved) and the
-// items' geometry records arrive in shared memory by one bulk copy into a double buffer
-// (the next tile's copy runs while this one is consumed); the directivity factors D of the
-// block's observers for the tile are computed once into shared memory (each stored twice,
-// as the operand pair of a packed instruction); then each lane adds, for its two
-// observers and its warp's two bands, the clipped energies of every item in packed FP32
-// (one f32x2 operation covers both bands).  The amplitude reads are warp-uniform (shared-
+// items' geometry records arrive in shared memory by one bulk copy into a ring of three
+// buffers (two tiles ahead of the one consumed); the directivity factors D of the block's
+// observers are computed into shared memory one tile ahead (double-buffered, each stored
+// twice, as the operand pair of a packed instruction), in the same phase as the current
+// tile's sums, so that one block barrier per tile separates the phases; each lane adds,
+// for its two observers and its warp's two bands, the clipped energies of every item in
+// packed FP32 (one f32x2 operation covers both bands).  The amplitude reads are warp-uniform (shared-
 // memory broadcasts), the D reads conflict-free.  FP32 partial sums over at most 1024
 // items are folded into FP64 sums private to the block's (observer tile, item range):
 // part[split][band][component][observer], reduced over the splits by bb_final_kernel.
@@ -540,13 +541,16 @@ constexpr int kGeoItemBytes = kGeo * 4;           // 64
 static_assert(kBands % 2 == 0, "band pairs");
 static_assert(kAmpItemBytes % 16 == 0 && kGeoItemBytes % 16 == 0, "bulk copy granularity");
 
-// dynamic shared memory of bb_obs_kernel: 2 x (amplitude tile + geometry tile), the D
-// tile (float4 (Dh, Dh, Dl, Dl) per item and observer), the block's observers, 2 mbarriers
+// dynamic shared memory of bb_obs_kernel: kObsRing x (amplitude tile + geometry tile), 2 D
+// tiles (float4 (Dh, Dh, Dl, Dl) per item and observer), the block's observers, kObsRing
+// mbarriers
+constexpr int kObsRing = 3;
 constexpr size_t kObsSmemA = (size_t)kTI * kAmpItemBytes;
 constexpr size_t kObsSmemG = (size_t)kTI * kGeoItemBytes;
 constexpr size_t kObsSmemBuf = kObsSmemA + kObsSmemG;
 constexpr size_t kObsSmemD = (size_t)kTI * kObsBlock * sizeof(float4);
-constexpr size_t kObsSmem = 2 * kObsSmemBuf + kObsSmemD + kObsBlock * 3 * sizeof(float) + 2 * sizeof(uint64_t);
+constexpr size_t kObsSmem =
+    kObsRing * kObsSmemBuf + 2 * kObsSmemD + kObsBlock * 3 * sizeof(float) + kObsRing * sizeof(uint64_t);
 
 __device__ __forceinline__ float2 bb_directivity(const float* geo, const float* obs, int o, float vx, float vy,
                                                  float vz, float aa, float iaMv)
@@ -591,9 +595,10 @@ __global__ void __launch_bounds__(kBpmThreads, 1) bb_obs_kernel(const float* __r
                                                                 DeviceErr* err)
 {
     extern __shared__ __align__(128) unsigned char sm[];
-    float4* sD = reinterpret_cast<float4*>(sm + 2 * kObsSmemBuf);  // [kTI][kObsBlock]
-    float* sObs = reinterpret_cast<float*>(sm + 2 * kObsSmemBuf + kObsSmemD);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + 2 * kObsSmemBuf + kObsSmemD + kObsBlock * 3 * sizeof(float));
+    float4* sD0 = reinterpret_cast<float4*>(sm + kObsRing * kObsSmemBuf);  // 2 x [kTI][kObsBlock]
+    float* sObs = reinterpret_cast<float*>(sm + kObsRing * kObsSmemBuf + 2 * kObsSmemD);
+    uint64_t* bars =
+        reinterpret_cast<uint64_t*>(sm + kObsRing * kObsSmemBuf + 2 * kObsSmemD + kObsBlock * 3 * sizeof(float));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;  // warp = band pair
     const int o0 = blockIdx.x * kObsBlock;
     const long long st_begin = (long long)blockIdx.y * per_split;
@@ -609,22 +614,41 @@ __global__ void __launch_bounds__(kBpmThreads, 1) bb_obs_kernel(const float* __r
         sObs[i] = o < O ? obs[3 * o0 + i] : 0.f;
     }
     if (threadIdx.x == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        for (int b = 0; b < kObsRing; ++b) mbar_init(&bars[b], 1);
         mbar_fence_init();
     }
     __syncthreads();
-    // tile j -> buffer j & 1: amplitudes then geometry of its items
+    // tile j -> buffer j % kObsRing (phase j / kObsRing of its barrier): amplitudes, then
+    // the geometry of its items
+    auto tile_n = [&](int j) { return (int)min((long long)kTI, st_end - (st_begin + (long long)j * kTI)); };
+    auto buf_of = [&](int j) { return sm + (size_t)(j % kObsRing) * kObsSmemBuf; };
     auto issue = [&](int j) {
         const long long t0 = st_begin + (long long)j * kTI;
-        const int n = (int)min((long long)kTI, st_end - t0);
-        unsigned char* buf = sm + (size_t)(j & 1) * kObsSmemBuf;
-        mbar_expect_tx(&bars[j & 1], (uint32_t)(n * (kAmpItemBytes + kGeoItemBytes)));
-        bulk_g2s(buf, amp + t0 * kBands * kAmp, (uint32_t)(n * kAmpItemBytes), &bars[j & 1]);
-        bulk_g2s(buf + kObsSmemA, geo + t0 * kGeo, (uint32_t)(n * kGeoItemBytes), &bars[j & 1]);
+        const int n = tile_n(j);
+        unsigned char* buf = buf_of(j);
+        mbar_expect_tx(&bars[j % kObsRing], (uint32_t)(n * (kAmpItemBytes + kGeoItemBytes)));
+        bulk_g2s(buf, amp + t0 * kBands * kAmp, (uint32_t)(n * kAmpItemBytes), &bars[j % kObsRing]);
+        bulk_g2s(buf + kObsSmemA, geo + t0 * kGeo, (uint32_t)(n * kGeoItemBytes), &bars[j % kObsRing]);
     };
+    auto wait_tile = [&](int j) {
+        return mbar_wait_bounded(&bars[j % kObsRing], (uint32_t)((j / kObsRing) & 1));
+    };
+    // D of every (item, observer) of tile j (bb_core.cu:515-530, 620-624) into D buffer j & 1
+    auto directivity = [&](int j) {
+        const int n = tile_n(j);
+        const float* sG = reinterpret_cast<const float*>(buf_of(j) + kObsSmemA);
+        float4* sD = sD0 + (size_t)(j & 1) * kTI * kObsBlock;
+#pragma unroll 1
+        for (int pidx = threadIdx.x; pidx < kTI * kObsBlock; pidx += blockDim.x) {
+            const int it = pidx / kObsBlock, ol = pidx % kObsBlock;
+            float2 D = make_float2(0.f, 0.f);
+            if (it < n && o0 + ol < O) D = bb_directivity(sG + it * kGeo, sObs, ol, vx, vy, vz, aa, iaMv);
+            sD[it * kObsBlock + ol] = make_float4(D.x, D.x, D.y, D.y);
+        }
+    };
+    int issued = 0;
     if (threadIdx.x == 0)
-        for (int j = 0; j < 2 && j < ntiles; ++j) issue(j);
+        for (; issued < kObsRing && issued < ntiles; ++issued) issue(issued);
 
     float2 acc[kObsPerLane][6];  // (band 2 warp, band 2 warp + 1)
 #pragma unroll
@@ -652,28 +676,22 @@ __global__ void __launch_bounds__(kBpmThreads, 1) bb_obs_kernel(const float* __r
         }
     };
     int aborted_at = -1;
+    if (ntiles > 0) {
+        const bool ok = wait_tile(0);
+        if (ok) directivity(0);
+        if (__syncthreads_or(!ok)) aborted_at = 0;
+    }
     int tiles = 0;
-    for (int j = 0; j < ntiles; ++j) {
-        const long long t0 = st_begin + (long long)j * kTI;
-        const int n = (int)min((long long)kTI, st_end - t0);
-        const unsigned char* buf = sm + (size_t)(j & 1) * kObsSmemBuf;
-        const bool ok = mbar_wait_bounded(&bars[j & 1], (uint32_t)((j >> 1) & 1));
-        if (__syncthreads_or(!ok)) {
-            if (threadIdx.x == 0) flag(err, ACUM_DEVERR_TIMEOUT, &err->timeout);
-            aborted_at = j;
-            break;
+    for (int j = 0; j < ntiles && aborted_at < 0; ++j) {
+        // the next tile's D, in the same phase as this tile's sums
+        bool ok = true;
+        if (j + 1 < ntiles) {
+            ok = wait_tile(j + 1);
+            if (ok) directivity(j + 1);
         }
-        const float4* sA = reinterpret_cast<const float4*>(buf);
-        const float* sG = reinterpret_cast<const float*>(buf + kObsSmemA);
-        // D of every (item, observer) of the tile (bb_core.cu:515-530, 620-624)
-#pragma unroll 1
-        for (int pidx = threadIdx.x; pidx < kTI * kObsBlock; pidx += blockDim.x) {
-            const int it = pidx / kObsBlock, ol = pidx % kObsBlock;
-            float2 D = make_float2(0.f, 0.f);
-            if (it < n && o0 + ol < O) D = bb_directivity(sG + it * kGeo, sObs, ol, vx, vy, vz, aa, iaMv);
-            sD[it * kObsBlock + ol] = make_float4(D.x, D.x, D.y, D.y);
-        }
-        __syncthreads();
+        const int n = tile_n(j);
+        const float4* sA = reinterpret_cast<const float4*>(buf_of(j));
+        const float4* sD = sD0 + (size_t)(j & 1) * kTI * kObsBlock;
 #pragma unroll 1
         for (int it = 0; it < n; ++it) {
             // the warp's band pair: fields (Ap, As), (Aa, Al), (At, Av), (gtip, -) of both bands
@@ -696,20 +714,25 @@ __global__ void __launch_bounds__(kBpmThreads, 1) bb_obs_kernel(const float* __r
                 if (tip) acc[q][5] = fma2(Av, clip2(mul2(Dh, Ag), 2.2204460492503131e-16f), acc[q][5]);  // tip
             }
         }
-        // every thread is done with this buffer and the D tile: refill with tile j + 2
-        __syncthreads();
-        if (threadIdx.x == 0 && j + 2 < ntiles) issue(j + 2);
+        // every thread is done with tile j's buffer and D tile, and tile j + 1's D is
+        // complete: refill the buffer with tile j + kObsRing
+        if (__syncthreads_or(!ok)) {
+            aborted_at = j + 1;
+            break;
+        }
+        if (threadIdx.x == 0 && j + kObsRing < ntiles) issue(issued++);
         if (++tiles == kFoldTiles) {
             fold();
             tiles = 0;
         }
     }
     if (aborted_at >= 0) {
-        // wait (bounded) for the copies still in flight (tiles j and j + 1) before the
-        // block exits
-        if (threadIdx.x == 0)
-            for (int j = aborted_at; j < ntiles && j < aborted_at + 2; ++j)
-                (void)mbar_wait_bounded(&bars[j & 1], (uint32_t)((j >> 1) & 1));
+        // wait (bounded) for the copies still in flight (tiles aborted_at .. issued - 1,
+        // counted by thread 0, which issues them) before the block exits
+        if (threadIdx.x == 0) {
+            flag(err, ACUM_DEVERR_TIMEOUT, &err->timeout);
+            for (int j = aborted_at; j < issued; ++j) (void)wait_tile(j);
+        }
         __syncthreads();
         return;
     }
