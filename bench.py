@@ -39,10 +39,10 @@ sys.path.insert(0, ROOT)
 METRIC = "elem·obs·step evals/s: mixed vs FP64 at ≤0.05 dB OASPL; adjoint/fwd ratio"
 ALG_FLOPS_PER_EVAL = 102  # FP ops per tonal evaluation (integrand + observer time + deposits)
 # DRAM bytes (read + write) of one workload-2 launch of the mixed kernel, measured with ncu
-# (one pass: dram__bytes_read.sum + dram__bytes_write.sum: 14.39 GB + 10.37 GB); the FP64
+# (one pass: dram__bytes_read.sum + dram__bytes_write.sum: 14.72 GB + 10.39 GB); the FP64
 # flushes of the FP32 bin rows and the reads they cause, the 3.69 GB of records being read
 # a few times at most
-TONAL_TRAFFIC_BYTES = 24.76e9
+TONAL_TRAFFIC_BYTES = 25.11e9
 WORKLOAD = "workload 2: 4-blade rotor, 32000 elements, 1440 steps/rev, 4096 observers, tonal mixed precision"
 
 
