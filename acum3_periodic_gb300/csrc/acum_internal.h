@@ -154,18 +154,8 @@ constexpr int batch_stages(int SE) { return SE == 8 ? 2 : 4; }
 size_t batch_smem(int W, int SE, int Tmax);
 int batch_blocks_per_sm(int W, int SE, int Tmax);
 size_t batch_static_smem(int SE);  // static shared memory to keep beside batch_smem
-// The constants of up to kParamCases cases passed by value to the batched kernel (kernel
-// parameters, read through the constant cache like the single-deck kernel's) instead of
-// copied per item from global into shared memory.
-constexpr int kParamCases = 112;
-struct BatchConsts {
-    KParams cases[kParamCases];
-};
-static_assert(sizeof(BatchConsts) + 128 <= 32764, "kernel parameter space");
-// h_cases: the same constants on the host (NULL, or more than kParamCases cases: shared-
-// memory copies from d_cases)
-cudaError_t launch_tonal_batch(const KParams* d_cases, const KParams* h_cases, int ncases, const BatchItem* d_items,
-                               int nitems, int* d_counter, int W, int SE, int Tmax, int grid, cudaStream_t s);
+cudaError_t launch_tonal_batch(const KParams* d_cases, const BatchItem* d_items, int nitems, int* d_counter, int W,
+                               int SE, int Tmax, int grid, cudaStream_t s);
 // acc [O][T][2] of every case -> pA [T][O] (overwrite)
 struct FinCase {
     const double* acc;

@@ -39,7 +39,6 @@ struct acum_batch {
     int fin_tiles = 0;
     DBuf<double> d_acc, d_out;
     DBuf<KParams> d_kp;
-    std::vector<KParams> h_kp;  // the same constants on the host (kernel parameters of the launch)
     DBuf<BatchItem> d_items;
     DBuf<FinCase> d_fin;
     DBuf<int> d_counter;
@@ -206,7 +205,6 @@ int plan(acum_batch* b)
     BK(b, b->d_fin.ensure(n));
     BK(b, b->d_items.ensure(b->items.size()));
     BK(b, cudaMemcpy(b->d_kp.p, kp.data(), n * sizeof(KParams), cudaMemcpyHostToDevice));
-    b->h_kp = kp;
     BK(b, cudaMemcpy(b->d_fin.p, fin.data(), n * sizeof(FinCase), cudaMemcpyHostToDevice));
     BK(b, cudaMemcpy(b->d_items.p, b->items.data(), b->items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice));
     b->drop_graph();
@@ -219,8 +217,8 @@ int enqueue_persistent(acum_batch* b, const BatchItem* d_items, int nitems, bool
 {
     BK(b, cudaMemsetAsync(b->d_counter.p, 0, sizeof(int), b->stream));
     BK(b, cudaMemsetAsync(b->d_acc.p, 0, b->acc_doubles * 8, b->stream));
-    BK(b, launch_tonal_batch(b->d_kp.p, b->h_kp.data(), (int)b->h_kp.size(), d_items, nitems, b->d_counter.p, b->W,
-                             b->SE, b->Tmax, b->num_sms, b->stream));
+    BK(b, launch_tonal_batch(b->d_kp.p, d_items, nitems, b->d_counter.p, b->W, b->SE, b->Tmax, b->num_sms,
+                             b->stream));
     if (finalize) BK(b, launch_finalize_batch(b->d_fin.p, (int)b->cases.size(), b->fin_tiles, b->stream));
     return ACUM_OK;
 }

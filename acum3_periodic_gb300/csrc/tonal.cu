@@ -33,7 +33,6 @@
 #include <stdint.h>
 
 #include <algorithm>
-#include <type_traits>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -1085,14 +1084,10 @@ __global__ void __launch_bounds__(512 / OPW, 1) tonal_mixed_kernel(const KParams
 // (largest first, as the host sorts them) until none are left.  Item k is (case,
 // observer tile, first element, end element); the case's constants are copied into
 // shared memory at the start of each item.
-struct NoConsts {
-};
-
-template <int SE, bool PARAM>
+template <int SE>
 __global__ void __launch_bounds__(512, 1)
-    tonal_batch_kernel(const KParams* __restrict__ cases,
-                       const __grid_constant__ typename std::conditional<PARAM, BatchConsts, NoConsts>::type bc,
-                       const BatchItem* __restrict__ items, int nitems, int* counter, int NS, size_t stage_off)
+    tonal_batch_kernel(const KParams* __restrict__ cases, const BatchItem* __restrict__ items, int nitems,
+                       int* counter, int NS, size_t stage_off)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ MixedShared<SE, 1> sh;
@@ -1108,15 +1103,11 @@ __global__ void __launch_bounds__(512, 1)
         __syncthreads();
         const BatchItem it = s_it;
         if (it.c < 0) break;
-        if constexpr (PARAM) {
-            mixed_item<SE, 1, false>(bc.cases[it.c], it.ot, it.e0, it.e1, smem, stage_off, sh, gbase);
-        } else {
-            constexpr int kWords = (int)(sizeof(KParams) / sizeof(int));
-            for (int k = threadIdx.x; k < kWords; k += blockDim.x)
-                reinterpret_cast<int*>(&sp)[k] = reinterpret_cast<const int*>(cases + it.c)[k];
-            __syncthreads();
-            mixed_item<SE, 1, false>(sp, it.ot, it.e0, it.e1, smem, stage_off, sh, gbase);
-        }
+        constexpr int kWords = (int)(sizeof(KParams) / sizeof(int));
+        for (int k = threadIdx.x; k < kWords; k += blockDim.x)
+            reinterpret_cast<int*>(&sp)[k] = reinterpret_cast<const int*>(cases + it.c)[k];
+        __syncthreads();
+        mixed_item<SE, 1, false>(sp, it.ot, it.e0, it.e1, smem, stage_off, sh, gbase);
         __syncthreads();
         if (sh.abort) {
             mixed_drain<SE, 1>(smem, stage_off, NS, sh);
@@ -1176,9 +1167,8 @@ size_t batch_static_smem(int SE)
     if (SE != 2 && SE != 4 && SE != 8) SE = 8;
     if (!v[SE]) {
         const size_t est = (size_t)16 * 3 * SE * sizeof(SmpF) + 768;
-        v[SE] = SE == 2   ? static_smem_of(tonal_batch_kernel<2, false>, est)
-                : SE == 4 ? static_smem_of(tonal_batch_kernel<4, false>, est)
-                          : static_smem_of(tonal_batch_kernel<8, false>, est);
+        v[SE] = SE == 2 ? static_smem_of(tonal_batch_kernel<2>, est)
+                        : SE == 4 ? static_smem_of(tonal_batch_kernel<4>, est) : static_smem_of(tonal_batch_kernel<8>, est);
     }
     return v[SE];
 }
@@ -1408,33 +1398,25 @@ size_t batch_smem(int W, int SE, int Tmax)
            (size_t)NS * 8;
 }
 
-template <int SE, bool PARAM>
-static cudaError_t launch_batch_t(const KParams* d_cases, const KParams* h_cases, int ncases,
-                                  const BatchItem* d_items, int nitems, int* d_counter, int W, int Tmax, int grid,
-                                  cudaStream_t s)
+template <int SE>
+static cudaError_t launch_batch_t(const KParams* d_cases, const BatchItem* d_items, int nitems, int* d_counter, int W,
+                                  int Tmax, int grid, cudaStream_t s)
 {
     static size_t configured = 0;
     const size_t smem = batch_smem(W, SE, Tmax);
     if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(tonal_batch_kernel<SE, PARAM>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(tonal_batch_kernel<SE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
     // as many resident blocks per SM as shared memory and registers allow
     int per_sm = 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<SE, PARAM>, 32 * W, smem) !=
-            cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<SE>, 32 * W, smem) != cudaSuccess ||
         per_sm < 1)
         per_sm = 1;
-    typename std::conditional<PARAM, BatchConsts, NoConsts>::type bc;
-    if constexpr (PARAM) {
-        memset(&bc, 0, sizeof(bc));
-        memcpy(bc.cases, h_cases, (size_t)ncases * sizeof(KParams));
-    }
-    tonal_batch_kernel<SE, PARAM><<<grid * per_sm, 32 * W, smem, s>>>(d_cases, bc, d_items, nitems, d_counter,
-                                                                      batch_stages(SE),
-                                                                      acc_region_bytes(W, Tmax + 2, 8));
+    tonal_batch_kernel<SE><<<grid * per_sm, 32 * W, smem, s>>>(d_cases, d_items, nitems, d_counter, batch_stages(SE),
+                                                               acc_region_bytes(W, Tmax + 2, 8));
     return cudaGetLastError();
 }
 
@@ -1442,27 +1424,20 @@ int batch_blocks_per_sm(int W, int SE, int Tmax)
 {
     int per_sm = 1;
     const size_t smem = batch_smem(W, SE, Tmax);
-    cudaError_t e =
-        SE == 2   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<2, false>, 32 * W, smem)
-        : SE == 8 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<8, false>, 32 * W, smem)
-                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<4, false>, 32 * W, smem);
+    cudaError_t e = SE == 2   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<2>, 32 * W, smem)
+                    : SE == 8 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<8>, 32 * W, smem)
+                              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<4>, 32 * W, smem);
     return (e == cudaSuccess && per_sm > 0) ? per_sm : 1;
 }
 
-// grid = SMs; the launch puts as many blocks on each SM as fit.  Up to kParamCases cases
-// with host constants go as kernel parameters, more from global memory per item.
-cudaError_t launch_tonal_batch(const KParams* d_cases, const KParams* h_cases, int ncases, const BatchItem* d_items,
-                               int nitems, int* d_counter, int W, int SE, int Tmax, int grid, cudaStream_t s)
+// grid = SMs; the launch puts as many blocks on each SM as fit
+cudaError_t launch_tonal_batch(const KParams* d_cases, const BatchItem* d_items, int nitems, int* d_counter, int W,
+                               int SE, int Tmax, int grid, cudaStream_t s)
 {
-    if (W < 1 || W > 16 || grid < 1 || ncases < 1) return cudaErrorInvalidValue;
-    const bool param = h_cases && ncases <= kParamCases;
-#define ACUM_BATCH_LAUNCH(se)                                                                                       \
-    return param ? launch_batch_t<se, true>(d_cases, h_cases, ncases, d_items, nitems, d_counter, W, Tmax, grid, s) \
-                 : launch_batch_t<se, false>(d_cases, h_cases, ncases, d_items, nitems, d_counter, W, Tmax, grid, s)
-    if (SE == 2) ACUM_BATCH_LAUNCH(2);
-    if (SE == 4) ACUM_BATCH_LAUNCH(4);
-    if (SE == 8) ACUM_BATCH_LAUNCH(8);
-#undef ACUM_BATCH_LAUNCH
+    if (W < 1 || W > 16 || grid < 1) return cudaErrorInvalidValue;
+    if (SE == 2) return launch_batch_t<2>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s);
+    if (SE == 4) return launch_batch_t<4>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s);
+    if (SE == 8) return launch_batch_t<8>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s);
     return cudaErrorInvalidValue;
 }
 
