@@ -120,17 +120,18 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
             __syncthreads();
         }
     }
-    const double two_dt = 2.0 * a.dTau;
-    const double D1 = 1.0 / (4.0 * M_PI * a.a0);
+    // central differences multiply by 1 / (2 dTau) (one rounding from the quotient)
+    const double two_dt = 2.0 * a.dTau, i2dt = 1.0 / two_dt;
+    const double D1 = 1.0 / (4.0 * M_PI * a.a0), ia0 = 1.0 / a.a0;
     for (int t = threadIdx.x; t < T; t += blockDim.x) {
         const int tm = t == 0 ? T - 1 : t - 1, tp = t == T - 1 ? 0 : t + 1;
         const int tmm = tm == 0 ? T - 1 : tm - 1, tpp = tp == T - 1 ? 0 : tp + 1;
         double Pd;
         if (a.periodic == 1) {
-            Pd = (P[tp] - P[tm]) / two_dt;
+            Pd = (P[tp] - P[tm]) * i2dt;
         } else {
             // central interior, ends by cubic extrapolation (mathfunc.cu:142-159)
-            auto cd = [&](int k) { return (P[k + 1] - P[k - 1]) / two_dt; };
+            auto cd = [&](int k) { return (P[k + 1] - P[k - 1]) * i2dt; };
             if (t == 0) Pd = 3 * cd(1) - 3 * cd(2) + cd(3);
             else if (t == T - 1) Pd = 3 * cd(T - 2) - 3 * cd(T - 3) + cd(T - 4);
             else Pd = cd(t);
@@ -144,12 +145,12 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
         for (int c = 0; c < 3; ++c) {
             x[c] = (double)r0[c] * a.cfd;
             n[c] = (double)r0[5 + c];
-            nd[c] = ((double)rp[5 + c] - (double)rm[5 + c]) / two_dt;
+            nd[c] = ((double)rp[5 + c] - (double)rm[5 + c]) * i2dt;
             double xp = (double)rp[c] * a.cfd, xm = (double)rm[c] * a.cfd;
             double xpp = (double)rpp[c] * a.cfd, xmm = (double)rmm[c] * a.cfd;
-            v[c] = (xp - xm) / two_dt;
-            double vp = (xpp - x[c]) / two_dt, vm = (x[c] - xmm) / two_dt;
-            vd[c] = (vp - vm) / two_dt;
+            v[c] = (xp - xm) * i2dt;
+            double vp = (xpp - x[c]) * i2dt, vm = (x[c] - xmm) * i2dt;
+            vd[c] = (vp - vm) * i2dt;
         }
         const double ds = (double)r0[4] * a.cfd * a.cfd;
         const double Pt = P[t];
@@ -163,7 +164,6 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
             f[16] = Pt; f[17] = Pd;
         }
         // records
-        const double ia0 = 1.0 / a.a0;
         double rec[20];
         rec[0] = x[0]; rec[1] = x[1]; rec[2] = x[2]; rec[3] = D1 * ds;
         rec[4] = v[0] * ia0; rec[5] = v[1] * ia0; rec[6] = v[2] * ia0;
