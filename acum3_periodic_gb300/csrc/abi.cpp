@@ -397,13 +397,25 @@ int acum_ctx::ensure_prep(bool need64, bool need32, bool need_fields)
     a.periodic = in.periodic;
     a.lowpass = in.lowpass;
     gauss_taps(a.gauss);
-    a.rec64 = do64 ? d_rec64.p : nullptr;
-    a.rec32 = do32 ? d_rec32.p : nullptr;
-    a.fields = need_fields ? d_fields.p : nullptr;
+    // the FP32 records always come from the FP32 preprocessing (the same records whatever
+    // else was asked for before); the FP64 records and the fields from the FP64 one
     CK(this, cudaEventRecord(ev[EV_PREP0], stream));
-    CK(this, launch_prep(a, stream));
+    if (do32) {
+        PrepArgs a32 = a;
+        a32.rec64 = nullptr;
+        a32.fields = nullptr;
+        a32.rec32 = d_rec32.p;
+        CK(this, launch_prep(a32, stream));
+        launches += 1;
+    }
+    if (do64 || need_fields) {
+        a.rec64 = do64 ? d_rec64.p : nullptr;
+        a.rec32 = nullptr;
+        a.fields = need_fields ? d_fields.p : nullptr;
+        CK(this, launch_prep(a, stream));
+        launches += 1;
+    }
     CK(this, cudaEventRecord(ev[EV_PREP1], stream));
-    launches += 1;
     prep_timed = true;
     if (do64) rec64_ok = true;
     if (do32) rec32_ok = true;

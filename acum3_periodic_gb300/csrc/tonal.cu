@@ -33,6 +33,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -54,13 +55,16 @@ struct dbl4 {
 
 // One block per element.  Shared memory: the element's rows [T][8] as float, then two
 // double series (P and a ping-pong buffer for the filters).
+// R = double: the FP64 records, the fields and the FP32 records rounded from FP64; R =
+// float: the FP32 records alone, computed in FP32 (the mixed form's preprocessing).
+template <typename R>
 __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
 {
     extern __shared__ __align__(16) unsigned char sm[];
     const int T = a.T;
     float* rows = reinterpret_cast<float*>(sm);                  // [T][8]
-    double* P = reinterpret_cast<double*>(sm + (size_t)T * 32);  // [T]
-    double* Q = P + T;                                           // [T]
+    R* P = reinterpret_cast<R*>(sm + (size_t)T * 32);  // [T]
+    R* Q = P + T;                                      // [T]
     const int e = blockIdx.x;
     const int s = a.e_surf[e];
     const int j = a.e_local[e];
@@ -75,21 +79,21 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
     }
     __syncthreads();
     // scaled pressure (preprocess.cu:279)
-    for (int t = threadIdx.x; t < T; t += blockDim.x) P[t] = (double)rows[t * 8 + 3] * a.pscale;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) P[t] = (R)rows[t * 8 + 3] * (R)a.pscale;
     __syncthreads();
     // make_periodic (mathfunc.cu:165-206): cubic through the end mismatch
     {
-        double p0 = P[0], p1 = P[1], pm = P[T - 2], pn = P[T - 1];
-        const double g0 = p0 - (p1 - p0);  // linear extrapolation before the first sample
-        double k2 = pn, k1 = g0, s2 = pn - pm, s1 = p0 - g0;
-        int xm = T;
-        double dd = k1, cc = s1 - s2;
-        double bb = -2.0 * (s1 - s2) / xm - 3.0 * (k1 - k2) / xm / xm;
-        double aa = -bb / xm - (s1 - s2) / xm / xm - (k1 - k2) / xm / xm / xm;
+        R p0 = P[0], p1 = P[1], pm = P[T - 2], pn = P[T - 1];
+        const R g0 = p0 - (p1 - p0);  // linear extrapolation before the first sample
+        R k2 = pn, k1 = g0, s2 = pn - pm, s1 = p0 - g0;
+        const R xm = (R)T;
+        R dd = k1, cc = s1 - s2;
+        R bb = (R)-2.0 * (s1 - s2) / xm - (R)3.0 * (k1 - k2) / xm / xm;
+        R aa = -bb / xm - (s1 - s2) / xm / xm - (k1 - k2) / xm / xm / xm;
         __syncthreads();
         for (int t = threadIdx.x; t < T; t += blockDim.x) {
-            int i = t + 1;
-            double cub = aa * i * i * i + bb * i * i + cc * i + dd;
+            const R i = (R)(t + 1);
+            R cub = aa * i * i * i + bb * i * i + cc * i + dd;
             P[t] = P[t] - (cub - k2);
         }
         __syncthreads();
@@ -99,21 +103,21 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
         // (preprocess.cu:323-333, mathfunc.cu:208-341 and 375-421)
         for (int pass = 0; pass < 2; ++pass) {
             for (int t = threadIdx.x; t < T; t += blockDim.x) {
-                double l = P[t == 0 ? T - 1 : t - 1], m = P[t], r = P[t == T - 1 ? 0 : t + 1];
-                double hi = l > m ? l : m;
+                R l = P[t == 0 ? T - 1 : t - 1], m = P[t], r = P[t == T - 1 ? 0 : t + 1];
+                R hi = l > m ? l : m;
                 hi = hi > r ? hi : r;
-                double lo = l < m ? l : m;
+                R lo = l < m ? l : m;
                 lo = lo < r ? lo : r;
                 Q[t] = (l < hi && l > lo) ? l : ((m < hi && m > lo) ? m : r);
             }
             __syncthreads();
             for (int t = threadIdx.x; t < T; t += blockDim.x) {
-                double acc = 0.0;
+                R acc = 0;
                 for (int k = 0; k < 13; ++k) {
                     int q = t + k - 6;
                     if (q < 0) q += T;
                     else if (q > T - 1) q -= T;
-                    acc += a.gauss[k] * Q[q];
+                    acc += (R)a.gauss[k] * Q[q];
                 }
                 P[t] = acc;
             }
@@ -121,12 +125,13 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
         }
     }
     // central differences multiply by 1 / (2 dTau) (one rounding from the quotient)
-    const double two_dt = 2.0 * a.dTau, i2dt = 1.0 / two_dt;
-    const double D1 = 1.0 / (4.0 * M_PI * a.a0), ia0 = 1.0 / a.a0;
+    const R two_dt = (R)(2.0 * a.dTau), i2dt = (R)(1.0 / (2.0 * a.dTau));
+    const R D1 = (R)(1.0 / (4.0 * M_PI * a.a0)), ia0 = (R)(1.0 / a.a0), cfd = (R)a.cfd;
+    (void)two_dt;
     for (int t = threadIdx.x; t < T; t += blockDim.x) {
         const int tm = t == 0 ? T - 1 : t - 1, tp = t == T - 1 ? 0 : t + 1;
         const int tmm = tm == 0 ? T - 1 : tm - 1, tpp = tp == T - 1 ? 0 : tp + 1;
-        double Pd;
+        R Pd;
         if (a.periodic == 1) {
             Pd = (P[tp] - P[tm]) * i2dt;
         } else {
@@ -141,20 +146,20 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
         const float* rp = rows + (size_t)tp * 8;
         const float* rmm = rows + (size_t)tmm * 8;
         const float* rpp = rows + (size_t)tpp * 8;
-        double x[3], n[3], nd[3], v[3], vd[3];
+        R x[3], n[3], nd[3], v[3], vd[3];
         for (int c = 0; c < 3; ++c) {
-            x[c] = (double)r0[c] * a.cfd;
-            n[c] = (double)r0[5 + c];
-            nd[c] = ((double)rp[5 + c] - (double)rm[5 + c]) * i2dt;
-            double xp = (double)rp[c] * a.cfd, xm = (double)rm[c] * a.cfd;
-            double xpp = (double)rpp[c] * a.cfd, xmm = (double)rmm[c] * a.cfd;
+            x[c] = (R)r0[c] * cfd;
+            n[c] = (R)r0[5 + c];
+            nd[c] = ((R)rp[5 + c] - (R)rm[5 + c]) * i2dt;
+            R xp = (R)rp[c] * cfd, xm = (R)rm[c] * cfd;
+            R xpp = (R)rpp[c] * cfd, xmm = (R)rmm[c] * cfd;
             v[c] = (xp - xm) * i2dt;
-            double vp = (xpp - x[c]) * i2dt, vm = (x[c] - xmm) * i2dt;
+            R vp = (xpp - x[c]) * i2dt, vm = (x[c] - xmm) * i2dt;
             vd[c] = (vp - vm) * i2dt;
         }
-        const double ds = (double)r0[4] * a.cfd * a.cfd;
-        const double Pt = P[t];
-        if (a.fields) {
+        const R ds = (R)r0[4] * cfd * cfd;
+        const R Pt = P[t];
+        if (std::is_same<R, double>::value && a.fields) {
             double* f = a.fields + ((size_t)e * T + t) * kFields;
             f[0] = x[0]; f[1] = x[1]; f[2] = x[2]; f[3] = ds;
             f[4] = n[0]; f[5] = n[1]; f[6] = n[2];
@@ -164,13 +169,13 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
             f[16] = Pt; f[17] = Pd;
         }
         // records
-        double rec[20];
+        R rec[20];
         rec[0] = x[0]; rec[1] = x[1]; rec[2] = x[2]; rec[3] = D1 * ds;
         rec[4] = v[0] * ia0; rec[5] = v[1] * ia0; rec[6] = v[2] * ia0;
         rec[7] = (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) * ia0 * ia0;
         rec[8] = vd[0] * ia0; rec[9] = vd[1] * ia0; rec[10] = vd[2] * ia0;
-        rec[11] = D1 * a.rho * (v[0] * n[0] + v[1] * n[1] + v[2] * n[2]) * a.a0 * ds;
-        double L[3], Ld[3];
+        rec[11] = D1 * (R)a.rho * (v[0] * n[0] + v[1] * n[1] + v[2] * n[2]) * (R)a.a0 * ds;
+        R L[3], Ld[3];
         for (int c = 0; c < 3; ++c) {
             L[c] = Pt * n[c];
             Ld[c] = Pd * n[c] + Pt * nd[c];
@@ -178,15 +183,15 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
         rec[12] = L[0]; rec[13] = L[1]; rec[14] = L[2];
         rec[15] = (L[0] * v[0] + L[1] * v[1] + L[2] * v[2]) * ia0;
         rec[16] = Ld[0]; rec[17] = Ld[1]; rec[18] = Ld[2];
-        rec[19] = x[0] * a.vinf[0] + x[1] * a.vinf[1] + x[2] * a.vinf[2];
+        rec[19] = x[0] * (R)a.vinf[0] + x[1] * (R)a.vinf[1] + x[2] * (R)a.vinf[2];
         const int w = t / kWin, lane = t % kWin;
         const size_t tile = ((size_t)e * a.nW + w) * (kGroups * kWin * 4);
         for (int q = 0; q < kGroups; ++q) {
             const size_t off = tile + ((size_t)q * kWin + lane) * 4;
-            if (a.rec64) {
+            if (std::is_same<R, double>::value && a.rec64) {
                 double2* d = reinterpret_cast<double2*>(a.rec64 + off);
-                d[0] = make_double2(rec[4 * q], rec[4 * q + 1]);
-                d[1] = make_double2(rec[4 * q + 2], rec[4 * q + 3]);
+                d[0] = make_double2((double)rec[4 * q], (double)rec[4 * q + 1]);
+                d[1] = make_double2((double)rec[4 * q + 2], (double)rec[4 * q + 3]);
             }
         }
         if (a.rec32) {
@@ -197,17 +202,25 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
     }
 }
 
-cudaError_t launch_prep(const PrepArgs& a, cudaStream_t s)
+template <typename R>
+static cudaError_t launch_prep_t(const PrepArgs& a, cudaStream_t s)
 {
-    size_t smem = (size_t)a.T * 32 + (size_t)a.T * 16;
+    const size_t smem = (size_t)a.T * 32 + (size_t)a.T * 2 * sizeof(R);
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {
-        cudaError_t err = cudaFuncSetAttribute(prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t err = cudaFuncSetAttribute(prep_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (err != cudaSuccess) return err;
         configured = smem;
     }
-    prep_kernel<<<a.E, 256, smem, s>>>(a);
+    prep_kernel<R><<<a.E, 256, smem, s>>>(a);
     return cudaGetLastError();
+}
+
+// FP64 when the FP64 records or the fields are asked for, else FP32 (the FP32 records of
+// the mixed form alone)
+cudaError_t launch_prep(const PrepArgs& a, cudaStream_t s)
+{
+    return (a.rec64 || a.fields) ? launch_prep_t<double>(a, s) : launch_prep_t<float>(a, s);
 }
 
 // records from the reference's AoS arrays; one thread per (element, step)
