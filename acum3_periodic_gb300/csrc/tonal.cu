@@ -55,16 +55,20 @@ struct dbl4 {
 
 // One block per element.  Shared memory: the element's rows [T][8] as float, then two
 // double series (P and a ping-pong buffer for the filters).
-// R = double: the FP64 records, the fields and the FP32 records rounded from FP64; R =
-// float: the FP32 records alone, computed in FP32 (the mixed form's preprocessing).
+// R = double: the FP64 records and the fields; R = float: the FP32 records (the mixed
+// form's preprocessing) with the geometry in FP32.  The pressure path (scaling,
+// make_periodic, low-pass, time derivative) is FP64 in both: its central difference of
+// nearby values loses ~1e-4 of the derivative in FP32.  The FP32 second difference of
+// the positions uses error-free differences (each difference's rounding error carried),
+// so that it is exact to one rounding.
 template <typename R>
 __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
 {
     extern __shared__ __align__(16) unsigned char sm[];
     const int T = a.T;
     float* rows = reinterpret_cast<float*>(sm);                  // [T][8]
-    R* P = reinterpret_cast<R*>(sm + (size_t)T * 32);  // [T]
-    R* Q = P + T;                                      // [T]
+    double* P = reinterpret_cast<double*>(sm + (size_t)T * 32);  // [T]
+    double* Q = P + T;                                           // [T]
     const int e = blockIdx.x;
     const int s = a.e_surf[e];
     const int j = a.e_local[e];
@@ -79,21 +83,21 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
     }
     __syncthreads();
     // scaled pressure (preprocess.cu:279)
-    for (int t = threadIdx.x; t < T; t += blockDim.x) P[t] = (R)rows[t * 8 + 3] * (R)a.pscale;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) P[t] = (double)rows[t * 8 + 3] * a.pscale;
     __syncthreads();
     // make_periodic (mathfunc.cu:165-206): cubic through the end mismatch
     {
-        R p0 = P[0], p1 = P[1], pm = P[T - 2], pn = P[T - 1];
-        const R g0 = p0 - (p1 - p0);  // linear extrapolation before the first sample
-        R k2 = pn, k1 = g0, s2 = pn - pm, s1 = p0 - g0;
-        const R xm = (R)T;
-        R dd = k1, cc = s1 - s2;
-        R bb = (R)-2.0 * (s1 - s2) / xm - (R)3.0 * (k1 - k2) / xm / xm;
-        R aa = -bb / xm - (s1 - s2) / xm / xm - (k1 - k2) / xm / xm / xm;
+        double p0 = P[0], p1 = P[1], pm = P[T - 2], pn = P[T - 1];
+        const double g0 = p0 - (p1 - p0);  // linear extrapolation before the first sample
+        double k2 = pn, k1 = g0, s2 = pn - pm, s1 = p0 - g0;
+        int xm = T;
+        double dd = k1, cc = s1 - s2;
+        double bb = -2.0 * (s1 - s2) / xm - 3.0 * (k1 - k2) / xm / xm;
+        double aa = -bb / xm - (s1 - s2) / xm / xm - (k1 - k2) / xm / xm / xm;
         __syncthreads();
         for (int t = threadIdx.x; t < T; t += blockDim.x) {
-            const R i = (R)(t + 1);
-            R cub = aa * i * i * i + bb * i * i + cc * i + dd;
+            int i = t + 1;
+            double cub = aa * i * i * i + bb * i * i + cc * i + dd;
             P[t] = P[t] - (cub - k2);
         }
         __syncthreads();
@@ -103,21 +107,21 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
         // (preprocess.cu:323-333, mathfunc.cu:208-341 and 375-421)
         for (int pass = 0; pass < 2; ++pass) {
             for (int t = threadIdx.x; t < T; t += blockDim.x) {
-                R l = P[t == 0 ? T - 1 : t - 1], m = P[t], r = P[t == T - 1 ? 0 : t + 1];
-                R hi = l > m ? l : m;
+                double l = P[t == 0 ? T - 1 : t - 1], m = P[t], r = P[t == T - 1 ? 0 : t + 1];
+                double hi = l > m ? l : m;
                 hi = hi > r ? hi : r;
-                R lo = l < m ? l : m;
+                double lo = l < m ? l : m;
                 lo = lo < r ? lo : r;
                 Q[t] = (l < hi && l > lo) ? l : ((m < hi && m > lo) ? m : r);
             }
             __syncthreads();
             for (int t = threadIdx.x; t < T; t += blockDim.x) {
-                R acc = 0;
+                double acc = 0.0;
                 for (int k = 0; k < 13; ++k) {
                     int q = t + k - 6;
                     if (q < 0) q += T;
                     else if (q > T - 1) q -= T;
-                    acc += (R)a.gauss[k] * Q[q];
+                    acc += a.gauss[k] * Q[q];
                 }
                 P[t] = acc;
             }
@@ -125,22 +129,23 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
         }
     }
     // central differences multiply by 1 / (2 dTau) (one rounding from the quotient)
-    const R two_dt = (R)(2.0 * a.dTau), i2dt = (R)(1.0 / (2.0 * a.dTau));
+    const double pi2dt = 1.0 / (2.0 * a.dTau);  // the pressure path's, FP64
+    const R i2dt = (R)pi2dt, i4dt2 = (R)(pi2dt * pi2dt);
     const R D1 = (R)(1.0 / (4.0 * M_PI * a.a0)), ia0 = (R)(1.0 / a.a0), cfd = (R)a.cfd;
-    (void)two_dt;
     for (int t = threadIdx.x; t < T; t += blockDim.x) {
         const int tm = t == 0 ? T - 1 : t - 1, tp = t == T - 1 ? 0 : t + 1;
         const int tmm = tm == 0 ? T - 1 : tm - 1, tpp = tp == T - 1 ? 0 : tp + 1;
-        R Pd;
+        double Pd64;
         if (a.periodic == 1) {
-            Pd = (P[tp] - P[tm]) * i2dt;
+            Pd64 = (P[tp] - P[tm]) * pi2dt;
         } else {
             // central interior, ends by cubic extrapolation (mathfunc.cu:142-159)
-            auto cd = [&](int k) { return (P[k + 1] - P[k - 1]) * i2dt; };
-            if (t == 0) Pd = 3 * cd(1) - 3 * cd(2) + cd(3);
-            else if (t == T - 1) Pd = 3 * cd(T - 2) - 3 * cd(T - 3) + cd(T - 4);
-            else Pd = cd(t);
+            auto cd = [&](int k) { return (P[k + 1] - P[k - 1]) * pi2dt; };
+            if (t == 0) Pd64 = 3 * cd(1) - 3 * cd(2) + cd(3);
+            else if (t == T - 1) Pd64 = 3 * cd(T - 2) - 3 * cd(T - 3) + cd(T - 4);
+            else Pd64 = cd(t);
         }
+        const R Pd = (R)Pd64;
         const float* r0 = rows + (size_t)t * 8;
         const float* rm = rows + (size_t)tm * 8;
         const float* rp = rows + (size_t)tp * 8;
@@ -154,11 +159,18 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
             R xp = (R)rp[c] * cfd, xm = (R)rm[c] * cfd;
             R xpp = (R)rpp[c] * cfd, xmm = (R)rmm[c] * cfd;
             v[c] = (xp - xm) * i2dt;
-            R vp = (xpp - x[c]) * i2dt, vm = (x[c] - xmm) * i2dt;
-            vd[c] = (vp - vm) * i2dt;
+            if constexpr (std::is_same<R, float>::value) {
+                // (xpp - x) - (x - xmm), each difference with its rounding error
+                const float d1 = xpp - x[c], b1 = d1 - xpp, e1 = (xpp - (d1 - b1)) + (-x[c] - b1);
+                const float d2 = x[c] - xmm, b2 = d2 - x[c], e2 = (x[c] - (d2 - b2)) + (-xmm - b2);
+                vd[c] = ((d1 - d2) + (e1 - e2)) * i4dt2;
+            } else {
+                R vp = (xpp - x[c]) * i2dt, vm = (x[c] - xmm) * i2dt;
+                vd[c] = (vp - vm) * i2dt;
+            }
         }
         const R ds = (R)r0[4] * cfd * cfd;
-        const R Pt = P[t];
+        const R Pt = (R)P[t];
         if (std::is_same<R, double>::value && a.fields) {
             double* f = a.fields + ((size_t)e * T + t) * kFields;
             f[0] = x[0]; f[1] = x[1]; f[2] = x[2]; f[3] = ds;
@@ -205,7 +217,7 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
 template <typename R>
 static cudaError_t launch_prep_t(const PrepArgs& a, cudaStream_t s)
 {
-    const size_t smem = (size_t)a.T * 32 + (size_t)a.T * 2 * sizeof(R);
+    const size_t smem = (size_t)a.T * 32 + (size_t)a.T * 2 * sizeof(double);
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {
         cudaError_t err = cudaFuncSetAttribute(prep_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
