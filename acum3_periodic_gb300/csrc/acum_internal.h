@@ -70,7 +70,6 @@ struct TonalTile {
 // preprocessing (tonal.cu)
 struct PrepArgs {
     const float* raw;      // [surf][T][E_i][8] device
-    const int* surf_of;    // not used
     int nsurf;
     const long long* raw_off;  // device: start (floats) of each surface's rows
     const int* e_surf;     // device: surface of each global element
@@ -81,7 +80,6 @@ struct PrepArgs {
     double vinf[3];
     int periodic, lowpass;
     double gauss[13];
-    float* ser;            // scratch [E][8][T] float
     double* rec64;         // [Epad][nW][5][32][4] or null
     float* rec32;          // pair-interleaved FP32 records (rec32_offset) or null
     double* fields;        // optional [E][T][18]
@@ -127,10 +125,8 @@ struct KParams {
     int Epad, T, nW, O;
     const float* obs32;
     const double* obs64;
-    // mixed constants
-    float a0f, alphaf, ialphaf, vxf, vyf, vzf, kbhi, kblo, invTf;
-    // the same as pairs (both halves equal), the operands of the packed FP32 instructions:
-    // -alpha, -vInf, a0, oM / dPsi
+    // mixed constants, as pairs (both halves equal: the operands of the packed FP32
+    // instructions): -alpha, -vInf, a0, oM / dPsi
     float2 nalpha2, nvx2, nvy2, nvz2, a02, kb2;
     unsigned tmod;  // ceil(2^32 / T): bin index modulo T by multiply-high
     int toff;       // a multiple of T >= 2^23, added to bin indices before the modulo

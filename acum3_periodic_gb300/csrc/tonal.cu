@@ -1366,22 +1366,15 @@ void fill_kparams(const TonalRun& r, KParams& kp)
     kp.oM = g.oM;
     kp.dPsi = g.dPsi;
     kp.lpi = g.T * g.dPsi;
-    kp.a0f = (float)g.a0;
-    kp.alphaf = (float)alpha;
-    kp.ialphaf = (float)(1.0 / alpha);
-    kp.vxf = (float)g.vinf[0];
-    kp.vyf = (float)g.vinf[1];
-    kp.vzf = (float)g.vinf[2];
-    const double kb = g.oM / g.dPsi;  // bins per second of retarded time
-    kp.kbhi = (float)kb;
-    kp.kblo = (float)(kb - (double)kp.kbhi);
-    kp.invTf = 1.0f / (float)g.T;
-    kp.nalpha2 = make_float2(-kp.alphaf, -kp.alphaf);
-    kp.nvx2 = make_float2(-kp.vxf, -kp.vxf);
-    kp.nvy2 = make_float2(-kp.vyf, -kp.vyf);
-    kp.nvz2 = make_float2(-kp.vzf, -kp.vzf);
-    kp.a02 = make_float2(kp.a0f, kp.a0f);
-    kp.kb2 = make_float2(kp.kbhi, kp.kbhi);
+    const float a0f = (float)g.a0, alphaf = (float)alpha;
+    const float vxf = (float)g.vinf[0], vyf = (float)g.vinf[1], vzf = (float)g.vinf[2];
+    const float kbf = (float)(g.oM / g.dPsi);  // bins per second of retarded time
+    kp.nalpha2 = make_float2(-alphaf, -alphaf);
+    kp.nvx2 = make_float2(-vxf, -vxf);
+    kp.nvy2 = make_float2(-vyf, -vyf);
+    kp.nvz2 = make_float2(-vzf, -vzf);
+    kp.a02 = make_float2(a0f, a0f);
+    kp.kb2 = make_float2(kbf, kbf);
     kp.tmod = (unsigned)((0x100000000ull + (unsigned long long)g.T - 1) / (unsigned long long)g.T);
     kp.toff = (int)(((1 << 23) + g.T - 1) / g.T * g.T);
     kp.W = r.t.W;
