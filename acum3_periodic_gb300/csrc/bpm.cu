@@ -21,7 +21,8 @@
 //      sections and steps in FP32 partial sums folded into FP64; lane = observer and
 //      warp = band pair, so each amplitude is read once per warp as a shared-memory
 //      broadcast and one packed FP32 instruction covers both bands.
-//  bb_final_kernel   the energy means over steps and the band sum, in FP64 dB
+//  bb_final_kernel   the energy means over steps per (observer, band), in FP64 dB
+//  bb_oaspl_kernel   the band sum (OASPL) per observer
 //      (bb_core.cu:563-583).
 //
 // The reference's repeated dB log-adds become plain energy sums, which removes most of
@@ -743,14 +744,15 @@ __global__ void __launch_bounds__(kBpmThreads, 1) bb_obs_kernel(const float* __r
 // of the clipped energies become the seven levels.  Components of `sums`: TBL pressure,
 // suction, separation, LBL, TEB, tip; of BBspl: total, separation, suction, pressure,
 // LBL, TEB, tip.
+// one thread per (band, observer), observers consecutive (coalesced reads of the sums):
+// the band's seven component levels
 __global__ void bb_final_kernel(const double* __restrict__ part, int nsplit, int O, int T,
-                                const double* __restrict__ seed_spl, const double* __restrict__ seed_oas,
-                                double* __restrict__ spl, double* __restrict__ oaspl)
+                                const double* __restrict__ seed_spl, double* __restrict__ spl)
 {
-    const int o = blockIdx.x * blockDim.x + threadIdx.x;
-    if (o >= O) return;
-    double oas = pow(10.0, seed_oas[o] / 10.0);
-    for (int f = 0; f < kBands; ++f) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)O * kBands) return;
+    const int f = (int)(idx / O), o = (int)(idx % O);
+    {
         double s[6];
         for (int c = 0; c < 6; ++c) {
             double v = 0.0;
@@ -763,8 +765,17 @@ __global__ void bb_final_kernel(const double* __restrict__ part, int nsplit, int
         double* out = spl + ((size_t)o * kBands + f) * 7;
         const double* seed = seed_spl + ((size_t)o * kBands + f) * 7;
         for (int c = 0; c < 7; ++c) out[c] = 10.0 * log10((pow(10.0, seed[c] / 10.0) + floor_t + comp[c]) / (double)T);
-        oas += pow(10.0, out[0] / 10.0);
     }
+}
+
+// one thread per observer: the OASPL, the band totals summed in band order
+__global__ void bb_oaspl_kernel(int O, const double* __restrict__ seed_oas, const double* __restrict__ spl,
+                                double* __restrict__ oaspl)
+{
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= O) return;
+    double oas = pow(10.0, seed_oas[o] / 10.0);
+    for (int f = 0; f < kBands; ++f) oas += pow(10.0, spl[((size_t)o * kBands + f) * 7] / 10.0);
     oaspl[o] = 10.0 * log10(oas);
 }
 
@@ -932,10 +943,11 @@ static int bpm_run(acum_ctx* ctx, int aa_mode, const double* seed_spl_h, const d
     bb_obs_kernel<<<grid, kBpmThreads, kObsSmem, st>>>(s->geo.p, s->amp.p, ctx->d_obs32.p, O, nst, per_split,
                                                        (float)d.vinf[0], (float)d.vinf[1], (float)d.vinf[2],
                                                        (float)d.a0, aa_mode, s->sums.p, ctx->d_err.p);
-    bb_final_kernel<<<(O + 127) / 128, 128, 0, st>>>(s->sums.p, split, O, T, s->seed_spl.p, s->seed_oas.p,
-                                                     s->spl.p, s->oaspl.p);
+    bb_final_kernel<<<(int)(((long long)O * kBands + 127) / 128), 128, 0, st>>>(s->sums.p, split, O, T,
+                                                                              s->seed_spl.p, s->spl.p);
+    bb_oaspl_kernel<<<(O + 127) / 128, 128, 0, st>>>(O, s->seed_oas.p, s->spl.p, s->oaspl.p);
     cudaEventRecord(ctx->ev[EV_BPM1], st);
-    ctx->launches += 5;
+    ctx->launches += 6;
     ctx->bpm_timed = true;
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(ctx, e, "bpm launch");
     ctx->h_spl.resize((size_t)O * kBands * 7);

@@ -76,7 +76,7 @@ def test_bpm_many_observers_and_sections(ctx):
     spl, oas = ctx.bpm(aa_mode=0)
     _check(spl, oas, ospl, ooas)
     ms, launches = ctx.timing(3)
-    assert ms > 0 and launches == 5
+    assert ms > 0 and launches == 6
 
 
 def test_bpm_file_dropin_and_writer(ctx, tmp_path):
