@@ -455,8 +455,8 @@ def main():
         nsec = sum(b.nsect for b in deck.bb)
         bpm_evals = nsec * deck.nObs * deck.nTime * 42
         bsel = np.arange(0, deck.nObs, max(1, deck.nObs // 8))[:8]
-        # gpu_ms: CUDA-event time of the five broadband kernels of one call (positions,
-        # per-(section, step) preparation, spectra, observer contraction, dB sums)
+        # gpu_ms: CUDA-event time of the six broadband kernels of one call (positions,
+        # per-(section, step) preparation, spectra, observer contraction, dB sums, OASPL)
         bpm = {"metric": "section·observer·band evals/s (per source step)", "sections": nsec,
                "evals": bpm_evals, "evals_per_s": bpm_evals / float(np.mean(bt)),
                "gpu_evals_per_s": bpm_evals / (bpm_kernel_ms * 1e-3), "gpu_ms": bpm_kernel_ms,
