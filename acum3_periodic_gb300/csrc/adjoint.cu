@@ -61,8 +61,8 @@ __device__ __forceinline__ float rcp_(float x) { return rcp_ftz(x); }
 __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
 __device__ __forceinline__ float sqrt_(float x) { return x * rsqrt_ftz(x); }
 
-// floor(t / dPsi): the FP64 form divides as the forward does; the FP32 form multiplies
-__device__ __forceinline__ int bin_floor(double t, double dPsi, double) { return (int)floor(t / dPsi); }
+// floor(t / dPsi) as floor(t * (1 / dPsi)), as the forward forms it
+__device__ __forceinline__ int bin_floor(double t, double, double idPsi) { return (int)floor(t * idPsi); }
 __device__ __forceinline__ int bin_floor(float t, float, float idPsi) { return (int)floorf(t * idPsi); }
 
 // n mod T for 0 <= n < 2^24 by multiply-high with m = ceil(2^32 / T)

@@ -298,13 +298,14 @@ struct __align__(16) SmpF {
 };
 
 struct SmpD {
-    int nb;     // floor(t / dPsi)
+    int nb;     // floor(t / dPsi), as floor(t * (1 / dPsi))
     double t;   // observer time [rad]
     double pt, pl;
 };
 
 __device__ __forceinline__ SmpD sample_f64(const dbl4& g0, const dbl4& g1, const dbl4& g2, const dbl4& g3,
-                                           const dbl4& g4, double ox, double oy, double oz, const KParams& p, int tau)
+                                           const dbl4& g4, double ox, double oy, double oz, const KParams& p, int tau,
+                                           double idPsi)
 {
     const double dx = ox - g0.x, dy = oy - g0.y, dz = oz - g0.z;
     const double c = dx * dx + dy * dy + dz * dz;
@@ -325,9 +326,12 @@ __device__ __forceinline__ SmpD sample_f64(const dbl4& g0, const dbl4& g1, const
     SmpD o;
     o.pt = g2.w * base * G * K;
     o.pl = g0.w * base * (Ldr + qa * (Lr - g3.w) + Lr * G * K);
-    // observer time (core.cu:156) and its bin floor
+    // observer time (core.cu:156) and its bin floor.  The product by 1 / dPsi may put a
+    // time within an ulp of a bin on the other side of it; the interpolated value of that
+    // bin is the same to rounding either way (its weight is 0 on one side, 1 on the other,
+    // and both intervals share this sample's bin floor)
     o.t = (tau * p.dTau + tr) * p.oM;
-    o.nb = (int)floor(o.t / p.dPsi);
+    o.nb = (int)floor(o.t * idPsi);
     return o;
 }
 
@@ -488,6 +492,7 @@ __global__ void __launch_bounds__(512, 1) tonal_f64_kernel(const KParams p)
     if (threadIdx.x == 0)
         for (int i = 0; i < NS && i < N; ++i) issue(i);
 
+    const double idPsi = 1.0 / p.dPsi;
     double ox = 0, oy = 0, oz = 0;
     if (obs_ok) {
         ox = p.obs64[3 * o];
@@ -525,7 +530,7 @@ __global__ void __launch_bounds__(512, 1) tonal_f64_kernel(const KParams p)
                     double2 u0 = pp[0], u1 = pp[1];
                     gg[q] = dbl4{u0.x, u0.y, u1.x, u1.y};
                 }
-                cur[j] = sample_f64(gg[0], gg[1], gg[2], gg[3], gg[4], ox, oy, oz, p, tau);
+                cur[j] = sample_f64(gg[0], gg[1], gg[2], gg[3], gg[4], ox, oy, oz, p, tau, idPsi);
             }
             const int last = min(31, T - 1 - w * kWin);
             const bool has_prev = valid && (lane > 0 || w > 0);
@@ -540,7 +545,7 @@ __global__ void __launch_bounds__(512, 1) tonal_f64_kernel(const KParams p)
                     // the periodic wrap: (t(T-1), t(0) + period] (core.cu:173-194)
                     SmpD f0 = first[j];
                     const double tw = f0.t + p.lpi;
-                    const int nw = (int)floor(tw / p.dPsi);
+                    const int nw = (int)floor(tw * idPsi);
                     deposit_f64(acc, T, p, carry[j], f0, p.lpi, nw - f0.nb, p.err);
                 }
             }
