@@ -29,7 +29,7 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-Wall", "-Wno-unused-function", "-I" + os.path.join(CUDA_HOME, "include"),
              "-I" + os.path.join(ROOT, "include"), "-pthread"]
 
-CU_SOURCES = ["tonal.cu", "bpm.cu", "adjoint.cu", "probe.cu", "noalloc.cu"]
+CU_SOURCES = ["tonal.cu", "bpm.cu", "adjoint.cu", "probe.cu", "noalloc.cu", "permeable.cu"]
 CPP_SOURCES = ["abi.cpp", "io.cpp", "batch.cpp"]
 
 

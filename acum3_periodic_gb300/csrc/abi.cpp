@@ -960,3 +960,110 @@ extern "C" int acum_preprocess_imper(float* Xham, float* Nham, float* Vham, floa
             }
     return ACUM_OK;
 }
+
+namespace {
+
+// device copies of the caller's five AoS arrays for one preprocess_per call
+struct PerBuffers {
+    void* d[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    long long* off = nullptr;
+    ~PerBuffers()
+    {
+        for (void* p : d)
+            if (p) cudaFree(p);
+        if (off) cudaFree(off);
+    }
+};
+
+template <typename S>
+int preprocess_per_t(S* Xham, S* Nham, S* Vham, S* Uham, S* PRham, int nSurf, const int* XPtr, const int* NPtr,
+                     const int* VPtr, const int* UPtr, const int* PRPtr, const int* E, int nTime, double dTau,
+                     double a0, double rhoRef, double Mref, double CFDscale, int periodic, int lowpass)
+{
+    if (!Xham || !Nham || !Vham || !Uham || !PRham || !XPtr || !NPtr || !VPtr || !UPtr || !PRPtr || !E ||
+        nSurf <= 0 || nTime < 6)
+        return fail(nullptr, ACUM_ERR_INVALID, "preprocess_per: bad argument (nTime must be at least 6)");
+    if (nTime > acum::kMaxPerSteps)
+        return fail(nullptr, ACUM_ERR_UNSUPPORTED, "preprocess_per: more than 4096 steps per period");
+    // per-element starts (variables.cu AoS: element j of surface i at Ptr[i] + j nTime k)
+    const int width[5] = {4, 6, 6, 6, 4};
+    const int* ptr[5] = {XPtr, NPtr, VPtr, UPtr, PRPtr};
+    long long etot = 0;
+    for (int i = 0; i < nSurf; ++i) {
+        if (E[i] < 0) return fail(nullptr, ACUM_ERR_INVALID, "preprocess_per: negative element count");
+        etot += E[i];
+    }
+    if (etot == 0) return ACUM_OK;
+    std::vector<long long> off((size_t)etot * 5);
+    long long extent[5] = {0, 0, 0, 0, 0};
+    long long e = 0;
+    for (int i = 0; i < nSurf; ++i)
+        for (int j = 0; j < E[i]; ++j, ++e)
+            for (int q = 0; q < 5; ++q) {
+                if (ptr[q][i] < 0) return fail(nullptr, ACUM_ERR_INVALID, "preprocess_per: negative offset");
+                const long long o = (long long)ptr[q][i] + (long long)j * nTime * width[q];
+                off[(size_t)q * etot + e] = o;
+                extent[q] = std::max(extent[q], o + (long long)nTime * width[q]);
+            }
+    int dev = 0;
+    cudaError_t ce = cudaGetDevice(&dev);
+    if (ce != cudaSuccess) return cuda_fail(nullptr, ce, "cudaGetDevice");
+    acum_ctx* c = dropin_ctx(dev);
+    if (!c) return fail(nullptr, ACUM_ERR_CUDA, "preprocess_per: cannot create a context");
+    cudaStream_t st = c->stream;
+    S* host[5] = {Xham, Nham, Vham, Uham, PRham};
+    PerBuffers b;
+    for (int q = 0; q < 5; ++q) {
+        CK(nullptr, cudaMalloc(&b.d[q], (size_t)extent[q] * sizeof(S)));
+        CK(nullptr, cudaMemcpyAsync(b.d[q], host[q], (size_t)extent[q] * sizeof(S), cudaMemcpyHostToDevice, st));
+    }
+    CK(nullptr, cudaMalloc(&b.off, off.size() * sizeof(long long)));
+    CK(nullptr, cudaMemcpyAsync(b.off, off.data(), off.size() * sizeof(long long), cudaMemcpyHostToDevice, st));
+    acum::PerArgs a;
+    memset(&a, 0, sizeof(a));
+    a.xoff = b.off;
+    a.noff = b.off + etot;
+    a.voff = b.off + 2 * etot;
+    a.uoff = b.off + 3 * etot;
+    a.proff = b.off + 4 * etot;
+    a.E = (int)etot;
+    a.T = nTime;
+    a.dTau = dTau;
+    a.a0 = a0;
+    a.a02 = pow(a0, 2);
+    a.rhoRef = rhoRef;
+    a.mref2 = pow(Mref, 2);
+    a.cfd = CFDscale;
+    a.periodic = periodic;
+    a.lowpass = lowpass;
+    acum::gauss_taps(a.gauss);
+    CK(nullptr, acum::launch_per_prep(b.d[0], b.d[1], b.d[2], b.d[3], b.d[4], sizeof(S) == 8, a, st));
+    c->launches += 1;
+    for (int q = 0; q < 5; ++q)
+        CK(nullptr, cudaMemcpyAsync(host[q], b.d[q], (size_t)extent[q] * sizeof(S), cudaMemcpyDeviceToHost, st));
+    CK(nullptr, cudaStreamSynchronize(st));
+    return ACUM_OK;
+}
+
+}  // namespace
+
+extern "C" int acum_preprocess_per(float* Xham, float* Nham, float* Vham, float* Uham, float* PRham, int nSurf,
+                                   const int* XPtr, const int* NPtr, const int* VPtr, const int* UPtr,
+                                   const int* PRPtr, const int* E, int nTime, float dTau, float a0, float rhoRef,
+                                   float Mref, float CFDscale, int periodic, int lowpass)
+{
+    acum::NvtxRange nvtx_range_("acum_preprocess_per");
+    return preprocess_per_t<float>(Xham, Nham, Vham, Uham, PRham, nSurf, XPtr, NPtr, VPtr, UPtr, PRPtr, E, nTime,
+                                   dTau, a0, rhoRef, Mref, CFDscale, periodic, lowpass);
+}
+
+extern "C" int acum_preprocess_per_f64(double* Xham, double* Nham, double* Vham, double* Uham, double* PRham,
+                                       int nSurf, const int* XPtr, const int* NPtr, const int* VPtr,
+                                       const int* UPtr, const int* PRPtr, const int* E, int nTime, double dTau,
+                                       double a0, double rhoRef, double Mref, double CFDscale, int periodic,
+                                       int lowpass)
+{
+    acum::NvtxRange nvtx_range_("acum_preprocess_per_f64");
+    return preprocess_per_t<double>(Xham, Nham, Vham, Uham, PRham, nSurf, XPtr, NPtr, VPtr, UPtr, PRPtr, E, nTime,
+                                    dTau, a0, rhoRef, Mref, CFDscale, periodic, lowpass);
+}

@@ -105,6 +105,22 @@ struct AosArgs {
 };
 cudaError_t launch_aos_records(const AosArgs& a, cudaStream_t s);
 
+// permeable preprocessing (preprocess_per) in place on reference-layout AoS arrays
+constexpr int kMaxPerSteps = 4096;
+struct PerArgs {
+    const long long* xoff;  // device: per-element start (elements of the storage type) in Xham
+    const long long* noff;  // ... in Nham
+    const long long* voff;  // ... in Vham
+    const long long* uoff;  // ... in Uham
+    const long long* proff; // ... in PRham (4 per step)
+    int E, T;
+    double dTau, a0, a02, rhoRef, mref2, cfd;  // a02 = pow(a0, 2), mref2 = pow(Mref, 2)
+    int periodic, lowpass;
+    double gauss[13];
+};
+cudaError_t launch_per_prep(void* X, void* N, void* V, void* U, void* PR, bool is_double, const PerArgs& a,
+                            cudaStream_t s);
+
 struct TonalRun {
     TonalGeom g;
     TonalTile t;

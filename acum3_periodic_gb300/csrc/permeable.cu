@@ -1,0 +1,169 @@
+// Permeable-surface preprocessing on the GPU: preprocess_per (preprocess.cu:8-226).
+//
+//  per_prep_kernel   one block per element; the element's series are read from the
+//                    reference's AoS arrays (variables.cu:11-42 field order, nPRham = 4
+//                    as main.cu:87 sets it for permeable decks) and written back in place.
+//
+// The arithmetic is FP64 whatever the storage type, and follows the reference's order of
+// operations with no fused multiply-adds (explicit __dmul_rn / __dadd_rn where the
+// compiler would contract), so that with double storage the outputs equal the
+// reference's FP64 build bit for bit, and with float storage they are those FP64 results
+// rounded once.  The reference's FP32 build rounds every intermediate to float instead.
+//
+// Work per element: five flow series (rho, u, v, w, P) scaled, optionally filtered (two
+// passes of a 3-point periodic median and a 13-tap periodic Gaussian, preprocess.cu:
+// 113-137) and differentiated (periodic or end-biased central differences, preprocess.cu:
+// 150-163); the normal's periodic derivative (166-168); the position scaled, its
+// derivative V and V's derivative (172-180).  Each series goes through two FP64 rows in
+// shared memory, one at a time, so 16 bytes per step suffice (64 KB at 4096 steps).
+#include "acum_internal.h"
+
+namespace acum {
+
+namespace {
+
+constexpr int kPerThreads = 256;
+
+template <typename S>
+struct PerPtrs {
+    S* X;   // [..][T][4]  x, y, z, ds
+    S* N;   // [..][T][6]  n, ndot
+    S* V;   // [..][T][6]  V, Vdot
+    S* U;   // [..][T][6]  u, udot
+    S* PR;  // [..][T][4]  P, Pdot, rho, rhodot
+};
+
+// central difference with the reference's division (mathfunc.cu:132-140)
+__device__ __forceinline__ double cdiff(double up, double um, double two_dt) { return (up - um) / two_dt; }
+
+// d/dtau of the series in row `src` at step t: periodic, or the end-biased form
+// (mathfunc.cu:142-159: central interior, ends from 3 du[1] - 3 du[2] + du[3])
+__device__ __forceinline__ double series_deriv(const double* src, int t, int T, double two_dt, bool biased)
+{
+    if (!biased || (t > 0 && t < T - 1)) {
+        const int tm = t == 0 ? T - 1 : t - 1, tp = t == T - 1 ? 0 : t + 1;
+        return cdiff(src[tp], src[tm], two_dt);
+    }
+    const int s = t == 0 ? 1 : -1;
+    const int k1 = t + s, k2 = t + 2 * s, k3 = t + 3 * s;
+    const double d1 = cdiff(src[k1 + 1], src[k1 - 1], two_dt);
+    const double d2 = cdiff(src[k2 + 1], src[k2 - 1], two_dt);
+    const double d3 = cdiff(src[k3 + 1], src[k3 - 1], two_dt);
+    return __dadd_rn(__dsub_rn(__dmul_rn(3.0, d1), __dmul_rn(3.0, d2)), d3);
+}
+
+// two passes of (3-point periodic median, 13-tap periodic Gaussian) on row P, Q scratch
+// (mathfunc.cu:208-341 and 375-421)
+__device__ void lowpass_rows(double* P, double* Q, int T, const double* w)
+{
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int t = threadIdx.x; t < T; t += blockDim.x) {
+            const double l = P[t == 0 ? T - 1 : t - 1], m = P[t], r = P[t == T - 1 ? 0 : t + 1];
+            double hi = l > m ? l : m;
+            hi = hi > r ? hi : r;
+            double lo = l < m ? l : m;
+            lo = lo < r ? lo : r;
+            Q[t] = (l < hi && l > lo) ? l : ((m < hi && m > lo) ? m : r);
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < T; t += blockDim.x) {
+            double acc = 0.0;
+#pragma unroll
+            for (int k = 0; k < 13; ++k) {
+                int q = t + k - 6;
+                if (q < 0) q += T;
+                else if (q > T - 1) q -= T;
+                acc = __dadd_rn(acc, __dmul_rn(w[k], Q[q]));
+            }
+            P[t] = acc;
+        }
+        __syncthreads();
+    }
+}
+
+template <typename S>
+__global__ void __launch_bounds__(kPerThreads) per_prep_kernel(PerPtrs<S> p, PerArgs a)
+{
+    extern __shared__ __align__(16) unsigned char sm[];
+    const int T = a.T;
+    double* P = reinterpret_cast<double*>(sm);  // [T]
+    double* Q = P + T;                           // [T]
+    const int e = blockIdx.x;
+    S* X = p.X + a.xoff[e];
+    S* N = p.N + a.noff[e];
+    S* V = p.V + a.voff[e];
+    S* U = p.U + a.uoff[e];
+    S* PR = p.PR + a.proff[e];
+    const double two_dt = 2.0 * a.dTau;
+    const bool biased = a.periodic != 1;
+
+    // flow series: rho (PR 2), u (U 0..2), P (PR 0), in the reference's order v1..v5
+    for (int v = 0; v < 5; ++v) {
+        S* col = v == 0 ? PR + 2 : (v == 4 ? PR : U + (v - 1));
+        const int stride = v == 0 || v == 4 ? 4 : 6;
+        S* dcol = v == 0 ? PR + 3 : (v == 4 ? PR + 1 : U + (v + 2));
+        for (int t = threadIdx.x; t < T; t += blockDim.x) {
+            const double raw = (double)col[(size_t)t * stride];
+            double s;
+            if (v == 0) s = raw * a.rhoRef;
+            else if (v == 4) s = raw * 0.5 * a.rhoRef * a.mref2 * a.a02;  // left to right (preprocess.cu:66)
+            else s = raw * a.a0;
+            P[t] = s;
+        }
+        __syncthreads();
+        if (a.lowpass == 1) lowpass_rows(P, Q, T, a.gauss);
+        for (int t = threadIdx.x; t < T; t += blockDim.x) {
+            col[(size_t)t * stride] = (S)P[t];
+            dcol[(size_t)t * stride] = (S)series_deriv(P, t, T, two_dt, biased);
+        }
+        __syncthreads();
+    }
+    // normal: periodic derivative of the unchanged n (preprocess.cu:166-168)
+    for (int t = threadIdx.x; t < T; t += blockDim.x) {
+        const int tm = t == 0 ? T - 1 : t - 1, tp = t == T - 1 ? 0 : t + 1;
+        for (int c = 0; c < 3; ++c)
+            N[(size_t)t * 6 + 3 + c] = (S)cdiff((double)N[(size_t)tp * 6 + c], (double)N[(size_t)tm * 6 + c], two_dt);
+        // panel area (preprocess.cu:56): (ds CFDscale) CFDscale
+        X[(size_t)t * 4 + 3] = (S)((double)X[(size_t)t * 4 + 3] * a.cfd * a.cfd);
+    }
+    // position: scaled x, V = dx/dtau, Vdot = dV/dtau, both periodic (preprocess.cu:172-180)
+    for (int c = 0; c < 3; ++c) {
+        for (int t = threadIdx.x; t < T; t += blockDim.x) P[t] = (double)X[(size_t)t * 4 + c] * a.cfd;
+        __syncthreads();
+        for (int t = threadIdx.x; t < T; t += blockDim.x) Q[t] = series_deriv(P, t, T, two_dt, false);
+        __syncthreads();
+        for (int t = threadIdx.x; t < T; t += blockDim.x) {
+            X[(size_t)t * 4 + c] = (S)P[t];
+            V[(size_t)t * 6 + c] = (S)Q[t];
+            V[(size_t)t * 6 + 3 + c] = (S)series_deriv(Q, t, T, two_dt, false);
+        }
+        __syncthreads();
+    }
+}
+
+template <typename S>
+cudaError_t launch_per_t(S* X, S* N, S* V, S* U, S* PR, const PerArgs& a, cudaStream_t s)
+{
+    const size_t smem = (size_t)a.T * 2 * sizeof(double);
+    if (smem > 48 * 1024) {
+        cudaError_t err =
+            cudaFuncSetAttribute(per_prep_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err != cudaSuccess) return err;
+    }
+    PerPtrs<S> p{X, N, V, U, PR};
+    per_prep_kernel<S><<<a.E, kPerThreads, smem, s>>>(p, a);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_per_prep(void* X, void* N, void* V, void* U, void* PR, bool is_double, const PerArgs& a,
+                            cudaStream_t s)
+{
+    if (a.E < 1 || a.T < 4 || a.T > kMaxPerSteps) return cudaErrorInvalidValue;
+    if (is_double)
+        return launch_per_t<double>((double*)X, (double*)N, (double*)V, (double*)U, (double*)PR, a, s);
+    return launch_per_t<float>((float*)X, (float*)N, (float*)V, (float*)U, (float*)PR, a, s);
+}
+
+}  // namespace acum

@@ -101,6 +101,10 @@ SIGNATURES = {
     "acum_noalloc_last_error": (C.c_char_p, []),
     "acum_preprocess_imper": (C.c_int, [C.c_void_p] * 4 + [C.c_int] + [C.c_void_p] * 5 +
                               [C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int]),
+    "acum_preprocess_per": (C.c_int, [C.c_void_p] * 5 + [C.c_int] + [C.c_void_p] * 6 +
+                            [C.c_int] + [C.c_float] * 5 + [C.c_int, C.c_int]),
+    "acum_preprocess_per_f64": (C.c_int, [C.c_void_p] * 5 + [C.c_int] + [C.c_void_p] * 6 +
+                                [C.c_int] + [C.c_double] * 5 + [C.c_int, C.c_int]),
     "acum_find_bb_noise": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_float] + [C.c_void_p] * 26 +
                            [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_float,
                             C.c_void_p, C.c_void_p]),
@@ -430,6 +434,28 @@ def selftest_tmem(device: int = 0):
     if rc != 0:
         raise AcumError(rc, "acum_selftest_tmem failed")
     return mis.value, rb
+
+
+def preprocess_per(ne, X, N, V, U, PR, dTau, a0, rhoRef, Mref, CFDscale, periodic=1, lowpass=0,
+                   dtype=np.float64):
+    """preprocess_per (preprocess.cu:8-226) on the GPU through acum_preprocess_per(_f64).
+
+    X [E][T][4], N, V, U [E][T][6], PR [E][T][4]: the reference's AoS rows with the
+    elements of all surfaces stacked (ne = elements per surface).  Works on copies in
+    `dtype` (float32: the FP32 storage form, float64: the FP64 build's) and returns the
+    updated (X, N, V, U, PR)."""
+    arrs = [np.array(a, dtype=dtype, order="C") for a in (X, N, V, U, PR)]
+    T = arrs[0].shape[1]
+    ne = np.asarray(ne, np.int32)
+    off = np.concatenate([[0], np.cumsum(ne)[:-1]]).astype(np.int64)
+    ptrs = [np.ascontiguousarray(off * T * w, dtype=np.int32) for w in (4, 6, 6, 6, 4)]
+    vp = lambda a: a.ctypes.data_as(C.c_void_p)
+    fn = lib().acum_preprocess_per_f64 if dtype == np.float64 else lib().acum_preprocess_per
+    rc = fn(*[vp(a) for a in arrs], len(ne), *[vp(q) for q in ptrs], vp(ne), T, dTau, a0, rhoRef, Mref, CFDscale,
+            int(periodic), int(lowpass))
+    if rc != 0:
+        raise AcumError(rc, lib().acum_last_global_error().decode())
+    return tuple(arrs)
 
 
 class PinnedBuffer:

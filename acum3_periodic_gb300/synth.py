@@ -359,3 +359,35 @@ def batch_deck(case: int, ncase: int = 64, shrink: Optional[dict] = None) -> Dec
                 setattr(spec, k, min(getattr(spec, k), v))
         spec.dpsi_deg = 360.0 / spec.ntime
     return rotor_deck(spec, observers(kind, O, rad), s, name="batch%d" % case)
+
+
+def permeable_rows(seed: int, ne, ntime: int, radius: float = 1.2, mach_tip: float = 0.55):
+    """Seeded rows of a permeable data surface for preprocess_per (preprocess.cu:8-226):
+    a ring of panels rotating about z (one rotor period over ntime steps) with a
+    periodic flow field on it.  Returns X (x, y, z, ds), N (n, 0), U (u, 0), PR (P, 0,
+    rho, 0), each [element][step][k], all surfaces' elements stacked (ne = elements per
+    surface), values in the non-dimensional units the reader sees (io.cu:286)."""
+    E = int(sum(ne))
+    u = uniform(seed, 5, E * 8).reshape(E, 8)
+    ph = 2.0 * np.pi * np.arange(ntime) / ntime
+    az = 2.0 * np.pi * np.arange(E) / E
+    X = np.zeros((E, ntime, 4))
+    N = np.zeros((E, ntime, 6))
+    U = np.zeros((E, ntime, 6))
+    PR = np.zeros((E, ntime, 4))
+    th = az[:, None] + ph[None, :]
+    r = radius * (1.0 + 0.05 * (u[:, 0:1] - 0.5))
+    z = 0.3 * (u[:, 1:2] - 0.5)
+    X[:, :, 0] = r * np.cos(th)
+    X[:, :, 1] = r * np.sin(th)
+    X[:, :, 2] = z
+    X[:, :, 3] = 0.01 * (1.0 + u[:, 2:3])
+    N[:, :, 0] = np.cos(th)
+    N[:, :, 1] = np.sin(th)
+    harm = np.sin(3.0 * th + 6.0 * u[:, 3:4]) + 0.2 * np.cos(7.0 * th)
+    U[:, :, 0] = -mach_tip * np.sin(th) * (1.0 + 0.1 * harm)
+    U[:, :, 1] = mach_tip * np.cos(th) * (1.0 + 0.1 * harm)
+    U[:, :, 2] = 0.05 * harm
+    PR[:, :, 0] = 0.8 * harm + 0.1 * (u[:, 4:5] - 0.5)
+    PR[:, :, 2] = 1.0 + 0.02 * harm
+    return X, N, U, PR

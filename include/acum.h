@@ -10,6 +10,7 @@
  *       acum_find_pressure_time_history_f64  the same call on the FP64 build's arrays
  *       acum_find_bb_noise                   replaces bb_core.cu:11 (called at main.cu:274)
  *       acum_preprocess_imper                replaces preprocess.cu:228 on caller arrays
+ *       acum_preprocess_per(_f64)            replaces preprocess.cu:8 (main.cu:87, permeable)
  *
  *  2. A context API that owns the deck on the device and runs the whole path: the file
  *     readers and writers keep the reference's formats (io.cu), preprocessing and all
@@ -267,6 +268,25 @@ const char* acum_noalloc_last_error(void);
 int acum_preprocess_imper(float* Xham, float* Nham, float* Vham, float* PRham, int nSurf, const int* XPtr,
                           const int* NPtr, const int* VPtr, const int* PRPtr, const int* E, int nTime, float dTau,
                           float a0, float rhoRef, float Mref, float CFDscale, int periodic, int lowpass);
+
+/* Replaces preprocess_per (preprocess.cu:8, called at main.cu:87 when impermeable = 0) on
+ * caller arrays: host AoS Xham [*4] (x, y, z, ds), Nham [*6] (n, ndot), Vham [*6] (V,
+ * Vdot), Uham [*6] (u, udot), PRham [*4] (P, Pdot, rho, rhodot), element j of surface i
+ * at Ptr[i] + j*nTime*width as the reference lays them out (variables.cu:11-42, E[]
+ * counts, host).  Updated in place with the same meaning: x, ds, u, rho, P scaled; u, rho,
+ * P low-passed when lowpass = 1; their derivatives periodic (periodic = 1) or end-biased;
+ * ndot, V, Vdot periodic.  The GPU computes in FP64 in the reference's order of
+ * operations: the _f64 form (the FP64 build's arrays) equals that build bit for bit, the
+ * float form gives those results rounded once to float.  6 <= nTime <= 4096 (the 13-tap
+ * filter's periodic index wraps once, the biased ends read du[3]): ACUM_ERR_INVALID
+ * below, ACUM_ERR_UNSUPPORTED above. */
+int acum_preprocess_per(float* Xham, float* Nham, float* Vham, float* Uham, float* PRham, int nSurf, const int* XPtr,
+                        const int* NPtr, const int* VPtr, const int* UPtr, const int* PRPtr, const int* E, int nTime,
+                        float dTau, float a0, float rhoRef, float Mref, float CFDscale, int periodic, int lowpass);
+int acum_preprocess_per_f64(double* Xham, double* Nham, double* Vham, double* Uham, double* PRham, int nSurf,
+                            const int* XPtr, const int* NPtr, const int* VPtr, const int* UPtr, const int* PRPtr,
+                            const int* E, int nTime, double dTau, double a0, double rhoRef, double Mref,
+                            double CFDscale, int periodic, int lowpass);
 
 /* Replaces findBBnoise (bb_core.cu:11) as called at main.cu:274: the same 39 arguments,
  * host pointers, FP32 storage; BBspl [nObs][nf2][7] and BBoaspl [nObs] are updated as the

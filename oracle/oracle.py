@@ -222,3 +222,42 @@ def differentiate(u: np.ndarray, dt: float, biased: bool = False) -> np.ndarray:
     du = np.zeros_like(u)
     lib().acumo_differentiate(_p(u), _p(du), dt, u.size, int(biased))
     return du
+
+
+def preprocess_per(X, N, U, PR, dTau, a0, rhoRef, Mref, CFDscale, periodic=1, lowpass_=0):
+    """preprocess_per (preprocess.cu:8-226), the permeable surfaces' preprocessing, in FP64.
+
+    Inputs are one element's series stacked as [element][step][k] (AoS of variables.cu:
+    11-42): X (x, y, z, ds), N (n, ndot), U (u, udot), PR (P, Pdot, rho, rhodot); only the
+    columns the reader fills (io.cu:286) are read.  Returns new arrays (X, N, V, U, PR):
+
+    * scaling (preprocess.cu:50-68): x by CFDscale, ds by CFDscale^2, rho by rhoRef, u by
+      a0, P by 0.5 rhoRef Mref^2 a0^2;
+    * optional lowpass of rho, u, P (preprocess.cu:113-137): twice median3 + Gaussian,
+      no make_periodic (commented out in the reference, preprocess.cu:105-109);
+    * d/dtau of rho, u, P periodic or end-biased (preprocess.cu:150-163), of n periodic
+      (166-168); V = d x/dtau and Vdot = d V/dtau, both periodic (172-180).
+    """
+    X = np.array(X, dtype=np.float64)
+    N = np.array(N, dtype=np.float64)
+    U = np.array(U, dtype=np.float64)
+    PR = np.array(PR, dtype=np.float64)
+    V = np.zeros(N.shape, np.float64)
+    X[:, :, 0:3] *= CFDscale
+    X[:, :, 3] = X[:, :, 3] * CFDscale * CFDscale  # (ds CFDscale) CFDscale, preprocess.cu:56
+    PR[:, :, 2] *= rhoRef
+    U[:, :, 0:3] *= a0
+    PR[:, :, 0] = PR[:, :, 0] * 0.5 * rhoRef * Mref ** 2 * a0 ** 2  # left to right, as preprocess.cu:66
+    biased = periodic != 1
+    for e in range(X.shape[0]):
+        flow = [PR[e, :, 2], U[e, :, 0], U[e, :, 1], U[e, :, 2], PR[e, :, 0]]
+        if lowpass_ == 1:
+            flow = [lowpass(s) for s in flow]
+        d = [differentiate(s, dTau, biased) for s in flow]
+        PR[e, :, 2], U[e, :, 0], U[e, :, 1], U[e, :, 2], PR[e, :, 0] = flow
+        PR[e, :, 3], U[e, :, 3], U[e, :, 4], U[e, :, 5], PR[e, :, 1] = d
+        for c in range(3):
+            N[e, :, 3 + c] = differentiate(N[e, :, c], dTau)
+            V[e, :, c] = differentiate(X[e, :, c], dTau)
+            V[e, :, 3 + c] = differentiate(V[e, :, c], dTau)
+    return X, N, V, U, PR

@@ -59,6 +59,8 @@ def lib(prec: str = "f64"):
         L.acumref_differentiate.argtypes = [_DP, _DP, C.c_double, C.c_int, C.c_int]
         L.acumref_core.argtypes = [_DP, C.c_int, C.c_int, C.c_int, _DP]
         L.acumref_bands.argtypes = [_DP]
+        L.acumref_preprocess_per.argtypes = [C.c_int, C.POINTER(C.c_int), C.c_int, _DP, C.c_int, C.c_int] + \
+            [_DP] * 5 + [C.c_int]
         _libs[prec] = L
     return _libs[prec]
 
@@ -164,3 +166,19 @@ def differentiate(u, dt, biased=False, prec="f64"):
     du = np.zeros_like(u)
     lib(prec).acumref_differentiate(_p(u), _p(du), dt, u.size, int(biased))
     return du
+
+
+def preprocess_per(ne, X, N, V, U, PR, dTau, a0, rhoRef, Mref, CFDscale, periodic=1, lowpass=0,
+                   prec: str = "f64"):
+    """The reference's preprocess_per (preprocess.cu:8-226) on copies of the given arrays,
+    [element][step][k] with the elements of all surfaces stacked (ne = elements per
+    surface).  Returns the updated (X, N, V, U, PR)."""
+    L = lib(prec)
+    arrs = [np.array(a, dtype=np.float64, order="C") for a in (X, N, V, U, PR)]
+    ne_c = (C.c_int * len(ne))(*[int(k) for k in ne])
+    scal = np.array([dTau, a0, rhoRef, Mref, CFDscale], np.float64)
+    rc = L.acumref_preprocess_per(len(ne), ne_c, arrs[0].shape[1], _p(scal), int(periodic), int(lowpass),
+                                  *[_p(a) for a in arrs], 1)
+    if rc != 0:
+        raise RuntimeError("acumref_preprocess_per failed: %d" % rc)
+    return tuple(arrs)

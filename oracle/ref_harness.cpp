@@ -258,3 +258,64 @@ extern "C" void acumref_bands(double* f)
 {
     for (int i = 0; i < nf2; i++) f[i] = ff[i];
 }
+
+/* preprocess_per (preprocess.cu:8-226), the permeable surfaces' preprocessing, on caller
+ * arrays laid out as [element][step][k] per surface, surface after surface (X k = 4, N 6,
+ * V 6, U 6, PR 4 = P, dP, rho, drho): the reference's globals are set as its reader and
+ * main.cu:87 leave them (impermeable = 0, nPRham = 4), the function runs, the arrays
+ * come back.  scal = dTau, a0, rhoRef, Mref, CFDscale. */
+extern "C" int acumref_preprocess_per(int nsurf, const int* ne, int nt, const double* scal, int periodic_,
+                                      int lowpass_, double* X, double* N, double* V, double* U, double* PR,
+                                      int quiet)
+{
+    if (nsurf <= 0 || nt < 4) return -1;
+    long etot_ = 0;
+    for (int i = 0; i < nsurf; i++) etot_ += ne[i];
+    nSurf = nsurf;
+    nTime = nt;
+    dTau = scal[0];
+    a0 = scal[1];
+    rhoRef = scal[2];
+    Mref = scal[3];
+    CFDscale = scal[4];
+    periodic = periodic_;
+    lowpass = lowpass_;
+    impermeable = 0;
+    nPRham = 4;
+    E = (int*)calloc(nsurf, sizeof(int));
+    XPtr = (int*)calloc(nsurf, sizeof(int));
+    NPtr = (int*)calloc(nsurf, sizeof(int));
+    VPtr = (int*)calloc(nsurf, sizeof(int));
+    UPtr = (int*)calloc(nsurf, sizeof(int));
+    PRPtr = (int*)calloc(nsurf, sizeof(int));
+    long off = 0;
+    for (int i = 0; i < nsurf; i++) {
+        E[i] = ne[i];
+        XPtr[i] = (int)(off * nt * 4);
+        NPtr[i] = (int)(off * nt * 6);
+        VPtr[i] = (int)(off * nt * 6);
+        UPtr[i] = (int)(off * nt * 6);
+        PRPtr[i] = (int)(off * nt * 4);
+        off += ne[i];
+    }
+    const long n = etot_ * nt;
+    Xham = (real*)calloc(n * 4, sizeof(real));
+    Nham = (real*)calloc(n * 6, sizeof(real));
+    Vham = (real*)calloc(n * 6, sizeof(real));
+    Uham = (real*)calloc(n * 6, sizeof(real));
+    PRham = (real*)calloc(n * 4, sizeof(real));
+    for (long i = 0; i < n * 4; i++) Xham[i] = X[i];
+    for (long i = 0; i < n * 6; i++) { Nham[i] = N[i]; Vham[i] = V[i]; Uham[i] = U[i]; }
+    for (long i = 0; i < n * 4; i++) PRham[i] = PR[i];
+    quiet_on(quiet);
+    preprocess_per();
+    quiet_off(quiet);
+    for (long i = 0; i < n * 4; i++) X[i] = Xham[i];
+    for (long i = 0; i < n * 6; i++) { N[i] = Nham[i]; V[i] = Vham[i]; U[i] = Uham[i]; }
+    for (long i = 0; i < n * 4; i++) PR[i] = PRham[i];
+    free(Xham); free(Nham); free(Vham); free(Uham); free(PRham);
+    free(E); free(XPtr); free(NPtr); free(VPtr); free(UPtr); free(PRPtr);
+    Xham = Nham = Vham = Uham = PRham = NULL;
+    E = XPtr = NPtr = VPtr = UPtr = PRPtr = NULL;
+    return 0;
+}

@@ -7,7 +7,8 @@ the reference tree is available:
 It writes a few small seeded decks (the reference's text formats) under
 tests/golden/decks/<name>/ and, for each, the FP64-build outputs (plus the as-written
 FP32-build outputs, for information) into tests/golden/<name>.npz; and unit vectors of
-the broadband shape curves and the preprocessing filters into tests/golden/units.npz.
+the broadband shape curves and the preprocessing filters into tests/golden/units.npz; and
+the permeable preprocessing of a seeded data surface into tests/golden/permeable.npz.
 """
 import os
 import sys
@@ -96,6 +97,18 @@ def main():
     units["diff_biased"] = ref.differentiate(series, 0.01, True)
     np.savez_compressed(os.path.join(OUT, "units.npz"), **units)
     print("wrote units")
+    # permeable preprocessing (preprocess_per) of a seeded rotating data surface, two
+    # surfaces; outputs for (periodic, lowpass) = (1, 0) and (0, 1)
+    ne, T = [5, 3], 48
+    X, N, U, PR = synth.permeable_rows(21, ne, T)
+    per = {"ne": np.array(ne), "X": X, "N": N, "U": U, "PR": PR,
+           "scal": np.array([0.0021, 340.0, 1.2, 0.08, 1.5])}
+    for periodic, lowpass in ((1, 0), (0, 1)):
+        outs = ref.preprocess_per(ne, X, N, np.zeros_like(N), U, PR, *per["scal"], periodic, lowpass)
+        for nm, a in zip("XNVUP", outs):
+            per["%s_p%d_l%d" % (nm, periodic, lowpass)] = a
+    np.savez_compressed(os.path.join(OUT, "permeable.npz"), **per)
+    print("wrote permeable")
 
 
 if __name__ == "__main__":

@@ -67,3 +67,14 @@ def test_unit_vectors():
     np.testing.assert_allclose(O.lowpass(u["series"]), u["lowpass"], rtol=0, atol=1e-14)
     np.testing.assert_allclose(O.differentiate(u["series"], 0.01), u["diff_periodic"], rtol=0, atol=1e-11)
     np.testing.assert_allclose(O.differentiate(u["series"], 0.01, True), u["diff_biased"], rtol=0, atol=1e-11)
+
+
+@pytest.mark.parametrize("periodic,lowpass", [(1, 0), (0, 1)])
+def test_permeable_preprocessing(periodic, lowpass):
+    """The oracle's preprocess_per against the reference's FP64 build on a seeded rotating
+    data surface (two surfaces): every output array bit for bit."""
+    g = np.load(os.path.join(GOLDEN, "permeable.npz"))
+    out = O.preprocess_per(g["X"], g["N"], g["U"], g["PR"], *g["scal"], periodic, lowpass)
+    for nm, a in zip("XNVUP", out):
+        want = g["%s_p%d_l%d" % (nm, periodic, lowpass)]
+        np.testing.assert_array_equal(a, want)

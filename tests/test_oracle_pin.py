@@ -86,3 +86,16 @@ def test_bpm_core_random_inputs(tmp_path):
         out = np.full(42 * 7, -100.0)
         O.lib().acumo_bpm_core(*args[:9], trip, *args[9:13], isect, 3, O._p(ff), 42, args[14], O._p(out))
         np.testing.assert_allclose(out.reshape(42, 7), want, rtol=0, atol=1e-9)
+
+
+@pytest.mark.parametrize("rep,ntime,periodic,lowpass", [(31, 24, 1, 1), (32, 61, 0, 0), (33, 200, 1, 0)])
+def test_permeable_preprocessing_random(rep, ntime, periodic, lowpass):
+    ne = [2 + rep % 3, 4, 1]
+    X, N, U, PR = synth.permeable_rows(rep, ne, ntime)
+    rng = np.random.default_rng(rep)
+    PR[:, :, 0] += 0.05 * rng.standard_normal(PR.shape[:2])  # not smooth: the median filter acts
+    args = (1.0 / (ntime * 7.3), 341.0, 1.18, 0.11, 2.5, periodic, lowpass)
+    want = R.preprocess_per(ne, X, N, np.zeros_like(N), U, PR, *args)
+    got = O.preprocess_per(X, N, U, PR, *args)
+    for a, b in zip(got, want):
+        np.testing.assert_array_equal(a, b)
