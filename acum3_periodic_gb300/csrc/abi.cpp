@@ -963,15 +963,82 @@ extern "C" int acum_preprocess_imper(float* Xham, float* Nham, float* Vham, floa
 
 namespace {
 
-// device copies of the caller's five AoS arrays for one preprocess_per call
+// The per-element starts of one preprocess_per layout (variables.cu AoS: element j of
+// surface i at Ptr[i] + j nTime width) and the extent of each array.
+struct PerLayout {
+    long long etot = 0;
+    std::vector<long long> off;  // [5][etot]: X, N, V, U, PR
+    long long extent[5] = {0, 0, 0, 0, 0};
+};
+
+int per_layout(int nSurf, const int* XPtr, const int* NPtr, const int* VPtr, const int* UPtr, const int* PRPtr,
+               const int* E, int nTime, PerLayout& L)
+{
+    if (!XPtr || !NPtr || !VPtr || !UPtr || !PRPtr || !E || nSurf <= 0 || nTime < 6)
+        return fail(nullptr, ACUM_ERR_INVALID, "preprocess_per: bad argument (nTime must be at least 6)");
+    if (nTime > acum::kMaxPerSteps)
+        return fail(nullptr, ACUM_ERR_UNSUPPORTED, "preprocess_per: more than 4096 steps per period");
+    const int width[5] = {4, 6, 6, 6, 4};
+    const int* ptr[5] = {XPtr, NPtr, VPtr, UPtr, PRPtr};
+    for (int i = 0; i < nSurf; ++i) {
+        if (E[i] < 0) return fail(nullptr, ACUM_ERR_INVALID, "preprocess_per: negative element count");
+        L.etot += E[i];
+    }
+    if (L.etot > (1LL << 31) - 1) return fail(nullptr, ACUM_ERR_UNSUPPORTED, "preprocess_per: too many elements");
+    L.off.resize((size_t)L.etot * 5);
+    long long e = 0;
+    for (int i = 0; i < nSurf; ++i)
+        for (int j = 0; j < E[i]; ++j, ++e)
+            for (int q = 0; q < 5; ++q) {
+                if (ptr[q][i] < 0) return fail(nullptr, ACUM_ERR_INVALID, "preprocess_per: negative offset");
+                const long long o = (long long)ptr[q][i] + (long long)j * nTime * width[q];
+                L.off[(size_t)q * L.etot + e] = o;
+                L.extent[q] = std::max(L.extent[q], o + (long long)nTime * width[q]);
+            }
+    return ACUM_OK;
+}
+
+// Enqueues the kernel on `st` over device arrays d[5] (X, N, V, U, PR); the offsets go
+// through a stream-ordered allocation.
+int per_enqueue(void* const d[5], bool is_double, const PerLayout& L, int nTime, double dTau, double a0,
+                double rhoRef, double Mref, double CFDscale, int periodic, int lowpass, cudaStream_t st)
+{
+    long long* off = nullptr;
+    CK(nullptr, cudaMallocAsync((void**)&off, L.off.size() * sizeof(long long), st));
+    cudaError_t e = cudaMemcpyAsync(off, L.off.data(), L.off.size() * sizeof(long long), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        acum::PerArgs a;
+        memset(&a, 0, sizeof(a));
+        a.xoff = off;
+        a.noff = off + L.etot;
+        a.voff = off + 2 * L.etot;
+        a.uoff = off + 3 * L.etot;
+        a.proff = off + 4 * L.etot;
+        a.E = (int)L.etot;
+        a.T = nTime;
+        a.dTau = dTau;
+        a.a0 = a0;
+        a.a02 = pow(a0, 2);
+        a.rhoRef = rhoRef;
+        a.mref2 = pow(Mref, 2);
+        a.cfd = CFDscale;
+        a.periodic = periodic;
+        a.lowpass = lowpass;
+        acum::gauss_taps(a.gauss);
+        e = acum::launch_per_prep(d[0], d[1], d[2], d[3], d[4], is_double, a, st);
+    }
+    cudaFreeAsync(off, st);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "preprocess_per");
+    return ACUM_OK;
+}
+
+// device copies of the caller's five host arrays for one preprocess_per call
 struct PerBuffers {
     void* d[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    long long* off = nullptr;
     ~PerBuffers()
     {
         for (void* p : d)
             if (p) cudaFree(p);
-        if (off) cudaFree(off);
     }
 };
 
@@ -980,31 +1047,11 @@ int preprocess_per_t(S* Xham, S* Nham, S* Vham, S* Uham, S* PRham, int nSurf, co
                      const int* VPtr, const int* UPtr, const int* PRPtr, const int* E, int nTime, double dTau,
                      double a0, double rhoRef, double Mref, double CFDscale, int periodic, int lowpass)
 {
-    if (!Xham || !Nham || !Vham || !Uham || !PRham || !XPtr || !NPtr || !VPtr || !UPtr || !PRPtr || !E ||
-        nSurf <= 0 || nTime < 6)
-        return fail(nullptr, ACUM_ERR_INVALID, "preprocess_per: bad argument (nTime must be at least 6)");
-    if (nTime > acum::kMaxPerSteps)
-        return fail(nullptr, ACUM_ERR_UNSUPPORTED, "preprocess_per: more than 4096 steps per period");
-    // per-element starts (variables.cu AoS: element j of surface i at Ptr[i] + j nTime k)
-    const int width[5] = {4, 6, 6, 6, 4};
-    const int* ptr[5] = {XPtr, NPtr, VPtr, UPtr, PRPtr};
-    long long etot = 0;
-    for (int i = 0; i < nSurf; ++i) {
-        if (E[i] < 0) return fail(nullptr, ACUM_ERR_INVALID, "preprocess_per: negative element count");
-        etot += E[i];
-    }
-    if (etot == 0) return ACUM_OK;
-    std::vector<long long> off((size_t)etot * 5);
-    long long extent[5] = {0, 0, 0, 0, 0};
-    long long e = 0;
-    for (int i = 0; i < nSurf; ++i)
-        for (int j = 0; j < E[i]; ++j, ++e)
-            for (int q = 0; q < 5; ++q) {
-                if (ptr[q][i] < 0) return fail(nullptr, ACUM_ERR_INVALID, "preprocess_per: negative offset");
-                const long long o = (long long)ptr[q][i] + (long long)j * nTime * width[q];
-                off[(size_t)q * etot + e] = o;
-                extent[q] = std::max(extent[q], o + (long long)nTime * width[q]);
-            }
+    if (!Xham || !Nham || !Vham || !Uham || !PRham)
+        return fail(nullptr, ACUM_ERR_INVALID, "preprocess_per: null array");
+    PerLayout L;
+    int rc = per_layout(nSurf, XPtr, NPtr, VPtr, UPtr, PRPtr, E, nTime, L);
+    if (rc != ACUM_OK || L.etot == 0) return rc;
     int dev = 0;
     cudaError_t ce = cudaGetDevice(&dev);
     if (ce != cudaSuccess) return cuda_fail(nullptr, ce, "cudaGetDevice");
@@ -1014,33 +1061,14 @@ int preprocess_per_t(S* Xham, S* Nham, S* Vham, S* Uham, S* PRham, int nSurf, co
     S* host[5] = {Xham, Nham, Vham, Uham, PRham};
     PerBuffers b;
     for (int q = 0; q < 5; ++q) {
-        CK(nullptr, cudaMalloc(&b.d[q], (size_t)extent[q] * sizeof(S)));
-        CK(nullptr, cudaMemcpyAsync(b.d[q], host[q], (size_t)extent[q] * sizeof(S), cudaMemcpyHostToDevice, st));
+        CK(nullptr, cudaMalloc(&b.d[q], (size_t)L.extent[q] * sizeof(S)));
+        CK(nullptr, cudaMemcpyAsync(b.d[q], host[q], (size_t)L.extent[q] * sizeof(S), cudaMemcpyHostToDevice, st));
     }
-    CK(nullptr, cudaMalloc(&b.off, off.size() * sizeof(long long)));
-    CK(nullptr, cudaMemcpyAsync(b.off, off.data(), off.size() * sizeof(long long), cudaMemcpyHostToDevice, st));
-    acum::PerArgs a;
-    memset(&a, 0, sizeof(a));
-    a.xoff = b.off;
-    a.noff = b.off + etot;
-    a.voff = b.off + 2 * etot;
-    a.uoff = b.off + 3 * etot;
-    a.proff = b.off + 4 * etot;
-    a.E = (int)etot;
-    a.T = nTime;
-    a.dTau = dTau;
-    a.a0 = a0;
-    a.a02 = pow(a0, 2);
-    a.rhoRef = rhoRef;
-    a.mref2 = pow(Mref, 2);
-    a.cfd = CFDscale;
-    a.periodic = periodic;
-    a.lowpass = lowpass;
-    acum::gauss_taps(a.gauss);
-    CK(nullptr, acum::launch_per_prep(b.d[0], b.d[1], b.d[2], b.d[3], b.d[4], sizeof(S) == 8, a, st));
+    rc = per_enqueue(b.d, sizeof(S) == 8, L, nTime, dTau, a0, rhoRef, Mref, CFDscale, periodic, lowpass, st);
+    if (rc != ACUM_OK) return rc;
     c->launches += 1;
     for (int q = 0; q < 5; ++q)
-        CK(nullptr, cudaMemcpyAsync(host[q], b.d[q], (size_t)extent[q] * sizeof(S), cudaMemcpyDeviceToHost, st));
+        CK(nullptr, cudaMemcpyAsync(host[q], b.d[q], (size_t)L.extent[q] * sizeof(S), cudaMemcpyDeviceToHost, st));
     CK(nullptr, cudaStreamSynchronize(st));
     return ACUM_OK;
 }
@@ -1066,4 +1094,21 @@ extern "C" int acum_preprocess_per_f64(double* Xham, double* Nham, double* Vham,
     acum::NvtxRange nvtx_range_("acum_preprocess_per_f64");
     return preprocess_per_t<double>(Xham, Nham, Vham, Uham, PRham, nSurf, XPtr, NPtr, VPtr, UPtr, PRPtr, E, nTime,
                                     dTau, a0, rhoRef, Mref, CFDscale, periodic, lowpass);
+}
+
+extern "C" int acum_preprocess_per_device(void* Xham, void* Nham, void* Vham, void* Uham, void* PRham, int is_double,
+                                          int nSurf, const int* XPtr, const int* NPtr, const int* VPtr,
+                                          const int* UPtr, const int* PRPtr, const int* E, int nTime, double dTau,
+                                          double a0, double rhoRef, double Mref, double CFDscale, int periodic,
+                                          int lowpass, void* stream)
+{
+    acum::NvtxRange nvtx_range_("acum_preprocess_per_device");
+    if (!Xham || !Nham || !Vham || !Uham || !PRham)
+        return fail(nullptr, ACUM_ERR_INVALID, "preprocess_per: null array");
+    PerLayout L;
+    int rc = per_layout(nSurf, XPtr, NPtr, VPtr, UPtr, PRPtr, E, nTime, L);
+    if (rc != ACUM_OK || L.etot == 0) return rc;
+    void* d[5] = {Xham, Nham, Vham, Uham, PRham};
+    return per_enqueue(d, is_double != 0, L, nTime, dTau, a0, rhoRef, Mref, CFDscale, periodic, lowpass,
+                       (cudaStream_t)stream);
 }

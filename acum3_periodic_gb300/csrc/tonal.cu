@@ -953,8 +953,22 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
                 deposit(acc[q], T, p.tmod, prev, cur[q][j], 0, ok_obs[q] && valid && !(first_win && lane == 0), bad,
                         more);
                 if (lane == 31) sh.carry[warp][(w + 1) & 1][q][j] = cur[q][j];
-                if (first_win && lane == 0) sh.first[warp][q][j] = cur[q][j];
-                if (last_win) {
+            }
+        }
+        // the first window's samples (kept for the wrap) and the periodic wrap itself are
+        // handled after the stage's deposits, one uniform branch each instead of one per
+        // sample (2.6 % faster at workload 2)
+        if (first_win && lane == 0) {
+#pragma unroll
+            for (int q = 0; q < OPW; ++q)
+#pragma unroll
+                for (int j = 0; j < SE; ++j) sh.first[warp][q][j] = cur[q][j];
+        }
+        if (last_win) {
+#pragma unroll
+            for (int q = 0; q < OPW; ++q) {
+#pragma unroll
+                for (int j = 0; j < SE; ++j) {
                     // the periodic wrap: (t(T-1), t(0) + period] (core.cu:173-194)
                     const SmpF lastS = shfl_idx(cur[q][j], min(31, T - 1 - w * kWin));
                     if (lane == 0) {

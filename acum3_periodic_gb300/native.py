@@ -105,6 +105,8 @@ SIGNATURES = {
                             [C.c_int] + [C.c_float] * 5 + [C.c_int, C.c_int]),
     "acum_preprocess_per_f64": (C.c_int, [C.c_void_p] * 5 + [C.c_int] + [C.c_void_p] * 6 +
                                 [C.c_int] + [C.c_double] * 5 + [C.c_int, C.c_int]),
+    "acum_preprocess_per_device": (C.c_int, [C.c_void_p] * 5 + [C.c_int, C.c_int] + [C.c_void_p] * 6 +
+                                   [C.c_int] + [C.c_double] * 5 + [C.c_int, C.c_int, C.c_void_p]),
     "acum_find_bb_noise": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_float] + [C.c_void_p] * 26 +
                            [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_float,
                             C.c_void_p, C.c_void_p]),

@@ -204,6 +204,98 @@ def adjoint_leg(native, device):
     return res
 
 
+PER_BYTES_PER_ELEMENT_STEP = 140  # float storage: 12 values read (x, y, z, ds, n, u, P, rho), 23 written
+
+
+def permeable_leg(native, device, steps=3, cpu=True, n_elem=8192, ntime=1440):
+    """Permeable-surface preprocessing (preprocess_per) of a data surface of `n_elem`
+    elements (two surfaces) over `ntime` steps, filters on (the reference's default
+    lowpass = 1), float storage as the reference's arrays: the device-resident call
+    (acum_preprocess_per_device, CUDA events on its stream), the host call with host
+    copies inside (acum_preprocess_per on pinned arrays), and the oracle port on a sample
+    of elements (one host thread, as the reference's loop)."""
+    import ctypes as C
+    import torch
+    from acum3_periodic_gb300 import synth
+    ne = [n_elem // 2, n_elem - n_elem // 2]
+    X, N, U, PR = synth.permeable_rows(7, ne, ntime)
+    V = np.zeros_like(N)
+    arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in (X, N, V, U, PR)]
+    # scalars as float, as the float entry point receives them
+    args = tuple(float(np.float32(x)) for x in (1.0 / (ntime * 9.0), 340.0, 1.2, 0.08, 1.0)) + (1, 1)
+    T = ntime
+    off = np.concatenate([[0], np.cumsum(ne)[:-1]])
+    ptrs = [np.ascontiguousarray(off * T * w, dtype=np.int32) for w in (4, 6, 6, 6, 4)]
+    E = np.array(ne, np.int32)
+    vp = lambda a: a.ctypes.data_as(C.c_void_p)
+    lib = native.lib()
+    dev = torch.device("cuda", device)
+    pristine = [torch.from_numpy(a).to(dev) for a in arrs]
+    work = [t.clone() for t in pristine]
+    stream = torch.cuda.Stream(device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    element_steps = n_elem * T
+
+    def device_call():
+        rc = lib.acum_preprocess_per_device(*[C.c_void_p(t.data_ptr()) for t in work], 0, 2,
+                                            *[vp(q) for q in ptrs], vp(E), T, *args, C.c_void_p(stream.cuda_stream))
+        if rc != 0:
+            raise native.AcumError(rc, lib.acum_last_global_error().decode())
+
+    dms = []
+    for i in range(3 + steps):
+        for w, p in zip(work, pristine):
+            w.copy_(p)
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        device_call()
+        e1.record(stream)
+        e1.synchronize()
+        if i >= 3:
+            dms.append(e0.elapsed_time(e1))
+    dev_ms = float(np.mean(dms))
+    got = [t.cpu().numpy() for t in work]
+    # host arrays in, host arrays out, through the reference-shaped entry point
+    pinned = [native.PinnedBuffer(a.shape, np.float32) for a in arrs]
+    hs = []
+    for i in range(1 + steps):
+        for pb, a in zip(pinned, arrs):
+            pb.array[...] = a
+        t0 = time.perf_counter()
+        rc = lib.acum_preprocess_per(*[C.c_void_p(pb.ptr) for pb in pinned], 2, *[vp(q) for q in ptrs], vp(E), T,
+                                     *args)
+        hs.append(time.perf_counter() - t0)
+        if rc != 0:
+            raise native.AcumError(rc, lib.acum_last_global_error().decode())
+    host_equal = all(np.array_equal(pb.array, g) for pb, g in zip(pinned, got))
+    for pb in pinned:
+        pb.close()
+    host_s = float(np.mean(hs[1:]))
+    nbytes = int(sum(a.nbytes for a in arrs))
+    out = {"workload": "permeable data surface: %d elements (2 surfaces), %d steps, filters on, periodic "
+                       "derivatives, float storage" % (n_elem, T),
+           "element_steps": element_steps, "device_call_ms": dev_ms,
+           "element_steps_per_s": element_steps / (dev_ms * 1e-3),
+           "hbm_view": {"algorithmic_bytes": element_steps * PER_BYTES_PER_ELEMENT_STEP,
+                        "achieved_gbs": element_steps * PER_BYTES_PER_ELEMENT_STEP / (dev_ms * 1e-3) / 1e9},
+           "e2e": {"ms": host_s * 1e3, "element_steps_per_s": element_steps / host_s, "h2d_bytes": nbytes,
+                   "d2h_bytes": nbytes, "api": "acum_preprocess_per (pinned host arrays in and out)"},
+           "host_call_equals_device_call": bool(host_equal)}
+    if cpu:
+        from oracle import oracle as O
+        ns = 512
+        f64 = lambda a: a[:ns].astype(np.float64)
+        t0 = time.perf_counter()
+        want = O.preprocess_per(f64(arrs[0]), f64(arrs[1]), f64(arrs[3]), f64(arrs[4]), *args)
+        cpu_s = time.perf_counter() - t0
+        out["bit_equal_to_oracle_sample"] = bool(all(
+            np.array_equal(g[:ns], w.astype(np.float32)) for g, w in zip(got, want)))
+        out["cpu_baseline"] = {"element_steps_per_s": ns * T / cpu_s, "cores": 1, "kind": "port",
+                               "sample": "first %d of %d elements, all steps (oracle preprocess_per, FP64)" % (
+                                   ns, n_elem)}
+    return out
+
+
 def batch_leg(native, device, steps=1, inflight=6):
     """Workload 4: 64 seeded rotor cases (2-6 blades, 500-20000 elements per blade, 180-1440
     steps, 64-2048 observers) resident on the GPU and solved in mixed precision (a) by one
@@ -319,6 +411,7 @@ def main():
     ap.add_argument("--no-bpm", action="store_true", help="skip the broadband leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg (workload 3)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched leg (workload 4)")
+    ap.add_argument("--no-permeable", action="store_true", help="skip the permeable preprocessing leg")
     ap.add_argument("--batch-steps", type=int, default=1, help="timed runs per mode of the batched leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if not args.small else args.warmup
@@ -475,6 +568,9 @@ def main():
         out["bpm"] = bpm
     if not args.no_adjoint:
         out["adjoint"] = adjoint_leg(native, local)
+    if not args.no_permeable:
+        out["permeable"] = permeable_leg(native, local, steps=max(1, args.steps // 2), cpu=not args.no_cpu,
+                                         n_elem=2048 if args.small else 8192)
     if rank == 0 and not args.no_cpu:
         nth = os.cpu_count() or 1
         v, info = cpu_baseline(deck, args.cpu_obs, nth)

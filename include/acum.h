@@ -287,6 +287,14 @@ int acum_preprocess_per_f64(double* Xham, double* Nham, double* Vham, double* Uh
                             const int* XPtr, const int* NPtr, const int* VPtr, const int* UPtr, const int* PRPtr,
                             const int* E, int nTime, double dTau, double a0, double rhoRef, double Mref,
                             double CFDscale, int periodic, int lowpass);
+/* The same on arrays already in device memory (float, or double when is_double = 1), for
+ * a caller whose surface data is on the GPU; XPtr ... PRPtr and E are host arrays.  Work
+ * is enqueued on `stream` (NULL = the default stream) and the call returns without
+ * waiting for it. */
+int acum_preprocess_per_device(void* Xham, void* Nham, void* Vham, void* Uham, void* PRham, int is_double, int nSurf,
+                               const int* XPtr, const int* NPtr, const int* VPtr, const int* UPtr, const int* PRPtr,
+                               const int* E, int nTime, double dTau, double a0, double rhoRef, double Mref,
+                               double CFDscale, int periodic, int lowpass, void* stream);
 
 /* Replaces findBBnoise (bb_core.cu:11) as called at main.cu:274: the same 39 arguments,
  * host pointers, FP32 storage; BBspl [nObs][nf2][7] and BBoaspl [nObs] are updated as the

@@ -101,3 +101,31 @@ def test_refused_sizes():
     with pytest.raises(native.AcumError) as e:
         native.preprocess_per([1], X, N, np.zeros_like(N), U, PR, 0.01, 340.0, 1.2, 0.08, 1.0, 1, 0)
     assert e.value.code == ERR_UNSUPPORTED
+
+
+def test_device_entry_matches_host_entry():
+    """acum_preprocess_per_device on arrays already in device memory (torch tensors, on a
+    side stream) gives the host entry's results, float and double."""
+    torch = pytest.importorskip("torch")
+    native = _native()
+    lib = native.lib()
+    ne, T = [6, 9], 144
+    X, N, U, PR = synth.permeable_rows(48, ne, T)
+    args = (0.0031, 340.0, 1.2, 0.08, 1.3, 1, 1)
+    off = np.concatenate([[0], np.cumsum(ne)[:-1]])
+    ptrs = [np.ascontiguousarray(off * T * w, dtype=np.int32) for w in (4, 6, 6, 6, 4)]
+    E = np.array(ne, np.int32)
+    vp = lambda a: a.ctypes.data_as(C.c_void_p)
+    for dt, tdt in ((np.float64, torch.float64), (np.float32, torch.float32)):
+        if dt == np.float32:  # the float host entry takes float scalars
+            args = tuple(float(np.float32(x)) for x in args[:5]) + args[5:]
+        want = native.preprocess_per(ne, X, N, np.zeros_like(N), U, PR, *args, dtype=dt)
+        dev = [torch.tensor(np.asarray(a, dt), device="cuda:0") for a in (X, N, np.zeros_like(N), U, PR)]
+        s = torch.cuda.Stream()
+        with torch.cuda.stream(s):
+            rc = lib.acum_preprocess_per_device(*[C.c_void_p(t.data_ptr()) for t in dev], int(dt == np.float64), 2,
+                                                *[vp(q) for q in ptrs], vp(E), T, *args, C.c_void_p(s.cuda_stream))
+        assert rc == 0, lib.acum_last_global_error()
+        s.synchronize()
+        for nm, t, w in zip("XNVUP", dev, want):
+            np.testing.assert_array_equal(t.cpu().numpy(), w, err_msg=nm)
