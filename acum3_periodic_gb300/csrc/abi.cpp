@@ -972,10 +972,12 @@ struct PerLayout {
 };
 
 int per_layout(int nSurf, const int* XPtr, const int* NPtr, const int* VPtr, const int* UPtr, const int* PRPtr,
-               const int* E, int nTime, PerLayout& L)
+               const int* E, int nTime, double dTau, PerLayout& L)
 {
     if (!XPtr || !NPtr || !VPtr || !UPtr || !PRPtr || !E || nSurf <= 0 || nTime < 6)
         return fail(nullptr, ACUM_ERR_INVALID, "preprocess_per: bad argument (nTime must be at least 6)");
+    if (!(dTau > 0.0) || !std::isfinite(dTau))
+        return fail(nullptr, ACUM_ERR_INVALID, "preprocess_per: dTau must be positive and finite");
     if (nTime > acum::kMaxPerSteps)
         return fail(nullptr, ACUM_ERR_UNSUPPORTED, "preprocess_per: more than 4096 steps per period");
     const int width[5] = {4, 6, 6, 6, 4};
@@ -1016,7 +1018,8 @@ int per_enqueue(void* const d[5], bool is_double, const PerLayout& L, int nTime,
         a.proff = off + 4 * L.etot;
         a.E = (int)L.etot;
         a.T = nTime;
-        a.dTau = dTau;
+        a.two_dt = 2.0 * dTau;
+        a.inv_two_dt = 1.0 / a.two_dt;
         a.a0 = a0;
         a.a02 = pow(a0, 2);
         a.rhoRef = rhoRef;
@@ -1050,7 +1053,7 @@ int preprocess_per_t(S* Xham, S* Nham, S* Vham, S* Uham, S* PRham, int nSurf, co
     if (!Xham || !Nham || !Vham || !Uham || !PRham)
         return fail(nullptr, ACUM_ERR_INVALID, "preprocess_per: null array");
     PerLayout L;
-    int rc = per_layout(nSurf, XPtr, NPtr, VPtr, UPtr, PRPtr, E, nTime, L);
+    int rc = per_layout(nSurf, XPtr, NPtr, VPtr, UPtr, PRPtr, E, nTime, dTau, L);
     if (rc != ACUM_OK || L.etot == 0) return rc;
     int dev = 0;
     cudaError_t ce = cudaGetDevice(&dev);
@@ -1106,7 +1109,7 @@ extern "C" int acum_preprocess_per_device(void* Xham, void* Nham, void* Vham, vo
     if (!Xham || !Nham || !Vham || !Uham || !PRham)
         return fail(nullptr, ACUM_ERR_INVALID, "preprocess_per: null array");
     PerLayout L;
-    int rc = per_layout(nSurf, XPtr, NPtr, VPtr, UPtr, PRPtr, E, nTime, L);
+    int rc = per_layout(nSurf, XPtr, NPtr, VPtr, UPtr, PRPtr, E, nTime, dTau, L);
     if (rc != ACUM_OK || L.etot == 0) return rc;
     void* d[5] = {Xham, Nham, Vham, Uham, PRham};
     return per_enqueue(d, is_double != 0, L, nTime, dTau, a0, rhoRef, Mref, CFDscale, periodic, lowpass,

@@ -114,7 +114,8 @@ struct PerArgs {
     const long long* uoff;  // ... in Uham
     const long long* proff; // ... in PRham (4 per step)
     int E, T;
-    double dTau, a0, a02, rhoRef, mref2, cfd;  // a02 = pow(a0, 2), mref2 = pow(Mref, 2)
+    double two_dt, inv_two_dt;                 // 2 dTau and RN(1 / (2 dTau))
+    double a0, a02, rhoRef, mref2, cfd;        // a02 = pow(a0, 2), mref2 = pow(Mref, 2)
     int periodic, lowpass;
     double gauss[13];
 };

@@ -9,6 +9,9 @@
 // compiler would contract), so that with double storage the outputs equal the
 // reference's FP64 build bit for bit, and with float storage they are those FP64 results
 // rounded once.  The reference's FP32 build rounds every intermediate to float instead.
+// The kernel is bound by the FP64 pipe: the quotients by 2 dTau are formed from its
+// reciprocal with FMA corrections that give the IEEE quotient (div_by), and the median's
+// comparisons run on integer keys.
 //
 // Work per element: five flow series (rho, u, v, w, P) scaled, optionally filtered (two
 // passes of a 3-point periodic median and a 13-tap periodic Gaussian, preprocess.cu:
@@ -33,22 +36,52 @@ struct PerPtrs {
     S* PR;  // [..][T][4]  P, Pdot, rho, rhodot
 };
 
-// central difference with the reference's division (mathfunc.cu:132-140)
-__device__ __forceinline__ double cdiff(double up, double um, double two_dt) { return (up - um) / two_dt; }
+// Correctly rounded a / b from y = RN(1/b) with FMA corrections: Markstein's theorem
+// (P. Markstein, IBM J. Res. Dev. 34(1), 1990; Cornea-Hasegan, Golliver & Markstein,
+// ARITH-14, 1999, Theorem 1): if y = RN(1/b) and q is within 1 ulp of a/b, then
+// r = a - b q is exact and RN(q + r y) = RN(a/b).  q = RN(a y) followed by one correction
+// is within 1 ulp; the second correction then gives the IEEE quotient, for a/b in the
+// normal range.  A zero numerator keeps its sign through the product a y.  Five FP64
+// operations instead of a full division (the FP64 pipe bounds this kernel).
+__device__ __forceinline__ double div_by(double a, double b, double y)
+{
+    double q = __dmul_rn(a, y);
+    double r = __fma_rn(-q, b, a);
+    q = __fma_rn(r, y, q);
+    r = __fma_rn(-q, b, a);
+    q = __fma_rn(r, y, q);
+    return a == 0.0 ? __dmul_rn(a, y) : q;
+}
+
+// central difference with the reference's division (mathfunc.cu:132-140);
+// y = RN(1 / two_dt)
+__device__ __forceinline__ double cdiff(double up, double um, double two_dt, double y)
+{
+    return div_by(up - um, two_dt, y);
+}
+
+// A key whose signed-integer order is the order of the (non-NaN) doubles, -0 and +0
+// equal: the median's comparisons run on the integer pipe instead of the FP64 pipe.
+__device__ __forceinline__ long long order_key(double v)
+{
+    long long b = __double_as_longlong(v);
+    b = b == (long long)0x8000000000000000ULL ? 0LL : b;
+    return b < 0 ? (b ^ 0x7FFFFFFFFFFFFFFFLL) : b;
+}
 
 // d/dtau of the series in row `src` at step t: periodic, or the end-biased form
 // (mathfunc.cu:142-159: central interior, ends from 3 du[1] - 3 du[2] + du[3])
-__device__ __forceinline__ double series_deriv(const double* src, int t, int T, double two_dt, bool biased)
+__device__ __forceinline__ double series_deriv(const double* src, int t, int T, double two_dt, double y, bool biased)
 {
     if (!biased || (t > 0 && t < T - 1)) {
         const int tm = t == 0 ? T - 1 : t - 1, tp = t == T - 1 ? 0 : t + 1;
-        return cdiff(src[tp], src[tm], two_dt);
+        return cdiff(src[tp], src[tm], two_dt, y);
     }
     const int s = t == 0 ? 1 : -1;
     const int k1 = t + s, k2 = t + 2 * s, k3 = t + 3 * s;
-    const double d1 = cdiff(src[k1 + 1], src[k1 - 1], two_dt);
-    const double d2 = cdiff(src[k2 + 1], src[k2 - 1], two_dt);
-    const double d3 = cdiff(src[k3 + 1], src[k3 - 1], two_dt);
+    const double d1 = cdiff(src[k1 + 1], src[k1 - 1], two_dt, y);
+    const double d2 = cdiff(src[k2 + 1], src[k2 - 1], two_dt, y);
+    const double d3 = cdiff(src[k3 + 1], src[k3 - 1], two_dt, y);
     return __dadd_rn(__dsub_rn(__dmul_rn(3.0, d1), __dmul_rn(3.0, d2)), d3);
 }
 
@@ -59,11 +92,9 @@ __device__ void lowpass_rows(double* P, double* Q, int T, const double* w)
     for (int pass = 0; pass < 2; ++pass) {
         for (int t = threadIdx.x; t < T; t += blockDim.x) {
             const double l = P[t == 0 ? T - 1 : t - 1], m = P[t], r = P[t == T - 1 ? 0 : t + 1];
-            double hi = l > m ? l : m;
-            hi = hi > r ? hi : r;
-            double lo = l < m ? l : m;
-            lo = lo < r ? lo : r;
-            Q[t] = (l < hi && l > lo) ? l : ((m < hi && m > lo) ? m : r);
+            const long long kl = order_key(l), km = order_key(m), kr = order_key(r);
+            const long long hi = max(max(kl, km), kr), lo = min(min(kl, km), kr);
+            Q[t] = (kl < hi && kl > lo) ? l : ((km < hi && km > lo) ? m : r);
         }
         __syncthreads();
         for (int t = threadIdx.x; t < T; t += blockDim.x) {
@@ -94,7 +125,7 @@ __global__ void __launch_bounds__(kPerThreads) per_prep_kernel(PerPtrs<S> p, Per
     S* V = p.V + a.voff[e];
     S* U = p.U + a.uoff[e];
     S* PR = p.PR + a.proff[e];
-    const double two_dt = 2.0 * a.dTau;
+    const double two_dt = a.two_dt, y = a.inv_two_dt;
     const bool biased = a.periodic != 1;
 
     // flow series: rho (PR 2), u (U 0..2), P (PR 0), in the reference's order v1..v5
@@ -114,7 +145,7 @@ __global__ void __launch_bounds__(kPerThreads) per_prep_kernel(PerPtrs<S> p, Per
         if (a.lowpass == 1) lowpass_rows(P, Q, T, a.gauss);
         for (int t = threadIdx.x; t < T; t += blockDim.x) {
             col[(size_t)t * stride] = (S)P[t];
-            dcol[(size_t)t * stride] = (S)series_deriv(P, t, T, two_dt, biased);
+            dcol[(size_t)t * stride] = (S)series_deriv(P, t, T, two_dt, y, biased);
         }
         __syncthreads();
     }
@@ -122,7 +153,8 @@ __global__ void __launch_bounds__(kPerThreads) per_prep_kernel(PerPtrs<S> p, Per
     for (int t = threadIdx.x; t < T; t += blockDim.x) {
         const int tm = t == 0 ? T - 1 : t - 1, tp = t == T - 1 ? 0 : t + 1;
         for (int c = 0; c < 3; ++c)
-            N[(size_t)t * 6 + 3 + c] = (S)cdiff((double)N[(size_t)tp * 6 + c], (double)N[(size_t)tm * 6 + c], two_dt);
+            N[(size_t)t * 6 + 3 + c] =
+                (S)cdiff((double)N[(size_t)tp * 6 + c], (double)N[(size_t)tm * 6 + c], two_dt, y);
         // panel area (preprocess.cu:56): (ds CFDscale) CFDscale
         X[(size_t)t * 4 + 3] = (S)((double)X[(size_t)t * 4 + 3] * a.cfd * a.cfd);
     }
@@ -130,12 +162,12 @@ __global__ void __launch_bounds__(kPerThreads) per_prep_kernel(PerPtrs<S> p, Per
     for (int c = 0; c < 3; ++c) {
         for (int t = threadIdx.x; t < T; t += blockDim.x) P[t] = (double)X[(size_t)t * 4 + c] * a.cfd;
         __syncthreads();
-        for (int t = threadIdx.x; t < T; t += blockDim.x) Q[t] = series_deriv(P, t, T, two_dt, false);
+        for (int t = threadIdx.x; t < T; t += blockDim.x) Q[t] = series_deriv(P, t, T, two_dt, y, false);
         __syncthreads();
         for (int t = threadIdx.x; t < T; t += blockDim.x) {
             X[(size_t)t * 4 + c] = (S)P[t];
             V[(size_t)t * 6 + c] = (S)Q[t];
-            V[(size_t)t * 6 + 3 + c] = (S)series_deriv(Q, t, T, two_dt, false);
+            V[(size_t)t * 6 + 3 + c] = (S)series_deriv(Q, t, T, two_dt, y, false);
         }
         __syncthreads();
     }

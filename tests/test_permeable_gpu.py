@@ -97,6 +97,11 @@ def test_refused_sizes():
     with pytest.raises(native.AcumError) as e:  # at least 6 steps
         native.preprocess_per([2], X, N, np.zeros_like(N), U, PR, 0.01, 340.0, 1.2, 0.08, 1.0, 1, 0)
     assert e.value.code == ERR_INVALID
+    X, N, U, PR = synth.permeable_rows(46, [2], 8)
+    for bad_dt in (0.0, -0.01, float("inf")):
+        with pytest.raises(native.AcumError) as e:
+            native.preprocess_per([2], X, N, np.zeros_like(N), U, PR, bad_dt, 340.0, 1.2, 0.08, 1.0, 1, 0)
+        assert e.value.code == ERR_INVALID
     X, N, U, PR = synth.permeable_rows(47, [1], 4097)
     with pytest.raises(native.AcumError) as e:
         native.preprocess_per([1], X, N, np.zeros_like(N), U, PR, 0.01, 340.0, 1.2, 0.08, 1.0, 1, 0)
@@ -129,3 +134,25 @@ def test_device_entry_matches_host_entry():
         s.synchronize()
         for nm, t, w in zip("XNVUP", dev, want):
             np.testing.assert_array_equal(t.cpu().numpy(), w, err_msg=nm)
+
+
+def test_signed_zeros_and_ties():
+    """Series with exact zeros of both signs and repeated values: the median's integer keys
+    treat -0 and +0 as equal (as the reference's comparisons do) and a zero difference
+    keeps the sign the IEEE quotient gives it."""
+    native = _native()
+    ne, T = [3], 40
+    X, N, U, PR = synth.permeable_rows(49, ne, T)
+    U[0, :, 2] = 0.0
+    U[0, ::3, 2] = -0.0
+    U[1, :, 2] = np.where(np.arange(T) % 4 < 2, 1.0, -1.0)
+    PR[2, :, 0] = np.round(PR[2, :, 0], 1)  # ties
+    N[0, :, 2] = -0.0
+    N[0, 5:9, 2] = 0.0
+    args = (0.004, 340.0, 1.2, 0.08, 1.0)
+    for periodic, lowpass in ((1, 1), (0, 1), (1, 0)):
+        want = O.preprocess_per(X, N, U, PR, *args, periodic, lowpass)
+        got = native.preprocess_per(ne, X, N, np.zeros_like(N), U, PR, *args, periodic, lowpass)
+        for nm, a, b in zip("XNVUP", got, want):
+            np.testing.assert_array_equal(a, b, err_msg=nm)
+            assert np.array_equal(np.signbit(a), np.signbit(b)), nm
