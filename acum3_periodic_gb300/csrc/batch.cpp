@@ -540,7 +540,10 @@ extern "C" int acum_batch_autotune(acum_batch* b, int probe_per_sm, double* best
     for (const acum_ctx* c : b->cases) b->Tmax = std::max(b->Tmax, c->T);
     const long target = (long)per_sm * b->num_sms;
     // 1. kernel throughput of every (observers per block, elements per stage): one
-    //    persistent launch over a spread of 32-element items from all cases
+    //    persistent launch over a spread of 128-element items from all cases (items of
+    //    the size real work lists use: with 32-element items the per-item start-up and
+    //    ring fill weigh on the deeper stages and the probe favoured 4 elements per
+    //    stage where 8 are faster)
     const int Ws[] = {8, 12, 16}, SEs[] = {2, 4, 8};
     double best_rate = 0;
     int bw = b->W, bse = b->SE;
@@ -553,7 +556,7 @@ extern "C" int acum_batch_autotune(acum_batch* b, int probe_per_sm, double* best
             b->SE = SE;
             int rc = plan(b);
             if (rc) return rc;
-            const double ev = probe_items(b, W, SE, 32, target, probe);
+            const double ev = probe_items(b, W, SE, 128, target, probe);
             double ms = 0;
             rc = time_items(b, d_probe, probe, &ms);
             if (rc) return rc;
@@ -571,11 +574,11 @@ extern "C" int acum_batch_autotune(acum_batch* b, int probe_per_sm, double* best
     b->SE = bse;
     int rc = plan(b);
     if (rc) return rc;
-    double ev1 = probe_items(b, bw, bse, 32, target, probe), ms1 = 0;
+    double ev1 = probe_items(b, bw, bse, 64, target, probe), ms1 = 0;
     const double n1 = (double)probe.size();
     rc = time_items(b, d_probe, probe, &ms1);
     if (rc) return rc;
-    double ev2 = probe_items(b, bw, bse, 128, target, probe), ms2 = 0;
+    double ev2 = probe_items(b, bw, bse, 256, target, probe), ms2 = 0;
     const double n2 = (double)probe.size();
     rc = time_items(b, d_probe, probe, &ms2);
     if (rc) return rc;

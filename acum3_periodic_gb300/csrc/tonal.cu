@@ -824,7 +824,7 @@ constexpr uint32_t kTmemCols = 512;  // NS x SE / 2 x 40 <= 320 for every stage 
 // the block has consumed before this item, so consecutive items of a block continue the
 // mbarrier phases of the same ring.  On entry every slot is free and all bin rows are
 // zero; on return (without abort) the same holds again.
-template <int SE, int OPW, bool TM>
+template <int SE, int OPW, bool TM, bool HOIST = true>
 __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot, int e0, int e1, unsigned char* smem,
                                            size_t stage_off, MixedShared<SE, OPW>& sh, unsigned& gbase)
 {
@@ -953,18 +953,31 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
                 deposit(acc[q], T, p.tmod, prev, cur[q][j], 0, ok_obs[q] && valid && !(first_win && lane == 0), bad,
                         more);
                 if (lane == 31) sh.carry[warp][(w + 1) & 1][q][j] = cur[q][j];
+                if (!HOIST) {
+                    if (first_win && lane == 0) sh.first[warp][q][j] = cur[q][j];
+                    if (last_win) {
+                        const SmpF lastS = shfl_idx(cur[q][j], min(31, T - 1 - w * kWin));
+                        if (lane == 0) {
+                            bool wrap_more = false;
+                            deposit(acc[q], T, p.tmod, lastS, sh.first[warp][q][j], T, ok_obs[q], bad, wrap_more);
+                            if (wrap_more)
+                                deposit_rest(acc[q], T, p.tmod, lastS, sh.first[warp][q][j], T, ok_obs[q], bad);
+                        }
+                    }
+                }
             }
         }
-        // the first window's samples (kept for the wrap) and the periodic wrap itself are
-        // handled after the stage's deposits, one uniform branch each instead of one per
-        // sample (2.6 % faster at workload 2)
-        if (first_win && lane == 0) {
+        // HOIST: the first window's samples (kept for the wrap) and the periodic wrap itself
+        // are handled after the stage's deposits, one uniform branch each instead of one
+        // per sample (2.6 % faster at workload 2 in the single-deck kernel; the batched
+        // kernel, with more live registers, keeps the per-sample form, which spills less)
+        if (HOIST && first_win && lane == 0) {
 #pragma unroll
             for (int q = 0; q < OPW; ++q)
 #pragma unroll
                 for (int j = 0; j < SE; ++j) sh.first[warp][q][j] = cur[q][j];
         }
-        if (last_win) {
+        if (HOIST && last_win) {
 #pragma unroll
             for (int q = 0; q < OPW; ++q) {
 #pragma unroll
@@ -1151,7 +1164,7 @@ __global__ void __launch_bounds__(512, 1)
         for (int k = threadIdx.x; k < kWords; k += blockDim.x)
             reinterpret_cast<int*>(&sp)[k] = reinterpret_cast<const int*>(cases + it.c)[k];
         __syncthreads();
-        mixed_item<SE, 1, false>(sp, it.ot, it.e0, it.e1, smem, stage_off, sh, gbase);
+        mixed_item<SE, 1, false, false>(sp, it.ot, it.e0, it.e1, smem, stage_off, sh, gbase);
         __syncthreads();
         if (sh.abort) {
             mixed_drain<SE, 1>(smem, stage_off, NS, sh);
