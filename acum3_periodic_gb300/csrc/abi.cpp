@@ -143,7 +143,8 @@ int acum_ctx::upload_deck_common(const acum_inputs& inp, int nob, const float* o
     if (ns <= 0) return fail(this, ACUM_ERR_INVALID, "no surfaces");
     if (inp.impermeable != 1)
         return fail(this, ACUM_ERR_UNSUPPORTED,
-                    "only the impermeable form is implemented (the reference runs no kernel otherwise)");
+                    "impermeable = 0: the reference runs no acoustic kernel for permeable decks "
+                    "(main.cu:236); their preprocessing is acum_preprocess_per");
     if (inp.oM == 0.0 || inp.dPsi == 0.0) return fail(this, ACUM_ERR_INVALID, "oM and dPsi must be non-zero");
     in = inp;
     derive(in, der);
