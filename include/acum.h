@@ -41,7 +41,7 @@ extern "C" {
 #define ACUM_ERR_STATE (-5)       /* call out of order (e.g. a run before a deck) */
 #define ACUM_ERR_TIMEOUT (-6)     /* a bounded device wait ran out; the context stays usable */
 #define ACUM_ERR_GEOMETRY (-7)    /* invalid geometry met on the device (see error word) */
-#define ACUM_ERR_UNSUPPORTED (-8) /* option outside what this build implements */
+#define ACUM_ERR_UNSUPPORTED (-8) /* option outside what the library implements */
 
 /* precision of the tonal forms */
 #define ACUM_PLAIN_FP64 0 /* FP64 end to end; matches the reference's FP64 build */

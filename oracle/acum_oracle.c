@@ -3,8 +3,9 @@
  * periodic acoustic hot path (dilharaj/ACUM3_periodic).
  *
  * TEST INFRASTRUCTURE: this is the oracle.  Only tests/, __graft_entry__.smoke() and the
- * CPU-baseline leg of bench.py may load it, and only as the checker (or as the timed CPU
- * port in that leg).  The GPU product never calls into it.
+ * CPU-baseline leg of bench.py may load it, and only as the reference the GPU results are
+ * compared with (or as the timed CPU port in that leg).  The GPU product never calls into
+ * it.
  *
  * Pinning: tests/test_oracle_pin.py compares every function here with the reference's
  * own sources compiled in FP64 (oracle/build_ref.sh -> oracle/_ref/libacumref_f64.so) on
