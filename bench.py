@@ -205,9 +205,14 @@ def adjoint_leg(native, device):
 
 
 PER_BYTES_PER_ELEMENT_STEP = 140  # float storage: 12 values read (x, y, z, ds, n, u, P, rho), 23 written
+# FP64 instructions per element-step of per_prep_kernel with the filters on: 2 passes x 5
+# series x 13-tap Gaussian (13 DMUL + 13 DADD) = 260, 14 central differences x (1 DADD +
+# 1 DMUL + 4 DFMA + ...) ~ 84, scaling ~ 13 (SASS opcode counters: DMUL 157, DADD 144,
+# DFMA 56)
+PER_FP64_INSTR_PER_ELEMENT_STEP = 357
 
 
-def permeable_leg(native, device, steps=3, cpu=True, n_elem=8192, ntime=1440):
+def permeable_leg(native, device, steps=3, cpu=True, n_elem=8192, ntime=1440, fp64_peak_tflops=None):
     """Permeable-surface preprocessing (preprocess_per) of a data surface of `n_elem`
     elements (two surfaces) over `ntime` steps, filters on (the reference's default
     lowpass = 1), float storage as the reference's arrays: the device-resident call
@@ -281,6 +286,15 @@ def permeable_leg(native, device, steps=3, cpu=True, n_elem=8192, ntime=1440):
            "e2e": {"ms": host_s * 1e3, "element_steps_per_s": element_steps / host_s, "h2d_bytes": nbytes,
                    "d2h_bytes": nbytes, "api": "acum_preprocess_per (pinned host arrays in and out)"},
            "host_call_equals_device_call": bool(host_equal)}
+    if fp64_peak_tflops:
+        # the FP64 pipe bounds the kernel: its instruction rate (one instruction per FMA)
+        instr = PER_FP64_INSTR_PER_ELEMENT_STEP * element_steps / (dev_ms * 1e-3)
+        peak = fp64_peak_tflops * 1e12 / 2.0
+        out["roofline"] = {"bound": "fp64", "achieved": instr, "peak": peak, "unit": "FP64 instructions/s",
+                           "frac": instr / peak,
+                           "fp64_instructions_per_element_step": PER_FP64_INSTR_PER_ELEMENT_STEP,
+                           "peak_source": "measured FP64 FMA throughput of this GPU (acum_measure_peak), "
+                                          "one instruction per FMA; the time is the whole device call"}
     if cpu:
         from oracle import oracle as O
         ns = 512
@@ -570,7 +584,7 @@ def main():
         out["adjoint"] = adjoint_leg(native, local)
     if not args.no_permeable:
         out["permeable"] = permeable_leg(native, local, steps=max(1, args.steps // 2), cpu=not args.no_cpu,
-                                         n_elem=2048 if args.small else 8192)
+                                         n_elem=2048 if args.small else 8192, fp64_peak_tflops=fp64_peak)
     if rank == 0 and not args.no_cpu:
         nth = os.cpu_count() or 1
         v, info = cpu_baseline(deck, args.cpu_obs, nth)
