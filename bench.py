@@ -8,12 +8,15 @@ GB300 arm (default).  One step = one pass of the tonal path over the deck with t
 surface rows already resident in HBM: GPU preprocessing (preprocess_imper) + the
 mixed-precision tonal kernel + the finalize transpose, i.e. acum_tonal_device.  `value`
 is element*observer*step evaluations per second over K timed steps (inputs larger than
-L2: 1.47 GB of surface rows and 2.9 GB of records per step).  `e2e` times the same
-metric through acum_tonal_from_host: pinned host rows in, pA out, copies inside.  The
-plain FP64 form is timed on every 8th observer (512) of the same deck, and the mixed
-result is compared with it there (OASPL dB and per-bin error).  `cpu_baseline` times
-the oracle port (the C restatement of the reference path) on this host's cores on a
-bounded sample of the same deck.
+L2: 1.47 GB of surface rows and 3.7 GB of records per step).  `e2e` times the same
+metric through acum_tonal_from_host_async: pinned host rows in, pA out, copies inside
+(each step's copies overlap the previous step's solve).  The plain FP64 form is timed on
+every 8th observer (512) of the same deck, and the mixed result is compared with it
+there (OASPL dB and per-bin error).  `cpu_baseline` times the oracle port (the C
+restatement of the reference path) on this host's cores on a bounded sample of the
+same deck.  Further legs (each with its own switch): broadband (BPM) on the workload's
+broadband deck, the adjoint on workload 3, the permeable preprocessing of an
+8192-element data surface, and the batched persistent launch on workload 4.
 
 Reference arm (--impl reference).  The reference's CPU implementation of the path: the
 oracle port in oracle/acum_oracle.c (the reference's sources are not shipped with this
