@@ -300,7 +300,7 @@ def permeable_leg(native, device, steps=3, cpu=True, n_elem=8192, ntime=1440, fp
                                           "one instruction per FMA; the time is the whole device call"}
     if cpu:
         from oracle import oracle as O
-        ns = 512
+        ns = min(2048, n_elem)
         f64 = lambda a: a[:ns].astype(np.float64)
         t0 = time.perf_counter()
         want = O.preprocess_per(f64(arrs[0]), f64(arrs[1]), f64(arrs[3]), f64(arrs[4]), *args)

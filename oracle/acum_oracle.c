@@ -236,6 +236,78 @@ int acumo_preprocess(const acumo_tonal* p, const double* raw, double* fields)
     return 0;
 }
 
+/* preprocess.cu:8-226 (preprocess_per), the permeable surfaces' preprocessing, in place
+ * on the elements of all surfaces stacked [element][step][k]: X (x, y, z, ds), N (n,
+ * ndot), V (V, Vdot), U (u, udot), PR (P, Pdot, rho, rhodot); scal = dTau, a0, rhoRef,
+ * Mref, CFDscale.  Scaling (preprocess.cu:50-68, left to right as written there), the
+ * optional low-pass of rho, u, P (113-137, no make_periodic), their derivatives periodic
+ * or end-biased (150-163), ndot periodic (166-168), V = dx/dtau and Vdot = dV/dtau
+ * periodic (172-180). */
+int acumo_preprocess_per(int E, int nt, const double* scal, int periodic, int lowpass, double* X, double* N,
+                         double* V, double* U, double* PR)
+{
+    const double dt = scal[0], a0 = scal[1], rho_ref = scal[2], mref = scal[3], cfd = scal[4];
+    const size_t n = (size_t)E * nt;
+    for (size_t i = 0; i < n; i++) {
+        double* x = X + 4 * i;
+        x[0] = x[0] * cfd;
+        x[1] = x[1] * cfd;
+        x[2] = x[2] * cfd;
+        x[3] = x[3] * cfd * cfd;
+        PR[4 * i + 2] = PR[4 * i + 2] * rho_ref;
+        U[6 * i + 0] = U[6 * i + 0] * a0;
+        U[6 * i + 1] = U[6 * i + 1] * a0;
+        U[6 * i + 2] = U[6 * i + 2] * a0;
+        PR[4 * i + 0] = PR[4 * i + 0] * 0.5 * rho_ref * pow(mref, 2) * pow(a0, 2);
+    }
+    double w[13];
+    o_gauss_taps(w, 13);
+    double* f = (double*)malloc(sizeof(double) * (size_t)nt);
+    double* d = (double*)malloc(sizeof(double) * (size_t)nt);
+    double* g = (double*)malloc(sizeof(double) * (size_t)nt);
+    for (int e = 0; e < E; e++) {
+        /* flow series in the reference's order v1..v5: rho, u, v, w, P */
+        double* base[5] = {PR + 2, U + 0, U + 1, U + 2, PR + 0};
+        double* dbase[5] = {PR + 3, U + 3, U + 4, U + 5, PR + 1};
+        const int stride[5] = {4, 6, 6, 6, 4};
+        for (int v = 0; v < 5; v++) {
+            double* col = base[v] + (size_t)e * nt * stride[v];
+            double* dcol = dbase[v] + (size_t)e * nt * stride[v];
+            for (int k = 0; k < nt; k++) f[k] = col[(size_t)k * stride[v]];
+            if (lowpass == 1)
+                for (int q = 0; q < 2; q++) {
+                    o_median3(f, nt);
+                    o_gauss_filter(f, w, nt, 13);
+                }
+            if (periodic == 1) o_diff_periodic(f, d, dt, nt);
+            else o_diff_biased(f, d, dt, nt);
+            for (int k = 0; k < nt; k++) {
+                col[(size_t)k * stride[v]] = f[k];
+                dcol[(size_t)k * stride[v]] = d[k];
+            }
+        }
+        double* ne = N + (size_t)e * nt * 6;
+        double* xe = X + (size_t)e * nt * 4;
+        double* ve = V + (size_t)e * nt * 6;
+        for (int c = 0; c < 3; c++) {
+            for (int k = 0; k < nt; k++) f[k] = ne[(size_t)k * 6 + c];
+            o_diff_periodic(f, d, dt, nt);
+            for (int k = 0; k < nt; k++) ne[(size_t)k * 6 + 3 + c] = d[k];
+            for (int k = 0; k < nt; k++) f[k] = xe[(size_t)k * 4 + c];
+            o_diff_periodic(f, d, dt, nt);
+            o_diff_periodic(d, g, dt, nt);
+            for (int k = 0; k < nt; k++) {
+                ve[(size_t)k * 6 + c] = d[k];
+                ve[(size_t)k * 6 + 3 + c] = g[k];
+            }
+        }
+    }
+    free(f);
+    free(d);
+    free(g);
+    return 0;
+}
+
 /* ------------------------------------------------------------------ core.cu */
 
 /* core.cu:261-279 -- convected retarded distance: the smaller positive root of

@@ -55,6 +55,7 @@ def lib():
         build()
         L = C.CDLL(LIB)
         L.acumo_preprocess.argtypes = [C.POINTER(_Tonal), _DP, _DP]
+        L.acumo_preprocess_per.argtypes = [C.c_int, C.c_int, _DP, C.c_int, C.c_int] + [_DP] * 5
         L.acumo_tonal_run.argtypes = [C.POINTER(_Tonal), _DP, _DP, C.c_int, C.c_int, _DP, _DP, _DP, C.c_int]
         L.acumo_bpm_run.argtypes = [C.POINTER(_Bpm), _DP, C.c_int, C.c_int, _DP, _DP, C.c_int]
         L.acumo_bpm_prep.argtypes = [C.POINTER(_Bpm), C.c_int, _DP, _DP, _DP, _DP]
@@ -225,7 +226,8 @@ def differentiate(u: np.ndarray, dt: float, biased: bool = False) -> np.ndarray:
 
 
 def preprocess_per(X, N, U, PR, dTau, a0, rhoRef, Mref, CFDscale, periodic=1, lowpass_=0):
-    """preprocess_per (preprocess.cu:8-226), the permeable surfaces' preprocessing, in FP64.
+    """preprocess_per (preprocess.cu:8-226), the permeable surfaces' preprocessing, in FP64
+    (acumo_preprocess_per in acum_oracle.c).
 
     Inputs are one element's series stacked as [element][step][k] (AoS of variables.cu:
     11-42): X (x, y, z, ds), N (n, ndot), U (u, udot), PR (P, Pdot, rho, rhodot); only the
@@ -238,26 +240,9 @@ def preprocess_per(X, N, U, PR, dTau, a0, rhoRef, Mref, CFDscale, periodic=1, lo
     * d/dtau of rho, u, P periodic or end-biased (preprocess.cu:150-163), of n periodic
       (166-168); V = d x/dtau and Vdot = d V/dtau, both periodic (172-180).
     """
-    X = np.array(X, dtype=np.float64)
-    N = np.array(N, dtype=np.float64)
-    U = np.array(U, dtype=np.float64)
-    PR = np.array(PR, dtype=np.float64)
+    X, N, U, PR = (np.array(a, dtype=np.float64, order="C") for a in (X, N, U, PR))
     V = np.zeros(N.shape, np.float64)
-    X[:, :, 0:3] *= CFDscale
-    X[:, :, 3] = X[:, :, 3] * CFDscale * CFDscale  # (ds CFDscale) CFDscale, preprocess.cu:56
-    PR[:, :, 2] *= rhoRef
-    U[:, :, 0:3] *= a0
-    PR[:, :, 0] = PR[:, :, 0] * 0.5 * rhoRef * Mref ** 2 * a0 ** 2  # left to right, as preprocess.cu:66
-    biased = periodic != 1
-    for e in range(X.shape[0]):
-        flow = [PR[e, :, 2], U[e, :, 0], U[e, :, 1], U[e, :, 2], PR[e, :, 0]]
-        if lowpass_ == 1:
-            flow = [lowpass(s) for s in flow]
-        d = [differentiate(s, dTau, biased) for s in flow]
-        PR[e, :, 2], U[e, :, 0], U[e, :, 1], U[e, :, 2], PR[e, :, 0] = flow
-        PR[e, :, 3], U[e, :, 3], U[e, :, 4], U[e, :, 5], PR[e, :, 1] = d
-        for c in range(3):
-            N[e, :, 3 + c] = differentiate(N[e, :, c], dTau)
-            V[e, :, c] = differentiate(X[e, :, c], dTau)
-            V[e, :, 3 + c] = differentiate(V[e, :, c], dTau)
+    scal = np.array([dTau, a0, rhoRef, Mref, CFDscale], np.float64)
+    lib().acumo_preprocess_per(X.shape[0], X.shape[1], _p(scal), int(periodic), int(lowpass_), _p(X), _p(N), _p(V),
+                               _p(U), _p(PR))
     return X, N, V, U, PR
