@@ -88,7 +88,8 @@ def test_bpm_core_random_inputs(tmp_path):
         np.testing.assert_allclose(out.reshape(42, 7), want, rtol=0, atol=1e-9)
 
 
-@pytest.mark.parametrize("rep,ntime,periodic,lowpass", [(31, 24, 1, 1), (32, 61, 0, 0), (33, 200, 1, 0)])
+@pytest.mark.parametrize("rep,ntime,periodic,lowpass", [(31, 24, 1, 1), (32, 61, 0, 0), (33, 200, 1, 0),
+                                                         (34, 6, 0, 1), (35, 7, 1, 1)])
 def test_permeable_preprocessing_random(rep, ntime, periodic, lowpass):
     ne = [2 + rep % 3, 4, 1]
     X, N, U, PR = synth.permeable_rows(rep, ne, ntime)
