@@ -764,7 +764,7 @@ int find_pth(const S* rObs, const S* tObs, S* pT, S* pL, S* pA, const S* Xham, c
     CK(nullptr, cudaMemcpyAsync(hv.data(), vInf, 3 * sizeof(S), cudaMemcpyDeviceToHost, st));
     CK(nullptr, cudaMemcpyAsync(ht.data(), tObs, nTime * sizeof(S), cudaMemcpyDeviceToHost, st));
     CK(nullptr, cudaStreamSynchronize(st));
-    // the walk of core.cu:199-231 assumes the uniform grid main.cu:248 builds
+    // the walk of core.cu:199-231 assumes the uniform grid main.cu:124 builds
     for (int t = 0; t < nTime; ++t) {
         const double want = (double)(S)(t * (S)dPsi);
         if (fabs((double)ht[t] - want) > 1e-6 * fabs(dPsi) * (1 + t))

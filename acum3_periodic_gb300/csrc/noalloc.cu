@@ -1,29 +1,34 @@
 // noalloc.cu -- acum_find_pressure_time_history_noalloc: the reference-shaped tonal
-// drop-in for callers that must not allocate memory.
+// drop-in for callers that must not allocate device memory.
 //
-// Who needs it: code that runs where allocation is not allowed or not safe -- inside a
-// host callback or a custom allocator's own call path, in a solver that has handed all
-// device memory to a pool it does not share, or between the capture of stream work
-// that must not be split by cudaMalloc/cudaFree (which synchronise the device).  Such a
-// caller still owns and passes its inputs and outputs; what the computation needs besides
-// them (the tiled per-step records and the FP64 bin sums) lives here in one fixed array
-// of device memory that every GPU loading this library reserves until process exit.
+// Who needs it: a solver or plugin host that has handed all device memory to its own pool
+// allocator and forbids its components to allocate outside it (a cudaMalloc there fails
+// for lack of memory or escapes the host's accounting), and a latency-bound loop that
+// cannot afford cudaMalloc/cudaFree, which synchronise the whole device and so stall the
+// loop's other streams.  Such a caller still owns and passes its inputs and outputs; what
+// the computation needs besides them (the tiled per-step records, the FP64 bin sums and
+// the device error word) lives here in one fixed array of device memory that every GPU
+// loading this library reserves until process exit.
 //
 // Limits and behaviour:
 //  * the scratch array is kNoAllocBytes = 128 MiB per device; a call whose records
-//    (80 bytes per element-step, elements rounded up to 4 and steps to 32) plus FP64 bin
+//    (80 bytes per element-step, elements rounded up to 8 and steps to 32) plus FP64 bin
 //    sums (16 bytes per observer-step) exceed it is rejected with ACUM_ERR_INVALID and a
-//    message that gives both sizes;
+//    message that gives both sizes; at most kMaxSurfaces surfaces;
+//  * it accepts the inputs the allocating drop-in accepts (nTime >= 4, tObs[t] = t * dPsi
+//    within the same tolerance) and refuses the others with the same status;
 //  * the first call on a device looks up the array's device address (cudaGetSymbolAddress)
-//    with that device current; make that first call before capturing stream work into a
-//    CUDA graph;
+//    with that device current; make that first call before any stream capture;
+//  * every call synchronises `stream` before it returns: it reads E, vInf and tObs back
+//    to the host, and after the kernels the device error word;
 //  * every call reuses the same array and leaves its contents behind; the call clears
 //    what must start at zero itself, and two calls whose GPU work overlaps (different
 //    streams or threads without ordering) race on the array -- serialise them;
-//  * no cudaMalloc/cudaFree, no host heap allocation: the small per-surface arrays are
-//    read into fixed stack buffers (at most kMaxSurfaces surfaces).
+//  * no cudaMalloc/cudaFree, no host heap allocation: the small per-surface arrays and
+//    tObs (in pieces) are read into fixed stack buffers.
 #include <cuda_runtime.h>
 #include <stdio.h>
+#include <math.h>
 #include <string.h>
 
 #include <mutex>
@@ -42,7 +47,9 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 static std::mutex g_na_mu;
 static void* g_na_ptr[kMaxDevices];
-static char g_na_msg[256];
+// the last message of this thread (no lock, no heap)
+static thread_local char g_na_msg[256];
+constexpr int kTobsPiece = 1024;  // tObs is checked in pieces of this many steps
 
 // Records straight from the reference's AoS arrays; the element's surface and offsets
 // are found from E[] and the X/N/V/PR pointer arrays on the device (no host tables).
@@ -99,16 +106,15 @@ extern "C" int acum_find_pressure_time_history_noalloc(const float* rObs, const 
                                                        const float* vInf, float oM, void* stream)
 {
     acum::NvtxRange nvtx_range_("acum_find_pressure_time_history_noalloc");
-    (void)tObs;
     auto bad = [](int code, const char* m) {
         snprintf(g_na_msg, sizeof g_na_msg, "%s", m);
         return code;
     };
-    if (!rObs || !pT || !pL || !pA || !Xham || !Nham || !Vham || !PRham || !XPtr || !NPtr || !VPtr || !PRPtr || !E ||
-        !vInf)
+    if (!rObs || !tObs || !pT || !pL || !pA || !Xham || !Nham || !Vham || !PRham || !XPtr || !NPtr || !VPtr ||
+        !PRPtr || !E || !vInf)
         return bad(ACUM_ERR_INVALID, "findPressureTimeHistory_noalloc: null argument");
-    if (nSurf <= 0 || nSurf > kMaxSurfaces || nObs <= 0 || nTime < 6)
-        return bad(ACUM_ERR_INVALID, "findPressureTimeHistory_noalloc: sizes (1..256 surfaces, nTime >= 6)");
+    if (nSurf <= 0 || nSurf > kMaxSurfaces || nObs <= 0 || nTime < 4)
+        return bad(ACUM_ERR_INVALID, "findPressureTimeHistory_noalloc: sizes (1..256 surfaces, nTime >= 4)");
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
         return bad(ACUM_ERR_CUDA, "findPressureTimeHistory_noalloc: no current device");
@@ -133,6 +139,21 @@ extern "C" int acum_find_pressure_time_history_noalloc(const float* rObs, const 
         cudaMemcpyAsync(hv, vInf, 3 * sizeof(float), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
         return bad(ACUM_ERR_CUDA, "findPressureTimeHistory_noalloc: reading E/vInf failed");
+    // the kernel bins on the uniform grid main.cu:124 builds; refuse another tObs, with the
+    // tolerance of the allocating drop-in
+    for (int t0 = 0; t0 < nTime; t0 += kTobsPiece) {
+        float ht[kTobsPiece];
+        const int n = nTime - t0 < kTobsPiece ? nTime - t0 : kTobsPiece;
+        if (cudaMemcpyAsync(ht, tObs + t0, n * sizeof(float), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            return bad(ACUM_ERR_CUDA, "findPressureTimeHistory_noalloc: reading tObs failed");
+        for (int k = 0; k < n; ++k) {
+            const int t = t0 + k;
+            const double want = (double)(float)(t * dPsi);
+            if (fabs((double)ht[k] - want) > 1e-6 * fabs((double)dPsi) * (1 + t))
+                return bad(ACUM_ERR_UNSUPPORTED, "findPressureTimeHistory_noalloc: tObs must be t*dPsi");
+        }
+    }
     long long Et = 0;
     for (int i = 0; i < nSurf; ++i) {
         if (hE[i] < 0) return bad(ACUM_ERR_INVALID, "findPressureTimeHistory_noalloc: negative element count");
@@ -160,6 +181,8 @@ extern "C" int acum_find_pressure_time_history_noalloc(const float* rObs, const 
     noalloc_records_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(Xham, Nham, Vham, PRham, E, XPtr, NPtr, VPtr,
                                                                    PRPtr, nSurf, (int)Et, nTime, nW, a0, rhoRef,
                                                                    (double)hv[0], (double)hv[1], (double)hv[2], rec);
+    if (cudaGetLastError() != cudaSuccess)
+        return bad(ACUM_ERR_CUDA, "findPressureTimeHistory_noalloc: launch of the records kernel failed");
     int sms = 0, optin = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);

@@ -21,7 +21,7 @@
 //                       writes -- no atomics.
 //  tonal_batch_kernel   the same work items of many decks in one persistent launch.
 //  tonal_f64_kernel     the plain FP64 form, same structure.
-//  finalize_kernel      [obs][bin][2] sums -> pT/pL/pA [bin][obs] (main.cu:224 layout).
+//  finalize_kernel      [obs][bin][2] sums -> pT/pL/pA [bin][obs] (main.cu:123-130 layout).
 //
 // Precision forms.  FP64: every quantity in double, observer time in radians as the
 // reference forms it; matches the reference's FP64 build.  Mixed: the integrand in FP32;

@@ -5,10 +5,10 @@
  *
  *  1. Reference-shaped drop-ins.  Same arguments, same meaning and the same accumulate
  *     semantics as the two hot-path calls of the reference driver, so a maintainer can
- *     swap them in at main.cu:360 and main.cu:274 with no other change:
- *       acum_find_pressure_time_history      replaces core.cu:18 (launched at main.cu:360)
+ *     swap them in at main.cu:236 and main.cu:150 with no other change:
+ *       acum_find_pressure_time_history      replaces core.cu:18 (launched at main.cu:236)
  *       acum_find_pressure_time_history_f64  the same call on the FP64 build's arrays
- *       acum_find_bb_noise                   replaces bb_core.cu:11 (called at main.cu:274)
+ *       acum_find_bb_noise                   replaces bb_core.cu:11 (called at main.cu:150)
  *       acum_preprocess_imper                replaces preprocess.cu:228 on caller arrays
  *       acum_preprocess_per(_f64)            replaces preprocess.cu:8 (main.cu:87, permeable)
  *
@@ -123,7 +123,7 @@ int acum_preprocess(acum_ctx* ctx);
  * x,y,z,ds, n(3), ndot(3), V(3), Vdot(3), P, Pdot (the contents of Xham/Nham/Vham/PRham). */
 int acum_get_fields(acum_ctx* ctx, double* host_fields);
 
-/* Tonal noise.  Outputs [nTime][nObs] (main.cu:224 layout), overwritten, host memory;
+/* Tonal noise.  Outputs [nTime][nObs] (main.cu:123-130 layout), overwritten, host memory;
  * any of pT/pL/pA may be NULL.  Preprocesses first if needed. */
 int acum_tonal(acum_ctx* ctx, int precision, double* pT, double* pL, double* pA);
 
@@ -158,7 +158,7 @@ int acum_tonal_from_host_async(acum_ctx* ctx, int precision, const float* raw, d
 int acum_stream(acum_ctx* ctx, void** stream);
 
 /* Broadband: BBspl [nObs][42][7] and BBoaspl [nObs] in dB (bb_core.cu:563-583 layout),
- * host memory, overwritten (the -100 dB seeding of main.cu:256-266 is applied inside).
+ * host memory, overwritten (the -100 dB seeding of main.cu:132-142 is applied inside).
  * aa_mode selects the convected emission time of bb_core.cu:517-520: 0 uses
  * aa = a0^2 - |vInf|^2 (the formula's intent), 1 uses aa = 0 (the value the reference's
  * uninitialised variable takes in a zero-initialising build). */
@@ -222,7 +222,7 @@ int acum_host_free(void* p);
 
 /* ------------------------------------------------- reference-shaped drop-ins */
 
-/* Replaces findPressureTimeHistory (core.cu:18) as launched at main.cu:360: the same
+/* Replaces findPressureTimeHistory (core.cu:18) as launched at main.cu:236: the same
  * arguments, all device pointers, FP32 storage; accumulates into pT, pL, pA [nTime][nObs].
  * The arrays are those preprocess_imper produced (AoS Xham/Nham/Vham/PRham with the
  * XPtr/NPtr/VPtr/PRPtr offsets and E[] counts, all in device memory as the reference
@@ -244,16 +244,19 @@ int acum_find_pressure_time_history_f64(const double* rObs, const double* tObs, 
                                         double oM, void* stream);
 
 /* The same call as acum_find_pressure_time_history for callers that cannot allocate
- * memory (no counterpart in the reference): code running where cudaMalloc/cudaFree are
- * not allowed or would synchronise work that must not be split, or a solver whose device
- * memory is all in its own pool.  It allocates nothing -- no cudaMalloc, no host heap --
- * and uses a fixed 128 MiB scratch array in device memory that every GPU loading this
- * library holds until exit.  Limit: records (80 B per element-step, elements rounded up to
- * 4 and steps to 32) plus 16 B per observer-step must fit in 128 MiB, else ACUM_ERR_INVALID
- * (acum_noalloc_last_error() gives the sizes); at most 256 surfaces.  The first call on a
- * device looks up the scratch address (with that device current), so make it before any
- * stream capture.  All calls share the scratch: calls whose GPU work overlaps race, so
- * serialise them.  tObs is not read (the grid is t*dPsi, as main.cu:248 builds it). */
+ * device memory (no counterpart in the reference): a solver or plugin host that has given
+ * all device memory to its own pool and forbids allocations outside it, or a latency-bound
+ * loop that cannot afford cudaMalloc/cudaFree, which synchronise the whole device.  It
+ * allocates nothing -- no cudaMalloc, no host heap -- and uses a fixed 128 MiB scratch
+ * array in device memory that every GPU loading this library holds until exit.  Limit:
+ * records (80 B per element-step, elements rounded up to 8 and steps to 32) plus 16 B per
+ * observer-step must fit in 128 MiB, else ACUM_ERR_INVALID (acum_noalloc_last_error()
+ * gives the sizes); at most 256 surfaces.  Otherwise it accepts and refuses the inputs the
+ * allocating call does (nTime >= 4; tObs[t] = t*dPsi, as main.cu:124 builds it, else
+ * ACUM_ERR_UNSUPPORTED).  The first call on a device looks up the scratch address (with
+ * that device current); make that first call before any stream capture.  Every call
+ * synchronises `stream` before it returns.  All calls share the scratch: calls whose GPU
+ * work overlaps race, so serialise them.  acum_noalloc_last_error() is per host thread. */
 int acum_find_pressure_time_history_noalloc(const float* rObs, const float* tObs, float* pT, float* pL, float* pA,
                                             const float* Xham, const float* Nham, const float* Vham,
                                             const float* PRham, int nSurf, const int* XPtr, const int* NPtr,
@@ -296,7 +299,7 @@ int acum_preprocess_per_device(void* Xham, void* Nham, void* Vham, void* Uham, v
                                const int* E, int nTime, double dTau, double a0, double rhoRef, double Mref,
                                double CFDscale, int periodic, int lowpass, void* stream);
 
-/* Replaces findBBnoise (bb_core.cu:11) as called at main.cu:274: the same 39 arguments,
+/* Replaces findBBnoise (bb_core.cu:11) as called at main.cu:150: the same 39 arguments,
  * host pointers, FP32 storage; BBspl [nObs][nf2][7] and BBoaspl [nObs] are updated as the
  * reference does (they arrive seeded, normally with -100 dB).  Computes on the GPU with
  * aa_mode 0 (see acum_bpm). */

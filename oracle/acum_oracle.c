@@ -21,7 +21,7 @@
  *   fields [element][step][18]  x,y,z,ds | n(3),ndot(3) | V(3),Vdot(3) | P,Pdot
  *          (the per-element-step contents of Xham/Nham/Vham/PRham, variables.cu:54)
  *   obs    [observer][3]        positions after OBSscale (io.cu:123-129)
- *   pT/pL/pA [step][observer]   as main.cu:224-254
+ *   pT/pL/pA [step][observer]   as main.cu:123-130
  */
 #include <math.h>
 #include <stdlib.h>
@@ -1005,7 +1005,7 @@ static void* o_bpm_shard(void* arg)
 }
 
 /* findBBnoise (bb_core.cu:11-586) over observers [obs0, obs0+nob).  spl[nob][nf][7] and
- * oaspl[nob] must arrive seeded (-100 dB in the reference driver, main.cu:256-266). */
+ * oaspl[nob] must arrive seeded (-100 dB in the reference driver, main.cu:132-142). */
 int acumo_bpm_run(const acumo_bpm* B, const double* obs, int obs0, int nob, double* spl, double* oaspl, int nthreads)
 {
     int nt = B->ntime;

@@ -5,12 +5,13 @@
 #   libacumref_f32.so  the sources as written (float storage), host C++
 #   libacumref_f64.so  the same sources with `float` promoted to `double` (ref_shim.h),
 #                      i.e. the FP64 build that the plain tonal form is held to
-#   core_sm103a.cubin  the reference's tonal kernel (core.cu) for the GPU, and
-#   core_sm103a.ptx    the same as PTX (oracle/ref_gpu.py times it on the GPU)
+#   core_sm103a.cubin  the reference's tonal kernel (core.cu) for the GPU (oracle/ref_gpu.py
+#                      times it there)
 #
 # TEST INFRASTRUCTURE ONLY.  Only the tests, the smoke check and bench.py's CPU baseline
 # leg may load these libraries.  They are built from the reference source tree in place;
-# on a machine without that tree the script exits 0 and builds nothing.
+# on a machine without that tree the script exits 0 and builds nothing.  The tree is
+# ACUM_REF_DIR when that is set, else the location this recipe was written for.
 #
 # Flags: -ftrivial-auto-var-init=zero makes the uninitialised locals of bb_core.cu
 # (notably `aa` in the convected-time formula at bb_core.cu:520) read as zero instead of
@@ -40,11 +41,9 @@ wait $P2
 mv "$OUT/libacumref_f32.so.tmp" "$OUT/libacumref_f32.so"
 mv "$OUT/libacumref_f64.so.tmp" "$OUT/libacumref_f64.so"
 echo "build_ref: built $OUT/libacumref_f32.so $OUT/libacumref_f64.so"
-# The reference's own tonal kernel (core.cu:18) for the GPU, unmodified: a cubin for
-# sm_103a and the same as PTX for the driver to compile where the cubin is not kept.
+# The reference's own tonal kernel (core.cu:18) for the GPU, unmodified: a cubin for sm_103a.
 NVCC="${NVCC:-nvcc}"
 if command -v "$NVCC" > /dev/null 2>&1; then
     "$NVCC" -cubin -gencode arch=compute_103a,code=sm_103a -O3 -I"$REF" "$REF/core.cu" -o "$OUT/core_sm103a.cubin"
-    "$NVCC" -ptx -arch=compute_103a -O3 -I"$REF" "$REF/core.cu" -o "$OUT/core_sm103a.ptx"
-    echo "build_ref: built $OUT/core_sm103a.cubin $OUT/core_sm103a.ptx"
+    echo "build_ref: built $OUT/core_sm103a.cubin"
 fi

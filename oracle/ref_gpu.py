@@ -1,8 +1,7 @@
 """MEASUREMENT INFRASTRUCTURE ONLY (the reference's own GPU tonal kernel as a baseline).
 
 Loads the reference's tonal kernel, `findPressureTimeHistory` (core.cu:18), compiled
-unmodified for sm_103a by oracle/build_ref.sh into oracle/_ref/core_sm103a.cubin (or its
-PTX), and launches it through the CUDA driver API with the launch shape main.cu:193-236
+unmodified for sm_103a by oracle/build_ref.sh into oracle/_ref/core_sm103a.cubin, and launches it through the CUDA driver API with the launch shape main.cu:194-236
 computes (blocks of 8 steps x 4 observers x 8 elements, at most 512 blocks per axis), on
 the reference's AoS arrays (variables.cu:54: Xham, Nham, Vham, PRham with the XPtr /
 NPtr / VPtr / PRPtr offsets) of a synthetic deck.  The AoS fields are this library's
@@ -54,22 +53,18 @@ def check(cu, rc, what):
 
 def load_kernel(cu):
     mod = C.c_void_p()
-    last = None
-    for name in ("core_sm103a.cubin", "core_sm103a.ptx"):
-        path = os.path.join(HERE, "_ref", name)
-        if not os.path.exists(path):
-            continue
-        rc = cu.cuModuleLoad(C.byref(mod), path.encode())
-        if rc == 0:
-            fn = C.c_void_p()
-            check(cu, cu.cuModuleGetFunction(C.byref(fn), mod, ENTRY), "cuModuleGetFunction")
-            return mod, fn, name
-        last = rc
-    raise RuntimeError("reference kernel not loadable (oracle/_ref/core_sm103a.* missing or rejected: %s)" % last)
+    name = "core_sm103a.cubin"
+    path = os.path.join(HERE, "_ref", name)
+    if not os.path.exists(path):
+        raise RuntimeError("reference kernel not built (oracle/_ref/%s missing)" % name)
+    check(cu, cu.cuModuleLoad(C.byref(mod), path.encode()), "cuModuleLoad")
+    fn = C.c_void_p()
+    check(cu, cu.cuModuleGetFunction(C.byref(fn), mod, ENTRY), "cuModuleGetFunction")
+    return mod, fn, name
 
 
 def launch_shape(nTime, nObs):
-    """main.cu:193-221"""
+    """main.cu:194-233"""
     ntpb_x, ntpb_y, ntpb_z, nb_max = 8, 4, 8, 512
     cround = lambda v: int(math.floor(v + 0.5))  # C round(): halves away from zero
     nb_t = min(cround(float(nTime // ntpb_x) + 0.5), nb_max)

@@ -7,11 +7,11 @@
  * under tests/golden/.  The product never links or loads this file.
  *
  * The harness replays what main.cu does around the two hot-path calls, minus CUDA:
- *   read_inputs / read_BB_inputs / read_observers / read_surf     (main.cu:180-202)
- *   preprocess_imper                                             (main.cu:212)
- *   tObs[t] = t*dPsi, pT/pL/pA zeroed, BBspl/BBoaspl set to -100   (main.cu:247-266)
- *   findBBnoise(...)                                             (main.cu:274)
- *   findPressureTimeHistory(...) run serially on the host        (main.cu:360)
+ *   read_inputs / read_BB_inputs / read_observers / read_surf     (main.cu:56-78)
+ *   preprocess_imper                                             (main.cu:88)
+ *   tObs[t] = t*dPsi, pT/pL/pA zeroed, BBspl/BBoaspl set to -100   (main.cu:122-142)
+ *   findBBnoise(...)                                             (main.cu:150)
+ *   findPressureTimeHistory(...) run serially on the host        (main.cu:236)
  * Every array crosses this boundary as double; in the FP32 build values are narrowed to
  * float on the way in (all fixtures hold float32-exact values, so nothing is lost).
  */
@@ -78,7 +78,7 @@ static void quiet_off(int q)
 
 extern "C" int acumref_real_bytes(void) { return (int)sizeof(real); }
 
-/* Reads a deck directory with the reference's own readers (main.cu:180-202). */
+/* Reads a deck directory with the reference's own readers (main.cu:56-78). */
 extern "C" int acumref_load(const char* dir, int quiet)
 {
     char cwd[4096];
@@ -144,7 +144,7 @@ extern "C" int acumref_preprocess(int quiet)
 }
 
 /* Serial run of findPressureTimeHistory (core.cu:18) over observers
- * [obs0, obs0+nob); outputs are [nTime][nob] (main.cu:224-254 layout). */
+ * [obs0, obs0+nob); outputs are [nTime][nob] (main.cu:123-130 layout). */
 extern "C" int acumref_tonal(int obs0, int nob, double* pTo, double* pLo, double* pAo, int quiet)
 {
     if (obs0 < 0 || nob <= 0 || obs0 + nob > nObs) return -1;
@@ -164,7 +164,7 @@ extern "C" int acumref_tonal(int obs0, int nob, double* pTo, double* pLo, double
 }
 
 /* findBBnoise (bb_core.cu:11) over observers [obs0, obs0+nob); outputs are
- * BBspl[nob][nf2][7] and BBoaspl[nob], both seeded with -100 dB as main.cu:256-266. */
+ * BBspl[nob][nf2][7] and BBoaspl[nob], both seeded with -100 dB as main.cu:132-142. */
 extern "C" int acumref_bpm(int obs0, int nob, double* splo, double* oaslo, int quiet)
 {
     if (BB_noise != 1 || obs0 < 0 || nob <= 0 || obs0 + nob > nObs) return -1;

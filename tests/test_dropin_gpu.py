@@ -1,7 +1,7 @@
 """The reference-shaped drop-ins on the GPU: acum_find_pressure_time_history (FP32 arrays,
 mixed kernel), acum_find_pressure_time_history_f64 (FP64 arrays, plain kernel) and
 acum_preprocess_imper, called with the reference's AoS arrays (device memory for the
-kernel entry points, as main.cu:280-360 passes them) and checked against the oracle."""
+kernel entry points, as main.cu:156-236 passes them) and checked against the oracle."""
 import ctypes as C
 
 import numpy as np
@@ -28,7 +28,8 @@ def aos_arrays(deck, fields, dtype):
     return X, N, V, P, ptr[4], ptr[6], ptr[6].copy(), ptr[2], np.array(ne, dtype=np.int32)
 
 
-def call_dropin(fn, deck, fields, dtype, torch):
+def call_dropin(fn, deck, fields, dtype, torch, tobs=None):
+    """Calls a reference-shaped tonal entry point; `tobs` replaces the grid t * dPsi."""
     der = deck.derived()
     T, Ob = deck.nTime, deck.nObs
     X, N, V, P, XP, NP_, VP, PP, E = aos_arrays(deck, fields, dtype)
@@ -36,7 +37,9 @@ def call_dropin(fn, deck, fields, dtype, torch):
     tX, tN, tV, tP = dev(X), dev(N), dev(V), dev(P)
     tXP, tNP, tVP, tPP, tE = dev(XP), dev(NP_), dev(VP), dev(PP), dev(E)
     robs = dev(np.asarray(deck.observers(), dtype=dtype))
-    tobs = dev((np.arange(T, dtype=dtype) * dtype(der["dPsi"])).astype(dtype))
+    if tobs is None:
+        tobs = (np.arange(T, dtype=dtype) * dtype(der["dPsi"])).astype(dtype)
+    tobs = dev(np.asarray(tobs, dtype=dtype))
     vinf = dev(np.asarray(der["vInf"], dtype=dtype))
     z = lambda: torch.zeros((T, Ob), dtype=torch.float64 if dtype == np.float64 else torch.float32, device="cuda")
     pT, pL, pA = z(), z(), z()

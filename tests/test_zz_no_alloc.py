@@ -43,3 +43,24 @@ def test_noalloc_rejects_oversized_problems():
     rc, *_ = call_dropin(L.acum_find_pressure_time_history_noalloc, d, f, np.float32, torch)
     assert rc == -1
     assert b"maximum is" in L.acum_noalloc_last_error()
+
+
+def test_noalloc_refuses_what_the_allocating_entry_point_refuses():
+    torch = pytest.importorskip("torch")
+    from acum3_periodic_gb300 import native
+    L = native.lib()
+    d = synth.config_deck(0, replicate=82, scale=dict(n_span=2, n_chord_side=2, ntime=40, nobs=3))
+    f = O.preprocess(d)
+    # a bin grid other than t * dPsi: both entry points refuse it with ACUM_ERR_UNSUPPORTED
+    tobs = np.arange(d.nTime, dtype=np.float32) * np.float32(d.derived()["dPsi"]) * np.float32(1.01)
+    rc_a, *_ = call_dropin(L.acum_find_pressure_time_history, d, f, np.float32, torch, tobs=tobs)
+    rc_n, *_ = call_dropin(L.acum_find_pressure_time_history_noalloc, d, f, np.float32, torch, tobs=tobs)
+    assert rc_a == rc_n == -8
+    assert b"tObs" in L.acum_noalloc_last_error()
+    # the shortest period both accept: 4 steps
+    d4 = synth.config_deck(0, replicate=83, scale=dict(n_span=2, n_chord_side=2, ntime=4, nobs=3))
+    f4 = O.preprocess(d4)
+    rc_a, aT, aL, aA = call_dropin(L.acum_find_pressure_time_history, d4, f4, np.float32, torch)
+    rc_n, nT, nL, nA = call_dropin(L.acum_find_pressure_time_history_noalloc, d4, f4, np.float32, torch)
+    assert rc_a == rc_n == 0, L.acum_noalloc_last_error()
+    assert per_bin_rms(nA, aA).max() < MIXED_RMS_TOL
