@@ -22,7 +22,7 @@ from metrics import oaspl_db, per_bin_rms
 pytestmark = pytest.mark.gpu
 
 OASPL_DB = 0.05
-FULL_BIN_RMS = 2e-3
+FULL_BIN_RMS = 1e-4
 KAT_FP64_REL = 1e-12
 KAT_MIXED_REL = 2e-5
 
