@@ -82,6 +82,7 @@ void acum_ctx::release_all()
     d_out.release();
     d_rec32.release();
     d_err.release();
+    for (auto& b : d_per) b.release();
     acum::release_bpm_state(this);
     acum::release_adj_state(this);
 }
@@ -141,13 +142,12 @@ int acum_ctx::upload_deck_common(const acum_inputs& inp, int nob, const float* o
     if (inp.nTime < 6) return fail(this, ACUM_ERR_INVALID, "nTime must be at least 6");
     if (nob <= 0) return fail(this, ACUM_ERR_INVALID, "no observers");
     if (ns <= 0) return fail(this, ACUM_ERR_INVALID, "no surfaces");
-    if (inp.impermeable != 1)
-        return fail(this, ACUM_ERR_UNSUPPORTED,
-                    "impermeable = 0: the reference runs no acoustic kernel for permeable decks "
-                    "(main.cu:236); their preprocessing is acum_preprocess_per");
+    if (inp.impermeable == 0 && inp.nTime > kMaxPerSteps)
+        return fail(this, ACUM_ERR_UNSUPPORTED, "permeable decks: at most 4096 steps per period");
     if (inp.oM == 0.0 || inp.dPsi == 0.0) return fail(this, ACUM_ERR_INVALID, "oM and dPsi must be non-zero");
     in = inp;
     derive(in, der);
+    ncol = surface_columns(in.impermeable);
     nobs = nob;
     nsurf = ns;
     nelem.assign(ne, ne + ns);
@@ -157,7 +157,7 @@ int acum_ctx::upload_deck_common(const acum_inputs& inp, int nob, const float* o
     for (int i = 0; i < ns; ++i) {
         if (nelem[i] < 0) return fail(this, ACUM_ERR_INVALID, "negative element count");
         raw_off[i] = off;
-        off += (long long)in.nTime * nelem[i] * 8;
+        off += (long long)in.nTime * nelem[i] * ncol;
         E += nelem[i];
     }
     if (E <= 0) return fail(this, ACUM_ERR_INVALID, "no elements");
@@ -197,6 +197,7 @@ int acum_ctx::upload_deck_common(const acum_inputs& inp, int nob, const float* o
     CK(this, d_raw.ensure(raw_floats));
     have_deck = true;
     invalidate();
+    per_ok = false;
     have_bb = false;
     have_tonal = false;
     have_bpm = false;
@@ -241,7 +242,8 @@ extern "C" int acum_read_deck_sizes(const char* dir, long long* out)
     BBDeck bb;
     if (in.BB_noise == 1 && !read_bb(d, ns, in.nTime, bb, &err)) return fail(nullptr, ACUM_ERR_IO, err);
     if (!read_observers(d, obs, nob, &err)) return fail(nullptr, ACUM_ERR_IO, err);
-    if (!read_surfaces(d, ns, in.nTime, ne, raw, &err)) return fail(nullptr, ACUM_ERR_IO, err);
+    if (!read_surfaces(d, ns, in.nTime, surface_columns(in.impermeable), ne, raw, &err))
+        return fail(nullptr, ACUM_ERR_IO, err);
     long long E = 0, bbs = 0;
     for (int x : ne) E += x;
     for (int n : bb.nsect) bbs += n;
@@ -264,8 +266,9 @@ extern "C" int acum_write_surface_cache(const char* dir)
     std::vector<float> raw;
     std::vector<int> ne;
     if (!read_inputs(d, in, ns, &err)) return fail(nullptr, ACUM_ERR_IO, err);
-    if (!read_surfaces(d, ns, in.nTime, ne, raw, &err)) return fail(nullptr, ACUM_ERR_IO, err);
-    if (!write_surface_cache(d, ns, in.nTime, ne, raw, &err)) return fail(nullptr, ACUM_ERR_IO, err);
+    const int ncol = surface_columns(in.impermeable);
+    if (!read_surfaces(d, ns, in.nTime, ncol, ne, raw, &err)) return fail(nullptr, ACUM_ERR_IO, err);
+    if (!write_surface_cache(d, ns, in.nTime, ncol, ne, raw, &err)) return fail(nullptr, ACUM_ERR_IO, err);
     return ACUM_OK;
 }
 
@@ -282,7 +285,8 @@ extern "C" int acum_load_deck(acum_ctx* ctx, const char* dir)
     BBDeck bb;
     if (in.BB_noise == 1 && !read_bb(d, ns, in.nTime, bb, &err)) return fail(ctx, ACUM_ERR_IO, err);
     if (!read_observers(d, obs, nob, &err)) return fail(ctx, ACUM_ERR_IO, err);
-    if (!read_surfaces(d, ns, in.nTime, ne, raw, &err)) return fail(ctx, ACUM_ERR_IO, err);
+    if (!read_surfaces(d, ns, in.nTime, surface_columns(in.impermeable), ne, raw, &err))
+        return fail(ctx, ACUM_ERR_IO, err);
     int rc = acum_set_deck(ctx, &in, nob, obs.data(), ns, ne.data(), raw.data(), 0);
     if (rc) return rc;
     if (in.BB_noise == 1) {
@@ -357,6 +361,11 @@ extern "C" int acum_set_obs_per_warp(acum_ctx* ctx, int obs_per_warp)
 int acum_ctx::ensure_prep(bool need64, bool need32, bool need_fields)
 {
     DeviceGuard g(device);
+    if (permeable())
+        return fail(this, ACUM_ERR_UNSUPPORTED,
+                    "a permeable deck (impermeable 0) has no impermeable records or fields: the reference "
+                    "runs no acoustic kernel for it (main.cu:236); acum_get_permeable_fields gives its "
+                    "preprocessed arrays");
     const bool do64 = need64 && !rec64_ok, do32 = need32 && !rec32_ok;
     if (!do64 && !do32 && !need_fields) return ACUM_OK;
     if (!d_raw.p) return fail(this, ACUM_ERR_STATE, "the surface rows were released after preprocessing");
@@ -429,7 +438,7 @@ extern "C" int acum_preprocess(acum_ctx* ctx)
     if (!ctx) return ACUM_ERR_INVALID;
     if (!ctx->have_deck) return fail(ctx, ACUM_ERR_STATE, "no deck");
     ctx->begin_run();
-    int rc = ctx->ensure_prep(true, true, false);
+    int rc = ctx->permeable() ? ctx->ensure_per_prep() : ctx->ensure_prep(true, true, false);
     if (rc) return rc;
     DeviceGuard g(ctx->device);
     CK(ctx, cudaStreamSynchronize(ctx->stream));
@@ -457,6 +466,17 @@ int acum_ctx::run_tonal(int precision, double* d_pT, double* d_pL, double* d_pA)
     if (precision != ACUM_PLAIN_FP64 && precision != ACUM_MIXED)
         return fail(this, ACUM_ERR_INVALID, "precision must be ACUM_PLAIN_FP64 or ACUM_MIXED");
     const bool f64 = precision == ACUM_PLAIN_FP64;
+    if (permeable()) {
+        // main.cu:87 preprocesses a permeable deck and main.cu:236 launches the kernel only
+        // for impermeable ones: the pressures stay as main.cu:123-130 zeroed them
+        int rc = ensure_per_prep();
+        if (rc) return rc;
+        DeviceGuard g(device);
+        const size_t n = (size_t)T * nobs * sizeof(double);
+        for (double* o : {d_pT, d_pL, d_pA})
+            if (o) CK(this, cudaMemsetAsync(o, 0, n, stream));
+        return ACUM_OK;
+    }
     int rc = ensure_prep(f64, !f64, false);
     if (rc) return rc;
     DeviceGuard g(device);
@@ -671,6 +691,7 @@ extern "C" int acum_last_timing(const acum_ctx* ctx, int which, double* ms, long
     case 3: a = EV_BPM0; b = EV_BPM1; have = ctx->bpm_timed; break;
     case 4: a = EV_ADJ0; b = EV_ADJ1; have = ctx->adj_timed; break;
     case 5: a = EV_CALL0; b = EV_CALL1; have = ctx->call_timed; break;
+    case 6: a = EV_BOBS0; b = EV_BOBS1; have = ctx->bpm_timed; break;
     default: return ACUM_ERR_INVALID;
     }
     if (!have) return ACUM_ERR_STATE;
@@ -1035,6 +1056,65 @@ int per_enqueue(void* const d[5], bool is_double, const PerLayout& L, int nTime,
     if (e != cudaSuccess) return cuda_fail(nullptr, e, "preprocess_per");
     return ACUM_OK;
 }
+
+}  // namespace
+
+// Permeable deck in a context: its rows into the AoS arrays, then preprocess_per on them
+// (FP64 storage, so the arrays equal the reference's FP64 build bit for bit).
+int acum_ctx::ensure_per_prep()
+{
+    if (per_ok) return ACUM_OK;
+    DeviceGuard g(device);
+    if (!d_raw.p) return fail(this, ACUM_ERR_STATE, "no surface rows");
+    const int width[5] = {4, 6, 6, 6, 4};
+    double* d[5];
+    for (int q = 0; q < 5; ++q) {
+        CK(this, d_per[q].ensure((size_t)E * T * width[q]));
+        d[q] = d_per[q].p;
+    }
+    CK(this, cudaEventRecord(ev[EV_PREP0], stream));
+    CK(this, launch_per_rows(raw_cur ? raw_cur : d_raw.p, d_rawoff.p, d_esurf.p, d_elocal.p, d_ecount.p, (int)E, T, d,
+                             stream));
+    PerLayout L;
+    L.etot = E;
+    L.off.resize((size_t)E * 5);
+    for (int q = 0; q < 5; ++q)
+        for (long long e = 0; e < E; ++e) L.off[(size_t)q * E + e] = e * T * width[q];
+    void* dv[5] = {d[0], d[1], d[2], d[3], d[4]};
+    int rc = per_enqueue(dv, true, L, T, der.dTau, in.a0, in.rhoRef, in.Mref, in.CFDscale, in.periodic, in.lowpass,
+                         stream);
+    if (rc) {
+        err = g_err;
+        return rc;
+    }
+    CK(this, cudaEventRecord(ev[EV_PREP1], stream));
+    launches += 2;
+    prep_timed = true;
+    per_ok = true;
+    return ACUM_OK;
+}
+
+extern "C" int acum_get_permeable_fields(acum_ctx* ctx, double* Xham, double* Nham, double* Vham, double* Uham,
+                                         double* PRham)
+{
+    acum::NvtxRange nvtx_range_("acum_get_permeable_fields");
+    if (!ctx || !Xham || !Nham || !Vham || !Uham || !PRham) return ACUM_ERR_INVALID;
+    if (!ctx->have_deck) return fail(ctx, ACUM_ERR_STATE, "no deck");
+    if (!ctx->permeable()) return fail(ctx, ACUM_ERR_STATE, "not a permeable deck (impermeable 1)");
+    ctx->begin_run();
+    int rc = ctx->ensure_per_prep();
+    if (rc) return rc;
+    DeviceGuard g(ctx->device);
+    double* h[5] = {Xham, Nham, Vham, Uham, PRham};
+    const int width[5] = {4, 6, 6, 6, 4};
+    for (int q = 0; q < 5; ++q)
+        CK(ctx, cudaMemcpyAsync(h[q], ctx->d_per[q].p, (size_t)ctx->E * ctx->T * width[q] * 8, cudaMemcpyDeviceToHost,
+                                ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return ACUM_OK;
+}
+
+namespace {
 
 // device copies of the caller's five host arrays for one preprocess_per call
 struct PerBuffers {

@@ -121,6 +121,11 @@ struct PerArgs {
 };
 cudaError_t launch_per_prep(void* X, void* N, void* V, void* U, void* PR, bool is_double, const PerArgs& a,
                             cudaStream_t s);
+// the 12-column rows of a permeable deck ([surface][step][element][12], raw_off per
+// surface) into FP64 AoS arrays d = X [E][T][4], N [E][T][6], V [E][T][6], U [E][T][6],
+// PR [E][T][4] (derivative columns and V zero)
+cudaError_t launch_per_rows(const float* raw, const long long* raw_off, const int* e_surf, const int* e_local,
+                            const int* e_count, int E, int T, double* const d[5], cudaStream_t s);
 
 struct TonalRun {
     TonalGeom g;

@@ -282,12 +282,61 @@ __global__ void adj_seed_kernel(const double* __restrict__ acc, int O, int T, do
 struct ChainDev {
     const double* cot;     // [E][T][19]
     const double* fields;  // [E][T][18] from the preprocessing
-    int E, T, periodic;
+    int E, T, periodic, lowpass;
     double a0, rho, pscale, cfd, dTau;
+    double gauss[13];
+    // the surface rows (Cp at column 3), to recompute the low-pass filter's inputs
+    const float* raw;
+    const long long* raw_off;
+    const int *e_surf, *e_local, *e_count;
     double* gcp;  // [E][T]
     double* gx;   // [E][T][3]
     double* gn;   // [E][T][3]
 };
+
+// Which input the 3-point median of the preprocessing picks (the forward's expression,
+// tonal.cu prep_kernel): 0 = left, 1 = middle, 2 = right neighbour.
+__device__ __forceinline__ int med_sel(double l, double m, double r)
+{
+    double hi = l > m ? l : m;
+    hi = hi > r ? hi : r;
+    double lo = l < m ? l : m;
+    lo = lo < r ? lo : r;
+    return (l < hi && l > lo) ? 0 : ((m < hi && m > lo) ? 1 : 2);
+}
+
+// Transpose of the periodic 13-tap Gaussian (its weights are symmetric, w[k] = w[12 - k],
+// so the transpose is the same stencil): out[q] = sum_k w[k] in[(q + k - 6) mod T].
+__device__ __forceinline__ void gauss_t(const double* in, double* out, int T, const double* w)
+{
+    for (int q = threadIdx.x; q < T; q += blockDim.x) {
+        double acc = 0.0;
+        for (int k = 0; k < 13; ++k) {
+            int t = q + k - 6;
+            if (t < 0) t += T;
+            else if (t > T - 1) t -= T;
+            acc += w[k] * in[t];
+        }
+        out[q] = acc;
+    }
+}
+
+// Transpose of the periodic 3-point median over the series x: the cotangent of each
+// output goes to the input it selected (the median is a selection, differentiable
+// wherever the three inputs are distinct): out[u] = sum of in[t] over t in {u-1, u, u+1}
+// whose median picked x[u].
+__device__ __forceinline__ void median_t(const double* x, const double* in, double* out, int T)
+{
+    for (int u = threadIdx.x; u < T; u += blockDim.x) {
+        const int um = u == 0 ? T - 1 : u - 1, up = u == T - 1 ? 0 : u + 1;
+        const int umm = um == 0 ? T - 1 : um - 1, upp = up == T - 1 ? 0 : up + 1;
+        double acc = 0.0;
+        if (med_sel(x[umm], x[um], x[u]) == 2) acc += in[um];  // median at u - 1, right input
+        if (med_sel(x[um], x[u], x[up]) == 1) acc += in[u];    // median at u, middle input
+        if (med_sel(x[u], x[up], x[upp]) == 0) acc += in[up];  // median at u + 1, left input
+        out[u] = acc;
+    }
+}
 
 __global__ void __launch_bounds__(256) adjoint_chain_kernel(ChainDev c)
 {
@@ -380,6 +429,63 @@ __global__ void __launch_bounds__(256) adjoint_chain_kernel(ChainDev c)
         }
     }
     __syncthreads();
+    if (c.lowpass == 1) {
+        // tmp holds dJ/dP of the filtered pressure.  The filter (preprocess.cu:323-333) is
+        // two passes of (median, Gaussian) after make_periodic; its inputs are recomputed
+        // here from Cp exactly as the preprocessing forms them, and the cotangent goes back
+        // through Gaussian^T, median^T, Gaussian^T, median^T.  The series live in the
+        // velocity rows, which are free by now.
+        double* Pm = bV;         // make_periodic(Cp pscale): the first median's input
+        double* Q1 = bV + T;     // first median's output
+        double* P1 = bV + 2 * T; // first Gaussian's output: the second median's input
+        double* A = bVd;
+        double* B = bVd + T;
+        const int s = c.e_surf[e], j = c.e_local[e], Es = c.e_count[s];
+        const float* base = c.raw + c.raw_off[s];
+        for (int t = threadIdx.x; t < T; t += blockDim.x) Pm[t] = (double)base[((size_t)t * Es + j) * 8 + 3] * c.pscale;
+        __syncthreads();
+        {
+            const double p0 = Pm[0], p1 = Pm[1], pm = Pm[T - 2], pn = Pm[T - 1];
+            const double g0 = p0 - (p1 - p0);
+            const double k2 = pn, k1 = g0, s2 = pn - pm, s1 = p0 - g0;
+            const int xm = T;
+            const double dd = k1, cc = s1 - s2;
+            const double bb = -2.0 * (s1 - s2) / xm - 3.0 * (k1 - k2) / xm / xm;
+            const double aa = -bb / xm - (s1 - s2) / xm / xm - (k1 - k2) / xm / xm / xm;
+            __syncthreads();
+            for (int t = threadIdx.x; t < T; t += blockDim.x) {
+                const int i = t + 1;
+                const double cub = aa * i * i * i + bb * i * i + cc * i + dd;
+                Pm[t] = Pm[t] - (cub - k2);
+            }
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < T; t += blockDim.x) {
+            const double l = Pm[t == 0 ? T - 1 : t - 1], m = Pm[t], r = Pm[t == T - 1 ? 0 : t + 1];
+            const int k = med_sel(l, m, r);
+            Q1[t] = k == 0 ? l : (k == 1 ? m : r);
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < T; t += blockDim.x) {
+            double acc = 0.0;
+            for (int k = 0; k < 13; ++k) {
+                int q = t + k - 6;
+                if (q < 0) q += T;
+                else if (q > T - 1) q -= T;
+                acc += c.gauss[k] * Q1[q];
+            }
+            P1[t] = acc;
+        }
+        __syncthreads();
+        gauss_t(tmp, A, T, c.gauss);  // second Gaussian
+        __syncthreads();
+        median_t(P1, A, B, T);        // second median
+        __syncthreads();
+        gauss_t(B, A, T, c.gauss);    // first Gaussian
+        __syncthreads();
+        median_t(Pm, A, tmp, T);      // first median
+        __syncthreads();
+    }
     // make_periodic (mathfunc.cu:165-206): P'[k] = P[k] - (cubic(k+1) - k2), the cubic
     // linear in k1 = 2 P0 - P1, k2 = P[T-1], s1 = P1 - P0, s2 = P[T-1] - P[T-2]
     if (threadIdx.x == 0) {
@@ -449,8 +555,6 @@ extern "C" int acum_tonal_adjoint(acum_ctx* ctx, int precision, const double* dJ
     if (!ctx) return ACUM_ERR_INVALID;
     if (!ctx->have_deck) return fail(ctx, ACUM_ERR_STATE, "no deck");
     if (precision != ACUM_PLAIN_FP64 && precision != ACUM_MIXED) return fail(ctx, ACUM_ERR_INVALID, "precision");
-    if (ctx->in.lowpass == 1)
-        return fail(ctx, ACUM_ERR_UNSUPPORTED, "the adjoint is built for lowpass = 0 (no median filter transpose)");
     DeviceGuard gd(ctx->device);
     AdjState* s = adj_state(ctx);
     const int T = ctx->T, O = ctx->nobs;
@@ -521,6 +625,13 @@ extern "C" int acum_tonal_adjoint(acum_ctx* ctx, int precision, const double* dJ
     c.E = (int)E;
     c.T = T;
     c.periodic = ctx->in.periodic;
+    c.lowpass = ctx->in.lowpass;
+    gauss_taps(c.gauss);
+    c.raw = ctx->d_raw.p;
+    c.raw_off = ctx->d_rawoff.p;
+    c.e_surf = ctx->d_esurf.p;
+    c.e_local = ctx->d_elocal.p;
+    c.e_count = ctx->d_ecount.p;
     c.a0 = ctx->in.a0;
     c.rho = ctx->in.rhoRef;
     c.pscale = 0.5 * ctx->in.rhoRef * (ctx->in.Mref * ctx->in.Mref) * (ctx->in.a0 * ctx->in.a0);

@@ -298,6 +298,8 @@ extern "C" int acum_batch_add(acum_batch* b, const acum_inputs* in, int nobs, co
         E += nelem[i];
     }
     if (E <= 0) return bfail(b, ACUM_ERR_INVALID, "acum_batch_add: no elements");
+    if (in->impermeable == 0)
+        return bfail(b, ACUM_ERR_UNSUPPORTED, "acum_batch_add: a permeable deck has no acoustic kernel (main.cu:236)");
     DeviceGuard g(b->device);
     // what the case holds while it is added (rows + records) and afterwards (records,
     // sums, results), against the device's free memory with 1 GiB to spare

@@ -940,9 +940,11 @@ static int bpm_run(acum_ctx* ctx, int aa_mode, const double* seed_spl_h, const d
     if ((e = s->sums.ensure((size_t)split * kBands * 6 * O)) != cudaSuccess) return cuda_fail(ctx, e, "bpm alloc");
     cudaMemsetAsync(s->sums.p, 0, (size_t)split * kBands * 6 * O * 8, st);
     dim3 grid(oblocks, split);
+    cudaEventRecord(ctx->ev[EV_BOBS0], st);
     bb_obs_kernel<<<grid, kBpmThreads, kObsSmem, st>>>(s->geo.p, s->amp.p, ctx->d_obs32.p, O, nst, per_split,
                                                        (float)d.vinf[0], (float)d.vinf[1], (float)d.vinf[2],
                                                        (float)d.a0, aa_mode, s->sums.p, ctx->d_err.p);
+    cudaEventRecord(ctx->ev[EV_BOBS1], st);
     bb_final_kernel<<<(int)(((long long)O * kBands + 127) / 128), 128, 0, st>>>(s->sums.p, split, O, T,
                                                                               s->seed_spl.p, s->spl.p);
     bb_oaspl_kernel<<<(O + 127) / 128, 128, 0, st>>>(O, s->seed_oas.p, s->spl.p, s->oaspl.p);

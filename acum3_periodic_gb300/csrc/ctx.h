@@ -62,7 +62,7 @@ struct Derived {
 
 enum {
     EV_PREP0, EV_PREP1, EV_TONAL0, EV_TONAL1, EV_FIN1, EV_BPM0, EV_BPM1, EV_ADJ0, EV_ADJ1, EV_CALL0, EV_CALL1,
-    kNumEvents
+    EV_BOBS0, EV_BOBS1, kNumEvents
 };
 
 int fail(struct ::acum_ctx* ctx, int code, const std::string& msg);
@@ -91,6 +91,7 @@ struct acum_ctx {
     std::vector<int> nelem;
     std::vector<long long> raw_off;
     size_t raw_floats = 0;
+    int ncol = 8;  // floats per surface row: 8 impermeable, 12 permeable (io.cu:286, 321)
     std::vector<float> obs_file_h;
     bool have_bb = false, bb_dirty = true;
     acum::BBDeck bb;
@@ -112,6 +113,10 @@ struct acum_ctx {
     acum::DBuf<double> d_rec64, d_fields, d_acc, d_out;
     acum::DBuf<float> d_rec32;
     acum::DBuf<acum::DeviceErr> d_err;
+    // permeable decks: the preprocessed AoS arrays of variables.cu:54 in FP64 (X, N, V, U,
+    // PR with nPRham = 4), the reference's layout (element after element, [T][width])
+    acum::DBuf<double> d_per[5];
+    bool per_ok = false;
     bool rec64_ok = false, rec32_ok = false;
     // layout (E, Epad, nW, T) the record buffers were last written for: the preprocessing
     // writes the real elements and steps only, so a buffer whose padding may hold records
@@ -134,10 +139,12 @@ struct acum_ctx {
     void* bpm_state = nullptr;
     void* adj_state = nullptr;
 
+    bool permeable() const { return in.impermeable == 0; }
     void invalidate()
     {
         rec64_ok = false;
         rec32_ok = false;
+        per_ok = false;
     }
     void begin_run()
     {
@@ -147,6 +154,7 @@ struct acum_ctx {
     void release_all();
     int upload_deck_common(const acum_inputs& inp, int nob, const float* obs_file, int ns, const int* ne);
     int ensure_prep(bool need64, bool need32, bool need_fields);
+    int ensure_per_prep();
     int run_tonal(int precision, double* d_pT, double* d_pL, double* d_pA);
     int finish_run();
 };

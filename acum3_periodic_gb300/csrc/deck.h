@@ -25,9 +25,11 @@ struct BBDeck {
 
 bool read_inputs(const std::string& dir, acum_inputs& in, int& nsurf, std::string* err);
 bool read_observers(const std::string& dir, std::vector<float>& obs, int& nobs, std::string* err);
-bool read_surfaces(const std::string& dir, int nsurf, int ntime, std::vector<int>& nelem, std::vector<float>& raw,
-                   std::string* err);
-bool write_surface_cache(const std::string& dir, int nsurf, int ntime, const std::vector<int>& nelem,
+// surface rows of `ncol` floats: 8 (impermeable decks) or 12 (permeable decks)
+inline int surface_columns(int impermeable) { return impermeable == 0 ? 12 : 8; }
+bool read_surfaces(const std::string& dir, int nsurf, int ntime, int ncol, std::vector<int>& nelem,
+                   std::vector<float>& raw, std::string* err);
+bool write_surface_cache(const std::string& dir, int nsurf, int ntime, int ncol, const std::vector<int>& nelem,
                          const std::vector<float>& raw, std::string* err);
 bool read_bb(const std::string& dir, int nsurf, int ntime, BBDeck& bb, std::string* err);
 bool write_time_history(const std::string& dir, int T, int O, double dpsi_deg, const double* pT, const double* pL,

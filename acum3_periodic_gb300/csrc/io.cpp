@@ -220,10 +220,11 @@ bool read_observers(const std::string& dir, std::vector<float>& obs, int& nobs, 
 }
 
 // Binary cache of the surface rows (surfaces/surfaces.acumbin): the float rows exactly as
-// read from the text files, with the size and modification time of each text file, so a
-// later load skips the text parse when none of them changed.
+// read from the text files (8 columns per row for impermeable decks, 12 for permeable
+// ones), with the size and modification time of each text file, so a later load skips
+// the text parse when none of them changed.
 namespace {
-const char kCacheMagic[8] = {'A', 'C', 'U', 'M', 'S', 'R', 'F', '1'};
+const char kCacheMagic[8] = {'A', 'C', 'U', 'M', 'S', 'R', 'F', '2'};
 
 struct FileStamp {
     int64_t size, mtime_ns;
@@ -245,17 +246,18 @@ std::string surface_file(const std::string& dir, int i)
 
 std::string cache_file(const std::string& dir) { return dir + "/surfaces/surfaces.acumbin"; }
 
-// rows from the cache if it exists and matches every text file; false otherwise
-bool read_surface_cache(const std::string& dir, int nsurf, int ntime, std::vector<int>& nelem,
+// rows from the cache if it exists and matches every text file and the row width; false
+// otherwise
+bool read_surface_cache(const std::string& dir, int nsurf, int ntime, int ncol, std::vector<int>& nelem,
                         std::vector<float>& raw)
 {
     FILE* f = fopen(cache_file(dir).c_str(), "rb");
     if (!f) return false;
     bool ok = false;
     char magic[8];
-    int32_t ns = 0, nt = 0;
+    int32_t ns = 0, nt = 0, nc = 0;
     if (fread(magic, 1, 8, f) == 8 && memcmp(magic, kCacheMagic, 8) == 0 && fread(&ns, 4, 1, f) == 1 &&
-        fread(&nt, 4, 1, f) == 1 && ns == nsurf && nt == ntime) {
+        fread(&nt, 4, 1, f) == 1 && fread(&nc, 4, 1, f) == 1 && ns == nsurf && nt == ntime && nc == ncol) {
         std::vector<int32_t> ne(ns);
         std::vector<FileStamp> st(ns);
         ok = fread(ne.data(), 4, ns, f) == (size_t)ns && fread(st.data(), sizeof(FileStamp), ns, f) == (size_t)ns;
@@ -264,7 +266,7 @@ bool read_surface_cache(const std::string& dir, int nsurf, int ntime, std::vecto
             FileStamp now;
             ok = ne[i] >= 0 && stamp_of(surface_file(dir, i), now) && now.size == st[i].size &&
                  now.mtime_ns == st[i].mtime_ns;
-            total += (size_t)ntime * ne[i] * 8;
+            total += (size_t)ntime * ne[i] * ncol;
         }
         if (ok) {
             raw.assign(total, 0.f);
@@ -278,7 +280,7 @@ bool read_surface_cache(const std::string& dir, int nsurf, int ntime, std::vecto
 }
 }  // namespace
 
-bool write_surface_cache(const std::string& dir, int nsurf, int ntime, const std::vector<int>& nelem,
+bool write_surface_cache(const std::string& dir, int nsurf, int ntime, int ncol, const std::vector<int>& nelem,
                          const std::vector<float>& raw, std::string* err)
 {
     std::vector<FileStamp> st(nsurf);
@@ -287,10 +289,11 @@ bool write_surface_cache(const std::string& dir, int nsurf, int ntime, const std
     const std::string tmp = cache_file(dir) + ".tmp";
     FILE* f = fopen(tmp.c_str(), "wb");
     if (!f) return set_err(err, "Unable to write " + tmp);
-    const int32_t ns = nsurf, nt = ntime;
+    const int32_t ns = nsurf, nt = ntime, nc = ncol;
     std::vector<int32_t> ne(nelem.begin(), nelem.end());
     bool ok = fwrite(kCacheMagic, 1, 8, f) == 8 && fwrite(&ns, 4, 1, f) == 1 && fwrite(&nt, 4, 1, f) == 1 &&
-              fwrite(ne.data(), 4, ns, f) == (size_t)ns && fwrite(st.data(), sizeof(FileStamp), ns, f) == (size_t)ns &&
+              fwrite(&nc, 4, 1, f) == 1 && fwrite(ne.data(), 4, ns, f) == (size_t)ns &&
+              fwrite(st.data(), sizeof(FileStamp), ns, f) == (size_t)ns &&
               fwrite(raw.data(), 4, raw.size(), f) == raw.size();
     ok = (fclose(f) == 0) && ok;
     if (!ok || rename(tmp.c_str(), cache_file(dir).c_str()) != 0) {
@@ -300,11 +303,13 @@ bool write_surface_cache(const std::string& dir, int nsurf, int ntime, const std
     return true;
 }
 
-// io.cu:206-333 (impermeable rows: x y z Cp A nx ny nz)
-bool read_surfaces(const std::string& dir, int nsurf, int ntime, std::vector<int>& nelem, std::vector<float>& raw,
-                   std::string* err)
+// io.cu:206-333: rows of 8 columns x y z Cp A nx ny nz for impermeable decks (io.cu:321),
+// of 12 columns x y z u v w P rho ds nx ny nz for permeable ones (io.cu:286)
+bool read_surfaces(const std::string& dir, int nsurf, int ntime, int ncol, std::vector<int>& nelem,
+                   std::vector<float>& raw, std::string* err)
 {
-    if (read_surface_cache(dir, nsurf, ntime, nelem, raw)) return true;
+    if (ncol != 8 && ncol != 12) return set_err(err, "surface rows have 8 or 12 columns");
+    if (read_surface_cache(dir, nsurf, ntime, ncol, nelem, raw)) return true;
     nelem.assign(nsurf, 0);
     std::vector<std::string> bufs(nsurf);
     size_t total = 0;
@@ -319,7 +324,7 @@ bool read_surfaces(const std::string& dir, int nsurf, int ntime, std::vector<int
             // nTime rows per element; so does this reader
         }
         nelem[i] = e;
-        total += (size_t)ntime * e * 8;
+        total += (size_t)ntime * e * ncol;
     }
     raw.assign(total, 0.f);
     size_t off = 0;
@@ -328,9 +333,9 @@ bool read_surfaces(const std::string& dir, int nsurf, int ntime, std::vector<int
         const char* end = p + bufs[i].size();
         while (p < end && *p != '\n') ++p;  // header line
         const size_t rows = (size_t)ntime * nelem[i];
-        if (!parse_rows_parallel(p, end, 8, rows, raw.data() + off))
+        if (!parse_rows_parallel(p, end, ncol, rows, raw.data() + off))
             return set_err(err, "surfaces/surface_" + std::to_string(i + 1) + ".dat: fewer rows than nTime*E");
-        off += rows * 8;
+        off += rows * ncol;
         std::string().swap(bufs[i]);
     }
     return true;

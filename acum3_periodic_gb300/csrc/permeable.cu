@@ -187,7 +187,44 @@ cudaError_t launch_per_t(S* X, S* N, S* V, S* U, S* PR, const PerArgs& a, cudaSt
     return cudaGetLastError();
 }
 
+// The rows of a permeable deck as read_surf leaves them (io.cu:263-293): each 12-column
+// row x y z u v w P rho ds nx ny nz goes to Xham (x, y, z, ds), Nham (n), Uham (u) and
+// PRham (P at 0, rho at 2); the derivative columns and Vham start at zero and are all
+// written by the preprocessing.  One thread per (element, step); FP64 storage.
+__global__ void per_rows_kernel(const float* __restrict__ raw, const long long* __restrict__ raw_off,
+                                const int* __restrict__ e_surf, const int* __restrict__ e_local,
+                                const int* __restrict__ e_count, int E, int T, double* X, double* N, double* V,
+                                double* U, double* PR)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)E * T) return;
+    const int e = (int)(idx / T), t = (int)(idx % T);
+    const int s = e_surf[e];
+    const float* r = raw + raw_off[s] + ((size_t)t * e_count[s] + e_local[e]) * 12;
+    const size_t k = (size_t)e * T + t;
+    double* x = X + k * 4;
+    double* n = N + k * 6;
+    double* v = V + k * 6;
+    double* u = U + k * 6;
+    double* pr = PR + k * 4;
+    x[0] = r[0]; x[1] = r[1]; x[2] = r[2]; x[3] = r[8];
+    u[0] = r[3]; u[1] = r[4]; u[2] = r[5]; u[3] = 0.0; u[4] = 0.0; u[5] = 0.0;
+    pr[0] = r[6]; pr[1] = 0.0; pr[2] = r[7]; pr[3] = 0.0;
+    n[0] = r[9]; n[1] = r[10]; n[2] = r[11]; n[3] = 0.0; n[4] = 0.0; n[5] = 0.0;
+    for (int c = 0; c < 6; ++c) v[c] = 0.0;
+}
+
 }  // namespace
+
+cudaError_t launch_per_rows(const float* raw, const long long* raw_off, const int* e_surf, const int* e_local,
+                            const int* e_count, int E, int T, double* const d[5], cudaStream_t s)
+{
+    const long long n = (long long)E * T;
+    if (n <= 0) return cudaErrorInvalidValue;
+    per_rows_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(raw, raw_off, e_surf, e_local, e_count, E, T, d[0],
+                                                               d[1], d[2], d[3], d[4]);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_per_prep(void* X, void* N, void* V, void* U, void* PR, bool is_double, const PerArgs& a,
                             cudaStream_t s)

@@ -664,36 +664,54 @@ __device__ __forceinline__ G2 load_g2(const float* half0)
 }
 
 // The samples of one step of an element pair, in packed FP32 (see the comment above for
-// the integrand and the anchored retarded time).  g[q] = group q of the pair's records.
-__device__ __forceinline__ void sample_mixed2(const G2* g, float ox, float oy, float oz, const Anchor& an,
-                                              const KParams& p, int tau, SmpF& oa, SmpF& ob)
+// the integrand and the anchored retarded time), in two parts: the retarded time and
+// the radiation vector from the positions (group 0) and x.v (group 4, w), then the
+// source terms from the other groups.  The tensor-memory form loads the other groups
+// while the first part runs.
+struct MixedGeom {
+    float2 dt, rx, ry, rz, ir;
+};
+
+__device__ __forceinline__ MixedGeom mixed_geom(const G2& g0, float2 xv, float ox, float oy, float oz,
+                                                const Anchor& an, const KParams& p)
 {
     const float2 OX = f2(ox), OY = f2(oy), OZ = f2(oz);
-    const float2 dx = sub2(OX, g[0].x), dy = sub2(OY, g[0].y), dz = sub2(OZ, g[0].z);
-    // anchored retarded time (g4.w = x.v): -num = x.(d + D0) - 2 t0 x.v
-    const float2 S = fma2(g[0].x, add2(dx, OX), fma2(g[0].y, add2(dy, OY), mul2(g[0].z, add2(dz, OZ))));
-    const float2 nnum = fma2(f2(-an.t2), g[4].w, S);
-    const float2 bp = sub2(f2(an.s0), g[4].w);
+    const float2 dx = sub2(OX, g0.x), dy = sub2(OY, g0.y), dz = sub2(OZ, g0.z);
+    // anchored retarded time (xv = x.v): -num = x.(d + D0) - 2 t0 x.v
+    const float2 S = fma2(g0.x, add2(dx, OX), fma2(g0.y, add2(dy, OY), mul2(g0.z, add2(dz, OZ))));
+    const float2 nnum = fma2(f2(-an.t2), xv, S);
+    const float2 bp = sub2(f2(an.s0), xv);
     const float2 q = fma2(p.nalpha2, nnum, mul2(bp, bp));
     const float2 den = fma2(q, make_float2(rsqrt_ftz(q.x), rsqrt_ftz(q.y)), bp);
-    const float2 dt = mul2(nnum, make_float2(-rcp_ftz(den.x), -rcp_ftz(den.y)));
-    const float2 tr = add2(f2(an.t0), dt);
-    const float2 rx = fma2(p.nvx2, tr, dx), ry = fma2(p.nvy2, tr, dy), rz = fma2(p.nvz2, tr, dz);
-    const float2 ir = rcp2(mul2(p.a02, tr));
-    const float2 Mr = mul2(fma2(g[1].x, rx, fma2(g[1].y, ry, mul2(g[1].z, rz))), ir);
-    const float2 Mdr = mul2(fma2(g[2].x, rx, fma2(g[2].y, ry, mul2(g[2].z, rz))), ir);
-    const float2 Lr = mul2(fma2(g[3].x, rx, fma2(g[3].y, ry, mul2(g[3].z, rz))), ir);
-    const float2 Ldr = mul2(fma2(g[4].x, rx, fma2(g[4].y, ry, mul2(g[4].z, rz))), ir);
+    MixedGeom m;
+    m.dt = mul2(nnum, make_float2(-rcp_ftz(den.x), -rcp_ftz(den.y)));
+    const float2 tr = add2(f2(an.t0), m.dt);
+    m.rx = fma2(p.nvx2, tr, dx);
+    m.ry = fma2(p.nvy2, tr, dy);
+    m.rz = fma2(p.nvz2, tr, dz);
+    m.ir = rcp2(mul2(p.a02, tr));
+    return m;
+}
+
+__device__ __forceinline__ void mixed_source(const MixedGeom& m, float2 dsD, const G2& g1, const G2& g2, const G2& g3,
+                                             const G2& g4, const Anchor& an, const KParams& p, int tau, SmpF& oa,
+                                             SmpF& ob)
+{
+    const float2 rx = m.rx, ry = m.ry, rz = m.rz, ir = m.ir;
+    const float2 Mr = mul2(fma2(g1.x, rx, fma2(g1.y, ry, mul2(g1.z, rz))), ir);
+    const float2 Mdr = mul2(fma2(g2.x, rx, fma2(g2.y, ry, mul2(g2.z, rz))), ir);
+    const float2 Lr = mul2(fma2(g3.x, rx, fma2(g3.y, ry, mul2(g3.z, rz))), ir);
+    const float2 Ldr = mul2(fma2(g4.x, rx, fma2(g4.y, ry, mul2(g4.z, rz))), ir);
     const float2 G = rcp2(sub2(f2(1.0f), Mr));
     const float2 qa = mul2(p.a02, ir);
-    const float2 K = fma2(qa, sub2(Mr, g[1].w), Mdr);
+    const float2 K = fma2(qa, sub2(Mr, g1.w), Mdr);
     const float2 base = mul2(mul2(ir, G), G);
-    const float2 pt = mul2(mul2(g[2].w, base), mul2(G, K));
-    const float2 pl = mul2(mul2(g[0].w, base), fma2(mul2(Lr, G), K, fma2(qa, sub2(Lr, g[3].w), Ldr)));
+    const float2 pt = mul2(mul2(g2.w, base), mul2(G, K));
+    const float2 pl = mul2(mul2(dsD, base), fma2(mul2(Lr, G), K, fma2(qa, sub2(Lr, g3.w), Ldr)));
     // observer time in bins: tau + round(t0 oM/dPsi) + x, x = frac(t0 oM/dPsi) + dt oM/dPsi;
     // outside the floor's range (or not finite) the fraction is NaN, which the deposit
     // rejects (and reports) whatever the integer part holds
-    const float2 x = fma2(dt, p.kb2, f2(an.kf));
+    const float2 x = fma2(m.dt, p.kb2, f2(an.kf));
     const float2 t = __fadd2_rd(x, f2(kRound));
     const float2 fr = sub2(x, add2(t, f2(-kRound)));
     const int kb = tau + an.ki - kRoundBits;
@@ -705,6 +723,26 @@ __device__ __forceinline__ void sample_mixed2(const G2* g, float ox, float oy, f
     ob.pt = pt.y;
     oa.pl = pl.x;
     ob.pl = pl.y;
+}
+
+// g[q] = group q of the pair's records
+__device__ __forceinline__ void sample_mixed2(const G2* g, float ox, float oy, float oz, const Anchor& an,
+                                              const KParams& p, int tau, SmpF& oa, SmpF& ob)
+{
+    const MixedGeom m = mixed_geom(g[0], g[4].w, ox, oy, oz, an, p);
+    mixed_source(m, g[0].w, g[1], g[2], g[3], g[4], an, p, tau, oa, ob);
+}
+
+// A group as tensor-memory columns 8q .. 8q + 7 of a pair hold it (half 0: f0 e, f0 e+1,
+// f1 e, f1 e+1; half 1: the same for fields 2, 3)
+__device__ __forceinline__ G2 g2_of(const uint32_t* r)
+{
+    G2 g;
+    g.x = make_float2(__uint_as_float(r[0]), __uint_as_float(r[1]));
+    g.y = make_float2(__uint_as_float(r[2]), __uint_as_float(r[3]));
+    g.z = make_float2(__uint_as_float(r[4]), __uint_as_float(r[5]));
+    g.w = make_float2(__uint_as_float(r[6]), __uint_as_float(r[7]));
+    return g;
 }
 
 __device__ __forceinline__ int mod_T(int n, int T, unsigned m)
@@ -915,30 +953,48 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
         const bool valid = tau < T;
         const float* st = stages + (size_t)s * SE * kTile;
         SmpF cur[OPW][SE];
+        if (TM) {
+            // records from tensor memory, in two loads per element pair: the positions and
+            // x.v (columns 0-7, 32-39) first; the other groups (columns 8-31) load while
+            // the retarded time is solved, and the next pair's first columns while this
+            // pair's source terms are formed
+            const uint32_t tq = sh.tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+            uint32_t ra[8], rb[8];
+            tmem_ld_x8(tq + tm_col<SE>(s, 0), ra);
+            tmem_ld_x8(tq + tm_col<SE>(s, 0) + 32u, rb);
+            tmem_wait_ld_tie(ra, rb);
 #pragma unroll
-        for (int jp = 0; jp < SE / 2; ++jp) {
-            G2 gg[kGroups];
-            if (TM) {
-                uint32_t r[40];
-                const uint32_t ta = sh.tmem + ((uint32_t)(32 * (warp & 3)) << 16) + tm_col<SE>(s, jp);
-                tmem_ld32(ta, r);
-                tmem_ld8(ta + 32u, r);
-                tmem_wait_ld(r);
+            for (int jp = 0; jp < SE / 2; ++jp) {
+                const uint32_t ta = tq + tm_col<SE>(s, jp);
+                uint32_t rc[16], rd[8];
+                tmem_ld_x16(ta + 8u, rc);
+                tmem_ld_x8(ta + 24u, rd);
+                const G2 g0 = g2_of(ra), g4 = g2_of(rb);
+                MixedGeom m[OPW];
 #pragma unroll
-                for (int q = 0; q < kGroups; ++q) {
-                    gg[q].x = make_float2(__uint_as_float(r[8 * q]), __uint_as_float(r[8 * q + 1]));
-                    gg[q].y = make_float2(__uint_as_float(r[8 * q + 2]), __uint_as_float(r[8 * q + 3]));
-                    gg[q].z = make_float2(__uint_as_float(r[8 * q + 4]), __uint_as_float(r[8 * q + 5]));
-                    gg[q].w = make_float2(__uint_as_float(r[8 * q + 6]), __uint_as_float(r[8 * q + 7]));
+                for (int q = 0; q < OPW; ++q) m[q] = mixed_geom(g0, g4.w, ox[q], oy[q], oz[q], anc[q], p);
+                tmem_wait_ld_tie(rc, rd, m[0].dt, m[0].rx, m[0].ry, m[0].ir);
+                if (jp + 1 < SE / 2) {
+                    tmem_ld_x8(ta + tm_col<SE>(0, 1), ra);
+                    tmem_ld_x8(ta + tm_col<SE>(0, 1) + 32u, rb);
                 }
-            } else {
+#pragma unroll
+                for (int q = 0; q < OPW; ++q)
+                    mixed_source(m[q], g0.w, g2_of(rc), g2_of(rc + 8), g2_of(rd), g4, anc[q], p, tau, cur[q][2 * jp],
+                                 cur[q][2 * jp + 1]);
+                if (jp + 1 < SE / 2) tmem_wait_ld_tie(ra, rb);
+            }
+        } else {
+#pragma unroll
+            for (int jp = 0; jp < SE / 2; ++jp) {
+                G2 gg[kGroups];
                 const float* tl = st + (size_t)(2 * jp) * kTile + lane * 4;
 #pragma unroll
                 for (int q = 0; q < kGroups; ++q) gg[q] = load_g2(tl + q * 2 * kWin * 4);
-            }
 #pragma unroll
-            for (int q = 0; q < OPW; ++q)
-                sample_mixed2(gg, ox[q], oy[q], oz[q], anc[q], p, tau, cur[q][2 * jp], cur[q][2 * jp + 1]);
+                for (int q = 0; q < OPW; ++q)
+                    sample_mixed2(gg, ox[q], oy[q], oz[q], anc[q], p, tau, cur[q][2 * jp], cur[q][2 * jp + 1]);
+            }
         }
         const bool first_win = w == 0, last_win = w == nW - 1;
         const int rot_src = (lane + 31) & 31;

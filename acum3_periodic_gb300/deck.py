@@ -107,7 +107,9 @@ class Deck:
     lowpass: int = 1
     BB_noise: int = 0
     obs_file: np.ndarray = None                 # [nObs, 3] as in obs.dat
-    surfaces: List[np.ndarray] = field(default_factory=list)  # each [nTime, E_i, 8]
+    # each [nTime, E_i, ncol]: 8 columns for impermeable decks (x y z Cp A nx ny nz,
+    # io.cu:321), 12 for permeable ones (x y z u v w P rho ds nx ny nz, io.cu:286)
+    surfaces: List[np.ndarray] = field(default_factory=list)
     t_del: int = 0
     bb: List[BBSurface] = field(default_factory=list)
     name: str = ""
@@ -116,6 +118,11 @@ class Deck:
     @property
     def nSurf(self) -> int:
         return len(self.surfaces)
+
+    @property
+    def ncol(self) -> int:
+        """columns per surface row: 12 for a permeable deck, 8 otherwise"""
+        return 12 if self.impermeable == 0 else 8
 
     @property
     def nObs(self) -> int:
@@ -155,7 +162,7 @@ class Deck:
         return (self.obs_file.astype(np.float32) * s).astype(np.float32)
 
     def raw_surfaces(self) -> np.ndarray:
-        """All surfaces concatenated surface-major: [sum_i nTime*E_i*8] float32.  When the
+        """All surfaces concatenated surface-major: [sum_i nTime*E_i*ncol] float32.  When the
         surfaces are consecutive float32 views of one buffer (as the synthetic decks are
         built) that buffer is returned without a copy."""
         ss = self.surfaces
@@ -200,7 +207,7 @@ def write_deck(deck: Deck, path: str) -> None:
             f.write("%s %s %s\n" % (fmt(r[0]), fmt(r[1]), fmt(r[2])))
     for i, s in enumerate(deck.surfaces):
         _write_rows(os.path.join(path, "surfaces", "surface_%d.dat" % (i + 1)),
-                    "%d %d\n" % (s.shape[1], s.shape[0]), s.reshape(-1, 8))
+                    "%d %d\n" % (s.shape[1], s.shape[0]), s.reshape(-1, s.shape[2]))
     if deck.BB_noise == 1:
         os.makedirs(os.path.join(path, "BB_inputs"), exist_ok=True)
         with open(os.path.join(path, "input_BB"), "w") as f:
@@ -280,7 +287,8 @@ def read_deck(path: str) -> Deck:
         with open(fn) as f:
             e, nt = (int(x) for x in f.readline().split())
             vals = _floats(f.read())
-        d.surfaces.append(vals[: d.nTime * e * 8].reshape(d.nTime, e, 8))
+        nc = d.ncol
+        d.surfaces.append(vals[: d.nTime * e * nc].reshape(d.nTime, e, nc))
     if d.BB_noise == 1:
         _read_bb(d, path)
     d.name = os.path.basename(os.path.normpath(path))

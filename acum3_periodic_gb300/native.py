@@ -65,6 +65,7 @@ SIGNATURES = {
     "acum_get_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
     "acum_preprocess": (C.c_int, [C.c_void_p]),
     "acum_get_fields": (C.c_int, [C.c_void_p, _DP]),
+    "acum_get_permeable_fields": (C.c_int, [C.c_void_p, _DP, _DP, _DP, _DP, _DP]),
     "acum_tonal": (C.c_int, [C.c_void_p, C.c_int, _DP, _DP, _DP]),
     "acum_tonal_from_host": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "acum_tonal_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -194,6 +195,8 @@ class Context:
     def set_deck(self, deck, bb: bool = True):
         obs = np.ascontiguousarray(deck.obs_file, dtype=np.float32)
         ne = np.array(deck.elements, dtype=np.int32)
+        if any(s.shape[2] != deck.ncol for s in deck.surfaces):
+            raise ValueError("surface rows must have %d columns for impermeable = %d" % (deck.ncol, deck.impermeable))
         raw = deck.raw_surfaces()
         inp = inputs_of(deck)
         self._ck(self.L.acum_set_deck(self.h, C.byref(inp), deck.nObs, _p(obs, _FP), deck.nSurf, _p(ne, _IP),
@@ -257,6 +260,13 @@ class Context:
         out = np.zeros((self.E, self.T, 18))
         self._ck(self.L.acum_get_fields(self.h, _p(out)))
         return out
+
+    def permeable_fields(self):
+        """A permeable deck's preprocessed AoS arrays (X, N, V, U, PR), each [E][T][width],
+        FP64 (acum_get_permeable_fields)."""
+        out = [np.zeros((self.E, self.T, w)) for w in (4, 6, 6, 6, 4)]
+        self._ck(self.L.acum_get_permeable_fields(self.h, *(_p(a) for a in out)))
+        return tuple(out)
 
     def tonal(self, precision: int = MIXED):
         pT, pL, pA = (np.zeros((self.T, self.O)) for _ in range(3))

@@ -391,3 +391,28 @@ def permeable_rows(seed: int, ne, ntime: int, radius: float = 1.2, mach_tip: flo
     PR[:, :, 0] = 0.8 * harm + 0.1 * (u[:, 4:5] - 0.5)
     PR[:, :, 2] = 1.0 + 0.02 * harm
     return X, N, U, PR
+
+
+def permeable_deck(seed: int, ne, ntime: int, nobs: int = 4, lowpass: int = 1, periodic: int = 1) -> Deck:
+    """A permeable deck (impermeable 0): the data surface of permeable_rows written as the
+    12-column rows read_surf reads for such decks, x y z u v w P rho ds nx ny nz
+    (io.cu:286), with a few observers on a 10 m circle.  The reference preprocesses such
+    a deck (preprocess_per, main.cu:87) and launches no acoustic kernel for it
+    (main.cu:236), so its pressure outputs are zero."""
+    X, N, U, PR = permeable_rows(seed, ne, ntime)
+    rows = np.zeros((int(sum(ne)), ntime, 12), dtype=np.float32)
+    rows[:, :, 0:3] = X[:, :, 0:3]
+    rows[:, :, 3:6] = U[:, :, 0:3]
+    rows[:, :, 6] = PR[:, :, 0]
+    rows[:, :, 7] = PR[:, :, 2]
+    rows[:, :, 8] = X[:, :, 3]
+    rows[:, :, 9:12] = N[:, :, 0:3]
+    surfs = []
+    e0 = 0
+    for n in ne:
+        surfs.append(np.ascontiguousarray(rows[e0:e0 + n].transpose(1, 0, 2)))
+        e0 += n
+    obs = observers("circle", nobs, 10.0, elevation_deg=-20.0)
+    return Deck(a0=340.0, rhoRef=1.2, pRef=101325.0, oM=150.0, nTime=ntime, dPsi=360.0 / ntime, Minf=0.0,
+                Mref=0.5, CFDscale=1.0, OBSscale=1.0, impermeable=0, periodic=periodic, lowpass=lowpass,
+                BB_noise=0, obs_file=obs.astype(np.float32), surfaces=surfs, name="permeable")

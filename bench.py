@@ -41,6 +41,11 @@ sys.path.insert(0, ROOT)
 
 METRIC = "elem·obs·step evals/s: mixed vs FP64 at ≤0.05 dB OASPL; adjoint/fwd ratio"
 ALG_FLOPS_PER_EVAL = 102  # FP ops per tonal evaluation (integrand + observer time + deposits)
+# FP ops per broadband evaluation (section, observer, step, band) in the observer
+# contraction: five component products and sums (packed over band pairs) and the tip term,
+# 12, plus the observer geometry (~45 FP ops per section, step and observer) shared by the
+# 42 bands, 1
+BPM_FLOPS_PER_EVAL = 13
 # DRAM bytes (read + write) of one workload-2 launch of the mixed kernel, measured with ncu
 # (one pass: dram__bytes_read.sum + dram__bytes_write.sum: 14.72 GB + 10.39 GB); the FP64
 # flushes of the FP32 bin rows and the reads they cause, the 3.69 GB of records being read
@@ -133,6 +138,19 @@ class ClockSampler:
                     reasons.add(n)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
                 "samples": len(sm), "reasons": sorted(reasons)}
+
+
+_SMS = {}
+
+
+def nominal_fp32_peak(clocks, device: int = 0) -> float:
+    """Nominal FP32 FMA rate in TFLOP/s: SMs x 128 FP32 lanes x 2 FLOP x the median SM
+    clock sampled under load (the maximum clock when no sample was taken)."""
+    if device not in _SMS:
+        import torch
+        _SMS[device] = torch.cuda.get_device_properties(device).multi_processor_count
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    return _SMS[device] * 128 * 2 * float(mhz) * 1e6 / 1e12
 
 
 class StreamTimer:
@@ -313,6 +331,44 @@ def permeable_leg(native, device, steps=3, cpu=True, n_elem=8192, ntime=1440, fp
     return out
 
 
+def profile_case(name, device=0):
+    """One small run of one kernel family, for ncu captures of single launches:
+    adjoint-fp64 / adjoint-mixed: the forward and the adjoint on workload 3;
+    bpm: the broadband kernels on workload 1's broadband deck (4 x 50 sections, 720
+    steps, 1024 observers); batch: four workload-4 cases shrunk to 30 x 2 x 12 panels per
+    blade and 400 observers (366 MB of records) in one persistent launch (16 observers per
+    block, 8 elements per stage, 8 items per SM); tonal-small: the mixed kernel on
+    workload 2 reduced to 25 x 2 x 10 panels per blade and 512 observers."""
+    from acum3_periodic_gb300 import native, synth
+    out = {"case": name}
+    if name.startswith("adjoint"):
+        ctx = native.Context(device)
+        ctx.set_deck(synth.config_deck(3), bb=False)
+        J, *_ = ctx.adjoint(native.PLAIN_FP64 if name == "adjoint-fp64" else native.MIXED)
+        out.update(J=J, adjoint_ms=ctx.timing(4)[0])
+    elif name == "bpm":
+        ctx = native.Context(device)
+        ctx.set_deck(synth.config_deck(1))
+        ctx.bpm(0)
+        out.update(bpm_ms=ctx.timing(3)[0], contraction_ms=ctx.timing(6)[0])
+    elif name == "batch":
+        b = native.Batch(device)
+        for c in (3, 9, 14, 27):
+            b.add(synth.batch_deck(c, shrink=dict(n_span=30, n_chord_side=12, nobs=400)))
+        b.set_tile(16, 8, 8)
+        b.run(mode=0)
+        out.update(batch_ms=b.timing()[0])
+    else:
+        ctx = native.Context(device)
+        ctx.set_deck(synth.config_deck(2, scale=dict(n_span=25, n_chord_side=10, ntime=1440, nobs=512)), bb=False)
+        ctx.tonal(native.MIXED)
+        out.update(tonal_ms=ctx.timing(0)[0])
+    print(json.dumps(out))
+
+
+PROFILE_CASES = ("adjoint-fp64", "adjoint-mixed", "bpm", "batch", "tonal-small")
+
+
 def batch_leg(native, device, steps=1, inflight=6):
     """Workload 4: 64 seeded rotor cases (2-6 blades, 500-20000 elements per blade, 180-1440
     steps, 64-2048 observers) resident on the GPU and solved in mixed precision (a) by one
@@ -430,9 +486,14 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched leg (workload 4)")
     ap.add_argument("--no-permeable", action="store_true", help="skip the permeable preprocessing leg")
     ap.add_argument("--batch-steps", type=int, default=1, help="timed runs per mode of the batched leg")
+    ap.add_argument("--case", choices=sorted(PROFILE_CASES), default=None,
+                    help="run one small case of one kernel family once and exit (for ncu captures)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if not args.small else args.warmup
 
+    if args.case:
+        profile_case(args.case)
+        return
     ws, rank, local, dist = dist_init()
     from acum3_periodic_gb300 import synth
     scale = dict(n_span=25, n_chord_side=10, ntime=1440, nobs=512) if args.small else None
@@ -537,6 +598,8 @@ def main():
                                 "finalize": float(np.mean(fin_ms))},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": TONAL_TRAFFIC_BYTES,
+                     "peak_nominal": nominal_fp32_peak(clocks, local),
+                     "frac_of_nominal": achieved / nominal_fp32_peak(clocks, local),
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one full-size "
                                        "launch of this kernel (bytes per launch; algorithmic: %d)" % rec_bytes,
                      "peak_source": "measured FP32 FMA throughput of this GPU (acum_measure_peak); "
@@ -562,6 +625,7 @@ def main():
             spl, oas = ctx.bpm(0)
             bt.append(timer.stop())
         bpm_kernel_ms = ctx.timing(3)[0]
+        obs_ms = ctx.timing(6)[0]
         nsec = sum(b.nsect for b in deck.bb)
         bpm_evals = nsec * deck.nObs * deck.nTime * 42
         bsel = np.arange(0, deck.nObs, max(1, deck.nObs // 8))[:8]
@@ -571,6 +635,16 @@ def main():
                "evals": bpm_evals, "evals_per_s": bpm_evals / float(np.mean(bt)),
                "gpu_evals_per_s": bpm_evals / (bpm_kernel_ms * 1e-3), "gpu_ms": bpm_kernel_ms,
                "per_section_observer_band_per_s": bpm_evals / float(np.mean(bt)) / deck.nTime}
+        # roofline of the contraction kernel (bb_obs_kernel): FP32-pipe bound; its special
+        # functions (one square root, two reciprocal square roots and two quotients per
+        # observer, section and step) are 0.12 per evaluation, a small share of the XU rate
+        bpm_ach = BPM_FLOPS_PER_EVAL * bpm_evals / (obs_ms * 1e-3) / 1e12
+        bpm["roofline"] = {"kernel": "bb_obs_kernel", "bound": "fp32", "kernel_ms": obs_ms,
+                           "achieved": bpm_ach, "unit": "TFLOP/s", "algorithmic_flops_per_eval": BPM_FLOPS_PER_EVAL,
+                           "peak": fp32_peak, "frac": bpm_ach / fp32_peak,
+                           "peak_nominal": nominal_fp32_peak(clocks, local),
+                           "frac_of_nominal": bpm_ach / nominal_fp32_peak(clocks, local),
+                           "xu_ops_per_eval": 5.0 / 42.0}
         if not args.no_cpu:
             from oracle import oracle as O
             sub = deck.subset_observers(bsel)

@@ -76,14 +76,31 @@ int acum_load_deck(acum_ctx* ctx, const char* dir);
 
 /* The same deck from memory.  `obs_file` [nobs][3] are obs.dat values (OBSscale is
  * applied as read_observers does); `raw` holds the surface_*.dat rows of all surfaces,
- * surface after surface, each [nTime][nelem[i]][8] = x,y,z,Cp,A,nx,ny,nz.  The arrays are
- * copied; `raw` may be pinned host memory or device memory (raw_on_device = 1). */
+ * surface after surface, each [nTime][nelem[i]][ncol]: ncol = 8, x,y,z,Cp,A,nx,ny,nz, for
+ * impermeable decks (io.cu:321), ncol = 12, x,y,z,u,v,w,P,rho,ds,nx,ny,nz, for permeable
+ * ones (in->impermeable = 0, io.cu:286).  The arrays are copied; `raw` may be pinned host
+ * memory or device memory (raw_on_device = 1).
+ *
+ * Permeable decks follow main.cu: acum_preprocess runs preprocess_per (main.cu:87) on the
+ * GPU, the tonal calls return pT = pL = pA = 0 (main.cu:236 launches no kernel for them;
+ * main.cu:123-130 zeroed the arrays), acum_write_outputs writes those zero files, and the
+ * broadband path is unaffected; the impermeable-only calls (fields, adjoint, batches)
+ * return ACUM_ERR_UNSUPPORTED.  At most 4096 steps per period. */
 int acum_set_deck(acum_ctx* ctx, const acum_inputs* in, int nobs, const float* obs_file, int nsurf,
                   const int* nelem, const float* raw, int raw_on_device);
 
 /* Replaces only the surface rows (same sizes as the deck), e.g. for a new flight state;
  * host or device memory.  Marks the deck for re-preprocessing. */
 int acum_update_surfaces(acum_ctx* ctx, const float* raw, int raw_on_device);
+
+/* A permeable deck's arrays after preprocess_per (preprocess.cu:8-226, main.cu:87), in
+ * the reference's AoS layout (variables.cu:54, elements surface after surface, each
+ * [nTime][width]): Xham [E][nTime][4] = x,y,z,ds; Nham [6] = n, ndot; Vham [6] = V, Vdot;
+ * Uham [6] = u, udot; PRham [4] = P, Pdot, rho, rhodot.  FP64, equal bit for bit to the
+ * reference's FP64 build on the same rows; host memory.  ACUM_ERR_STATE for an
+ * impermeable deck. */
+int acum_get_permeable_fields(acum_ctx* ctx, double* Xham, double* Nham, double* Vham, double* Uham,
+                              double* PRham);
 
 /* Broadband inputs from memory (read_BB_inputs layout, io.cu:337-700).  Per BB surface
  * i: span, omega, ccw, psi_offset, trip, rotate[3], translate[3]; nsect[i] sections with
@@ -179,7 +196,8 @@ int acum_tonal_adjoint(acum_ctx* ctx, int precision, const double* dJ_dpA, doubl
 int acum_device_error_word(acum_ctx* ctx, uint32_t* out, int reset);
 
 /* Timing of the last run's kernels, measured with CUDA events on the launching stream:
- * which = 0 tonal kernel, 1 preprocess, 2 finalize, 3 bpm, 4 adjoint, 5 whole call.
+ * which = 0 tonal kernel, 1 preprocess, 2 finalize, 3 bpm (its six kernels), 4 adjoint,
+ * 5 whole call, 6 the broadband observer contraction alone (bb_obs_kernel).
  * *launches is the number of kernel launches of this library in the last run. */
 int acum_last_timing(const acum_ctx* ctx, int which, double* ms, long long* launches);
 

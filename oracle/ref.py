@@ -61,6 +61,9 @@ def lib(prec: str = "f64"):
         L.acumref_bands.argtypes = [_DP]
         L.acumref_preprocess_per.argtypes = [C.c_int, C.POINTER(C.c_int), C.c_int, _DP, C.c_int, C.c_int] + \
             [_DP] * 5 + [C.c_int]
+        L.acumref_preprocess_per_loaded.argtypes = [C.c_int]
+        L.acumref_fields_per.argtypes = [_DP] * 5
+        L.acumref_write_zero_history.argtypes = [C.c_char_p]
         _libs[prec] = L
     return _libs[prec]
 
@@ -100,6 +103,26 @@ class RefDeck:
         self.L.acumref_fields(_p(X), _p(N), _p(V), _p(P))
         E, T = self.E, self.nTime
         return X.reshape(E, T, 4), N.reshape(E, T, 6), V.reshape(E, T, 6), P.reshape(E, T, self.nPRham)
+
+    def permeable_fields(self):
+        """A loaded permeable deck after preprocess_per (main.cu:87): (Xham, Nham, Vham,
+        Uham, PRham) reshaped [E][T][k]."""
+        if self.impermeable != 0:
+            raise RuntimeError("not a permeable deck")
+        if not self.preprocessed:
+            if self.L.acumref_preprocess_per_loaded(1) != 0:
+                raise RuntimeError("acumref_preprocess_per_loaded failed")
+            self.preprocessed = True
+        E, T = self.E, self.nTime
+        out = [np.zeros(E * T * w) for w in (4, 6, 6, 6, 4)]
+        self.L.acumref_fields_per(*[_p(a) for a in out])
+        return tuple(a.reshape(E, T, -1) for a in out)
+
+    def write_zero_history(self, out_dir: str) -> None:
+        """pT.out, pL.out, pA.out as the reference writes them for a permeable deck."""
+        rc = self.L.acumref_write_zero_history(os.path.abspath(out_dir).encode())
+        if rc != 0:
+            raise RuntimeError("acumref_write_zero_history failed: %d" % rc)
 
     def preprocess(self) -> None:
         if not self.preprocessed:

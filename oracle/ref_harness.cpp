@@ -319,3 +319,40 @@ extern "C" int acumref_preprocess_per(int nsurf, const int* ne, int nt, const do
     E = XPtr = NPtr = VPtr = UPtr = PRPtr = NULL;
     return 0;
 }
+
+/* preprocess_per (main.cu:87) on the deck loaded by acumref_load (a permeable deck:
+ * read_surf filled Xham, Uham, PRham and Nham from the 12-column rows, io.cu:263-293). */
+extern "C" int acumref_preprocess_per_loaded(int quiet)
+{
+    if (impermeable != 0) return -1;
+    quiet_on(quiet);
+    preprocess_per();
+    quiet_off(quiet);
+    return 0;
+}
+
+/* The five AoS arrays of a loaded permeable deck (Xham, Nham, Vham, Uham, PRham; sizes
+ * nXtot, nNtot, nVtot, nUtot, nPRtot with nPRham = 4). */
+extern "C" void acumref_fields_per(double* X, double* N, double* V, double* U, double* PR)
+{
+    for (long i = 0; i < nXtot; i++) X[i] = Xham[i];
+    for (long i = 0; i < nNtot; i++) N[i] = Nham[i];
+    for (long i = 0; i < nVtot; i++) V[i] = Vham[i];
+    for (long i = 0; i < nUtot; i++) U[i] = Uham[i];
+    for (long i = 0; i < nPRtot; i++) PR[i] = PRham[i];
+}
+
+/* The reference's writer (io.cu:137-203) run in `dir` on the zeroed pT/pL/pA that
+ * main.cu:123-130 prepares, which is what it writes for a permeable deck (main.cu:236
+ * launches no kernel for it). */
+extern "C" int acumref_write_zero_history(const char* dir)
+{
+    char cwd[4096];
+    if (!getcwd(cwd, sizeof cwd)) return -1;
+    if (chdir(dir) != 0) return -2;
+    real* z = (real*)calloc((size_t)nTime * nObs, sizeof(real));
+    writeTimeHistory(z, z, z);
+    free(z);
+    if (chdir(cwd) != 0) return -3;
+    return 0;
+}

@@ -8,7 +8,9 @@ It writes a few small seeded decks (the reference's text formats) under
 tests/golden/decks/<name>/ and, for each, the FP64-build outputs (plus the as-written
 FP32-build outputs, for information) into tests/golden/<name>.npz; and unit vectors of
 the broadband shape curves and the preprocessing filters into tests/golden/units.npz; and
-the permeable preprocessing of a seeded data surface into tests/golden/permeable.npz.
+the permeable preprocessing of a seeded data surface into tests/golden/permeable.npz; and
+a permeable deck directory with its preprocessed arrays (tests/golden/permeable_deck.npz)
+and the reference's pressure files for it (decks/permeable_deck/expected/).
 """
 import os
 import sys
@@ -109,6 +111,19 @@ def main():
             per["%s_p%d_l%d" % (nm, periodic, lowpass)] = a
     np.savez_compressed(os.path.join(OUT, "permeable.npz"), **per)
     print("wrote permeable")
+    # a permeable deck directory (impermeable 0, 12-column surface rows, filters on),
+    # loaded by the reference's own readers: its preprocess_per arrays (FP64 build) and the
+    # pressure files the reference writes for it (FP32 build, the program as shipped)
+    d = synth.permeable_deck(22, [6, 4], 40, nobs=3)
+    path = os.path.join(OUT, "decks", "permeable_deck")
+    write_deck(d, path)
+    rd = ref.RefDeck(path, "f64")
+    pd = dict(zip(("X", "N", "V", "U", "PR"), rd.permeable_fields()))
+    np.savez_compressed(os.path.join(OUT, "permeable_deck.npz"), **pd)
+    exp = os.path.join(path, "expected")
+    os.makedirs(exp, exist_ok=True)
+    ref.RefDeck(path, "f32").write_zero_history(exp)
+    print("wrote permeable_deck")
 
 
 if __name__ == "__main__":

@@ -152,3 +152,35 @@ def test_foreign_surface_cache_ignored(tonal_deck, tmp_path):
         f.write(b"not a cache" * 10)
     rc, s, _ = sizes(p)
     assert rc == 0 and s == [d.nSurf, d.nTime, d.nObs, d.E, 0, 0]
+
+
+PERM_DECK = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "decks", "permeable_deck")
+
+
+def test_permeable_deck_read(tmp_path):
+    """A permeable deck (impermeable 0): 12-column rows (io.cu:263-293); a file cut short
+    is refused; the surface cache keeps the 12-column rows and a cache of another row
+    width is not used."""
+    p = tmp_path / "perm"
+    shutil.copytree(PERM_DECK, p, ignore=shutil.ignore_patterns("expected"))
+    rc, s, msg = sizes(p)
+    assert rc == 0, msg
+    assert s == [2, 40, 3, 10, 0, 0]
+    assert write_cache(p) == 0
+    rc, s2, _ = sizes(p)
+    assert rc == 0 and s2 == s
+    # the same rows read as an impermeable deck (8 columns) do not match the cached width:
+    # the text is parsed again, with 8 columns per row
+    inp = open(p / "input").read().replace("impermeable 0", "impermeable 1")
+    with open(p / "input", "w") as f:
+        f.write(inp)
+    rc, s3, _ = sizes(p)
+    assert rc == 0 and s3 == s
+    q = tmp_path / "perm_short"
+    shutil.copytree(PERM_DECK, q, ignore=shutil.ignore_patterns("expected"))
+    fn = q / "surfaces" / "surface_2.dat"
+    lines = open(fn).read().splitlines()
+    with open(fn, "w") as f:
+        f.write("\n".join(lines[:-1]) + "\n")
+    rc, _, msg = sizes(q)
+    assert rc == IO_ERR and "surface_2" in msg

@@ -1,7 +1,7 @@
 """Edge cases of the tonal path: the smallest decks the readers accept, the longest period
 the preprocessing supports (4096 steps, where the bin rows of one observer take 32 KB of
 shared memory and the blocks hold few observers), and the decks the library refuses with
-a status instead of running (no observers, too few or too many steps, permeable)."""
+a status instead of running (no observers, too few or too many steps)."""
 import numpy as np
 import pytest
 
@@ -76,12 +76,5 @@ def test_refused_decks(ctx):
     with pytest.raises(native.AcumError) as e:
         ctx.tonal(native.MIXED)
     assert e.value.code == ERR_UNSUPPORTED
-    # a permeable deck: the reference runs no acoustic kernel for it (main.cu:236)
-    perm = synth.config_deck(0, replicate=85, scale=dict(n_span=2, n_chord_side=2, ntime=24, nobs=3))
-    perm.impermeable = 0
-    with pytest.raises(native.AcumError) as e:
-        ctx.set_deck(perm, bb=False)
-    assert e.value.code == ERR_UNSUPPORTED
-    assert "acum_preprocess_per" in str(e.value)
     # the context still solves a valid deck afterwards
     _against_oracle(ctx, d)

@@ -78,3 +78,26 @@ def test_permeable_preprocessing(periodic, lowpass):
     for nm, a in zip("XNVUP", out):
         want = g["%s_p%d_l%d" % (nm, periodic, lowpass)]
         np.testing.assert_array_equal(a, want)
+
+
+def test_permeable_deck_preprocessing():
+    """The oracle's preprocess_per on the golden permeable deck as the Python reader reads
+    it (12-column rows) against the reference's FP64 build on the same directory, loaded
+    with its own readers: every array bit for bit."""
+    from acum3_periodic_gb300.deck import read_deck
+    d = read_deck(os.path.join(GOLDEN, "decks", "permeable_deck"))
+    assert d.impermeable == 0 and d.ncol == 12
+    der = d.derived()
+    rows = np.concatenate([s.transpose(1, 0, 2) for s in d.surfaces], axis=0).astype(np.float64)
+    X = np.zeros(rows.shape[:2] + (4,))
+    N = np.zeros(rows.shape[:2] + (6,))
+    U = np.zeros(rows.shape[:2] + (6,))
+    PR = np.zeros(rows.shape[:2] + (4,))
+    X[..., 0:3], X[..., 3] = rows[..., 0:3], rows[..., 8]
+    N[..., 0:3], U[..., 0:3] = rows[..., 9:12], rows[..., 3:6]
+    PR[..., 0], PR[..., 2] = rows[..., 6], rows[..., 7]
+    out = O.preprocess_per(X, N, U, PR, der["dTau"], der["a0"], der["rhoRef"], der["Mref"], der["CFDscale"],
+                           der["periodic"], der["lowpass"])
+    g = np.load(os.path.join(GOLDEN, "permeable_deck.npz"))
+    for a, k in zip(out, ("X", "N", "V", "U", "PR")):
+        np.testing.assert_array_equal(a, g[k])
