@@ -370,7 +370,8 @@ int acum_ctx::ensure_prep(bool need64, bool need32, bool need_fields)
     if (!do64 && !do32 && !need_fields) return ACUM_OK;
     if (!d_raw.p) return fail(this, ACUM_ERR_STATE, "the surface rows were released after preprocessing");
     if (T > 4096) return fail(this, ACUM_ERR_UNSUPPORTED, "nTime above 4096 is not supported by the preprocessing");
-    const size_t nrec = (size_t)Epad * nW * kGroups * kWin * 4;
+    const size_t nrec = (size_t)Epad * nW * kGroups * kWin * 4;     // FP64 records
+    const size_t nrec32 = (size_t)Epad * nW * kGroups32 * kWin * 4;  // FP32 records
     const long long layout[4] = {(long long)E, (long long)Epad, (long long)nW, (long long)T};
     const auto same = [&](const long long* l) { return std::equal(l, l + 4, layout); };
     if (do64) {
@@ -380,9 +381,9 @@ int acum_ctx::ensure_prep(bool need64, bool need32, bool need_fields)
         std::copy(layout, layout + 4, rec64_layout);
     }
     if (do32) {
-        const bool clear = d_rec32.n < nrec || !same(rec32_layout);
-        CK(this, d_rec32.ensure(nrec));
-        if (clear) CK(this, cudaMemsetAsync(d_rec32.p, 0, nrec * 4, stream));
+        const bool clear = d_rec32.n < nrec32 || !same(rec32_layout);
+        CK(this, d_rec32.ensure(nrec32));
+        if (clear) CK(this, cudaMemsetAsync(d_rec32.p, 0, nrec32 * 4, stream));
         std::copy(layout, layout + 4, rec32_layout);
     }
     if (need_fields) CK(this, d_fields.ensure((size_t)E * T * kFields));
@@ -810,7 +811,7 @@ int find_pth(const S* rObs, const S* tObs, S* pT, S* pL, S* pA, const S* Xham, c
     CK(nullptr, cudaMemcpyAsync(c->d_off.p + E, no.data(), E * 8, cudaMemcpyHostToDevice, st));
     CK(nullptr, cudaMemcpyAsync(c->d_off.p + 2 * E, vo.data(), E * 8, cudaMemcpyHostToDevice, st));
     CK(nullptr, cudaMemcpyAsync(c->d_off.p + 3 * E, po.data(), E * 8, cudaMemcpyHostToDevice, st));
-    const size_t nrec = (size_t)Epad * nW * kGroups * kWin * 4;
+    const size_t nrec = (size_t)Epad * nW * (f64 ? kGroups : kGroups32) * kWin * 4;
     AosArgs a;
     memset(&a, 0, sizeof(a));
     a.X = Xham;

@@ -11,30 +11,40 @@
 
 namespace acum {
 
-// Record layout of one element-step for the tonal kernels: 5 groups of 4 reals, so a
-// lane reads its step with 128-bit (FP32) or 2x128-bit (FP64) loads.
+// Record layout of one element-step for the tonal kernels.
+// FP64 records (the plain form and the adjoints): 5 groups of 4 reals, a lane reads its
+// step with 2x128-bit loads per group.
 //   g0: x, y, z, dsD          (dsD   = D1 * ds,              D1 = 1/(4 pi a0))
 //   g1: Mx, My, Mz, M2        (M     = V / a0,  M2 = |V|^2 / a0^2)
 //   g2: Mdx, Mdy, Mdz, ATD    (Md    = Vdot / a0, ATD = D1 * rho0 * (V.n) * a0 * ds)
 //   g3: Lx, Ly, Lz, Lm        (L     = P n,  Lm = L.V / a0)
-//   g4: Ldx, Ldy, Ldz, xv     (Ldot  = Pdot n + P ndot, xv = x.vInf for the anchored
-//                              retarded time of the mixed form)
+//   g4: Ldx, Ldy, Ldz, xv     (Ldot  = Pdot n + P ndot, xv = x.vInf)
+// FP32 records (the mixed form): the 16 fields the integrand cannot do without, 4 groups
+// of 4 floats, so that a lane reads an element pair's step with 8 128-bit loads; the
+// panel weight dsD is folded into the loading vectors, and |M|^2, L.M and x.vInf are
+// recomputed from the fields they are made of:
+//   g0: x, y, z, ATD
+//   g1: Mx, My, Mz, Ldx'      (Ld' = dsD Ldot)
+//   g2: Mdx, Mdy, Mdz, Ldy'
+//   g3: Lx', Ly', Lz', Ldz'   (L'  = dsD L)
 // In HBM the FP64 records are tiled [element][window][group][32 steps][4]: an (element,
 // 32-step window) tile is contiguous (5120 B), which is what one bulk (TMA) copy moves
 // into shared memory.  The FP32 records interleave pairs of elements so that the mixed
 // kernel reads the two elements' values of a field as one register pair (the operand of
 // a packed FP32 instruction): [element pair][window][group][half][32 steps][4], half 0 =
 // (f0 of e, f0 of e+1, f1 of e, f1 of e+1), half 1 = the same for fields 2 and 3; an
-// (element pair, window) tile is 5120 B.
-constexpr int kGroups = 5;
+// (element pair, window) tile is 4096 B.
+constexpr int kGroups = 5;    // FP64 records
+constexpr int kGroups32 = 4;  // FP32 records
 constexpr int kWin = 32;
 constexpr int kFields = 18;  // x,y,z,ds, n(3), ndot(3), V(3), Vdot(3), P, Pdot
 
-// float offset of field c (0..3) of group q of element e at step t in the FP32 records
+// float offset of field c (0..3) of group q (0..3) of element e at step t in the FP32
+// records
 __host__ __device__ __forceinline__ size_t rec32_offset(int e, int nW, int t, int q, int c)
 {
     const int w = t / kWin, lane = t % kWin;
-    return ((((size_t)(e >> 1) * nW + w) * kGroups + q) * 2 + (c >> 1)) * (kWin * 4) + (size_t)lane * 4 +
+    return ((((size_t)(e >> 1) * nW + w) * kGroups32 + q) * 2 + (c >> 1)) * (kWin * 4) + (size_t)lane * 4 +
            (size_t)((c & 1) * 2 + (e & 1));
 }
 
@@ -85,6 +95,18 @@ struct PrepArgs {
     double* fields;        // optional [E][T][18]
 };
 cudaError_t launch_prep(const PrepArgs& a, cudaStream_t s);
+
+// The 16 FP32 record fields (g0..g3 above) of one element-step from the quantities of the
+// preprocessing, R = double or float (the products are formed in R, then rounded).
+template <typename R>
+__host__ __device__ __forceinline__ void rec32_fields(const R* x, R dsD, R ATD, const R* M, const R* Md, const R* L,
+                                                      const R* Ld, float* f)
+{
+    f[0] = (float)x[0]; f[1] = (float)x[1]; f[2] = (float)x[2]; f[3] = (float)ATD;
+    f[4] = (float)M[0]; f[5] = (float)M[1]; f[6] = (float)M[2]; f[7] = (float)(dsD * Ld[0]);
+    f[8] = (float)Md[0]; f[9] = (float)Md[1]; f[10] = (float)Md[2]; f[11] = (float)(dsD * Ld[1]);
+    f[12] = (float)(dsD * L[0]); f[13] = (float)(dsD * L[1]); f[14] = (float)(dsD * L[2]); f[15] = (float)(dsD * Ld[2]);
+}
 
 // records straight from reference-layout AoS arrays (for the drop-in entry points)
 struct AosArgs {

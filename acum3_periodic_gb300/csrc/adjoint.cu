@@ -40,7 +40,7 @@ constexpr int kAdjStride = 30;  // new samples per window
 constexpr int kCot = 19;        // record-field cotangents per element-step
 
 struct AdjDev {
-    const void* rec;  // forward record tiles [Epad][nW][5][32][4]
+    const void* rec;  // FP64 record tiles [Epad][nW][5][32][4]
     int E, nW, T, O, nWa;
     const void* obs;  // [O][3]
     const void* g;    // [O][T]
@@ -78,25 +78,18 @@ struct Fwd {
     R dx, dy, dz, c, beta, s, tr, rx, ry, rz, ir, Mr, Mdr, Lr, Ldr, G, qa, K, base, Y, pt, pl, t;
 };
 
-// the 20 record fields of (element, step): FP64 tiles [element][window][group][32][4],
-// FP32 tiles of element pairs (rec32_offset)
-__device__ __forceinline__ void load_rec(const double* rec, int nW, int e, int step, double* f)
+// the 20 record fields of (element, step) from the FP64 tiles [element][window][group][32]
+// [4], in the adjoint's precision (the FP32 adjoint rounds them once; the mixed form's
+// FP32 records hold a reduced field set, so both adjoints read the FP64 ones)
+template <typename R>
+__device__ __forceinline__ void load_rec(const double* rec, int nW, int e, int step, R* f)
 {
     const double* tile = rec + ((size_t)e * nW + step / kWin) * (kGroups * kWin * 4);
     const int lane = step % kWin;
 #pragma unroll
     for (int q = 0; q < kGroups; ++q)
 #pragma unroll
-        for (int c = 0; c < 4; ++c) f[4 * q + c] = tile[((size_t)q * kWin + lane) * 4 + c];
-}
-
-__device__ __forceinline__ void load_rec(const float* rec, int nW, int e, int step, float* f)
-{
-    const float* base = rec + rec32_offset(e, nW, step, 0, 0);
-#pragma unroll
-    for (int q = 0; q < kGroups; ++q)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) f[4 * q + c] = base[rec32_offset(0, 1, 0, q, c)];
+        for (int c = 0; c < 4; ++c) f[4 * q + c] = (R)tile[((size_t)q * kWin + lane) * 4 + c];
 }
 
 template <typename R>
@@ -212,7 +205,7 @@ __global__ void __launch_bounds__(128) adjoint_kernel(AdjDev p)
     const int step = tau < 0 ? tau + p.T : (tau >= p.T ? tau - p.T : tau);
     const bool owner = lane >= 1 && lane <= kAdjStride && tau >= 0 && tau < p.T;
     R f[20];
-    load_rec(reinterpret_cast<const R*>(p.rec), p.nW, e, step, f);
+    load_rec<R>(reinterpret_cast<const double*>(p.rec), p.nW, e, step, f);
     R acc[kCot];
 #pragma unroll
     for (int k = 0; k < kCot; ++k) acc[k] = 0;
@@ -561,8 +554,9 @@ extern "C" int acum_tonal_adjoint(acum_ctx* ctx, int precision, const double* dJ
     const long long E = ctx->E;
     const bool f64 = precision == ACUM_PLAIN_FP64;
     ctx->begin_run();
-    // forward (both record layouts are built; the FP64 fields feed the chain kernel)
-    int rc = ctx->ensure_prep(f64, !f64, true);
+    // forward; both adjoints read the FP64 records, and the FP64 fields feed the chain
+    // kernel
+    int rc = ctx->ensure_prep(true, !f64, true);
     if (rc) return rc;
     const size_t n = (size_t)T * O;
     CKA(ctx->d_out.ensure(3 * n));
@@ -612,7 +606,7 @@ extern "C" int acum_tonal_adjoint(acum_ctx* ctx, int precision, const double* dJ
         p.g = s->g64.p;
         adjoint_kernel<double><<<blocks, 128, 0, st>>>(p);
     } else {
-        p.rec = ctx->d_rec32.p;
+        p.rec = ctx->d_rec64.p;
         p.obs = ctx->d_obs32.p;
         p.g = s->g32.p;
         adjoint_kernel<float><<<blocks, 128, 0, st>>>(p);

@@ -135,7 +135,7 @@ void build_items(const acum_batch* b, int W, int SE, int ips, std::vector<BatchI
         int nchunk = (int)std::ceil(per_tile / std::max(target, 1.0));
         // element chunks of at most ~32 MB of records (as the single-deck plan), so that
         // the items of one chunk, which run close together in time, share it in L2
-        const size_t per_elem = (size_t)c->nW * kGroups * kWin * 4 * sizeof(float);
+        const size_t per_elem = (size_t)c->nW * kGroups32 * kWin * 4 * sizeof(float);
         const int max_groups = std::max(1, (int)(((size_t)32 << 20) / per_elem) / SE);
         nchunk = std::max(nchunk, (groups + max_groups - 1) / max_groups);
         nchunk = std::max(1, std::min(nchunk, groups));
@@ -304,7 +304,7 @@ extern "C" int acum_batch_add(acum_batch* b, const acum_inputs* in, int nobs, co
     // what the case holds while it is added (rows + records) and afterwards (records,
     // sums, results), against the device's free memory with 1 GiB to spare
     const long long T = in->nTime, nW = (T + kWin - 1) / kWin, Epad = (E + 7) / 8 * 8;
-    const double rows = (double)E * T * 8 * 4, recs = (double)Epad * nW * kGroups * kWin * 4 * 4;
+    const double rows = (double)E * T * 8 * 4, recs = (double)Epad * nW * kGroups32 * kWin * 4 * 4;
     const double sums = (double)nobs * T * 8 * 3;
     size_t free_b = 0, total_b = 0;
     BK(b, cudaMemGetInfo(&free_b, &total_b));

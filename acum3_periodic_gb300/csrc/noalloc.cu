@@ -12,7 +12,7 @@
 //
 // Limits and behaviour:
 //  * the scratch array is kNoAllocBytes = 128 MiB per device; a call whose records
-//    (80 bytes per element-step, elements rounded up to 8 and steps to 32) plus FP64 bin
+//    (64 bytes per element-step, elements rounded up to 8 and steps to 32) plus FP64 bin
 //    sums (16 bytes per observer-step) exceed it is rejected with ACUM_ERR_INVALID and a
 //    message that gives both sizes; at most kMaxSurfaces surfaces;
 //  * it accepts the inputs the allocating drop-in accepts (nTime >= 4, tObs[t] = t * dPsi
@@ -86,9 +86,11 @@ __global__ void noalloc_records_kernel(const float* __restrict__ X, const float*
     r[12] = L[0]; r[13] = L[1]; r[14] = L[2]; r[15] = (L[0] * vx + L[1] * vy + L[2] * vz) * ia0;
     r[16] = Pd * nx + P * (double)n[3]; r[17] = Pd * ny + P * (double)n[4]; r[18] = Pd * nz + P * (double)n[5];
     r[19] = (double)x[0] * vx_inf + (double)x[1] * vy_inf + (double)x[2] * vz_inf;
+    float f32[16];
+    rec32_fields<double>(r, r[3], r[11], r + 4, r + 8, r + 12, r + 16, f32);
     float* r32 = rec + rec32_offset(e, nW, t, 0, 0);
-    for (int q = 0; q < kGroups; ++q)
-        for (int c = 0; c < 4; ++c) r32[rec32_offset(0, 1, 0, q, c)] = (float)r[4 * q + c];
+    for (int q = 0; q < kGroups32; ++q)
+        for (int c = 0; c < 4; ++c) r32[rec32_offset(0, 1, 0, q, c)] = f32[4 * q + c];
 }
 
 }  // namespace acum
@@ -162,7 +164,7 @@ extern "C" int acum_find_pressure_time_history_noalloc(const float* rObs, const 
     if (Et <= 0) return bad(ACUM_ERR_INVALID, "findPressureTimeHistory_noalloc: no elements");
     const int nW = (nTime + kWin - 1) / kWin;
     const long long Epad = (Et + 7) / 8 * 8;
-    const size_t rec_bytes = (size_t)Epad * nW * kGroups * kWin * 4 * sizeof(float);
+    const size_t rec_bytes = (size_t)Epad * nW * kGroups32 * kWin * 4 * sizeof(float);
     const size_t acc_off = (rec_bytes + 255) / 256 * 256;
     const size_t acc_bytes = (size_t)nObs * nTime * 2 * sizeof(double);
     if (acc_off + acc_bytes > kNoAllocBytes) {

@@ -207,9 +207,11 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
             }
         }
         if (a.rec32) {
+            float f32[16];
+            rec32_fields<R>(rec, rec[3], rec[11], rec + 4, rec + 8, rec + 12, rec + 16, f32);
             float* r32 = a.rec32 + rec32_offset(e, a.nW, t, 0, 0);
-            for (int q = 0; q < kGroups; ++q)
-                for (int c = 0; c < 4; ++c) r32[rec32_offset(0, 1, 0, q, c)] = (float)rec[4 * q + c];
+            for (int q = 0; q < kGroups32; ++q)
+                for (int c = 0; c < 4; ++c) r32[rec32_offset(0, 1, 0, q, c)] = f32[4 * q + c];
         }
     }
 }
@@ -274,9 +276,11 @@ __global__ void aos_record_kernel(AosArgs a)
         }
     }
     if (a.rec32) {
+        float f32[16];
+        rec32_fields<double>(rec, rec[3], rec[11], rec + 4, rec + 8, rec + 12, rec + 16, f32);
         float* r32 = a.rec32 + rec32_offset(e, a.nW, t, 0, 0);
-        for (int q = 0; q < kGroups; ++q)
-            for (int c = 0; c < 4; ++c) r32[rec32_offset(0, 1, 0, q, c)] = (float)rec[4 * q + c];
+        for (int q = 0; q < kGroups32; ++q)
+            for (int c = 0; c < 4; ++c) r32[rec32_offset(0, 1, 0, q, c)] = f32[4 * q + c];
     }
 }
 
@@ -665,22 +669,24 @@ __device__ __forceinline__ G2 load_g2(const float* half0)
 
 // The samples of one step of an element pair, in packed FP32 (see the comment above for
 // the integrand and the anchored retarded time), in two parts: the retarded time and
-// the radiation vector from the positions (group 0) and x.v (group 4, w), then the
-// source terms from the other groups.  The tensor-memory form loads the other groups
-// while the first part runs.
+// the radiation vector from the positions (group 0), then the source terms from the
+// other groups.  The tensor-memory form loads the other groups while the first part
+// runs.
 struct MixedGeom {
     float2 dt, rx, ry, rz, ir;
 };
 
-__device__ __forceinline__ MixedGeom mixed_geom(const G2& g0, float2 xv, float ox, float oy, float oz,
-                                                const Anchor& an, const KParams& p)
+__device__ __forceinline__ MixedGeom mixed_geom(const G2& g0, float ox, float oy, float oz, const Anchor& an,
+                                                const KParams& p)
 {
     const float2 OX = f2(ox), OY = f2(oy), OZ = f2(oz);
     const float2 dx = sub2(OX, g0.x), dy = sub2(OY, g0.y), dz = sub2(OZ, g0.z);
-    // anchored retarded time (xv = x.v): -num = x.(d + D0) - 2 t0 x.v
+    // x.(-vInf), recomputed from the position (nv = -vInf)
+    const float2 xnv = fma2(g0.x, p.nvx2, fma2(g0.y, p.nvy2, mul2(g0.z, p.nvz2)));
+    // anchored retarded time: -num = x.(d + D0) - 2 t0 x.v
     const float2 S = fma2(g0.x, add2(dx, OX), fma2(g0.y, add2(dy, OY), mul2(g0.z, add2(dz, OZ))));
-    const float2 nnum = fma2(f2(-an.t2), xv, S);
-    const float2 bp = sub2(f2(an.s0), xv);
+    const float2 nnum = fma2(f2(an.t2), xnv, S);
+    const float2 bp = add2(f2(an.s0), xnv);
     const float2 q = fma2(p.nalpha2, nnum, mul2(bp, bp));
     const float2 den = fma2(q, make_float2(rsqrt_ftz(q.x), rsqrt_ftz(q.y)), bp);
     MixedGeom m;
@@ -693,21 +699,25 @@ __device__ __forceinline__ MixedGeom mixed_geom(const G2& g0, float2 xv, float o
     return m;
 }
 
-__device__ __forceinline__ void mixed_source(const MixedGeom& m, float2 dsD, const G2& g1, const G2& g2, const G2& g3,
-                                             const G2& g4, const Anchor& an, const KParams& p, int tau, SmpF& oa,
+// g0..g3: the FP32 record groups (x, ATD | M, Ld'x | Md, Ld'y | L', Ld'z)
+__device__ __forceinline__ void mixed_source(const MixedGeom& m, const G2& g0, const G2& g1, const G2& g2,
+                                             const G2& g3, const Anchor& an, const KParams& p, int tau, SmpF& oa,
                                              SmpF& ob)
 {
     const float2 rx = m.rx, ry = m.ry, rz = m.rz, ir = m.ir;
+    // |M|^2 and L'.M from the fields they are made of
+    const float2 M2 = fma2(g1.x, g1.x, fma2(g1.y, g1.y, mul2(g1.z, g1.z)));
+    const float2 Lm = fma2(g3.x, g1.x, fma2(g3.y, g1.y, mul2(g3.z, g1.z)));
     const float2 Mr = mul2(fma2(g1.x, rx, fma2(g1.y, ry, mul2(g1.z, rz))), ir);
     const float2 Mdr = mul2(fma2(g2.x, rx, fma2(g2.y, ry, mul2(g2.z, rz))), ir);
     const float2 Lr = mul2(fma2(g3.x, rx, fma2(g3.y, ry, mul2(g3.z, rz))), ir);
-    const float2 Ldr = mul2(fma2(g4.x, rx, fma2(g4.y, ry, mul2(g4.z, rz))), ir);
+    const float2 Ldr = mul2(fma2(g1.w, rx, fma2(g2.w, ry, mul2(g3.w, rz))), ir);
     const float2 G = rcp2(sub2(f2(1.0f), Mr));
     const float2 qa = mul2(p.a02, ir);
-    const float2 K = fma2(qa, sub2(Mr, g1.w), Mdr);
+    const float2 K = fma2(qa, sub2(Mr, M2), Mdr);
     const float2 base = mul2(mul2(ir, G), G);
-    const float2 pt = mul2(mul2(g2.w, base), mul2(G, K));
-    const float2 pl = mul2(mul2(dsD, base), fma2(mul2(Lr, G), K, fma2(qa, sub2(Lr, g3.w), Ldr)));
+    const float2 pt = mul2(mul2(g0.w, base), mul2(G, K));
+    const float2 pl = mul2(base, fma2(mul2(Lr, G), K, fma2(qa, sub2(Lr, Lm), Ldr)));
     // observer time in bins: tau + round(t0 oM/dPsi) + x, x = frac(t0 oM/dPsi) + dt oM/dPsi;
     // outside the floor's range (or not finite) the fraction is NaN, which the deposit
     // rejects (and reports) whatever the integer part holds
@@ -725,12 +735,12 @@ __device__ __forceinline__ void mixed_source(const MixedGeom& m, float2 dsD, con
     ob.pl = pl.y;
 }
 
-// g[q] = group q of the pair's records
+// g[q] = group q of the pair's FP32 records
 __device__ __forceinline__ void sample_mixed2(const G2* g, float ox, float oy, float oz, const Anchor& an,
                                               const KParams& p, int tau, SmpF& oa, SmpF& ob)
 {
-    const MixedGeom m = mixed_geom(g[0], g[4].w, ox, oy, oz, an, p);
-    mixed_source(m, g[0].w, g[1], g[2], g[3], g[4], an, p, tau, oa, ob);
+    const MixedGeom m = mixed_geom(g[0], ox, oy, oz, an, p);
+    mixed_source(m, g[0], g[1], g[2], g[3], an, p, tau, oa, ob);
 }
 
 // A group as tensor-memory columns 8q .. 8q + 7 of a pair hold it (half 0: f0 e, f0 e+1,
@@ -845,14 +855,14 @@ struct __align__(16) MixedShared {
     uint32_t tmem;           // tensor-memory form: base address of the block's columns
 };
 
-// Tensor-memory form: stage slot s, element pair jp of the stage, occupies the 40 columns
-// from tm_col(s, jp) (10 blocks of 4: group q, half h at 4 (2q + h)).
+// Tensor-memory form: stage slot s, element pair jp of the stage, occupies the 32 columns
+// from tm_col(s, jp) (8 blocks of 4: group q, half h at 4 (2q + h)).
 template <int SE>
 __device__ __forceinline__ uint32_t tm_col(int s, int jp)
 {
-    return (uint32_t)((s * (SE / 2) + jp) * 40);
+    return (uint32_t)((s * (SE / 2) + jp) * 32);
 }
-constexpr uint32_t kTmemCols = 512;  // NS x SE / 2 x 40 <= 320 for every stage shape
+constexpr uint32_t kTmemCols = 512;  // NS x SE / 2 x 32 <= 512 for every stage shape the plan allows
 
 // One work item of the mixed form: observers [ot*W, ot*W + W) and elements [e0, e1)
 // (a multiple of SE) of the deck `p`; each warp evaluates OPW observers on the records it
@@ -866,7 +876,7 @@ template <int SE, int OPW, bool TM, bool HOIST = true>
 __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot, int e0, int e1, unsigned char* smem,
                                            size_t stage_off, MixedShared<SE, OPW>& sh, unsigned& gbase)
 {
-    constexpr int kTile = kGroups * kWin * 4;
+    constexpr int kTile = kGroups32 * kWin * 4;  // floats per (element, window) of the FP32 records
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nwarps = blockDim.x >> 5;
     const int W = p.W;  // observers per block = OPW x warps
@@ -929,7 +939,7 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
                     tmem_fence_after();
                     const float* st = stages + (size_t)s * SE * kTile;
                     for (int jp = 0; jp < SE / 2; ++jp)
-                        for (int b = 0; b < 2 * kGroups; ++b)
+                        for (int b = 0; b < 2 * kGroups32; ++b)
                             tmem_cp_32x128b_warpx4(sh.tmem + tm_col<SE>(s, jp) + 4u * b,
                                                    smem_desc_plain(st + (size_t)(2 * jp) * kTile + b * kWin * 4, 128, 128));
                     tmem_commit(&sh.tfull[s]);
@@ -954,43 +964,39 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
         const float* st = stages + (size_t)s * SE * kTile;
         SmpF cur[OPW][SE];
         if (TM) {
-            // records from tensor memory, in two loads per element pair: the positions and
-            // x.v (columns 0-7, 32-39) first; the other groups (columns 8-31) load while
-            // the retarded time is solved, and the next pair's first columns while this
-            // pair's source terms are formed
+            // records from tensor memory, in two loads per element pair: the positions
+            // (columns 0-7) first; the other groups (columns 8-31) load while the retarded
+            // time is solved, and the next pair's positions while this pair's source terms
+            // are formed
             const uint32_t tq = sh.tmem + ((uint32_t)(32 * (warp & 3)) << 16);
-            uint32_t ra[8], rb[8];
+            uint32_t ra[8], rz[8];
             tmem_ld_x8(tq + tm_col<SE>(s, 0), ra);
-            tmem_ld_x8(tq + tm_col<SE>(s, 0) + 32u, rb);
-            tmem_wait_ld_tie(ra, rb);
+            tmem_wait_ld_tie(ra, rz);
 #pragma unroll
             for (int jp = 0; jp < SE / 2; ++jp) {
                 const uint32_t ta = tq + tm_col<SE>(s, jp);
                 uint32_t rc[16], rd[8];
                 tmem_ld_x16(ta + 8u, rc);
                 tmem_ld_x8(ta + 24u, rd);
-                const G2 g0 = g2_of(ra), g4 = g2_of(rb);
+                const G2 g0 = g2_of(ra);
                 MixedGeom m[OPW];
 #pragma unroll
-                for (int q = 0; q < OPW; ++q) m[q] = mixed_geom(g0, g4.w, ox[q], oy[q], oz[q], anc[q], p);
+                for (int q = 0; q < OPW; ++q) m[q] = mixed_geom(g0, ox[q], oy[q], oz[q], anc[q], p);
                 tmem_wait_ld_tie(rc, rd, m[0].dt, m[0].rx, m[0].ry, m[0].ir);
-                if (jp + 1 < SE / 2) {
-                    tmem_ld_x8(ta + tm_col<SE>(0, 1), ra);
-                    tmem_ld_x8(ta + tm_col<SE>(0, 1) + 32u, rb);
-                }
+                if (jp + 1 < SE / 2) tmem_ld_x8(ta + tm_col<SE>(0, 1), ra);
 #pragma unroll
                 for (int q = 0; q < OPW; ++q)
-                    mixed_source(m[q], g0.w, g2_of(rc), g2_of(rc + 8), g2_of(rd), g4, anc[q], p, tau, cur[q][2 * jp],
+                    mixed_source(m[q], g0, g2_of(rc), g2_of(rc + 8), g2_of(rd), anc[q], p, tau, cur[q][2 * jp],
                                  cur[q][2 * jp + 1]);
-                if (jp + 1 < SE / 2) tmem_wait_ld_tie(ra, rb);
+                if (jp + 1 < SE / 2) tmem_wait_ld_tie(ra, rz);
             }
         } else {
 #pragma unroll
             for (int jp = 0; jp < SE / 2; ++jp) {
-                G2 gg[kGroups];
+                G2 gg[kGroups32];
                 const float* tl = st + (size_t)(2 * jp) * kTile + lane * 4;
 #pragma unroll
-                for (int q = 0; q < kGroups; ++q) gg[q] = load_g2(tl + q * 2 * kWin * 4);
+                for (int q = 0; q < kGroups32; ++q) gg[q] = load_g2(tl + q * 2 * kWin * 4);
 #pragma unroll
                 for (int q = 0; q < OPW; ++q)
                     sample_mixed2(gg, ox[q], oy[q], oz[q], anc[q], p, tau, cur[q][2 * jp], cur[q][2 * jp + 1]);
@@ -1025,8 +1031,8 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
         }
         // HOIST: the first window's samples (kept for the wrap) and the periodic wrap itself
         // are handled after the stage's deposits, one uniform branch each instead of one
-        // per sample (2.6 % faster at workload 2 in the single-deck kernel; the batched
-        // kernel, with more live registers, keeps the per-sample form, which spills less)
+        // per sample (2.6 % faster at workload 2 in the single-deck kernel, 9 % in the
+        // batched one; the per-sample form, HOIST = false, needs fewer registers)
         if (HOIST && first_win && lane == 0) {
 #pragma unroll
             for (int q = 0; q < OPW; ++q)
@@ -1103,7 +1109,7 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
 template <int SE, int OPW>
 __device__ __forceinline__ void mixed_init(unsigned char* smem, size_t stage_off, int NS, MixedShared<SE, OPW>& sh)
 {
-    constexpr int kTile = kGroups * kWin * 4;
+    constexpr int kTile = kGroups32 * kWin * 4;
     float2* acc_all = reinterpret_cast<float2*>(smem);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + stage_off + (size_t)NS * SE * kTile * sizeof(float));
     for (size_t i = threadIdx.x; i < stage_off / sizeof(float2); i += blockDim.x) acc_all[i] = make_float2(0.f, 0.f);
@@ -1126,7 +1132,7 @@ __device__ __forceinline__ void mixed_init(unsigned char* smem, size_t stage_off
 template <int SE, int OPW>
 __device__ __forceinline__ void mixed_drain(unsigned char* smem, size_t stage_off, int NS, MixedShared<SE, OPW>& sh)
 {
-    constexpr int kTile = kGroups * kWin * 4;
+    constexpr int kTile = kGroups32 * kWin * 4;
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + stage_off + (size_t)NS * SE * kTile * sizeof(float));
     if (threadIdx.x == 0)
         for (int k = 0; k < NS; ++k) {
@@ -1220,7 +1226,7 @@ __global__ void __launch_bounds__(512, 1)
         for (int k = threadIdx.x; k < kWords; k += blockDim.x)
             reinterpret_cast<int*>(&sp)[k] = reinterpret_cast<const int*>(cases + it.c)[k];
         __syncthreads();
-        mixed_item<SE, 1, false, false>(sp, it.ot, it.e0, it.e1, smem, stage_off, sh, gbase);
+        mixed_item<SE, 1, false, true>(sp, it.ot, it.e0, it.e1, smem, stage_off, sh, gbase);
         __syncthreads();
         if (sh.abort) {
             mixed_drain<SE, 1>(smem, stage_off, NS, sh);
@@ -1290,7 +1296,8 @@ static size_t tonal_smem(int W, int T, int NS, int SE, int real_bytes)
 {
     // FP64: double2 per bin; mixed: float2 per bin plus the overflow and scratch slots per row
     const size_t acc = real_bytes == 8 ? acc_region_bytes(W, T, 16) : acc_region_bytes(W, T + 2, 8);
-    return acc + (size_t)NS * SE * kGroups * kWin * 4 * real_bytes + (size_t)NS * 8;
+    const int groups = real_bytes == 8 ? kGroups : kGroups32;  // FP64 or FP32 records
+    return acc + (size_t)NS * SE * groups * kWin * 4 * real_bytes + (size_t)NS * 8;
 }
 
 cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int num_sms, size_t smem_optin,
@@ -1337,7 +1344,7 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
     }
     // tensor-memory form: the ring's stages fit in the block's kTmemCols columns, and one
     // block per SM holds them all
-    if (tm) NS = std::max(1, std::min(NS, (int)kTmemCols / (20 * SE)));
+    if (tm) NS = std::max(1, std::min(NS, (int)kTmemCols / (16 * SE)));
     TonalTile& t = r.t;
     t.flush_elems = 1 << 30;
     t.W = W;
@@ -1360,7 +1367,7 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
         // smaller if needed to give every slot `items_per_sm` items (default 8).  The FP32
         // bin rows are flushed to the FP64 sums once per item (at most 512 elements):
         // larger chunks would re-read records, smaller ones would add FP64 flush traffic.
-        const size_t per_elem = (size_t)r.g.nW * kGroups * kWin * 4 * sizeof(float);
+        const size_t per_elem = (size_t)r.g.nW * kGroups32 * kWin * 4 * sizeof(float);
         long chunk = (long)std::max<size_t>((size_t)SE, ((size_t)32 << 20) / per_elem);
         chunk = std::min<long>(chunk, 512);
         const int ips = items_per_sm > 0 ? items_per_sm : 8;
@@ -1500,7 +1507,7 @@ cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s)
 size_t batch_smem(int W, int SE, int Tmax)
 {
     const int NS = batch_stages(SE);
-    return acc_region_bytes(W, Tmax + 2, 8) + (size_t)NS * SE * kGroups * kWin * 4 * sizeof(float) +
+    return acc_region_bytes(W, Tmax + 2, 8) + (size_t)NS * SE * kGroups32 * kWin * 4 * sizeof(float) +
            (size_t)NS * 8;
 }
 

@@ -580,7 +580,7 @@ def main():
     fp32_peak = native.measure_peak(local, 0)
     fp64_peak = native.measure_peak(local, 1)
     achieved = ALG_FLOPS_PER_EVAL * evals / (kms * 1e-3) / 1e12
-    rec_bytes = deck.E * deck.nTime * 20 * 4
+    rec_bytes = deck.E * deck.nTime * 16 * 4
 
     out = {
         "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws, "steps": args.steps,

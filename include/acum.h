@@ -267,7 +267,7 @@ int acum_find_pressure_time_history_f64(const double* rObs, const double* tObs, 
  * loop that cannot afford cudaMalloc/cudaFree, which synchronise the whole device.  It
  * allocates nothing -- no cudaMalloc, no host heap -- and uses a fixed 128 MiB scratch
  * array in device memory that every GPU loading this library holds until exit.  Limit:
- * records (80 B per element-step, elements rounded up to 8 and steps to 32) plus 16 B per
+ * records (64 B per element-step, elements rounded up to 8 and steps to 32) plus 16 B per
  * observer-step must fit in 128 MiB, else ACUM_ERR_INVALID (acum_noalloc_last_error()
  * gives the sizes); at most 256 surfaces.  Otherwise it accepts and refuses the inputs the
  * allocating call does (nTime >= 4; tObs[t] = t*dPsi, as main.cu:124 builds it, else
