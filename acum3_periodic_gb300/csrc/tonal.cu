@@ -797,7 +797,8 @@ __device__ __forceinline__ void deposit(float2* acc, int T, unsigned tm, const S
     bad |= (active && !ok) ? 1u : 0u;
     const bool one = active && ok && cnt >= 1, two = one && cnt >= 2;
     more |= two && cnt > 2;
-    const float inv = rcp_ftz(ok ? du : 1.0f);
+    // not finite when !ok; both slots are then the scratch slot, which is never read out
+    const float inv = rcp_ftz(du);
     const float2 pa = make_float2(a.pt, a.pl), dp = sub2(make_float2(b.pt, b.pl), pa);
     const int idx = mod_T(a.k + 1, T, tm);  // used only when `one`
     const float w1 = (1.0f - a.f) * inv;
