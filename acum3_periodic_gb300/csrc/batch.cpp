@@ -103,7 +103,7 @@ TonalRun case_run(const acum_batch* b, const acum_ctx* c, double* acc)
     r.t.W = b->W;
     r.t.SE = b->SE;
     r.t.NS = batch_stages(b->SE);
-    r.t.flush_elems = 128;
+    r.t.flush_elems = 512;  // FP32 bin sums over at most 512 elements, as the single-deck plan
     r.t.opw = 1;
     r.t.chunk = c->Epad;
     r.t.nchunk = 1;

@@ -8,7 +8,7 @@ GB300 arm (default).  One step = one pass of the tonal path over the deck with t
 surface rows already resident in HBM: GPU preprocessing (preprocess_imper) + the
 mixed-precision tonal kernel + the finalize transpose, i.e. acum_tonal_device.  `value`
 is element*observer*step evaluations per second over K timed steps (inputs larger than
-L2: 1.47 GB of surface rows and 3.7 GB of records per step).  `e2e` times the same
+L2: 1.47 GB of surface rows and 2.95 GB of records per step).  `e2e` times the same
 metric through acum_tonal_from_host_async: pinned host rows in, pA out, copies inside
 (each step's copies overlap the previous step's solve).  The plain FP64 form is timed on
 every 8th observer (512) of the same deck, and the mixed result is compared with it
@@ -47,10 +47,10 @@ ALG_FLOPS_PER_EVAL = 102  # FP ops per tonal evaluation (integrand + observer ti
 # 42 bands, 1
 BPM_FLOPS_PER_EVAL = 13
 # DRAM bytes (read + write) of one workload-2 launch of the mixed kernel, measured with ncu
-# (one pass: dram__bytes_read.sum + dram__bytes_write.sum: 14.72 GB + 10.39 GB); the FP64
-# flushes of the FP32 bin rows and the reads they cause, the 3.69 GB of records being read
-# a few times at most
-TONAL_TRAFFIC_BYTES = 25.11e9
+# (one pass: dram__bytes_read.sum + dram__bytes_write.sum: 11.85 GB + 8.30 GB); the FP64
+# flushes of the FP32 bin rows and the reads they cause, the 2.95 GB of records being read
+# about once
+TONAL_TRAFFIC_BYTES = 20.15e9
 WORKLOAD = "workload 2: 4-blade rotor, 32000 elements, 1440 steps/rev, 4096 observers, tonal mixed precision"
 
 
@@ -338,7 +338,8 @@ def profile_case(name, device=0):
     steps, 1024 observers); batch: four workload-4 cases shrunk to 30 x 2 x 12 panels per
     blade and 400 observers (366 MB of records) in one persistent launch (16 observers per
     block, 8 elements per stage, 8 items per SM); tonal-small: the mixed kernel on
-    workload 2 reduced to 25 x 2 x 10 panels per blade and 512 observers."""
+    workload 2 reduced to 25 x 2 x 10 panels per blade and 512 observers; tonal-full: the
+    mixed kernel on workload 2 (for one-pass captures only)."""
     from acum3_periodic_gb300 import native, synth
     out = {"case": name}
     if name.startswith("adjoint"):
@@ -360,13 +361,14 @@ def profile_case(name, device=0):
         out.update(batch_ms=b.timing()[0])
     else:
         ctx = native.Context(device)
-        ctx.set_deck(synth.config_deck(2, scale=dict(n_span=25, n_chord_side=10, ntime=1440, nobs=512)), bb=False)
+        scale = None if name == "tonal-full" else dict(n_span=25, n_chord_side=10, ntime=1440, nobs=512)
+        ctx.set_deck(synth.config_deck(2, scale=scale), bb=False)
         ctx.tonal(native.MIXED)
         out.update(tonal_ms=ctx.timing(0)[0])
     print(json.dumps(out))
 
 
-PROFILE_CASES = ("adjoint-fp64", "adjoint-mixed", "bpm", "batch", "tonal-small")
+PROFILE_CASES = ("adjoint-fp64", "adjoint-mixed", "bpm", "batch", "tonal-small", "tonal-full")
 
 
 def batch_leg(native, device, steps=1, inflight=6):
@@ -587,7 +589,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded rotor deck)",
         "config": {"workload": WORKLOAD, "elements": deck.E, "steps": deck.nTime, "observers": deck.nObs,
-                   "precision": "mixed", "l2": "inputs larger than L2 (1.47 GB rows, 3.7 GB records per step)",
+                   "precision": "mixed", "l2": "inputs larger than L2 (1.47 GB rows, 2.95 GB records per step)",
                    "parallelism": "replicas" if ws > 1 else "1 GPU"},
         "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": int(raw.nbytes),
                 "api": "acum_tonal_from_host_async (pinned rows in, pA out; copies overlap the previous step)",
