@@ -331,7 +331,7 @@ extern "C" int acum_last_plan(const acum_ctx* ctx, int* out)
 extern "C" int acum_set_tile(acum_ctx* ctx, int obs_per_block, int elems_per_stage, int items_per_sm)
 {
     if (!ctx) return ACUM_ERR_INVALID;
-    if (obs_per_block < 0 || obs_per_block > 16 || items_per_sm < 0 || items_per_sm > 64 ||
+    if (obs_per_block < 0 || obs_per_block > 32 || items_per_sm < 0 || items_per_sm > 64 ||
         (elems_per_stage != 0 && elems_per_stage != 2 && elems_per_stage != 4 && elems_per_stage != 8))
         return fail(ctx, ACUM_ERR_INVALID, "acum_set_tile: out of range");
     ctx->tile_W = obs_per_block;
@@ -356,6 +356,38 @@ extern "C" int acum_set_obs_per_warp(acum_ctx* ctx, int obs_per_warp)
     return ACUM_OK;
 }
 
+extern "C" int acum_set_ring(acum_ctx* ctx, int mode)
+{
+    if (!ctx) return ACUM_ERR_INVALID;
+    if (mode < 0 || mode > 1) return fail(ctx, ACUM_ERR_INVALID, "acum_set_ring: out of range");
+    ctx->tile_rows = mode;
+    return ACUM_OK;
+}
+
+extern "C" int acum_last_plan_ring(acum_ctx* ctx, int* out)
+{
+    if (!ctx || !out) return ACUM_ERR_INVALID;
+    if (!ctx->have_tonal_plan) return ACUM_ERR_STATE;
+    out[0] = ctx->last_tile.ring;
+    out[1] = ctx->last_rows.W;
+    out[2] = ctx->last_rows.SE;
+    out[3] = ctx->last_rows.NS;
+    out[4] = 0;
+    if (ctx->last_tile.ring > 0) {
+        // the test both kernels make, from the same radius
+        DeviceGuard g(ctx->device);
+        unsigned bits = 0;
+        CK(ctx, cudaStreamSynchronize(ctx->stream));
+        CK(ctx, cudaMemcpy(&bits, ctx->d_rmax.p, sizeof(bits), cudaMemcpyDeviceToHost));
+        float r;
+        memcpy(&r, &bits, sizeof(r));
+        const double reach = ring_reach_bins(r, ctx->der.vinf[0], ctx->der.vinf[1], ctx->der.vinf[2], ctx->in.a0,
+                                             ctx->der.oM / ctx->der.dPsi);
+        out[4] = ring_fits_bins(reach, ctx->last_tile.ring) ? 1 : 0;
+    }
+    return ACUM_OK;
+}
+
 // ------------------------------------------------------------ preprocessing
 
 int acum_ctx::ensure_prep(bool need64, bool need32, bool need_fields)
@@ -371,7 +403,7 @@ int acum_ctx::ensure_prep(bool need64, bool need32, bool need_fields)
     if (!d_raw.p) return fail(this, ACUM_ERR_STATE, "the surface rows were released after preprocessing");
     if (T > 4096) return fail(this, ACUM_ERR_UNSUPPORTED, "nTime above 4096 is not supported by the preprocessing");
     const size_t nrec = (size_t)Epad * nW * kGroups * kWin * 4;     // FP64 records
-    const size_t nrec32 = (size_t)Epad * nW * kGroups32 * kWin * 4;  // FP32 records
+    const size_t nrec32 = (size_t)Epad * nwin32(T) * kGroups32 * kWin * 4;  // FP32 records
     const long long layout[4] = {(long long)E, (long long)Epad, (long long)nW, (long long)T};
     const auto same = [&](const long long* l) { return std::equal(l, l + 4, layout); };
     if (do64) {
@@ -385,6 +417,8 @@ int acum_ctx::ensure_prep(bool need64, bool need32, bool need_fields)
         CK(this, d_rec32.ensure(nrec32));
         if (clear) CK(this, cudaMemsetAsync(d_rec32.p, 0, nrec32 * 4, stream));
         std::copy(layout, layout + 4, rec32_layout);
+        CK(this, d_rmax.ensure(1));
+        CK(this, cudaMemsetAsync(d_rmax.p, 0, sizeof(unsigned), stream));
     }
     if (need_fields) CK(this, d_fields.ensure((size_t)E * T * kFields));
     PrepArgs a;
@@ -416,6 +450,7 @@ int acum_ctx::ensure_prep(bool need64, bool need32, bool need_fields)
         a32.rec64 = nullptr;
         a32.fields = nullptr;
         a32.rec32 = d_rec32.p;
+        a32.rmax = d_rmax.p;
         CK(this, launch_prep(a32, stream));
         launches += 1;
     }
@@ -496,7 +531,8 @@ int acum_ctx::run_tonal(int precision, double* d_pT, double* d_pL, double* d_pA)
     r.g.lpi = T * der.dPsi;
     for (int c = 0; c < 3; ++c) r.g.vinf[c] = der.vinf[c];
     r.precision = precision;
-    CK(this, plan_tonal(r, tile_W, tile_SE, tile_ips, num_sms, smem_optin, tile_opw, tile_tm));
+    r.rmax = f64 ? nullptr : d_rmax.p;
+    CK(this, plan_tonal(r, tile_W, tile_SE, tile_ips, num_sms, smem_optin, tile_opw, tile_tm, tile_rows));
     r.rec = f64 ? (const void*)d_rec64.p : (const void*)d_rec32.p;
     r.obs64 = d_obs64.p;
     r.obs32 = d_obs32.p;
@@ -504,6 +540,7 @@ int acum_ctx::run_tonal(int precision, double* d_pT, double* d_pL, double* d_pA)
     r.acc = d_acc.p;
     r.err = d_err.p;
     last_tile = r.t;
+    last_rows = r.rows;
     have_tonal_plan = true;
     // the mixed form always adds into the FP64 sums; the FP64 form stores when one block
     // owns an observer's whole element range
@@ -513,7 +550,7 @@ int acum_ctx::run_tonal(int precision, double* d_pT, double* d_pL, double* d_pA)
     CK(this, cudaEventRecord(ev[EV_TONAL1], stream));
     CK(this, launch_finalize(d_acc.p, nobs, T, d_pT, d_pL, d_pA, 0, stream));
     CK(this, cudaEventRecord(ev[EV_FIN1], stream));
-    launches += 2;
+    launches += r.t.ring > 0 ? 3 : 2;
     tonal_timed = true;
     return ACUM_OK;
 }
@@ -811,7 +848,7 @@ int find_pth(const S* rObs, const S* tObs, S* pT, S* pL, S* pA, const S* Xham, c
     CK(nullptr, cudaMemcpyAsync(c->d_off.p + E, no.data(), E * 8, cudaMemcpyHostToDevice, st));
     CK(nullptr, cudaMemcpyAsync(c->d_off.p + 2 * E, vo.data(), E * 8, cudaMemcpyHostToDevice, st));
     CK(nullptr, cudaMemcpyAsync(c->d_off.p + 3 * E, po.data(), E * 8, cudaMemcpyHostToDevice, st));
-    const size_t nrec = (size_t)Epad * nW * (f64 ? kGroups : kGroups32) * kWin * 4;
+    const size_t nrec = f64 ? (size_t)Epad * nW * kGroups * kWin * 4 : (size_t)Epad * nwin32(nTime) * kGroups32 * kWin * 4;
     AosArgs a;
     memset(&a, 0, sizeof(a));
     a.X = Xham;
@@ -838,6 +875,9 @@ int find_pth(const S* rObs, const S* tObs, S* pT, S* pL, S* pA, const S* Xham, c
         CK(nullptr, c->d_rec32.ensure(nrec));
         CK(nullptr, cudaMemsetAsync(c->d_rec32.p, 0, nrec * 4, st));
         a.rec32 = c->d_rec32.p;
+        CK(nullptr, c->d_rmax.ensure(1));
+        CK(nullptr, cudaMemsetAsync(c->d_rmax.p, 0, sizeof(unsigned), st));
+        a.rmax = c->d_rmax.p;
     }
     CK(nullptr, launch_aos_records(a, st));
     // observers in both precisions
@@ -869,6 +909,7 @@ int find_pth(const S* rObs, const S* tObs, S* pT, S* pL, S* pA, const S* Xham, c
     r.g.lpi = nTime * dPsi;
     for (int q = 0; q < 3; ++q) r.g.vinf[q] = (double)hv[q];
     r.precision = f64 ? ACUM_PLAIN_FP64 : ACUM_MIXED;
+    r.rmax = f64 ? nullptr : c->d_rmax.p;
     CK(nullptr, plan_tonal(r, 0, 0, 0, c->num_sms, c->smem_optin));
     r.rec = f64 ? (const void*)c->d_rec64.p : (const void*)c->d_rec32.p;
     r.obs64 = c->d_obs64.p;

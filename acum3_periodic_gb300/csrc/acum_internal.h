@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
 #include <string>
 #include <vector>
@@ -31,22 +32,77 @@ namespace acum {
 // 32-step window) tile is contiguous (5120 B), which is what one bulk (TMA) copy moves
 // into shared memory.  The FP32 records interleave pairs of elements so that the mixed
 // kernel reads the two elements' values of a field as one register pair (the operand of
-// a packed FP32 instruction): [element pair][window][group][half][32 steps][4], half 0 =
+// a packed FP32 instruction): [element pair][window][group][half][32 lanes][4], half 0 =
 // (f0 of e, f0 of e+1, f1 of e, f1 of e+1), half 1 = the same for fields 2 and 3; an
-// (element pair, window) tile is 4096 B.
+// (element pair, window) tile is 4096 B.  Their windows overlap: window w, lane l holds
+// step (31 w + l) mod T for 31 w + l = 0 .. T (lanes past T hold zeros), so lane l - 1
+// of the same window holds the left end of lane l's source interval and the last window
+// reaches step T, which is step 0 one period on (the periodic wrap of core.cu:173-194).
+// ceil(T / 31) windows.
 constexpr int kGroups = 5;    // FP64 records
 constexpr int kGroups32 = 4;  // FP32 records
 constexpr int kWin = 32;
+constexpr int kStride32 = 31;  // steps between the FP32 records' windows
 constexpr int kFields = 18;  // x,y,z,ds, n(3), ndot(3), V(3), Vdot(3), P, Pdot
 
-// float offset of field c (0..3) of group q (0..3) of element e at step t in the FP32
-// records
-__host__ __device__ __forceinline__ size_t rec32_offset(int e, int nW, int t, int q, int c)
+__host__ __device__ __forceinline__ int nwin32(int T) { return (T + kStride32 - 1) / kStride32; }
+
+// float offset of field c (0..3) of group q (0..3) of element e at lane `lane` of window
+// w of the FP32 records
+__host__ __device__ __forceinline__ size_t rec32_offset(int e, int nW32, int w, int lane, int q, int c)
 {
-    const int w = t / kWin, lane = t % kWin;
-    return ((((size_t)(e >> 1) * nW + w) * kGroups32 + q) * 2 + (c >> 1)) * (kWin * 4) + (size_t)lane * 4 +
+    return ((((size_t)(e >> 1) * nW32 + w) * kGroups32 + q) * 2 + (c >> 1)) * (kWin * 4) + (size_t)lane * 4 +
            (size_t)((c & 1) * 2 + (e & 1));
 }
+
+// Stores the 16 FP32 fields f of element e at step t into every slot of the FP32 records
+// that holds that step: lane t mod 31 of window t / 31, also lane 31 of the window before
+// when t is a multiple of 31, and for t = 0 also the slot of step T.
+__host__ __device__ __forceinline__ void rec32_store(float* rec, int e, int nW32, int T, int t, const float* f)
+{
+    for (int k = 0; k < 2; ++k) {
+        if (k == 1 && t != 0) break;
+        const int tau = k == 0 ? t : T;
+        const int w = tau / kStride32, l = tau - w * kStride32;
+        for (int a = 0; a < 2; ++a) {
+            const int ww = a == 0 ? w : w - 1, ll = a == 0 ? l : kStride32;
+            if (a == 1 && (l != 0 || w == 0)) break;
+            if (ww >= nW32) continue;
+            for (int q = 0; q < kGroups32; ++q)
+                for (int c = 0; c < 4; ++c) rec[rec32_offset(e, nW32, ww, ll, q, c)] = f[4 * q + c];
+        }
+    }
+}
+
+// Mixed ring form: a bound, in observer-time bins and with a margin, on how far a
+// sample's observer time lies from its step plus the observer's anchor (the retarded
+// time of the origin): |t - t0| <= |x| / (a0 - |vInf|), because the travel time through a
+// uniformly moving medium changes by at most 1 / (a0 - |vInf|) per unit of source
+// displacement; r = the records' largest |x|, kb = oM / dPsi bins per second.  1e30 when
+// r is not finite or the flight is not subsonic.
+__host__ __device__ __forceinline__ double ring_reach_bins(float r, double vx, double vy, double vz, double a0,
+                                                           double kb)
+{
+    const double vm = sqrt(vx * vx + vy * vy + vz * vz);
+    if (!(r <= 1.0e30f) || !(vm < 0.999 * a0)) return 1.0e30;
+    return (double)r * kb / (a0 - vm) * 1.0001 + 2.0;
+}
+// whether a ring of R slots holds every bin a window of 31 intervals can reach
+__host__ __device__ __forceinline__ bool ring_fits_bins(double reach, int R) { return 2.0 * reach + 40.0 <= (double)R; }
+
+#ifdef __CUDACC__
+// The largest source distance from the origin |x| among the records a kernel writes, as
+// the bits of a non-negative float in *word (unsigned order = float order; a NaN
+// distance is above every finite one): a warp-wide maximum, then one atomic per warp.
+// Every lane of the warp that is still running calls it.
+__device__ __forceinline__ void note_radius(unsigned* word, float r)
+{
+    if (!word) return;
+    const unsigned mask = __activemask();
+    const unsigned m = __reduce_max_sync(mask, __float_as_uint(fabsf(r)));
+    if ((threadIdx.x & 31) == (unsigned)(__ffs(mask) - 1)) atomicMax(word, m);
+}
+#endif
 
 struct DeviceErr {
     unsigned int bits;
@@ -74,6 +130,7 @@ struct TonalTile {
     int flush_elems;  // mixed: elements summed in FP32 before the FP64 flush
     int opw;          // observers per warp
     bool tm;          // mixed: record stages copied into tensor memory and read from there
+    int ring;         // mixed: bin slots per observer of the sliding ring (a power of 2), 0 = whole rows
     size_t smem;
 };
 
@@ -92,6 +149,7 @@ struct PrepArgs {
     double gauss[13];
     double* rec64;         // [Epad][nW][5][32][4] or null
     float* rec32;          // pair-interleaved FP32 records (rec32_offset) or null
+    unsigned* rmax;        // with rec32: the largest |x| (note_radius), or null
     double* fields;        // optional [E][T][18]
 };
 cudaError_t launch_prep(const PrepArgs& a, cudaStream_t s);
@@ -124,6 +182,7 @@ struct AosArgs {
     double vinf[3];
     double* rec64;
     float* rec32;
+    unsigned* rmax;  // with rec32: the largest |x| (note_radius), or null
 };
 cudaError_t launch_aos_records(const AosArgs& a, cudaStream_t s);
 
@@ -151,7 +210,9 @@ cudaError_t launch_per_rows(const float* raw, const long long* raw_off, const in
 
 struct TonalRun {
     TonalGeom g;
-    TonalTile t;
+    TonalTile t;          // the plan; mixed with t.ring > 0: the ring kernel, and
+    TonalTile rows;       // the whole-row kernel launched after it, which runs when the ring is too short
+    const unsigned* rmax; // mixed: the records' largest |x| (note_radius bits)
     const void* rec;      // rec64 or rec32
     const double* obs64;  // [O][3]
     const float* obs32;
@@ -160,13 +221,17 @@ struct TonalRun {
     int precision;
 };
 cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int num_sms, size_t smem_optin,
-                       int opw_req = 0, int tm_req = 0);
+                       int opw_req = 0, int tm_req = 0, int rows_only = 0);
 cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s);
 
 // Constants of one tonal launch (one case), as the kernels read them.
 struct KParams {
     const void* rec;
     int Epad, T, nW, O;
+    int nW32;               // windows of the FP32 records
+    int ring;               // mixed: ring slots per observer (ring kernel), 0 = whole rows
+    int dual;               // mixed: a ring kernel and a whole-row kernel are both launched
+    const unsigned* rmax;   // mixed: the records' largest |x| (note_radius bits)
     const float* obs32;
     const double* obs64;
     // mixed constants, as pairs (both halves equal: the operands of the packed FP32
@@ -182,7 +247,8 @@ struct KParams {
     double* acc;
     DeviceErr* err;
 };
-void fill_kparams(const TonalRun& r, KParams& kp);
+void fill_kparams(const TonalRun& r, KParams& kp);  // of the plan r.t
+void fill_kparams(const TonalRun& r, const TonalTile& tile, KParams& kp);
 
 // Batched (persistent) mixed launch over many cases.  Work item = (case, observer tile,
 // element range [e0, e1)); the kernel takes items in array order from *counter.
@@ -192,12 +258,14 @@ struct BatchItem {
 // ring stages of the batched kernel: 4, or 2 for stages of 8 elements
 constexpr int batch_stages(int SE) { return SE == 8 ? 2 : 4; }
 // dynamic shared memory of the persistent kernel for W observers per block, elements per
-// stage SE and the longest case's nTime
-size_t batch_smem(int W, int SE, int Tmax);
-int batch_blocks_per_sm(int W, int SE, int Tmax);
-size_t batch_static_smem(int SE);  // static shared memory to keep beside batch_smem
+// stage SE and rows of `rowlen` slots (the longest case's nTime for whole rows, the ring's
+// slots for ring cases, whichever is larger)
+size_t batch_smem(int W, int SE, int rowlen);
+int batch_blocks_per_sm(int W, int SE, int opw, int rowlen);
+size_t batch_static_smem(int SE, int opw);  // static shared memory to keep beside batch_smem
 cudaError_t launch_tonal_batch(const KParams* d_cases, const BatchItem* d_items, int nitems, int* d_counter, int W,
-                               int SE, int Tmax, int grid, cudaStream_t s);
+                               int SE, int opw, int rowlen, int grid, cudaStream_t s);
+constexpr int kRingSlots = 512;  // bin slots per observer of the mixed ring kernels (single deck and batched)
 // acc [O][T][2] of every case -> pA [T][O] (overwrite)
 struct FinCase {
     const double* acc;

@@ -29,10 +29,12 @@ struct acum_batch {
     std::string err;
     std::vector<acum_ctx*> cases;
 
-    // tile shape and plan
-    int W = 16, SE = 8, ips = 8;
+    // tile shape and plan: W observers per block, opw per warp, SE elements per stage;
+    // rowlen = slots per bin row (the longest whole-row case's nTime, or the ring's)
+    int W = 32, SE = 4, opw = 2, ips = 8;
     bool planned = false;
-    int Tmax = 0;
+    int Tmax = 0, rowlen = 0;
+    std::vector<char> ring;  // per case: its records fit the bin ring
     int nitems = 0;
     std::vector<BatchItem> items;
     std::vector<size_t> acc_off, out_off;
@@ -104,10 +106,11 @@ TonalRun case_run(const acum_batch* b, const acum_ctx* c, double* acc)
     r.t.SE = b->SE;
     r.t.NS = batch_stages(b->SE);
     r.t.flush_elems = 512;  // FP32 bin sums over at most 512 elements, as the single-deck plan
-    r.t.opw = 1;
+    r.t.opw = b->opw;
     r.t.chunk = c->Epad;
     r.t.nchunk = 1;
     r.rec = c->d_rec32.p;
+    r.rmax = c->d_rmax.p;
     r.obs32 = c->d_obs32.p;
     r.obs64 = c->d_obs64.p;
     r.acc = acc;
@@ -135,7 +138,7 @@ void build_items(const acum_batch* b, int W, int SE, int ips, std::vector<BatchI
         int nchunk = (int)std::ceil(per_tile / std::max(target, 1.0));
         // element chunks of at most ~32 MB of records (as the single-deck plan), so that
         // the items of one chunk, which run close together in time, share it in L2
-        const size_t per_elem = (size_t)c->nW * kGroups32 * kWin * 4 * sizeof(float);
+        const size_t per_elem = (size_t)nwin32(c->T) * kGroups32 * kWin * 4 * sizeof(float);
         const int max_groups = std::max(1, (int)(((size_t)32 << 20) / per_elem) / SE);
         nchunk = std::max(nchunk, (groups + max_groups - 1) / max_groups);
         nchunk = std::max(1, std::min(nchunk, groups));
@@ -154,18 +157,46 @@ void build_items(const acum_batch* b, int W, int SE, int ips, std::vector<BatchI
     for (const Cost& x : v) out.push_back(x.it);
 }
 
-bool shape_fits(const acum_batch* b, int W, int SE)
+bool shape_fits(const acum_batch* b, int W, int SE, int opw)
 {
-    return batch_smem(W, SE, b->Tmax) + batch_static_smem(SE) <= b->smem_optin;
+    if (opw == 2 && SE == 8) return false;
+    return batch_smem(W, SE, b->rowlen) + batch_static_smem(SE, opw) <= b->smem_optin;
+}
+
+// Which cases' records fit the bin ring (from each case's largest |x|, read once), and
+// the slots per bin row the batch needs.
+int ring_cases(acum_batch* b)
+{
+    const size_t n = b->cases.size();
+    if (b->ring.size() != n) {
+        b->ring.assign(n, 0);
+        for (size_t i = 0; i < n; ++i) {
+            const acum_ctx* c = b->cases[i];
+            unsigned bits = 0;
+            BK(b, cudaMemcpy(&bits, c->d_rmax.p, sizeof(bits), cudaMemcpyDeviceToHost));
+            float r;
+            memcpy(&r, &bits, sizeof(r));
+            const double reach = ring_reach_bins(r, c->der.vinf[0], c->der.vinf[1], c->der.vinf[2], c->in.a0,
+                                                 c->der.oM / c->der.dPsi);
+            b->ring[i] = ring_fits_bins(reach, kRingSlots) ? 1 : 0;
+        }
+    }
+    b->Tmax = 0;
+    b->rowlen = 0;
+    for (size_t i = 0; i < n; ++i) {
+        b->Tmax = std::max(b->Tmax, b->cases[i]->T);
+        b->rowlen = std::max(b->rowlen, b->ring[i] ? kRingSlots : b->cases[i]->T);
+    }
+    return ACUM_OK;
 }
 
 int plan(acum_batch* b)
 {
     if (b->cases.empty()) return bfail(b, ACUM_ERR_STATE, "the batch has no cases");
     DeviceGuard g(b->device);
-    b->Tmax = 0;
-    for (const acum_ctx* c : b->cases) b->Tmax = std::max(b->Tmax, c->T);
-    if (!shape_fits(b, b->W, b->SE))
+    int rc0 = ring_cases(b);
+    if (rc0) return rc0;
+    if (!shape_fits(b, b->W, b->SE, b->opw))
         return bfail(b, ACUM_ERR_INVALID, "tile shape does not fit in shared memory for the longest case");
     // pools of sums and results
     const size_t n = b->cases.size();
@@ -190,6 +221,8 @@ int plan(acum_batch* b)
         const acum_ctx* c = b->cases[i];
         TonalRun r = case_run(b, c, b->d_acc.p + b->acc_off[i]);
         fill_kparams(r, kp[i]);
+        kp[i].ring = b->ring[i] ? kRingSlots : 0;  // the batched kernel picks the form per case
+        kp[i].dual = 0;
         fin[i].acc = b->d_acc.p + b->acc_off[i];
         fin[i].pA = b->d_out.p + b->out_off[i];
         fin[i].O = c->nobs;
@@ -217,8 +250,8 @@ int enqueue_persistent(acum_batch* b, const BatchItem* d_items, int nitems, bool
 {
     BK(b, cudaMemsetAsync(b->d_counter.p, 0, sizeof(int), b->stream));
     BK(b, cudaMemsetAsync(b->d_acc.p, 0, b->acc_doubles * 8, b->stream));
-    BK(b, launch_tonal_batch(b->d_kp.p, d_items, nitems, b->d_counter.p, b->W, b->SE, b->Tmax, b->num_sms,
-                             b->stream));
+    BK(b, launch_tonal_batch(b->d_kp.p, d_items, nitems, b->d_counter.p, b->W, b->SE, b->opw, b->rowlen,
+                             b->num_sms, b->stream));
     if (finalize) BK(b, launch_finalize_batch(b->d_fin.p, (int)b->cases.size(), b->fin_tiles, b->stream));
     return ACUM_OK;
 }
@@ -303,8 +336,8 @@ extern "C" int acum_batch_add(acum_batch* b, const acum_inputs* in, int nobs, co
     DeviceGuard g(b->device);
     // what the case holds while it is added (rows + records) and afterwards (records,
     // sums, results), against the device's free memory with 1 GiB to spare
-    const long long T = in->nTime, nW = (T + kWin - 1) / kWin, Epad = (E + 7) / 8 * 8;
-    const double rows = (double)E * T * 8 * 4, recs = (double)Epad * nW * kGroups32 * kWin * 4 * 4;
+    const long long T = in->nTime, nW32 = nwin32((int)T), Epad = (E + 7) / 8 * 8;
+    const double rows = (double)E * T * 8 * 4, recs = (double)Epad * nW32 * kGroups32 * kWin * 4 * 4;
     const double sums = (double)nobs * T * 8 * 3;
     size_t free_b = 0, total_b = 0;
     BK(b, cudaMemGetInfo(&free_b, &total_b));
@@ -446,6 +479,27 @@ extern "C" int acum_batch_set_tile(acum_batch* b, int obs_per_block, int elems_p
     if (obs_per_block) b->W = obs_per_block;
     if (elems_per_stage) b->SE = elems_per_stage;
     if (items_per_sm) b->ips = items_per_sm;
+    b->opw = 1;
+    b->planned = false;
+    b->drop_graph();
+    return ACUM_OK;
+}
+
+extern "C" int acum_batch_set_tile2(acum_batch* b, int obs_per_block, int elems_per_stage, int items_per_sm,
+                                    int obs_per_warp)
+{
+    if (!b) return ACUM_ERR_INVALID;
+    if (obs_per_warp != 1 && obs_per_warp != 2)
+        return bfail(b, ACUM_ERR_INVALID, "acum_batch_set_tile2: obs_per_warp 1 or 2");
+    if (obs_per_warp == 1) return acum_batch_set_tile(b, obs_per_block, elems_per_stage, items_per_sm);
+    if (obs_per_block < 0 || obs_per_block > 32 || obs_per_block % 2 != 0 || items_per_sm < 0 ||
+        (elems_per_stage != 0 && elems_per_stage != 2 && elems_per_stage != 4))
+        return bfail(b, ACUM_ERR_INVALID,
+                     "acum_batch_set_tile2: two observers per warp: obs_per_block 2..32 (even), elems_per_stage 2 or 4");
+    b->W = obs_per_block ? obs_per_block : 32;
+    b->SE = elems_per_stage ? elems_per_stage : 4;
+    if (items_per_sm) b->ips = items_per_sm;
+    b->opw = 2;
     b->planned = false;
     b->drop_graph();
     return ACUM_OK;
@@ -457,6 +511,13 @@ extern "C" int acum_batch_get_tile(const acum_batch* b, int* obs_per_block, int*
     if (obs_per_block) *obs_per_block = b->W;
     if (elems_per_stage) *elems_per_stage = b->SE;
     if (items_per_sm) *items_per_sm = b->ips;
+    return ACUM_OK;
+}
+
+extern "C" int acum_batch_get_obs_per_warp(const acum_batch* b, int* obs_per_warp)
+{
+    if (!b || !obs_per_warp) return ACUM_ERR_INVALID;
+    *obs_per_warp = b->opw;
     return ACUM_OK;
 }
 
@@ -538,42 +599,53 @@ extern "C" int acum_batch_autotune(acum_batch* b, int probe_per_sm, double* best
     if (probe_per_sm < 0) return bfail(b, ACUM_ERR_INVALID, "probe_per_sm must be >= 0");
     const int per_sm = probe_per_sm > 0 ? probe_per_sm : 8;
     DeviceGuard g(b->device);
-    b->Tmax = 0;
-    for (const acum_ctx* c : b->cases) b->Tmax = std::max(b->Tmax, c->T);
+    int rc0 = ring_cases(b);
+    if (rc0) return rc0;
     const long target = (long)per_sm * b->num_sms;
     // 1. kernel throughput of every (observers per block, elements per stage): one
     //    persistent launch over a spread of 128-element items from all cases (items of
     //    the size real work lists use: with 32-element items the per-item start-up and
     //    ring fill weigh on the deeper stages and the probe favoured 4 elements per
     //    stage where 8 are faster)
-    const int Ws[] = {8, 12, 16}, SEs[] = {2, 4, 8};
+    //    (one observer per warp: 8, 12, 16 observers per block x 2, 4, 8 elements per stage;
+    //    two: 16, 24, 32 x 2, 4)
+    struct Shape {
+        int W, SE, opw;
+    };
+    std::vector<Shape> shapes;
+    for (int W : {8, 12, 16})
+        for (int SE : {2, 4, 8}) shapes.push_back({W, SE, 1});
+    for (int W : {16, 24, 32})
+        for (int SE : {2, 4}) shapes.push_back({W, SE, 2});
     double best_rate = 0;
-    int bw = b->W, bse = b->SE;
+    int bw = b->W, bse = b->SE, bopw = b->opw;
     DBuf<BatchItem> d_probe;
     std::vector<BatchItem> probe;
-    for (int W : Ws)
-        for (int SE : SEs) {
-            if (!shape_fits(b, W, SE)) continue;
-            b->W = W;
-            b->SE = SE;
-            int rc = plan(b);
-            if (rc) return rc;
-            const double ev = probe_items(b, W, SE, 128, target, probe);
-            double ms = 0;
-            rc = time_items(b, d_probe, probe, &ms);
-            if (rc) return rc;
-            const double rate = ev / std::max(ms, 1e-6);
-            if (rate > best_rate) {
-                best_rate = rate;
-                bw = W;
-                bse = SE;
-            }
+    for (const Shape& sh : shapes) {
+        if (!shape_fits(b, sh.W, sh.SE, sh.opw)) continue;
+        b->W = sh.W;
+        b->SE = sh.SE;
+        b->opw = sh.opw;
+        int rc = plan(b);
+        if (rc) return rc;
+        const double ev = probe_items(b, sh.W, sh.SE, 128, target, probe);
+        double ms = 0;
+        rc = time_items(b, d_probe, probe, &ms);
+        if (rc) return rc;
+        const double rate = ev / std::max(ms, 1e-6);
+        if (rate > best_rate) {
+            best_rate = rate;
+            bw = sh.W;
+            bse = sh.SE;
+            bopw = sh.opw;
         }
+    }
     // 2. for the fastest shape, the per-item and per-evaluation costs from two probes of
     //    different item sizes, then items per SM by the predicted makespan of the
     //    largest-first dynamic schedule
     b->W = bw;
     b->SE = bse;
+    b->opw = bopw;
     int rc = plan(b);
     if (rc) return rc;
     double ev1 = probe_items(b, bw, bse, 64, target, probe), ms1 = 0;
@@ -585,7 +657,7 @@ extern "C" int acum_batch_autotune(acum_batch* b, int probe_per_sm, double* best
     rc = time_items(b, d_probe, probe, &ms2);
     if (rc) return rc;
     d_probe.release();
-    const int slots = b->num_sms * batch_blocks_per_sm(bw, bse, b->Tmax);
+    const int slots = b->num_sms * batch_blocks_per_sm(bw, bse, bopw, b->rowlen);
     // ms = (n ov + ev c) / slots for a launch whose items spread over all slots
     double c_ev = 0, ov = 0;
     const double det = n1 * ev2 - n2 * ev1;

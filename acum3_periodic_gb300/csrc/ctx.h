@@ -113,6 +113,7 @@ struct acum_ctx {
     acum::DBuf<double> d_rec64, d_fields, d_acc, d_out;
     acum::DBuf<float> d_rec32;
     acum::DBuf<acum::DeviceErr> d_err;
+    acum::DBuf<unsigned> d_rmax;  // the FP32 records' largest |x| (note_radius bits)
     // permeable decks: the preprocessed AoS arrays of variables.cu:54 in FP64 (X, N, V, U,
     // PR with nPRham = 4), the reference's layout (element after element, [T][width])
     acum::DBuf<double> d_per[5];
@@ -131,8 +132,8 @@ struct acum_ctx {
     unsigned err_bits = 0;
     long long launches = 0;
     bool prep_timed = false, tonal_timed = false, bpm_timed = false, adj_timed = false, call_timed = false;
-    int tile_W = 0, tile_SE = 0, tile_ips = 0, tile_opw = 0, tile_tm = 0;
-    acum::TonalTile last_tile;
+    int tile_W = 0, tile_SE = 0, tile_ips = 0, tile_opw = 0, tile_tm = 0, tile_rows = 0;
+    acum::TonalTile last_tile, last_rows;
     bool have_tonal_plan = false;
 
     // broadband / adjoint state lives in their own translation units

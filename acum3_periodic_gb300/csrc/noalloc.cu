@@ -12,9 +12,10 @@
 //
 // Limits and behaviour:
 //  * the scratch array is kNoAllocBytes = 128 MiB per device; a call whose records
-//    (64 bytes per element-step, elements rounded up to 8 and steps to 32) plus FP64 bin
-//    sums (16 bytes per observer-step) exceed it is rejected with ACUM_ERR_INVALID and a
-//    message that gives both sizes; at most kMaxSurfaces surfaces;
+//    (64 bytes per element and record slot: elements rounded up to 8, ceil(nTime / 31)
+//    windows of 32 slots) plus FP64 bin sums (16 bytes per observer-step) exceed it is
+//    rejected with ACUM_ERR_INVALID and a message that gives both sizes; at most
+//    kMaxSurfaces surfaces;
 //  * it accepts the inputs the allocating drop-in accepts (nTime >= 4, tObs[t] = t * dPsi
 //    within the same tolerance) and refuses the others with the same status;
 //  * the first call on a device looks up the array's device address (cudaGetSymbolAddress)
@@ -57,9 +58,9 @@ __global__ void noalloc_records_kernel(const float* __restrict__ X, const float*
                                        const float* __restrict__ V, const float* __restrict__ PR,
                                        const int* __restrict__ E, const int* __restrict__ XPtr,
                                        const int* __restrict__ NPtr, const int* __restrict__ VPtr,
-                                       const int* __restrict__ PRPtr, int nSurf, int Etot, int T, int nW, double a0,
+                                       const int* __restrict__ PRPtr, int nSurf, int Etot, int T, int nW32, double a0,
                                        double rho, double vx_inf, double vy_inf, double vz_inf,
-                                       float* __restrict__ rec)
+                                       float* __restrict__ rec, unsigned* rmax)
 {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long long)Etot * T) return;
@@ -88,9 +89,8 @@ __global__ void noalloc_records_kernel(const float* __restrict__ X, const float*
     r[19] = (double)x[0] * vx_inf + (double)x[1] * vy_inf + (double)x[2] * vz_inf;
     float f32[16];
     rec32_fields<double>(r, r[3], r[11], r + 4, r + 8, r + 12, r + 16, f32);
-    float* r32 = rec + rec32_offset(e, nW, t, 0, 0);
-    for (int q = 0; q < kGroups32; ++q)
-        for (int c = 0; c < 4; ++c) r32[rec32_offset(0, 1, 0, q, c)] = f32[4 * q + c];
+    rec32_store(rec, e, nW32, T, t, f32);
+    note_radius(rmax, sqrtf(f32[0] * f32[0] + f32[1] * f32[1] + f32[2] * f32[2]));
 }
 
 }  // namespace acum
@@ -162,9 +162,9 @@ extern "C" int acum_find_pressure_time_history_noalloc(const float* rObs, const 
         Et += hE[i];
     }
     if (Et <= 0) return bad(ACUM_ERR_INVALID, "findPressureTimeHistory_noalloc: no elements");
-    const int nW = (nTime + kWin - 1) / kWin;
+    const int nW = (nTime + kWin - 1) / kWin, nW32 = nwin32(nTime);
     const long long Epad = (Et + 7) / 8 * 8;
-    const size_t rec_bytes = (size_t)Epad * nW * kGroups32 * kWin * 4 * sizeof(float);
+    const size_t rec_bytes = (size_t)Epad * nW32 * kGroups32 * kWin * 4 * sizeof(float);
     const size_t acc_off = (rec_bytes + 255) / 256 * 256;
     const size_t acc_bytes = (size_t)nObs * nTime * 2 * sizeof(double);
     if (acc_off + acc_bytes > kNoAllocBytes) {
@@ -176,13 +176,24 @@ extern "C" int acum_find_pressure_time_history_noalloc(const float* rObs, const 
     }
     float* rec = reinterpret_cast<float*>(scratch);
     double* acc = reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(scratch) + acc_off);
-    // the array keeps the previous call's contents: clear the record padding and the sums
-    if (cudaMemsetAsync(rec, 0, rec_bytes, st) != cudaSuccess || cudaMemsetAsync(acc, 0, acc_bytes, st) != cudaSuccess)
+    // the device error word and the records' largest |x| live in the scratch too (after
+    // the sums)
+    const size_t err_off = (acc_off + acc_bytes + 255) / 256 * 256;
+    const size_t err_bytes = (sizeof(DeviceErr) + 15) / 16 * 16 + 16;
+    if (err_off + err_bytes > kNoAllocBytes)
+        return bad(ACUM_ERR_INVALID, "findPressureTimeHistory_noalloc: no room for the error word");
+    DeviceErr* derr = reinterpret_cast<DeviceErr*>(reinterpret_cast<unsigned char*>(scratch) + err_off);
+    unsigned* rmax = reinterpret_cast<unsigned*>(reinterpret_cast<unsigned char*>(derr) + err_bytes - 16);
+    // the array keeps the previous call's contents: clear the record padding, the sums,
+    // the error word and the radius
+    if (cudaMemsetAsync(rec, 0, rec_bytes, st) != cudaSuccess || cudaMemsetAsync(acc, 0, acc_bytes, st) != cudaSuccess ||
+        cudaMemsetAsync(derr, 0, err_bytes, st) != cudaSuccess)
         return bad(ACUM_ERR_CUDA, "findPressureTimeHistory_noalloc: clearing scratch failed");
     const long long n = Et * nTime;
     noalloc_records_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(Xham, Nham, Vham, PRham, E, XPtr, NPtr, VPtr,
-                                                                   PRPtr, nSurf, (int)Et, nTime, nW, a0, rhoRef,
-                                                                   (double)hv[0], (double)hv[1], (double)hv[2], rec);
+                                                                   PRPtr, nSurf, (int)Et, nTime, nW32, a0, rhoRef,
+                                                                   (double)hv[0], (double)hv[1], (double)hv[2], rec,
+                                                                   rmax);
     if (cudaGetLastError() != cudaSuccess)
         return bad(ACUM_ERR_CUDA, "findPressureTimeHistory_noalloc: launch of the records kernel failed");
     int sms = 0, optin = 0;
@@ -206,16 +217,11 @@ extern "C" int acum_find_pressure_time_history_noalloc(const float* rObs, const 
     if (plan_tonal(r, 0, 0, 0, sms, (size_t)optin) != cudaSuccess)
         return bad(ACUM_ERR_UNSUPPORTED, "findPressureTimeHistory_noalloc: no tile shape fits this nTime");
     r.rec = rec;
+    r.rmax = rmax;
     r.obs32 = rObs;
     r.obs64 = nullptr;
     r.acc = acc;
-    // the device error word lives in the scratch too (after the sums), cleared per call
-    const size_t err_off = (acc_off + acc_bytes + 255) / 256 * 256;
-    if (err_off + sizeof(DeviceErr) > kNoAllocBytes)
-        return bad(ACUM_ERR_INVALID, "findPressureTimeHistory_noalloc: no room for the error word");
-    r.err = reinterpret_cast<DeviceErr*>(reinterpret_cast<unsigned char*>(scratch) + err_off);
-    if (cudaMemsetAsync(r.err, 0, sizeof(DeviceErr), st) != cudaSuccess)
-        return bad(ACUM_ERR_CUDA, "findPressureTimeHistory_noalloc: clearing scratch failed");
+    r.err = derr;
     if (launch_tonal(r, st) != cudaSuccess || launch_finalize(acc, nObs, nTime, pT, pL, pA, 2, st) != cudaSuccess)
         return bad(ACUM_ERR_CUDA, "findPressureTimeHistory_noalloc: launch failed");
     DeviceErr h;

@@ -132,6 +132,8 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
     const double pi2dt = 1.0 / (2.0 * a.dTau);  // the pressure path's, FP64
     const R i2dt = (R)pi2dt, i4dt2 = (R)(pi2dt * pi2dt);
     const R D1 = (R)(1.0 / (4.0 * M_PI * a.a0)), ia0 = (R)(1.0 / a.a0), cfd = (R)a.cfd;
+    const int nW32 = nwin32(T);
+    float rad = 0.f;  // the largest |x| of this thread's FP32 records
     for (int t = threadIdx.x; t < T; t += blockDim.x) {
         const int tm = t == 0 ? T - 1 : t - 1, tp = t == T - 1 ? 0 : t + 1;
         const int tmm = tm == 0 ? T - 1 : tm - 1, tpp = tp == T - 1 ? 0 : tp + 1;
@@ -209,11 +211,12 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a)
         if (a.rec32) {
             float f32[16];
             rec32_fields<R>(rec, rec[3], rec[11], rec + 4, rec + 8, rec + 12, rec + 16, f32);
-            float* r32 = a.rec32 + rec32_offset(e, a.nW, t, 0, 0);
-            for (int q = 0; q < kGroups32; ++q)
-                for (int c = 0; c < 4; ++c) r32[rec32_offset(0, 1, 0, q, c)] = f32[4 * q + c];
+            rec32_store(a.rec32, e, nW32, T, t, f32);
+            const float r = sqrtf(f32[0] * f32[0] + f32[1] * f32[1] + f32[2] * f32[2]);
+            rad = (r > rad || r != r) ? r : rad;  // a NaN distance is kept
         }
     }
+    if (a.rec32) note_radius(a.rmax, rad);
 }
 
 template <typename R>
@@ -278,9 +281,8 @@ __global__ void aos_record_kernel(AosArgs a)
     if (a.rec32) {
         float f32[16];
         rec32_fields<double>(rec, rec[3], rec[11], rec + 4, rec + 8, rec + 12, rec + 16, f32);
-        float* r32 = a.rec32 + rec32_offset(e, a.nW, t, 0, 0);
-        for (int q = 0; q < kGroups32; ++q)
-            for (int c = 0; c < 4; ++c) r32[rec32_offset(0, 1, 0, q, c)] = f32[4 * q + c];
+        rec32_store(a.rec32, e, nwin32(a.T), a.T, t, f32);
+        note_radius(a.rmax, sqrtf(f32[0] * f32[0] + f32[1] * f32[1] + f32[2] * f32[2]));
     }
 }
 
@@ -432,6 +434,32 @@ __device__ __forceinline__ void flush_bins(float2* acc, double* g, int T, int la
             atomicAdd(g + 2 * n + 1, (double)v.y);
         }
         acc[n] = make_float2(0.f, 0.f);
+    }
+    __syncwarp();
+}
+
+// Adds the ring slots of bins b0 .. b0 + nb - 1 (nb <= R; b0 >= 0, with the anchor's
+// multiple of T) of a warp's observer row to the global FP64 sums [obs][bin mod T][2] and
+// clears them; slot 0 takes the overflow slot R with it.
+__device__ __forceinline__ void ring_flush(float2* row, int R, int b0, int nb, double* g, int T, unsigned tm,
+                                           int lane, DeviceErr* err)
+{
+    __syncwarp();
+    for (int m = lane; m < nb; m += 32) {
+        const int b = b0 + m, sl = b & (R - 1);
+        float2 v = row[sl];
+        row[sl] = make_float2(0.f, 0.f);
+        if (sl == 0) {
+            v = add2(v, row[R]);
+            row[R] = make_float2(0.f, 0.f);
+        }
+        if (!(fabsf(v.x) < 3.0e38f) || !(fabsf(v.y) < 3.0e38f)) flag(err, ACUM_DEVERR_NONFINITE, &err->nonfinite);
+        if (v.x != 0.0f || v.y != 0.0f) {
+            int n = b - (int)__umulhi((unsigned)b, tm) * T;
+            n = n < 0 ? n + T : n;
+            atomicAdd(g + 2 * n, (double)v.x);
+            atomicAdd(g + 2 * n + 1, (double)v.y);
+        }
     }
     __syncwarp();
 }
@@ -773,25 +801,34 @@ __device__ __forceinline__ void add_bin(float2* acc, int idx, float w, float2 pa
     acc[idx] = fma2(f2(w), dp, add2(acc[idx], pa));
 }
 
-// A warp's observer row: T bins, then an overflow slot (index T, bin 0 of the next
-// period, added into bin 0 when the row is flushed) and a scratch slot (index T + 1,
-// never read).
+// Slot of bin index n >= 0 in a warp's observer row: whole rows hold the T bins of the
+// period (n mod T by multiply-high, m = ceil(2^32 / T)); a ring holds R = m + 1 (a power
+// of two) consecutive bins (n mod R).
+template <bool RING>
+__device__ __forceinline__ int bin_slot(int n, int T, unsigned m)
+{
+    return RING ? (int)((unsigned)n & m) : mod_T(n, T, m);
+}
+
+// A warp's observer row: `nb` slots (the T bins of the period, or the R slots of the
+// ring), then an overflow slot (index nb: the slot after the last, i.e. slot 0, added
+// into it when the row is flushed) and a scratch slot (index nb + 1, never read).
 //
-// Bins n with u(a) < n <= u(b) + kshift: n = k(a) + 1 ... k(b) + kshift, the value
-// interpolated between the two samples.  For |Mr| < 1 an interval holds at most 2 bins
-// (u(b) - u(a) = 1 - Mr < 2).  Both are written by every lane without a branch: the
-// first at the first bin modulo T, the second at the slot after it (which may be the
-// overflow slot); a lane with fewer bins adds into the scratch slot instead.  The bins of
-// the lanes of a warp are disjoint (observer time increases with the step), so only the
-// scratch slot is written by more than one lane.  A decreasing or non-finite observer
-// time sets `bad` and deposits nothing.  Intervals of more than two bins (|Mr| >= 1) set
-// `more`: the caller then adds their other bins with deposit_rest.  The integer parts k
-// carry a multiple of T of at least 2^23 (the anchor's), which keeps the bin index
-// non-negative for the modulo.
-__device__ __forceinline__ void deposit(float2* acc, int T, unsigned tm, const SmpF& a, const SmpF& b, int kshift,
+// Bins n with u(a) < n <= u(b): n = k(a) + 1 ... k(b), the value interpolated between the
+// two samples.  For |Mr| < 1 an interval holds at most 2 bins (u(b) - u(a) = 1 - Mr < 2).
+// Both are written by every lane without a branch: the first at its slot, the second at
+// the slot after it (which may be the overflow slot); a lane with fewer bins adds into
+// the scratch slot instead.  The bins of the lanes of a warp are disjoint (observer time
+// increases with the step), so only the scratch slot is written by more than one lane.
+// A decreasing or non-finite observer time sets `bad` and deposits nothing.  Intervals
+// of more than two bins (|Mr| >= 1) set `more`: the caller then adds their other bins
+// with deposit_rest.  The integer parts k carry a multiple of T of at least 2^23 (the
+// anchor's), which keeps the bin index non-negative.
+template <bool RING>
+__device__ __forceinline__ void deposit(float2* acc, int nb, int T, unsigned m, const SmpF& a, const SmpF& b,
                                         bool active, unsigned& bad, bool& more)
 {
-    const int cnt = b.k + kshift - a.k;
+    const int cnt = b.k - a.k;
     const float du = small_int_to_float(cnt) + (b.f - a.f);
     const bool ok = du > 0.0f;  // false for NaN
     bad |= (active && !ok) ? 1u : 0u;
@@ -800,9 +837,9 @@ __device__ __forceinline__ void deposit(float2* acc, int T, unsigned tm, const S
     // not finite when !ok; both slots are then the scratch slot, which is never read out
     const float inv = rcp_ftz(du);
     const float2 pa = make_float2(a.pt, a.pl), dp = sub2(make_float2(b.pt, b.pl), pa);
-    const int idx = mod_T(a.k + 1, T, tm);  // used only when `one`
+    const int idx = bin_slot<RING>(a.k + 1, T, m);  // used only when `one`
     const float w1 = (1.0f - a.f) * inv;
-    const int i1 = one ? idx : T + 1, i2 = two ? idx + 1 : T + 1;
+    const int i1 = one ? idx : nb + 1, i2 = two ? idx + 1 : nb + 1;
     // i1 != i2 unless both are the scratch slot, so both bins are read before either is
     // written (one shared-memory round trip per sample instead of two in sequence)
     const float2 v1 = acc[i1], v2 = acc[i2];
@@ -811,24 +848,26 @@ __device__ __forceinline__ void deposit(float2* acc, int T, unsigned tm, const S
 }
 
 // The bins after the first two of an interval that holds more (see deposit); an interval
-// of more than T bins sets `bad` instead.
-__device__ __forceinline__ void deposit_rest(float2* acc, int T, unsigned tm, const SmpF& a, const SmpF& b,
-                                             int kshift, bool active, unsigned& bad)
+// of more bins than the row has slots sets `bad` instead.
+template <bool RING>
+__device__ __forceinline__ void deposit_rest(float2* acc, int nb, int T, unsigned m, const SmpF& a, const SmpF& b,
+                                             bool active, unsigned& bad)
 {
-    const int cnt = b.k + kshift - a.k;
+    const int cnt = b.k - a.k;
     const float du = small_int_to_float(cnt) + (b.f - a.f);
     if (!(active && du > 0.0f && cnt > 2)) return;
-    if (cnt > T) {
+    if (cnt > nb) {
         bad = 1u;
         return;
     }
     const float inv = rcp_ftz(du);
     const float2 pa = make_float2(a.pt, a.pl), dp = sub2(make_float2(b.pt, b.pl), pa);
     const float w1 = (1.0f - a.f) * inv;
-    int i = mod_T(a.k + 1, T, tm);
-    for (int m = 1; m < cnt; ++m) {
-        if (++i >= T) i -= T;
-        if (m >= 2) acc[i] = add2(acc[i], fma2(f2(w1 + (float)m * inv), dp, pa));
+    int i = bin_slot<RING>(a.k + 1, T, m);
+    for (int q = 1; q < cnt; ++q) {
+        if (RING) i = (int)((unsigned)(i + 1) & m);
+        else if (++i >= T) i -= T;
+        if (q >= 2) acc[i] = add2(acc[i], fma2(f2(w1 + (float)q * inv), dp, pa));
     }
 }
 
@@ -845,13 +884,11 @@ __device__ __forceinline__ SmpF shfl_idx(const SmpF& v, int src)
 // Block-wide shared state of the mixed kernels besides the dynamic shared memory.
 template <int SE, int OPW>
 struct __align__(16) MixedShared {
-    SmpF carry[16 / OPW][2][OPW][SE];  // per warp and observer: left neighbour of lane 0, by window parity
-    SmpF first[16 / OPW][OPW][SE];     // per warp and observer: first sample of each element (periodic wrap)
-    uint64_t tfull[kMaxStages];        // tensor-memory form: a slot's copy into tensor memory is complete
+    uint64_t tfull[kMaxStages];  // tensor-memory form: a slot's copy into tensor memory is complete
     int abort;
     int release[kMaxStages];
     int last[kMaxStages];
-    int claim[kMaxStages];  // tensor-memory form: warps that reached the slot's stage (the first copies)
+    int claim[kMaxStages];   // tensor-memory form: warps that reached the slot's stage (the first copies)
     int copied[kMaxStages];  // tensor-memory form: stage of the slot's last copy, -1 = none
     uint32_t tmem;           // tensor-memory form: base address of the block's columns
 };
@@ -865,15 +902,38 @@ __device__ __forceinline__ uint32_t tm_col(int s, int jp)
 }
 constexpr uint32_t kTmemCols = 512;  // NS x SE / 2 x 32 <= 512 for every stage shape the plan allows
 
+// Ring form: the largest distance of a sample's bin from its step plus the anchor's, in
+// bins (ring_reach_bins with the records' largest |x|).
+__device__ __forceinline__ double ring_reach(const KParams& p)
+{
+    return ring_reach_bins(__uint_as_float(*p.rmax), p.vx, p.vy, p.vz, p.a0, p.oM / p.dPsi);
+}
+
 // One work item of the mixed form: observers [ot*W, ot*W + W) and elements [e0, e1)
 // (a multiple of SE) of the deck `p`; each warp evaluates OPW observers on the records it
-// loads once.  The dynamic shared memory holds the FP32 bin rows (W rows of T + 2 float2,
-// laid out for the item's T) followed by the NS-stage ring;
-// `stage_off` is where the ring starts (fixed for a launch).  `gbase` counts the stages
-// the block has consumed before this item, so consecutive items of a block continue the
-// mbarrier phases of the same ring.  On entry every slot is free and all bin rows are
-// zero; on return (without abort) the same holds again.
-template <int SE, int OPW, bool TM, bool HOIST = true>
+// loads once.  The dynamic shared memory holds the FP32 bin rows (W rows of nb + 2
+// float2: nb = T bins of the period, or the R slots of a ring) followed by the NS-stage
+// ring of record stages; `stage_off` is where the stages start (fixed for a launch).
+// `gbase` counts the stages the block has consumed before this item, so consecutive
+// items of a block continue the mbarrier phases of the same stage ring.  On entry every
+// stage slot is free and all bin rows are zero; on return (without abort) the same holds
+// again.
+//
+// A stage holds SE elements' records of one 32-step window (windows overlap by one step:
+// lane l of window w is step 31 w + l, up to step T = step 0 of the next period).  Lane
+// l >= 1 deposits the interval between its sample and lane l - 1's, so every interval of
+// the period, the wrap (T - 1, T] included, is deposited once, by the window that holds
+// both its ends.
+//
+// Whole rows (RING = false): the stages take the windows of an element group in turn, and
+// the rows are added into the FP64 sums after the group's last window (every
+// `flush_groups` groups).  Ring (RING = true): the stages take every element group of a
+// window before the next window.  The bins that window w reaches lie within a span of 31
+// + 2 x reach (ring_reach) bins that moves by 31 per window, so each row is a ring of R
+// slots (bin n in slot n mod R) and after a window's last group its lowest 31 bins, which
+// no later window reaches, are added into the FP64 sums and cleared; the rest at the end
+// of the item.
+template <int SE, int OPW, bool TM, bool RING>
 __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot, int e0, int e1, unsigned char* smem,
                                            size_t stage_off, MixedShared<SE, OPW>& sh, unsigned& gbase)
 {
@@ -881,7 +941,9 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nwarps = blockDim.x >> 5;
     const int W = p.W;  // observers per block = OPW x warps
-    const int T = p.T, NS = p.NS, nW = p.nW;
+    const int T = p.T, NS = p.NS, nW = p.nW32;
+    const int nb = RING ? p.ring : T;                                // slots per row
+    const unsigned mm = RING ? (unsigned)(p.ring - 1) : p.tmod;      // their index modulus
     float2* acc_all = reinterpret_cast<float2*>(smem);
     float* stages = reinterpret_cast<float*>(smem + stage_off);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + stage_off + (size_t)NS * SE * kTile * sizeof(float));
@@ -889,12 +951,24 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
     const int N = ngroups * nW;
     const unsigned g0 = gbase;
 
+    // stage i: element group and window
+    const auto stage_gw = [&](int i, int& g, int& w) {
+        if (RING) {
+            w = i / ngroups;
+            g = i - w * ngroups;
+        } else {
+            g = i / nW;
+            w = i - g * nW;
+        }
+    };
     // stage = SE / 2 element-pair tiles of one window (2 kTile floats each)
     const float* rec = reinterpret_cast<const float*>(p.rec);
     const uint32_t pair_bytes = 2 * kTile * sizeof(float);
     auto issue = [&](int i) {
         const unsigned gi = g0 + (unsigned)i;
-        const int s = (int)(gi % (unsigned)NS), g = i / nW, w = i % nW;
+        const int s = (int)(gi % (unsigned)NS);
+        int g, w;
+        stage_gw(i, g, w);
         sh.last[s] = (int)gi;
         mbar_expect_tx(&bars[s], pair_bytes * (SE / 2));
         for (int jp = 0; jp < SE / 2; ++jp) {
@@ -911,6 +985,8 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
     float ox[OPW], oy[OPW], oz[OPW];
     float2* acc[OPW];
     Anchor anc[OPW];
+    int lo[OPW];  // ring: the lowest bin window 0 reaches
+    const double reach = RING ? ring_reach(p) : 0.0;
 #pragma unroll
     for (int q = 0; q < OPW; ++q) {
         o[q] = ot * W + warp * OPW + q;
@@ -919,13 +995,16 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
         ox[q] = p.obs32[3 * oc];
         oy[q] = p.obs32[3 * oc + 1];
         oz[q] = p.obs32[3 * oc + 2];
-        acc[q] = acc_all + (size_t)(warp * OPW + q) * (T + 2);  // T bins, the overflow and the scratch slot
+        acc[q] = acc_all + (size_t)(warp * OPW + q) * (nb + 2);  // nb slots, the overflow and the scratch slot
         anc[q] = make_anchor(p, ox[q], oy[q], oz[q]);
+        // a sample at step tau has bin k = tau + ki + floor(x), x >= kf - reach, and lane
+        // tau >= 31 w + 1 deposits bins above k(tau - 1)
+        lo[q] = RING ? anc[q].ki + (int)floor((double)anc[q].kf - reach) + 1 : 0;
     }
     unsigned bad = 0;
     bool more = false;
 
-    int s = (int)(g0 % (unsigned)NS), w = 0, g = 0, since_flush = 0;
+    int s = (int)(g0 % (unsigned)NS), since_flush = 0;
     uint32_t par = (g0 / (unsigned)NS) & 1u;
     for (int i = 0; i < N; ++i) {
         bool ok;
@@ -960,8 +1039,11 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
             break;
         }
         if (*(volatile int*)&sh.abort) break;
-        const int tau = w * kWin + lane;
-        const bool valid = tau < T;
+        int g, w;
+        stage_gw(i, g, w);
+        const int tau = w * kStride32 + lane;
+        // lane 0 holds only the left end of lane 1's interval; lanes past step T hold nothing
+        const bool dep_lane = lane > 0 && tau <= T;
         const float* st = stages + (size_t)s * SE * kTile;
         SmpF cur[OPW][SE];
         if (TM) {
@@ -1003,56 +1085,15 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
                     sample_mixed2(gg, ox[q], oy[q], oz[q], anc[q], p, tau, cur[q][2 * jp], cur[q][2 * jp + 1]);
             }
         }
-        const bool first_win = w == 0, last_win = w == nW - 1;
+        // the left neighbour: lane l - 1 of the same window (lane 0 receives lane 31's
+        // sample and deposits nothing)
         const int rot_src = (lane + 31) & 31;
 #pragma unroll
         for (int q = 0; q < OPW; ++q) {
 #pragma unroll
             for (int j = 0; j < SE; ++j) {
-                // the left neighbour: lane l - 1, or for lane 0 the previous window's lane
-                // 31 (kept in shared memory, double-buffered by window parity)
-                SmpF prev = shfl_idx(cur[q][j], rot_src);
-                if (lane == 0) prev = sh.carry[warp][w & 1][q][j];
-                deposit(acc[q], T, p.tmod, prev, cur[q][j], 0, ok_obs[q] && valid && !(first_win && lane == 0), bad,
-                        more);
-                if (lane == 31) sh.carry[warp][(w + 1) & 1][q][j] = cur[q][j];
-                if (!HOIST) {
-                    if (first_win && lane == 0) sh.first[warp][q][j] = cur[q][j];
-                    if (last_win) {
-                        const SmpF lastS = shfl_idx(cur[q][j], min(31, T - 1 - w * kWin));
-                        if (lane == 0) {
-                            bool wrap_more = false;
-                            deposit(acc[q], T, p.tmod, lastS, sh.first[warp][q][j], T, ok_obs[q], bad, wrap_more);
-                            if (wrap_more)
-                                deposit_rest(acc[q], T, p.tmod, lastS, sh.first[warp][q][j], T, ok_obs[q], bad);
-                        }
-                    }
-                }
-            }
-        }
-        // HOIST: the first window's samples (kept for the wrap) and the periodic wrap itself
-        // are handled after the stage's deposits, one uniform branch each instead of one
-        // per sample (2.6 % faster at workload 2 in the single-deck kernel, 9 % in the
-        // batched one; the per-sample form, HOIST = false, needs fewer registers)
-        if (HOIST && first_win && lane == 0) {
-#pragma unroll
-            for (int q = 0; q < OPW; ++q)
-#pragma unroll
-                for (int j = 0; j < SE; ++j) sh.first[warp][q][j] = cur[q][j];
-        }
-        if (HOIST && last_win) {
-#pragma unroll
-            for (int q = 0; q < OPW; ++q) {
-#pragma unroll
-                for (int j = 0; j < SE; ++j) {
-                    // the periodic wrap: (t(T-1), t(0) + period] (core.cu:173-194)
-                    const SmpF lastS = shfl_idx(cur[q][j], min(31, T - 1 - w * kWin));
-                    if (lane == 0) {
-                        bool wrap_more = false;
-                        deposit(acc[q], T, p.tmod, lastS, sh.first[warp][q][j], T, ok_obs[q], bad, wrap_more);
-                        if (wrap_more) deposit_rest(acc[q], T, p.tmod, lastS, sh.first[warp][q][j], T, ok_obs[q], bad);
-                    }
-                }
+                const SmpF prev = shfl_idx(cur[q][j], rot_src);
+                deposit<RING>(acc[q], nb, T, mm, prev, cur[q][j], ok_obs[q] && dep_lane, bad, more);
             }
         }
         // intervals of more than two bins (|Mr| >= 1): their other bins, for the whole warp
@@ -1061,17 +1102,27 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
             for (int q = 0; q < OPW; ++q) {
 #pragma unroll
                 for (int j = 0; j < SE; ++j) {
-                    SmpF prev = shfl_idx(cur[q][j], rot_src);
-                    if (lane == 0) prev = sh.carry[warp][w & 1][q][j];
-                    deposit_rest(acc[q], T, p.tmod, prev, cur[q][j], 0,
-                                 ok_obs[q] && valid && !(first_win && lane == 0), bad);
+                    const SmpF prev = shfl_idx(cur[q][j], rot_src);
+                    deposit_rest<RING>(acc[q], nb, T, mm, prev, cur[q][j], ok_obs[q] && dep_lane, bad);
                 }
             }
             more = false;
         }
-        // FP32 partial sums cover at most `flush_groups` element groups before they are
-        // added to the FP64 sums in global memory
-        if (last_win && (++since_flush == p.flush_groups || g == ngroups - 1)) {
+        if (RING) {
+            // after a window's last group: the 31 bins no later window reaches, and after
+            // the last window the rest of the ring
+            if (g == ngroups - 1) {
+#pragma unroll
+                for (int q = 0; q < OPW; ++q) {
+                    if (!ok_obs[q]) continue;
+                    double* gs = p.acc + (size_t)o[q] * T * 2;
+                    ring_flush(acc[q], nb, lo[q] + kStride32 * w, kStride32, gs, T, p.tmod, lane, p.err);
+                    if (w == nW - 1) ring_flush(acc[q], nb, lo[q] + kStride32 * nW, nb, gs, T, p.tmod, lane, p.err);
+                }
+            }
+        } else if (w == nW - 1 && (++since_flush == p.flush_groups || g == ngroups - 1)) {
+            // FP32 partial sums cover at most `flush_groups` element groups before they are
+            // added to the FP64 sums in global memory
 #pragma unroll
             for (int q = 0; q < OPW; ++q)
                 if (ok_obs[q]) flush_bins(acc[q], p.acc + (size_t)o[q] * T * 2, T, lane, false, p.err);
@@ -1092,17 +1143,13 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
             s = 0;
             par ^= 1u;
         }
-        if (++w == nW) {
-            w = 0;
-            ++g;
-        }
     }
     // the scratch slot holds whatever the lanes without a bin added; the next item's rows
     // (of another length in a batch) may cover it
     __syncwarp();
     if (lane == 0)
 #pragma unroll
-        for (int q = 0; q < OPW; ++q) acc[q][T + 1] = make_float2(0.f, 0.f);
+        for (int q = 0; q < OPW; ++q) acc[q][nb + 1] = make_float2(0.f, 0.f);
     if (__any_sync(0xffffffffu, bad != 0) && lane == 0) flag(p.err, ACUM_DEVERR_ORDER, &p.err->order);
     gbase = g0 + (unsigned)N;
 }
@@ -1148,14 +1195,17 @@ __device__ __forceinline__ void mixed_drain(unsigned char* smem, size_t stage_of
 // element chunk, then tile within the group, one at a time from a counter in global
 // memory.  The blocks running at any time therefore share one or two chunks of records
 // in L2 (each record is read from HBM about once per group), and the FP64 sums they add
-// into belong to one group of tiles.
-template <int SE, int OPW, bool TM>
-__global__ void __launch_bounds__(512 / OPW, 1) tonal_mixed_kernel(const KParams p)
+// into belong to one group of tiles.  A ring kernel (RING) and a whole-row kernel are
+// launched one after the other when the plan has a ring (p.dual): each tests the
+// records' reach against the ring, and the one that does not match returns at once.
+template <int SE, int OPW, bool TM, bool RING>
+__global__ void __launch_bounds__(512, 1) tonal_mixed_kernel(const KParams p)
 {
+    if (p.dual && ring_fits_bins(ring_reach(p), p.ring) != RING) return;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ MixedShared<SE, OPW> sh;
     __shared__ int s_item;
-    const size_t stage_off = acc_region_bytes(p.W, p.T + 2, 8);
+    const size_t stage_off = acc_region_bytes(p.W, (RING ? p.ring : p.T) + 2, 8);
     if (TM && threadIdx.x < 32) {  // one block per SM: the allocation does not wait
         tmem_alloc(&sh.tmem, kTmemCols);
         tmem_relinquish();
@@ -1179,7 +1229,7 @@ __global__ void __launch_bounds__(512 / OPW, 1) tonal_mixed_kernel(const KParams
         const int ec = r / gn, ot = g * G + (r - ec * gn);
         const int e0 = ec * p.chunk;
         const int e1 = min(e0 + p.chunk, p.Epad);
-        mixed_item<SE, OPW, TM>(p, ot, e0, e1, smem, stage_off, sh, gbase);
+        mixed_item<SE, OPW, TM, RING>(p, ot, e0, e1, smem, stage_off, sh, gbase);
         __syncthreads();
         if (sh.abort) {
             mixed_drain<SE, OPW>(smem, stage_off, p.NS, sh);
@@ -1203,17 +1253,19 @@ __global__ void __launch_bounds__(512 / OPW, 1) tonal_mixed_kernel(const KParams
 // Many decks: one block per SM (as many as fit) takes work items from a shared counter
 // (largest first, as the host sorts them) until none are left.  Item k is (case,
 // observer tile, first element, end element); the case's constants are copied into
-// shared memory at the start of each item.
-template <int SE>
+// shared memory at the start of each item, and a case whose records fit the bin ring
+// (ring > 0 in its constants, decided by the host) runs the ring form, the others whole
+// rows.
+template <int SE, int OPW>
 __global__ void __launch_bounds__(512, 1)
     tonal_batch_kernel(const KParams* __restrict__ cases, const BatchItem* __restrict__ items, int nitems,
                        int* counter, int NS, size_t stage_off)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ MixedShared<SE, 1> sh;
+    __shared__ MixedShared<SE, OPW> sh;
     __shared__ __align__(16) KParams sp;
     __shared__ BatchItem s_it;
-    mixed_init<SE, 1>(smem, stage_off, NS, sh);
+    mixed_init<SE, OPW>(smem, stage_off, NS, sh);
     unsigned gbase = 0;
     for (;;) {
         if (threadIdx.x == 0) {
@@ -1227,17 +1279,21 @@ __global__ void __launch_bounds__(512, 1)
         for (int k = threadIdx.x; k < kWords; k += blockDim.x)
             reinterpret_cast<int*>(&sp)[k] = reinterpret_cast<const int*>(cases + it.c)[k];
         __syncthreads();
-        mixed_item<SE, 1, false, true>(sp, it.ot, it.e0, it.e1, smem, stage_off, sh, gbase);
+        if (sp.ring > 0)
+            mixed_item<SE, OPW, false, true>(sp, it.ot, it.e0, it.e1, smem, stage_off, sh, gbase);
+        else
+            mixed_item<SE, OPW, false, false>(sp, it.ot, it.e0, it.e1, smem, stage_off, sh, gbase);
         __syncthreads();
         if (sh.abort) {
-            mixed_drain<SE, 1>(smem, stage_off, NS, sh);
+            mixed_drain<SE, OPW>(smem, stage_off, NS, sh);
             break;
         }
     }
 }
 
-constexpr int kMixedSE = 8;   // samples in flight per lane of the mixed kernel (SE x OPW)
-constexpr int kMixedOPW = 1;  // observers per warp of the mixed kernel
+constexpr int kMixedSE = 8;   // elements per stage of the whole-row mixed kernel (one observer per warp)
+constexpr int kRingSE = 4;    // elements per stage of the ring kernel
+constexpr int kRingOPW = 2;   // observers per warp of the ring kernel
 constexpr bool kMixedTmem = false;  // record stages read from tensor memory by default
 static_assert(kMaxStages >= 4, "stage bookkeeping");
 static_assert(sizeof(SmpF) == 16, "sample record");
@@ -1256,41 +1312,50 @@ static size_t static_smem_of(K kernel, size_t estimate)
     return a.sharedSizeBytes;
 }
 
+// static shared memory of the mixed kernels (the ring and whole-row forms of a shape have
+// the same)
 static size_t mixed_static_smem(int SE, int opw, bool tm)
 {
     static size_t v[2][3][9] = {};
     if (SE != 2 && SE != 4 && SE != 8) SE = 8;
     if (opw != 2) opw = 1;
-    if (opw == 2) tm = false;
+    if (opw == 2) {
+        tm = false;
+        if (SE == 8) SE = 4;
+    }
     size_t& x = v[tm ? 1 : 0][opw][SE];
     if (!x) {
-        const size_t est = (size_t)16 * 3 * SE * sizeof(SmpF) + 512;
+        const size_t est = (size_t)1024;
         if (opw == 2)
-            x = SE == 2   ? static_smem_of(tonal_mixed_kernel<2, 2, false>, est)
-                : SE == 4 ? static_smem_of(tonal_mixed_kernel<4, 2, false>, est)
-                          : static_smem_of(tonal_mixed_kernel<8, 2, false>, est);
+            x = SE == 2 ? static_smem_of(tonal_mixed_kernel<2, 2, false, true>, est)
+                        : static_smem_of(tonal_mixed_kernel<4, 2, false, true>, est);
         else if (tm)
-            x = SE == 2   ? static_smem_of(tonal_mixed_kernel<2, 1, true>, est)
-                : SE == 4 ? static_smem_of(tonal_mixed_kernel<4, 1, true>, est)
-                          : static_smem_of(tonal_mixed_kernel<8, 1, true>, est);
+            x = SE == 2   ? static_smem_of(tonal_mixed_kernel<2, 1, true, false>, est)
+                : SE == 4 ? static_smem_of(tonal_mixed_kernel<4, 1, true, false>, est)
+                          : static_smem_of(tonal_mixed_kernel<8, 1, true, false>, est);
         else
-            x = SE == 2   ? static_smem_of(tonal_mixed_kernel<2, 1, false>, est)
-                : SE == 4 ? static_smem_of(tonal_mixed_kernel<4, 1, false>, est)
-                          : static_smem_of(tonal_mixed_kernel<8, 1, false>, est);
+            x = SE == 2   ? static_smem_of(tonal_mixed_kernel<2, 1, false, false>, est)
+                : SE == 4 ? static_smem_of(tonal_mixed_kernel<4, 1, false, false>, est)
+                          : static_smem_of(tonal_mixed_kernel<8, 1, false, false>, est);
     }
     return x;
 }
 
-size_t batch_static_smem(int SE)
+size_t batch_static_smem(int SE, int opw)
 {
-    static size_t v[9] = {};
+    static size_t v[3][9] = {};
     if (SE != 2 && SE != 4 && SE != 8) SE = 8;
-    if (!v[SE]) {
-        const size_t est = (size_t)16 * 3 * SE * sizeof(SmpF) + 768;
-        v[SE] = SE == 2 ? static_smem_of(tonal_batch_kernel<2>, est)
-                        : SE == 4 ? static_smem_of(tonal_batch_kernel<4>, est) : static_smem_of(tonal_batch_kernel<8>, est);
+    if (opw != 2) opw = 1;
+    if (opw == 2 && SE == 8) SE = 4;
+    if (!v[opw][SE]) {
+        const size_t est = 1024;
+        v[opw][SE] = opw == 2 ? (SE == 2 ? static_smem_of(tonal_batch_kernel<2, 2>, est)
+                                         : static_smem_of(tonal_batch_kernel<4, 2>, est))
+                              : (SE == 2   ? static_smem_of(tonal_batch_kernel<2, 1>, est)
+                                 : SE == 4 ? static_smem_of(tonal_batch_kernel<4, 1>, est)
+                                           : static_smem_of(tonal_batch_kernel<8, 1>, est));
     }
-    return v[SE];
+    return v[opw][SE];
 }
 
 static size_t tonal_smem(int W, int T, int NS, int SE, int real_bytes)
@@ -1301,92 +1366,134 @@ static size_t tonal_smem(int W, int T, int NS, int SE, int real_bytes)
     return acc + (size_t)NS * SE * groups * kWin * 4 * real_bytes + (size_t)NS * 8;
 }
 
-cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int num_sms, size_t smem_optin,
-                       int opw_req, int tm_req)
+// One mixed tile: W observers per block (opw per warp), SE elements per stage, rows of
+// `ring` slots (0: the T bins of the period); as many stages as the shared memory left
+// over holds, and the element chunks of the work items.
+static cudaError_t plan_mixed_tile(const TonalRun& r, TonalTile& t, int W_req, int SE_req, int opw, bool tm, int ring,
+                                   int items_per_sm, int num_sms, size_t smem_optin)
 {
-    const bool f64 = r.precision == ACUM_PLAIN_FP64;
-    const int rb = f64 ? 8 : 4;
-    // FP64: elements per stage 2, one observer per warp.  Mixed: elements per stage 2, 4
-    // or 8 and observers per warp 1 or 2 (default: kMixedSE / kMixedOPW elements of
-    // kMixedOPW observers).  A stage of 8 needs only 2 ring stages.
-    int SE = kSE64, opw = 1;
-    if (!f64) {
-        opw = (opw_req == 1 || opw_req == 2) ? opw_req : kMixedOPW;
-        SE = (SE_req == 2 || SE_req == 4 || SE_req == 8) ? SE_req : kMixedSE / opw;
-
-    }
+    const int T = r.g.T, rowlen = ring > 0 ? ring : T;
+    int SE = (SE_req == 2 || SE_req == 4 || SE_req == 8) ? SE_req : (opw == 2 ? kRingSE : kMixedSE);
+    if (opw == 2 && SE == 8) SE = 4;  // the two-observer form spills at 8
     const int NSmin = SE == 8 ? 2 : 4;
-    r.t.opw = opw;
-    const int T = r.g.T;
-    // at most 16 observers per block: 16 warps of one, or 8 of two (the register limit of
-    // the two-observer form's 256 threads)
-    int W = W_req > 0 ? W_req : 16;
-    W = std::min(W, 16);
-    // keep room in the per-block limit for the kernels' static shared memory
-    // tensor-memory record stages: mixed form with one observer per warp only
-    const bool tm = !f64 && opw == 1 && (tm_req == 1 || (tm_req == 0 && kMixedTmem));
-    r.t.tm = tm;
-    const size_t budget = smem_optin - (f64 ? 1024 : mixed_static_smem(SE, opw, tm));
-    while (W > opw && tonal_smem(W, T, NSmin, SE, rb) > budget) W -= opw;
-    if (tonal_smem(W, T, NSmin, SE, rb) > budget) return cudaErrorInvalidValue;
+    // at most 16 warps (the register limit of 512 threads of 128 registers)
+    int W = W_req > 0 ? W_req : 16 * opw;
+    W = std::min(W, 16 * opw);
+    // keep room in the per-block limit for the kernel's static shared memory
+    const size_t budget = smem_optin - mixed_static_smem(SE, opw, tm);
+    while (W > opw && tonal_smem(W, rowlen, NSmin, SE, 4) > budget) W -= opw;
+    if (tonal_smem(W, rowlen, NSmin, SE, 4) > budget) return cudaErrorInvalidValue;
     if (W_req <= 0) {
         // do not spread few observers over many idle warps
         W = std::max(opw, std::min(W, (r.g.O + opw - 1) / opw * opw));
     }
     W = (W + opw - 1) / opw * opw;
-    // mixed: as many ring stages (4..8) as the shared memory left over by the bins holds,
-    // without lowering the blocks per SM (registers, ~128 per thread, allow 65536 / (128 *
-    // 32 W) blocks of W warps)
+    // as many stages (4..8) as the shared memory left over by the bins holds, without
+    // lowering the blocks per SM (registers, ~128 per thread, allow 65536 / (128 * 32 x
+    // warps) blocks)
     int NS = NSmin;
-    if (!f64) {
-        const auto per_sm_at = [&](int ns) { return (int)((228 * 1024) / (tonal_smem(W, T, ns, SE, rb) + 1024)); };
-        const int resident = std::max(1, std::min(per_sm_at(NSmin), 65536 / (128 * 32 * (W / opw))));
-        while (NS < kMaxStages && tonal_smem(W, T, NS + 1, SE, rb) <= budget && per_sm_at(NS + 1) >= resident) ++NS;
-    }
-    // tensor-memory form: the ring's stages fit in the block's kTmemCols columns, and one
-    // block per SM holds them all
+    const auto per_sm_at = [&](int ns) { return (int)((228 * 1024) / (tonal_smem(W, rowlen, ns, SE, 4) + 1024)); };
+    const int resident = std::max(1, std::min(per_sm_at(NSmin), 65536 / (128 * 32 * (W / opw))));
+    while (NS < kMaxStages && tonal_smem(W, rowlen, NS + 1, SE, 4) <= budget && per_sm_at(NS + 1) >= resident) ++NS;
+    // tensor-memory form: the stages fit in the block's kTmemCols columns, and one block per
+    // SM holds them all
     if (tm) NS = std::max(1, std::min(NS, (int)kTmemCols / (16 * SE)));
-    TonalTile& t = r.t;
-    t.flush_elems = 1 << 30;
     t.W = W;
     t.SE = SE;
     t.NS = NS;
-    t.smem = tonal_smem(W, T, NS, SE, rb);
+    t.opw = opw;
+    t.tm = tm;
+    t.ring = ring;
+    t.smem = tonal_smem(W, rowlen, NS, SE, 4);
     // more than half of the shared memory keeps a second block off the SM (a second
     // allocation of the tensor-memory columns would wait for the first block to end)
     if (tm) t.smem = std::max(t.smem, std::min(budget, smem_optin / 2 + 1024));
     const int obs_tiles = (r.g.O + W - 1) / W;
-    // resident blocks per SM: shared memory, and registers (~128 per thread)
     const int per_sm =
         tm ? 1 : std::max(1, std::min((int)((228 * 1024) / (t.smem + 1024)), 65536 / (128 * 32 * (W / opw))));
     const int slots = num_sms * per_sm;
-    const int groups = r.g.Epad / SE;
+    // Element chunks whose FP32 records (nW32 x 2048 B per element) take about 32 MB, so
+    // that the blocks running at one time (which work on one chunk) find the chunk in L2
+    // and each record is read from HBM a few times per launch at most; smaller if needed to
+    // give every slot `items_per_sm` items (default 8).  The FP32 bins are added into the
+    // FP64 sums within each item (at most 512 elements): larger chunks would re-read
+    // records, smaller ones would add FP64 flush traffic.
+    const size_t per_elem = (size_t)nwin32(T) * kGroups32 * kWin * 4 * sizeof(float);
+    long chunk = (long)std::max<size_t>((size_t)SE, ((size_t)32 << 20) / per_elem);
+    chunk = std::min<long>(chunk, 512);
+    const int ips = items_per_sm > 0 ? items_per_sm : 8;
+    const long want = std::max<long>(1, ((long)ips * slots + obs_tiles - 1) / obs_tiles);
+    chunk = std::min(chunk, ((long)r.g.Epad + want - 1) / want);
+    chunk = std::max<long>(SE, chunk / SE * SE);
+    t.chunk = (int)chunk;
+    t.nchunk = (int)(((long)r.g.Epad + chunk - 1) / chunk);
+    t.items = obs_tiles * t.nchunk;
+    // one group of all observer tiles: grouping them so that their FP64 sums stay in L2
+    // re-reads the records once per group and measured no faster
+    t.tile_group = obs_tiles;
+    t.grid = std::min(t.items, slots);
+    t.flush_elems = t.chunk;
+    return cudaSuccess;
+}
+
+cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int num_sms, size_t smem_optin,
+                       int opw_req, int tm_req, int rows_only)
+{
+    const bool f64 = r.precision == ACUM_PLAIN_FP64;
+    memset(&r.rows, 0, sizeof(r.rows));
     if (!f64) {
-        // Mixed: element chunks whose FP32 records (nW x 2560 B per element) take about
-        // 32 MB, so that the blocks running at one time (which work on one chunk) find the
-        // chunk in L2 and each record is read from HBM a few times per launch at most;
-        // smaller if needed to give every slot `items_per_sm` items (default 8).  The FP32
-        // bin rows are flushed to the FP64 sums once per item (at most 512 elements):
-        // larger chunks would re-read records, smaller ones would add FP64 flush traffic.
-        const size_t per_elem = (size_t)r.g.nW * kGroups32 * kWin * 4 * sizeof(float);
-        long chunk = (long)std::max<size_t>((size_t)SE, ((size_t)32 << 20) / per_elem);
-        chunk = std::min<long>(chunk, 512);
-        const int ips = items_per_sm > 0 ? items_per_sm : 8;
-        const long want = std::max<long>(1, ((long)ips * slots + obs_tiles - 1) / obs_tiles);
-        chunk = std::min(chunk, ((long)r.g.Epad + want - 1) / want);
-        chunk = std::max<long>(SE, chunk / SE * SE);
-        t.chunk = (int)chunk;
-        t.nchunk = (int)(((long)r.g.Epad + chunk - 1) / chunk);
-        t.items = obs_tiles * t.nchunk;
-        // one group of all observer tiles: grouping them so that their FP64 sums stay in
-        // L2 re-reads the records once per group and measured no faster
-        t.tile_group = obs_tiles;
-        t.grid = std::min(t.items, slots);
-        t.flush_elems = t.chunk;
+        // Mixed: the ring kernel (observers per warp 1 or 2, default 2; elements per stage
+        // 2 or 4, or 8 with one observer) with the whole-row kernel (one observer per warp)
+        // behind it for records that reach too far for the ring; whole rows alone when
+        // asked for, with tensor-memory stages, or without the records' reach.
+        const bool tm = tm_req == 1 || (tm_req == 0 && kMixedTmem);
+        TonalTile rows;
+        memset(&rows, 0, sizeof(rows));
+        cudaError_t e = plan_mixed_tile(r, rows, std::min(W_req, 16), SE_req, 1, tm, 0, items_per_sm, num_sms,
+                                        smem_optin);
+        if (e != cudaSuccess) return e;
+        if (tm || rows_only || !r.rmax) {
+            r.t = rows;
+            return cudaSuccess;
+        }
+        const int opw = opw_req == 1 ? 1 : kRingOPW;
+        TonalTile ring;
+        memset(&ring, 0, sizeof(ring));
+        if (plan_mixed_tile(r, ring, W_req, SE_req, opw, false, kRingSlots, items_per_sm, num_sms, smem_optin) !=
+            cudaSuccess) {
+            r.t = rows;
+            return cudaSuccess;
+        }
+        r.t = ring;
+        r.rows = rows;
         return cudaSuccess;
     }
+    // FP64: elements per stage 2, one observer per warp
+    const int SE = kSE64, opw = 1;
+    const int NSmin = 4;
+    const int T = r.g.T;
+    int W = W_req > 0 ? W_req : 16;
+    W = std::min(W, 16);
+    const size_t budget = smem_optin - 1024;
+    while (W > opw && tonal_smem(W, T, NSmin, SE, 8) > budget) W -= opw;
+    if (tonal_smem(W, T, NSmin, SE, 8) > budget) return cudaErrorInvalidValue;
+    if (W_req <= 0) W = std::max(1, std::min(W, r.g.O));
+    TonalTile& t = r.t;
+    t.flush_elems = 1 << 30;
+    t.W = W;
+    t.SE = SE;
+    t.NS = NSmin;
+    t.opw = 1;
+    t.tm = false;
+    t.ring = 0;
+    t.smem = tonal_smem(W, T, NSmin, SE, 8);
+    const int obs_tiles = (r.g.O + W - 1) / W;
+    // resident blocks per SM: shared memory, and registers (~128 per thread)
+    const int per_sm = std::max(1, std::min((int)((228 * 1024) / (t.smem + 1024)), 65536 / (128 * 32 * W)));
+    const int slots = num_sms * per_sm;
+    const int groups = r.g.Epad / SE;
     const int ips = items_per_sm > 0 ? items_per_sm : 64;
-    // FP64: number of element chunks among 1 .. ips work items per slot with the smallest
+    // number of element chunks among 1 .. ips work items per slot with the smallest
     // wave-quantisation loss (a small charge per extra chunk for its prologue and its
     // flush of the bins); one block per item
     int best = 1;
@@ -1426,21 +1533,23 @@ static cudaError_t launch_f64_t(const KParams& kp, int items, int threads, size_
     return cudaGetLastError();
 }
 
-template <int SE, int OPW, bool TM>
+template <int SE, int OPW, bool TM, bool RING>
 static cudaError_t launch_mixed_t(const KParams& kp, int grid, int threads, size_t smem, cudaStream_t s)
 {
     static size_t configured = 0;
     if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(tonal_mixed_kernel<SE, OPW, TM>,
+        cudaError_t e = cudaFuncSetAttribute(tonal_mixed_kernel<SE, OPW, TM, RING>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
-    tonal_mixed_kernel<SE, OPW, TM><<<grid, threads, smem, s>>>(kp);
+    tonal_mixed_kernel<SE, OPW, TM, RING><<<grid, threads, smem, s>>>(kp);
     return cudaGetLastError();
 }
 
-void fill_kparams(const TonalRun& r, KParams& kp)
+void fill_kparams(const TonalRun& r, KParams& kp) { fill_kparams(r, r.t, kp); }
+
+void fill_kparams(const TonalRun& r, const TonalTile& tile, KParams& kp)
 {
     memset(&kp, 0, sizeof(kp));
     const TonalGeom& g = r.g;
@@ -1448,6 +1557,10 @@ void fill_kparams(const TonalRun& r, KParams& kp)
     kp.Epad = g.Epad;
     kp.T = g.T;
     kp.nW = g.nW;
+    kp.nW32 = nwin32(g.T);
+    kp.ring = r.t.ring;  // the ring kernel's slots, also in the whole-row kernel launched behind it
+    kp.dual = r.t.ring > 0 ? 1 : 0;
+    kp.rmax = r.rmax;
     kp.O = g.O;
     kp.obs32 = r.obs32;
     kp.obs64 = r.obs64;
@@ -1473,15 +1586,37 @@ void fill_kparams(const TonalRun& r, KParams& kp)
     kp.kb2 = make_float2(kbf, kbf);
     kp.tmod = (unsigned)((0x100000000ull + (unsigned long long)g.T - 1) / (unsigned long long)g.T);
     kp.toff = (int)(((1 << 23) + g.T - 1) / g.T * g.T);
-    kp.W = r.t.W;
-    kp.NS = r.t.NS;
-    kp.chunk = r.t.chunk;
-    kp.nchunk = r.t.nchunk;
-    kp.obs_tiles = (g.O + r.t.W - 1) / r.t.W;
-    kp.tile_group = r.t.tile_group > 0 ? r.t.tile_group : kp.obs_tiles;
-    kp.flush_groups = std::max(1, r.t.flush_elems / r.t.SE);
+    kp.W = tile.W;
+    kp.NS = tile.NS;
+    kp.chunk = tile.chunk;
+    kp.nchunk = tile.nchunk;
+    kp.obs_tiles = (g.O + tile.W - 1) / tile.W;
+    kp.tile_group = tile.tile_group > 0 ? tile.tile_group : kp.obs_tiles;
+    kp.flush_groups = std::max(1, tile.flush_elems / tile.SE);
     kp.acc = r.acc;
     kp.err = r.err;
+}
+
+static cudaError_t launch_mixed_tile(const KParams& kp, const TonalTile& t, cudaStream_t s)
+{
+    const int threads = 32 * (t.W / t.opw);
+    if (t.ring > 0) {
+        if (t.opw == 2) {
+            if (t.SE == 2) return launch_mixed_t<2, 2, false, true>(kp, t.grid, threads, t.smem, s);
+            return launch_mixed_t<4, 2, false, true>(kp, t.grid, threads, t.smem, s);
+        }
+        if (t.SE == 2) return launch_mixed_t<2, 1, false, true>(kp, t.grid, threads, t.smem, s);
+        if (t.SE == 4) return launch_mixed_t<4, 1, false, true>(kp, t.grid, threads, t.smem, s);
+        return launch_mixed_t<8, 1, false, true>(kp, t.grid, threads, t.smem, s);
+    }
+    if (t.tm) {
+        if (t.SE == 2) return launch_mixed_t<2, 1, true, false>(kp, t.grid, threads, t.smem, s);
+        if (t.SE == 8) return launch_mixed_t<8, 1, true, false>(kp, t.grid, threads, t.smem, s);
+        return launch_mixed_t<4, 1, true, false>(kp, t.grid, threads, t.smem, s);
+    }
+    if (t.SE == 2) return launch_mixed_t<2, 1, false, false>(kp, t.grid, threads, t.smem, s);
+    if (t.SE == 8) return launch_mixed_t<8, 1, false, false>(kp, t.grid, threads, t.smem, s);
+    return launch_mixed_t<4, 1, false, false>(kp, t.grid, threads, t.smem, s);
 }
 
 cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s)
@@ -1489,69 +1624,76 @@ cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s)
     KParams kp;
     fill_kparams(r, kp);
     if (r.precision == ACUM_PLAIN_FP64) return launch_f64_t<kSE64>(kp, r.t.items, 32 * r.t.W, r.t.smem, s);
-    const int threads = 32 * (r.t.W / r.t.opw);
-    if (r.t.opw == 2) {
-        if (r.t.SE == 2) return launch_mixed_t<2, 2, false>(kp, r.t.grid, threads, r.t.smem, s);
-        if (r.t.SE == 4) return launch_mixed_t<4, 2, false>(kp, r.t.grid, threads, r.t.smem, s);
-        return launch_mixed_t<8, 2, false>(kp, r.t.grid, threads, r.t.smem, s);
-    }
-    if (r.t.tm) {
-        if (r.t.SE == 2) return launch_mixed_t<2, 1, true>(kp, r.t.grid, threads, r.t.smem, s);
-        if (r.t.SE == 8) return launch_mixed_t<8, 1, true>(kp, r.t.grid, threads, r.t.smem, s);
-        return launch_mixed_t<4, 1, true>(kp, r.t.grid, threads, r.t.smem, s);
-    }
-    if (r.t.SE == 2) return launch_mixed_t<2, 1, false>(kp, r.t.grid, threads, r.t.smem, s);
-    if (r.t.SE == 8) return launch_mixed_t<8, 1, false>(kp, r.t.grid, threads, r.t.smem, s);
-    return launch_mixed_t<4, 1, false>(kp, r.t.grid, threads, r.t.smem, s);
+    cudaError_t e = launch_mixed_tile(kp, r.t, s);
+    if (e != cudaSuccess || r.t.ring == 0) return e;
+    // the whole-row kernel behind the ring kernel: it runs when the records reach too far
+    // for the ring, and returns at once otherwise
+    KParams kr;
+    fill_kparams(r, r.rows, kr);
+    return launch_mixed_tile(kr, r.rows, s);
 }
 
-size_t batch_smem(int W, int SE, int Tmax)
+size_t batch_smem(int W, int SE, int rowlen)
 {
     const int NS = batch_stages(SE);
-    return acc_region_bytes(W, Tmax + 2, 8) + (size_t)NS * SE * kGroups32 * kWin * 4 * sizeof(float) +
+    return acc_region_bytes(W, rowlen + 2, 8) + (size_t)NS * SE * kGroups32 * kWin * 4 * sizeof(float) +
            (size_t)NS * 8;
 }
 
-template <int SE>
+template <int SE, int OPW>
+static int batch_per_sm_t(int W, size_t smem)
+{
+    int per_sm = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<SE, OPW>, 32 * (W / OPW), smem) !=
+            cudaSuccess ||
+        per_sm < 1) {
+        (void)cudaGetLastError();
+        per_sm = 1;
+    }
+    return per_sm;
+}
+
+template <int SE, int OPW>
 static cudaError_t launch_batch_t(const KParams* d_cases, const BatchItem* d_items, int nitems, int* d_counter, int W,
-                                  int Tmax, int grid, cudaStream_t s)
+                                  int rowlen, int grid, cudaStream_t s)
 {
     static size_t configured = 0;
-    const size_t smem = batch_smem(W, SE, Tmax);
+    const size_t smem = batch_smem(W, SE, rowlen);
     if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(tonal_batch_kernel<SE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(tonal_batch_kernel<SE, OPW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
     // as many resident blocks per SM as shared memory and registers allow
-    int per_sm = 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<SE>, 32 * W, smem) != cudaSuccess ||
-        per_sm < 1)
-        per_sm = 1;
-    tonal_batch_kernel<SE><<<grid * per_sm, 32 * W, smem, s>>>(d_cases, d_items, nitems, d_counter, batch_stages(SE),
-                                                               acc_region_bytes(W, Tmax + 2, 8));
+    const int per_sm = batch_per_sm_t<SE, OPW>(W, smem);
+    tonal_batch_kernel<SE, OPW><<<grid * per_sm, 32 * (W / OPW), smem, s>>>(d_cases, d_items, nitems, d_counter,
+                                                                             batch_stages(SE),
+                                                                             acc_region_bytes(W, rowlen + 2, 8));
     return cudaGetLastError();
 }
 
-int batch_blocks_per_sm(int W, int SE, int Tmax)
+int batch_blocks_per_sm(int W, int SE, int opw, int rowlen)
 {
-    int per_sm = 1;
-    const size_t smem = batch_smem(W, SE, Tmax);
-    cudaError_t e = SE == 2   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<2>, 32 * W, smem)
-                    : SE == 8 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<8>, 32 * W, smem)
-                              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tonal_batch_kernel<4>, 32 * W, smem);
-    return (e == cudaSuccess && per_sm > 0) ? per_sm : 1;
+    const size_t smem = batch_smem(W, SE, rowlen);
+    if (opw == 2) return SE == 2 ? batch_per_sm_t<2, 2>(W, smem) : batch_per_sm_t<4, 2>(W, smem);
+    return SE == 2 ? batch_per_sm_t<2, 1>(W, smem) : SE == 8 ? batch_per_sm_t<8, 1>(W, smem) : batch_per_sm_t<4, 1>(W, smem);
 }
 
 // grid = SMs; the launch puts as many blocks on each SM as fit
 cudaError_t launch_tonal_batch(const KParams* d_cases, const BatchItem* d_items, int nitems, int* d_counter, int W,
-                               int SE, int Tmax, int grid, cudaStream_t s)
+                               int SE, int opw, int rowlen, int grid, cudaStream_t s)
 {
-    if (W < 1 || W > 16 || grid < 1) return cudaErrorInvalidValue;
-    if (SE == 2) return launch_batch_t<2>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s);
-    if (SE == 4) return launch_batch_t<4>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s);
-    if (SE == 8) return launch_batch_t<8>(d_cases, d_items, nitems, d_counter, W, Tmax, grid, s);
+    if (opw != 1 && opw != 2) return cudaErrorInvalidValue;
+    if (W < opw || W > 16 * opw || W % opw != 0 || grid < 1) return cudaErrorInvalidValue;
+    if (opw == 2) {
+        if (SE == 2) return launch_batch_t<2, 2>(d_cases, d_items, nitems, d_counter, W, rowlen, grid, s);
+        if (SE == 4) return launch_batch_t<4, 2>(d_cases, d_items, nitems, d_counter, W, rowlen, grid, s);
+        return cudaErrorInvalidValue;
+    }
+    if (SE == 2) return launch_batch_t<2, 1>(d_cases, d_items, nitems, d_counter, W, rowlen, grid, s);
+    if (SE == 4) return launch_batch_t<4, 1>(d_cases, d_items, nitems, d_counter, W, rowlen, grid, s);
+    if (SE == 8) return launch_batch_t<8, 1>(d_cases, d_items, nitems, d_counter, W, rowlen, grid, s);
     return cudaErrorInvalidValue;
 }
 

@@ -87,6 +87,8 @@ SIGNATURES = {
     "acum_set_tile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "acum_set_obs_per_warp": (C.c_int, [C.c_void_p, C.c_int]),
     "acum_set_tensor_memory": (C.c_int, [C.c_void_p, C.c_int]),
+    "acum_set_ring": (C.c_int, [C.c_void_p, C.c_int]),
+    "acum_last_plan_ring": (C.c_int, [C.c_void_p, _IP]),
     "acum_measure_peak": (C.c_int, [C.c_int, C.c_int, _DP]),
     "acum_host_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t]),
     "acum_host_free": (C.c_int, [C.c_void_p]),
@@ -121,6 +123,8 @@ SIGNATURES = {
     "acum_batch_timing": (C.c_int, [C.c_void_p, _DP, C.POINTER(C.c_longlong)]),
     "acum_batch_set_tile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "acum_batch_get_tile": (C.c_int, [C.c_void_p, _IP, _IP, _IP]),
+    "acum_batch_set_tile2": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "acum_batch_get_obs_per_warp": (C.c_int, [C.c_void_p, _IP]),
     "acum_batch_count": (C.c_int, [C.c_void_p, _IP]),
     "acum_batch_case_timing": (C.c_int, [C.c_void_p, C.c_int, _DP]),
     "acum_batch_autotune": (C.c_int, [C.c_void_p, C.c_int, _DP]),
@@ -314,17 +318,26 @@ class Context:
     def write_outputs(self, path: str):
         self._ck(self.L.acum_write_outputs(self.h, os.fsencode(path)))
 
-    def set_tile(self, obs_per_block=0, elems_per_stage=0, items_per_sm=0, obs_per_warp=0, tensor_memory=0):
+    def set_tile(self, obs_per_block=0, elems_per_stage=0, items_per_sm=0, obs_per_warp=0, tensor_memory=0,
+                 whole_rows=0):
         self._ck(self.L.acum_set_tile(self.h, obs_per_block, elems_per_stage, items_per_sm))
         self._ck(self.L.acum_set_obs_per_warp(self.h, obs_per_warp))
         self._ck(self.L.acum_set_tensor_memory(self.h, tensor_memory))
+        self._ck(self.L.acum_set_ring(self.h, whole_rows))
 
     def last_plan(self) -> dict:
+        """The last tonal plan; for the mixed form also `ring_slots` (0: whole rows only)
+        and `ring_used` (the records fit the ring, so the ring kernel did the work)."""
         v = (C.c_int * 8)()
         self._ck(self.L.acum_last_plan(self.h, v))
         keys = ("obs_per_block", "elems_per_stage", "stages", "elems_per_item", "element_chunks", "work_items",
                 "obs_per_warp", "tensor_memory")
-        return dict(zip(keys, (int(x) for x in v)))
+        out = dict(zip(keys, (int(x) for x in v)))
+        r = (C.c_int * 5)()
+        self._ck(self.L.acum_last_plan_ring(self.h, r))
+        out.update(ring_slots=int(r[0]), rows_obs_per_block=int(r[1]), rows_elems_per_stage=int(r[2]),
+                   rows_stages=int(r[3]), ring_used=int(r[4]))
+        return out
 
     def timing(self, which: int):
         ms = C.c_double()
@@ -393,8 +406,13 @@ class Batch:
     def prepare(self):
         self._ck(self.L.acum_batch_prepare(self.h))
 
-    def set_tile(self, obs_per_block=0, elems_per_stage=0, items_per_sm=0):
-        self._ck(self.L.acum_batch_set_tile(self.h, obs_per_block, elems_per_stage, items_per_sm))
+    def set_tile(self, obs_per_block=0, elems_per_stage=0, items_per_sm=0, obs_per_warp=1):
+        self._ck(self.L.acum_batch_set_tile2(self.h, obs_per_block, elems_per_stage, items_per_sm, obs_per_warp))
+
+    def obs_per_warp(self) -> int:
+        v = C.c_int()
+        self._ck(self.L.acum_batch_get_obs_per_warp(self.h, C.byref(v)))
+        return v.value
 
     def tile(self):
         a, b, c = C.c_int(), C.c_int(), C.c_int()

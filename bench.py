@@ -417,7 +417,8 @@ def _batch_compare(native, device, make_deck, steps, inflight):
     tune_s = time.perf_counter() - t0
     tile = b.tile()
     res = {"cases": ncase, "evals": total, "deck_generation_s": gen_s, "autotune_s": tune_s,
-           "tile": {"obs_per_block": tile[0], "elems_per_stage": tile[1], "items_per_sm": tile[2]},
+           "tile": {"obs_per_block": tile[0], "elems_per_stage": tile[1], "items_per_sm": tile[2],
+                    "obs_per_warp": b.obs_per_warp()},
            "autotune_estimate_ms": est_ms}
     for name, mode in (("persistent_graph", 2), ("per_case", 1)):
         b.run(mode=mode)

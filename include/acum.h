@@ -202,15 +202,26 @@ int acum_device_error_word(acum_ctx* ctx, uint32_t* out, int reset);
 int acum_last_timing(const acum_ctx* ctx, int which, double* ms, long long* launches);
 
 /* Tile shape of the tonal kernels (0 = let the library choose): observers per block
- * (1..16), elements per pipeline stage (mixed form: 2, 4 or 8) and work items per SM. */
+ * (1..16; the mixed ring kernel with two observers per warp 1..32), elements per pipeline
+ * stage (mixed form: 2, 4 or 8; 2 or 4 with two observers per warp) and work items per
+ * SM. */
 int acum_set_tile(acum_ctx* ctx, int obs_per_block, int elems_per_stage, int items_per_sm);
-/* Observers evaluated per warp of the mixed tonal kernel on the records it loads once:
- * 1 or 2 (0 = let the library choose). */
+/* Observers evaluated per warp of the mixed tonal ring kernel on the records it loads
+ * once: 1 or 2 (0 = let the library choose; the whole-row kernel evaluates one). */
 int acum_set_obs_per_warp(acum_ctx* ctx, int obs_per_warp);
-/* Record stages of the mixed tonal kernel (one observer per warp) copied once into tensor
- * memory and read from there by every warp, instead of read by every warp from shared
- * memory: 1 = yes, 2 = no, 0 = let the library choose. */
+/* Record stages of the mixed tonal kernel (whole rows, one observer per warp) copied once
+ * into tensor memory and read from there by every warp, instead of read by every warp
+ * from shared memory: 1 = yes, 2 = no, 0 = let the library choose. */
 int acum_set_tensor_memory(acum_ctx* ctx, int use);
+/* Bins of the mixed tonal kernel: 0 = a sliding ring of bins per observer (the ring
+ * kernel), with the whole-row kernel launched behind it for records whose retarded times
+ * spread too far for the ring (the default); 1 = whole rows of the period only. */
+int acum_set_ring(acum_ctx* ctx, int mode);
+/* The ring side of the last tonal plan (out holds 5 ints): out[0] ring slots per
+ * observer (0: whole rows only), [1] observers per block, [2] elements per stage and [3]
+ * pipeline stages of the whole-row kernel behind the ring kernel, [4] 1 if the records
+ * fit the ring (the ring kernel did the work; synchronises the context's stream). */
+int acum_last_plan_ring(acum_ctx* ctx, int* out);
 /* The plan of the last tonal run (out holds 8 ints): out[0] observers per block,
  * [1] elements per stage, [2] pipeline stages, [3] elements per work item, [4] element
  * chunks, [5] work items, [6] observers per warp, [7] 1 if the record stages were read
@@ -267,8 +278,9 @@ int acum_find_pressure_time_history_f64(const double* rObs, const double* tObs, 
  * loop that cannot afford cudaMalloc/cudaFree, which synchronise the whole device.  It
  * allocates nothing -- no cudaMalloc, no host heap -- and uses a fixed 128 MiB scratch
  * array in device memory that every GPU loading this library holds until exit.  Limit:
- * records (64 B per element-step, elements rounded up to 8 and steps to 32) plus 16 B per
- * observer-step must fit in 128 MiB, else ACUM_ERR_INVALID (acum_noalloc_last_error()
+ * records (64 B per element and record slot: elements rounded up to 8, ceil(nTime / 31)
+ * windows of 32 slots) plus 16 B per observer-step must fit in 128 MiB, else
+ * ACUM_ERR_INVALID (acum_noalloc_last_error()
  * gives the sizes); at most 256 surfaces.  Otherwise it accepts and refuses the inputs the
  * allocating call does (nTime >= 4; tObs[t] = t*dPsi, as main.cu:124 builds it, else
  * ACUM_ERR_UNSUPPORTED).  The first call on a device looks up the scratch address (with
@@ -335,17 +347,20 @@ int acum_find_bb_noise(int nSurf_BB, int nObs, int nTime, float dTau, const floa
 /* No reference counterpart: the reference solves one deck per process (main.cu).  A batch
  * holds many independent decks ("cases") resident on one device and runs all their tonal
  * solves (mixed precision) in one persistent launch: one block per SM takes work items
- * (case, observer tile, element range) from a device counter, largest first.  The tile
- * shape -- observers per block, elements per pipeline stage, work items per SM -- is set
- * by acum_batch_set_tile or chosen by acum_batch_autotune. */
+ * (case, observer tile, element range) from a device counter, largest first.  A case
+ * whose records fit the mixed bin ring runs the ring form, the others whole rows (the
+ * test of acum_set_ring, per case).  The tile shape -- observers per block, observers per
+ * warp, elements per pipeline stage, work items per SM -- is set by acum_batch_set_tile /
+ * acum_batch_set_tile2 or chosen by acum_batch_autotune (default 32 observers per block,
+ * two per warp, 4 elements per stage). */
 typedef struct acum_batch acum_batch;
 
 int acum_batch_create(acum_batch** out, int device);
 int acum_batch_destroy(acum_batch* b);
 const char* acum_batch_last_error(const acum_batch* b);
 /* Adds a case (same argument meaning as acum_set_deck with host rows) and preprocesses it
- * on the device at once; the rows are not kept, only the mixed-form records (2560 bytes
- * per element and 32 steps).  Fails with ACUM_ERR_NOMEM, adding nothing, when the
+ * on the device at once; the rows are not kept, only the mixed-form records (2048 bytes
+ * per element and window of 31 steps).  Fails with ACUM_ERR_NOMEM, adding nothing, when the
  * device has less free memory than the case needs plus 1 GiB.  *case_id = its index. */
 int acum_batch_add(acum_batch* b, const acum_inputs* in, int nobs, const float* obs_file, int nsurf,
                    const int* nelem, const float* raw, int* case_id);
@@ -364,11 +379,17 @@ int acum_batch_result(acum_batch* b, int case_id, double* pA);
 int acum_batch_timing(const acum_batch* b, double* ms, long long* launches);
 /* Device time of one case's tonal kernel in the last mode-1 run. */
 int acum_batch_case_timing(const acum_batch* b, int case_id, double* ms);
-/* obs_per_block 1..16, elems_per_stage 2, 4 or 8, items_per_sm >= 1 (0 keeps a value). */
+/* One observer per warp: obs_per_block 1..16, elems_per_stage 2, 4 or 8, items_per_sm >= 1
+ * (0 keeps a value). */
 int acum_batch_set_tile(acum_batch* b, int obs_per_block, int elems_per_stage, int items_per_sm);
+/* As acum_batch_set_tile with obs_per_warp 1 or 2; two: obs_per_block 2..32 (even; 0 =
+ * 32), elems_per_stage 2 or 4 (0 = 4). */
+int acum_batch_set_tile2(acum_batch* b, int obs_per_block, int elems_per_stage, int items_per_sm, int obs_per_warp);
 int acum_batch_get_tile(const acum_batch* b, int* obs_per_block, int* elems_per_stage, int* items_per_sm);
+int acum_batch_get_obs_per_warp(const acum_batch* b, int* obs_per_warp);
 /* Chooses the tile shape.  (1) For every observers-per-block in {8, 12, 16} x elements-per-
- * stage in {2, 4, 8} whose shared memory fits, one persistent launch over a probe of
+ * stage in {2, 4, 8} (one observer per warp) and {16, 24, 32} x {2, 4} (two per warp)
+ * whose shared memory fits, one persistent launch over a probe of
  * 128-element work items spread over all cases (about probe_per_sm items per SM; 0 = 8)
  * gives the kernel's throughput; the fastest shape is kept.  (2) Two probes of that shape
  * with 64- and 256-element items give its cost per work item and per evaluation, from

@@ -48,15 +48,16 @@ def test_smallest_deck(ctx):
     d = synth.config_deck(0, replicate=80, scale=dict(n_span=1, n_chord_side=1, ntime=8, nobs=1))
     assert d.nObs == 1 and d.E == 4
     plan = _against_oracle(ctx, d)
-    assert plan["obs_per_block"] == 1
+    assert plan["obs_per_block"] == plan["obs_per_warp"]  # one warp
 
 
 def test_longest_period(ctx):
-    """4096 steps per period: the mixed kernel's blocks hold only as many observer rows as
-    fit in shared memory (fewer than 16)."""
+    """4096 steps per period: the retarded times spread over more bins than the mixed
+    ring holds, and the whole-row kernel's blocks hold only as many observer rows as fit
+    in shared memory (fewer than 16)."""
     d = synth.config_deck(0, replicate=81, scale=dict(n_span=2, n_chord_side=2, ntime=4096, nobs=9))
     plan = _against_oracle(ctx, d, rms_norm=True)
-    assert plan["obs_per_block"] < 9
+    assert plan["ring_used"] == 0 and plan["rows_obs_per_block"] < 9
 
 
 def test_refused_decks(ctx):

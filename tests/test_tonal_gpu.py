@@ -170,30 +170,61 @@ def test_timing_and_launch_count(ctx):
     assert ms > 0 and launches >= 3
 
 
-@pytest.mark.parametrize("W,SE,opw,tm", [(16, 8, 1, 2), (16, 4, 1, 2), (16, 2, 1, 2), (7, 8, 1, 2),
-                                         (16, 2, 2, 2), (16, 4, 2, 2), (16, 8, 2, 2), (6, 4, 2, 2),
-                                         (16, 8, 1, 1), (16, 4, 1, 1), (16, 2, 1, 1), (5, 8, 1, 1)])
-def test_mixed_tile_shapes_against_oracle(ctx, W, SE, opw, tm):
-    """Every tile shape of the mixed kernel (observers per block, elements per stage,
-    observers per warp, record stages in shared or tensor memory) on a deck whose
-    observers, steps and elements are not multiples of the tile; the plan reports the
-    shape that ran."""
+@pytest.mark.parametrize("W,SE,opw,tm,rows", [
+    # the ring kernel
+    (32, 4, 2, 2, 0), (32, 2, 2, 2, 0), (16, 4, 2, 2, 0), (6, 4, 2, 2, 0),
+    (16, 8, 1, 2, 0), (16, 4, 1, 2, 0), (16, 2, 1, 2, 0), (7, 8, 1, 2, 0),
+    # whole rows only
+    (16, 8, 1, 2, 1), (16, 4, 1, 2, 1), (16, 2, 1, 2, 1), (7, 8, 1, 2, 1),
+    # whole rows with the record stages in tensor memory
+    (16, 8, 1, 1, 0), (16, 4, 1, 1, 0), (16, 2, 1, 1, 0), (5, 8, 1, 1, 0)])
+def test_mixed_tile_shapes_against_oracle(ctx, W, SE, opw, tm, rows):
+    """Every tile shape of the mixed kernels (observers per block, elements per stage,
+    observers per warp; the bin ring or whole rows; record stages in shared or tensor
+    memory) on a deck whose observers, steps and elements are not multiples of the tile;
+    the plan reports the shape that ran."""
     from acum3_periodic_gb300 import native
     d = synth.config_deck(0, replicate=34, scale=dict(n_span=7, n_chord_side=5, ntime=75, nobs=29))
     oT, oL, oA, bad = O.tonal(d)
     assert bad == 0
     ctx.set_deck(d, bb=False)
     try:
-        ctx.set_tile(W, SE, 0, opw, tm)
+        ctx.set_tile(W, SE, 0, opw, tm, rows)
         _, _, mA = ctx.tonal(native.MIXED)
         plan = ctx.last_plan()
     finally:
         ctx.set_tile()
     assert (plan["obs_per_block"], plan["elems_per_stage"], plan["obs_per_warp"]) == (W, SE, opw)
     assert plan["tensor_memory"] == (1 if tm == 1 else 0)
+    ring = tm != 1 and not rows
+    assert plan["ring_slots"] == (512 if ring else 0)
+    assert plan["ring_used"] == (1 if ring else 0)
     assert per_bin_rms(mA, oA).max() < MIXED_RMS_TOL
     assert np.abs(oaspl_db(mA) - oaspl_db(oA)).max() < OASPL_TOL_DB
     assert ctx.error_word(reset=True) == 0
+
+
+def test_records_reaching_past_the_ring(ctx):
+    """A hovering rotor whose retarded times spread over more bins than the ring holds
+    (tip Mach 0.8 over 2048 steps per revolution: the source's distance from the origin
+    is worth up to 0.8 x 2048 / 2 pi = 261 bins either side): the whole-row kernel
+    launched behind the ring kernel does the work, and matches the oracle; the same rotor
+    at 180 steps (23 bins) runs on the ring."""
+    from acum3_periodic_gb300 import native
+    for T, used in ((2048, 0), (180, 1)):
+        d = synth.config_deck(0, replicate=37, scale=dict(n_span=4, n_chord_side=3, ntime=T, nobs=6, tip_mach=0.8,
+                                                           minf=0.0))
+        oT, oL, oA, bad = O.tonal(d)
+        assert bad == 0
+        ctx.set_deck(d, bb=False)
+        pT, pL, mA = ctx.tonal(native.MIXED)
+        plan = ctx.last_plan()
+        assert plan["ring_slots"] == 512 and plan["ring_used"] == used, T
+        assert plan["rows_obs_per_block"] > 0
+        assert per_bin_rms(mA, oA).max() < MIXED_RMS_TOL, T
+        rms = np.sqrt(np.mean(oA ** 2, axis=0, keepdims=True))
+        assert (np.abs(pT - oT) / rms).max() < MIXED_RMS_TOL, T
+        assert ctx.error_word(reset=True) == 0
 
 
 def test_decks_in_sequence_on_one_context(ctx):
