@@ -173,6 +173,7 @@ int acum_ctx::upload_deck_common(const acum_inputs& inp, int nob, const float* o
         o64[i] = (double)obs_file[i] * in.OBSscale;
         o32[i] = (float)o64[i];
     }
+    obs_rmin = obs_min_distance(o32.data(), nob);
     DeviceGuard g(device);
     CK(this, d_obs64.ensure(o64.size()));
     CK(this, d_obs32.ensure(o32.size()));
@@ -381,9 +382,10 @@ extern "C" int acum_last_plan_ring(acum_ctx* ctx, int* out)
         CK(ctx, cudaMemcpy(&bits, ctx->d_rmax.p, sizeof(bits), cudaMemcpyDeviceToHost));
         float r;
         memcpy(&r, &bits, sizeof(r));
-        const double reach = ring_reach_bins(r, ctx->der.vinf[0], ctx->der.vinf[1], ctx->der.vinf[2], ctx->in.a0,
-                                             ctx->der.oM / ctx->der.dPsi);
-        out[4] = ring_fits_bins(reach, ctx->last_tile.ring) ? 1 : 0;
+        out[4] = ring_ok(r, ctx->der.vinf[0], ctx->der.vinf[1], ctx->der.vinf[2], ctx->in.a0,
+                         ctx->der.oM / ctx->der.dPsi, ctx->obs_rmin, ctx->last_tile.ring)
+                     ? 1
+                     : 0;
     }
     return ACUM_OK;
 }
@@ -530,6 +532,7 @@ int acum_ctx::run_tonal(int precision, double* d_pT, double* d_pL, double* d_pA)
     r.g.dTau = der.dTau;
     r.g.lpi = T * der.dPsi;
     for (int c = 0; c < 3; ++c) r.g.vinf[c] = der.vinf[c];
+    r.g.obs_rmin = obs_rmin;
     r.precision = precision;
     r.rmax = f64 ? nullptr : d_rmax.p;
     CK(this, plan_tonal(r, tile_W, tile_SE, tile_ips, num_sms, smem_optin, tile_opw, tile_tm, tile_rows));
@@ -894,6 +897,7 @@ int find_pth(const S* rObs, const S* tObs, S* pT, S* pL, S* pA, const S* Xham, c
     }
     CK(nullptr, cudaMemcpyAsync(c->d_obs64.p, o64.data(), o64.size() * 8, cudaMemcpyHostToDevice, st));
     CK(nullptr, cudaMemcpyAsync(c->d_obs32.p, o32.data(), o32.size() * 4, cudaMemcpyHostToDevice, st));
+    const double obs_rmin = obs_min_distance(o32.data(), nObs);
     TonalRun r;
     memset(&r, 0, sizeof(r));
     r.g.E = (int)E;
@@ -908,6 +912,7 @@ int find_pth(const S* rObs, const S* tObs, S* pT, S* pL, S* pA, const S* Xham, c
     r.g.dTau = dTau;
     r.g.lpi = nTime * dPsi;
     for (int q = 0; q < 3; ++q) r.g.vinf[q] = (double)hv[q];
+    r.g.obs_rmin = obs_rmin;
     r.precision = f64 ? ACUM_PLAIN_FP64 : ACUM_MIXED;
     r.rmax = f64 ? nullptr : c->d_rmax.p;
     CK(nullptr, plan_tonal(r, 0, 0, 0, c->num_sms, c->smem_optin));

@@ -87,8 +87,36 @@ __host__ __device__ __forceinline__ double ring_reach_bins(float r, double vx, d
     if (!(r <= 1.0e30f) || !(vm < 0.999 * a0)) return 1.0e30;
     return (double)r * kb / (a0 - vm) * 1.0001 + 2.0;
 }
-// whether a ring of R slots holds every bin a window of 31 intervals can reach
-__host__ __device__ __forceinline__ bool ring_fits_bins(double reach, int R) { return 2.0 * reach + 40.0 <= (double)R; }
+// Whether the ring kernel serves a deck: a ring of R slots holds every bin a window of 31
+// intervals can reach, and the observer-time offset of every sample is bounded by the
+// reach, so that the ring kernel needs no per-sample range check.  The second holds when
+// the term b = alpha t0 + D0.v + (D0 - x).v of the retarded-time difference quadratic
+// stays positive for every source point x and observer D0 (then its denominator b +
+// sqrt(q) >= b > 0 and |dt| keeps its bound |x| / (a0 - |vInf|)): b >= sqrt(alpha)
+// |D0| - |x| |vInf|, so it suffices that sqrt(alpha) min|D0| > 1.01 |x|max |vInf|; with no
+// flight b = alpha t0 >= 0 and a zero b comes with a non-negative discriminant term.
+// obs_rmin = the smallest observer distance from the origin (< 0: unknown).
+__host__ __device__ __forceinline__ bool ring_ok(float r, double vx, double vy, double vz, double a0, double kb,
+                                                 double obs_rmin, int R)
+{
+    const double reach = ring_reach_bins(r, vx, vy, vz, a0, kb);
+    if (!(2.0 * reach + 40.0 <= (double)R)) return false;
+    const double vm = sqrt(vx * vx + vy * vy + vz * vz);
+    if (vm == 0.0) return true;
+    return obs_rmin >= 0.0 && sqrt(a0 * a0 - vm * vm) * obs_rmin > 1.01 * (double)r * vm;
+}
+
+// the smallest distance from the origin of n observers given as FP32 (x, y, z) triples
+inline double obs_min_distance(const float* xyz, long long n)
+{
+    double m = n > 0 ? 1.0e300 : -1.0;
+    for (long long i = 0; i < n; ++i) {
+        const double x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+        const double d = sqrt(x * x + y * y + z * z);
+        if (!(d >= m)) m = d;  // a NaN distance makes the minimum NaN (unknown)
+    }
+    return m;
+}
 
 #ifdef __CUDACC__
 // The largest source distance from the origin |x| among the records a kernel writes, as
@@ -116,6 +144,7 @@ struct TonalGeom {
     int E, Epad, T, nW, O;
     double a0, rho, oM, dPsi, dTau, lpi;  // dPsi in radians
     double vinf[3];
+    double obs_rmin;  // smallest observer distance from the origin (of the FP32 positions; < 0 unknown)
 };
 
 struct TonalTile {
@@ -232,6 +261,7 @@ struct KParams {
     int ring;               // mixed: ring slots per observer (ring kernel), 0 = whole rows
     int dual;               // mixed: a ring kernel and a whole-row kernel are both launched
     const unsigned* rmax;   // mixed: the records' largest |x| (note_radius bits)
+    double obs_rmin;        // mixed: the smallest observer distance from the origin (ring_ok)
     const float* obs32;
     const double* obs64;
     // mixed constants, as pairs (both halves equal: the operands of the packed FP32

@@ -31,7 +31,7 @@ struct acum_batch {
 
     // tile shape and plan: W observers per block, opw per warp, SE elements per stage;
     // rowlen = slots per bin row (the longest whole-row case's nTime, or the ring's)
-    int W = 32, SE = 4, opw = 2, ips = 8;
+    int W = 32, SE = 8, opw = 2, ips = 8;
     bool planned = false;
     int Tmax = 0, rowlen = 0;
     std::vector<char> ring;  // per case: its records fit the bin ring
@@ -101,6 +101,7 @@ TonalRun case_run(const acum_batch* b, const acum_ctx* c, double* acc)
     r.g.dTau = c->der.dTau;
     r.g.lpi = c->T * c->der.dPsi;
     for (int k = 0; k < 3; ++k) r.g.vinf[k] = c->der.vinf[k];
+    r.g.obs_rmin = c->obs_rmin;
     r.precision = ACUM_MIXED;
     r.t.W = b->W;
     r.t.SE = b->SE;
@@ -159,7 +160,6 @@ void build_items(const acum_batch* b, int W, int SE, int ips, std::vector<BatchI
 
 bool shape_fits(const acum_batch* b, int W, int SE, int opw)
 {
-    if (opw == 2 && SE == 8) return false;
     return batch_smem(W, SE, b->rowlen) + batch_static_smem(SE, opw) <= b->smem_optin;
 }
 
@@ -176,9 +176,10 @@ int ring_cases(acum_batch* b)
             BK(b, cudaMemcpy(&bits, c->d_rmax.p, sizeof(bits), cudaMemcpyDeviceToHost));
             float r;
             memcpy(&r, &bits, sizeof(r));
-            const double reach = ring_reach_bins(r, c->der.vinf[0], c->der.vinf[1], c->der.vinf[2], c->in.a0,
-                                                 c->der.oM / c->der.dPsi);
-            b->ring[i] = ring_fits_bins(reach, kRingSlots) ? 1 : 0;
+            b->ring[i] = ring_ok(r, c->der.vinf[0], c->der.vinf[1], c->der.vinf[2], c->in.a0,
+                                 c->der.oM / c->der.dPsi, c->obs_rmin, kRingSlots)
+                             ? 1
+                             : 0;
         }
     }
     b->Tmax = 0;
@@ -493,11 +494,11 @@ extern "C" int acum_batch_set_tile2(acum_batch* b, int obs_per_block, int elems_
         return bfail(b, ACUM_ERR_INVALID, "acum_batch_set_tile2: obs_per_warp 1 or 2");
     if (obs_per_warp == 1) return acum_batch_set_tile(b, obs_per_block, elems_per_stage, items_per_sm);
     if (obs_per_block < 0 || obs_per_block > 32 || obs_per_block % 2 != 0 || items_per_sm < 0 ||
-        (elems_per_stage != 0 && elems_per_stage != 2 && elems_per_stage != 4))
+        (elems_per_stage != 0 && elems_per_stage != 2 && elems_per_stage != 4 && elems_per_stage != 8))
         return bfail(b, ACUM_ERR_INVALID,
-                     "acum_batch_set_tile2: two observers per warp: obs_per_block 2..32 (even), elems_per_stage 2 or 4");
+                     "acum_batch_set_tile2: two observers per warp: obs_per_block 2..32 (even), elems_per_stage 2, 4 or 8");
     b->W = obs_per_block ? obs_per_block : 32;
-    b->SE = elems_per_stage ? elems_per_stage : 4;
+    b->SE = elems_per_stage ? elems_per_stage : 8;
     if (items_per_sm) b->ips = items_per_sm;
     b->opw = 2;
     b->planned = false;
@@ -608,7 +609,7 @@ extern "C" int acum_batch_autotune(acum_batch* b, int probe_per_sm, double* best
     //    ring fill weigh on the deeper stages and the probe favoured 4 elements per
     //    stage where 8 are faster)
     //    (one observer per warp: 8, 12, 16 observers per block x 2, 4, 8 elements per stage;
-    //    two: 16, 24, 32 x 2, 4)
+    //    two: 16, 24, 32 x 2, 4, 8)
     struct Shape {
         int W, SE, opw;
     };
@@ -616,7 +617,7 @@ extern "C" int acum_batch_autotune(acum_batch* b, int probe_per_sm, double* best
     for (int W : {8, 12, 16})
         for (int SE : {2, 4, 8}) shapes.push_back({W, SE, 1});
     for (int W : {16, 24, 32})
-        for (int SE : {2, 4}) shapes.push_back({W, SE, 2});
+        for (int SE : {2, 4, 8}) shapes.push_back({W, SE, 2});
     double best_rate = 0;
     int bw = b->W, bse = b->SE, bopw = b->opw;
     DBuf<BatchItem> d_probe;

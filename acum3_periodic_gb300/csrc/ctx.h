@@ -114,6 +114,7 @@ struct acum_ctx {
     acum::DBuf<float> d_rec32;
     acum::DBuf<acum::DeviceErr> d_err;
     acum::DBuf<unsigned> d_rmax;  // the FP32 records' largest |x| (note_radius bits)
+    double obs_rmin = -1.0;       // the observers' smallest distance from the origin (FP32 positions)
     // permeable decks: the preprocessed AoS arrays of variables.cu:54 in FP64 (X, N, V, U,
     // PR with nPRham = 4), the reference's layout (element after element, [T][width])
     acum::DBuf<double> d_per[5];

@@ -20,8 +20,8 @@
 //    within the same tolerance) and refuses the others with the same status;
 //  * the first call on a device looks up the array's device address (cudaGetSymbolAddress)
 //    with that device current; make that first call before any stream capture;
-//  * every call synchronises `stream` before it returns: it reads E, vInf and tObs back
-//    to the host, and after the kernels the device error word;
+//  * every call synchronises `stream` before it returns: it reads E, vInf, tObs and the
+//    observers back to the host, and after the kernels the device error word;
 //  * every call reuses the same array and leaves its contents behind; the call clears
 //    what must start at zero itself, and two calls whose GPU work overlaps (different
 //    streams or threads without ordering) race on the array -- serialise them;
@@ -156,6 +156,19 @@ extern "C" int acum_find_pressure_time_history_noalloc(const float* rObs, const 
                 return bad(ACUM_ERR_UNSUPPORTED, "findPressureTimeHistory_noalloc: tObs must be t*dPsi");
         }
     }
+    // the observers' smallest distance from the origin (the mixed ring kernel's test),
+    // read in pieces
+    double obs_rmin = 1.0e300;
+    for (int o0 = 0; o0 < nObs; o0 += kTobsPiece / 3) {
+        float ho[kTobsPiece];
+        const int n = nObs - o0 < kTobsPiece / 3 ? nObs - o0 : kTobsPiece / 3;
+        if (cudaMemcpyAsync(ho, rObs + 3 * (size_t)o0, 3 * (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, st) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            return bad(ACUM_ERR_CUDA, "findPressureTimeHistory_noalloc: reading rObs failed");
+        const double m = obs_min_distance(ho, n);
+        if (!(m >= obs_rmin)) obs_rmin = m;
+    }
     long long Et = 0;
     for (int i = 0; i < nSurf; ++i) {
         if (hE[i] < 0) return bad(ACUM_ERR_INVALID, "findPressureTimeHistory_noalloc: negative element count");
@@ -213,6 +226,7 @@ extern "C" int acum_find_pressure_time_history_noalloc(const float* rObs, const 
     r.g.dTau = dTau;
     r.g.lpi = nTime * (double)dPsi;
     for (int q = 0; q < 3; ++q) r.g.vinf[q] = hv[q];
+    r.g.obs_rmin = obs_rmin;
     r.precision = ACUM_MIXED;
     if (plan_tonal(r, 0, 0, 0, sms, (size_t)optin) != cudaSuccess)
         return bad(ACUM_ERR_UNSUPPORTED, "findPressureTimeHistory_noalloc: no tile shape fits this nTime");

@@ -727,7 +727,10 @@ __device__ __forceinline__ MixedGeom mixed_geom(const G2& g0, float ox, float oy
     return m;
 }
 
-// g0..g3: the FP32 record groups (x, ATD | M, Ld'x | Md, Ld'y | L', Ld'z)
+// g0..g3: the FP32 record groups (x, ATD | M, Ld'x | Md, Ld'y | L', Ld'z).  RANGE: a
+// fraction whose x lies outside the floor's range is made NaN (the ring kernel, whose
+// decks bound x by the reach, ring_ok, leaves that test out)
+template <bool RANGE>
 __device__ __forceinline__ void mixed_source(const MixedGeom& m, const G2& g0, const G2& g1, const G2& g2,
                                              const G2& g3, const Anchor& an, const KParams& p, int tau, SmpF& oa,
                                              SmpF& ob)
@@ -755,8 +758,8 @@ __device__ __forceinline__ void mixed_source(const MixedGeom& m, const G2& g0, c
     const int kb = tau + an.ki - kRoundBits;
     oa.k = kb + __float_as_int(t.x);
     ob.k = kb + __float_as_int(t.y);
-    oa.f = fabsf(x.x) < 4.0e6f ? fr.x : __int_as_float(0x7fc00000);
-    ob.f = fabsf(x.y) < 4.0e6f ? fr.y : __int_as_float(0x7fc00000);
+    oa.f = !RANGE || fabsf(x.x) < 4.0e6f ? fr.x : __int_as_float(0x7fc00000);
+    ob.f = !RANGE || fabsf(x.y) < 4.0e6f ? fr.y : __int_as_float(0x7fc00000);
     oa.pt = pt.x;
     ob.pt = pt.y;
     oa.pl = pl.x;
@@ -764,11 +767,12 @@ __device__ __forceinline__ void mixed_source(const MixedGeom& m, const G2& g0, c
 }
 
 // g[q] = group q of the pair's FP32 records
+template <bool RANGE>
 __device__ __forceinline__ void sample_mixed2(const G2* g, float ox, float oy, float oz, const Anchor& an,
                                               const KParams& p, int tau, SmpF& oa, SmpF& ob)
 {
     const MixedGeom m = mixed_geom(g[0], ox, oy, oz, an, p);
-    mixed_source(m, g[0], g[1], g[2], g[3], an, p, tau, oa, ob);
+    mixed_source<RANGE>(m, g[0], g[1], g[2], g[3], an, p, tau, oa, ob);
 }
 
 // A group as tensor-memory columns 8q .. 8q + 7 of a pair hold it (half 0: f0 e, f0 e+1,
@@ -1069,8 +1073,8 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
                 if (jp + 1 < SE / 2) tmem_ld_x8(ta + tm_col<SE>(0, 1), ra);
 #pragma unroll
                 for (int q = 0; q < OPW; ++q)
-                    mixed_source(m[q], g0, g2_of(rc), g2_of(rc + 8), g2_of(rd), anc[q], p, tau, cur[q][2 * jp],
-                                 cur[q][2 * jp + 1]);
+                    mixed_source<!RING>(m[q], g0, g2_of(rc), g2_of(rc + 8), g2_of(rd), anc[q], p, tau,
+                                        cur[q][2 * jp], cur[q][2 * jp + 1]);
                 if (jp + 1 < SE / 2) tmem_wait_ld_tie(ra, rz);
             }
         } else {
@@ -1082,7 +1086,8 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
                 for (int q = 0; q < kGroups32; ++q) gg[q] = load_g2(tl + q * 2 * kWin * 4);
 #pragma unroll
                 for (int q = 0; q < OPW; ++q)
-                    sample_mixed2(gg, ox[q], oy[q], oz[q], anc[q], p, tau, cur[q][2 * jp], cur[q][2 * jp + 1]);
+                    sample_mixed2<!RING>(gg, ox[q], oy[q], oz[q], anc[q], p, tau, cur[q][2 * jp],
+                                         cur[q][2 * jp + 1]);
             }
         }
         // the left neighbour: lane l - 1 of the same window (lane 0 receives lane 31's
@@ -1201,7 +1206,8 @@ __device__ __forceinline__ void mixed_drain(unsigned char* smem, size_t stage_of
 template <int SE, int OPW, bool TM, bool RING>
 __global__ void __launch_bounds__(512, 1) tonal_mixed_kernel(const KParams p)
 {
-    if (p.dual && ring_fits_bins(ring_reach(p), p.ring) != RING) return;
+    if (p.dual && ring_ok(__uint_as_float(*p.rmax), p.vx, p.vy, p.vz, p.a0, p.oM / p.dPsi, p.obs_rmin, p.ring) != RING)
+        return;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ MixedShared<SE, OPW> sh;
     __shared__ int s_item;
@@ -1296,7 +1302,7 @@ __global__ void __launch_bounds__(512, 1)
 }
 
 constexpr int kMixedSE = 8;   // elements per stage of the whole-row mixed kernel (one observer per warp)
-constexpr int kRingSE = 4;    // elements per stage of the ring kernel
+constexpr int kRingSE = 8;    // elements per stage of the ring kernel
 constexpr int kRingOPW = 2;   // observers per warp of the ring kernel
 constexpr bool kMixedTmem = false;  // record stages read from tensor memory by default
 static_assert(kMaxStages >= 4, "stage bookkeeping");
@@ -1323,16 +1329,14 @@ static size_t mixed_static_smem(int SE, int opw, bool tm)
     static size_t v[2][3][9] = {};
     if (SE != 2 && SE != 4 && SE != 8) SE = 8;
     if (opw != 2) opw = 1;
-    if (opw == 2) {
-        tm = false;
-        if (SE == 8) SE = 4;
-    }
+    if (opw == 2) tm = false;
     size_t& x = v[tm ? 1 : 0][opw][SE];
     if (!x) {
         const size_t est = (size_t)1024;
         if (opw == 2)
-            x = SE == 2 ? static_smem_of(tonal_mixed_kernel<2, 2, false, true>, est)
-                        : static_smem_of(tonal_mixed_kernel<4, 2, false, true>, est);
+            x = SE == 2   ? static_smem_of(tonal_mixed_kernel<2, 2, false, true>, est)
+                : SE == 4 ? static_smem_of(tonal_mixed_kernel<4, 2, false, true>, est)
+                          : static_smem_of(tonal_mixed_kernel<8, 2, false, true>, est);
         else if (tm)
             x = SE == 2   ? static_smem_of(tonal_mixed_kernel<2, 1, true, false>, est)
                 : SE == 4 ? static_smem_of(tonal_mixed_kernel<4, 1, true, false>, est)
@@ -1350,11 +1354,11 @@ size_t batch_static_smem(int SE, int opw)
     static size_t v[3][9] = {};
     if (SE != 2 && SE != 4 && SE != 8) SE = 8;
     if (opw != 2) opw = 1;
-    if (opw == 2 && SE == 8) SE = 4;
     if (!v[opw][SE]) {
         const size_t est = 1024;
-        v[opw][SE] = opw == 2 ? (SE == 2 ? static_smem_of(tonal_batch_kernel<2, 2>, est)
-                                         : static_smem_of(tonal_batch_kernel<4, 2>, est))
+        v[opw][SE] = opw == 2 ? (SE == 2   ? static_smem_of(tonal_batch_kernel<2, 2>, est)
+                                 : SE == 4 ? static_smem_of(tonal_batch_kernel<4, 2>, est)
+                                           : static_smem_of(tonal_batch_kernel<8, 2>, est))
                               : (SE == 2   ? static_smem_of(tonal_batch_kernel<2, 1>, est)
                                  : SE == 4 ? static_smem_of(tonal_batch_kernel<4, 1>, est)
                                            : static_smem_of(tonal_batch_kernel<8, 1>, est));
@@ -1378,7 +1382,6 @@ static cudaError_t plan_mixed_tile(const TonalRun& r, TonalTile& t, int W_req, i
 {
     const int T = r.g.T, rowlen = ring > 0 ? ring : T;
     int SE = (SE_req == 2 || SE_req == 4 || SE_req == 8) ? SE_req : (opw == 2 ? kRingSE : kMixedSE);
-    if (opw == 2 && SE == 8) SE = 4;  // the two-observer form spills at 8
     const int NSmin = SE == 8 ? 2 : 4;
     // at most 16 warps (the register limit of 512 threads of 128 registers)
     int W = W_req > 0 ? W_req : 16 * opw;
@@ -1565,6 +1568,7 @@ void fill_kparams(const TonalRun& r, const TonalTile& tile, KParams& kp)
     kp.ring = r.t.ring;  // the ring kernel's slots, also in the whole-row kernel launched behind it
     kp.dual = r.t.ring > 0 ? 1 : 0;
     kp.rmax = r.rmax;
+    kp.obs_rmin = g.obs_rmin;
     kp.O = g.O;
     kp.obs32 = r.obs32;
     kp.obs64 = r.obs64;
@@ -1607,7 +1611,8 @@ static cudaError_t launch_mixed_tile(const KParams& kp, const TonalTile& t, cuda
     if (t.ring > 0) {
         if (t.opw == 2) {
             if (t.SE == 2) return launch_mixed_t<2, 2, false, true>(kp, t.grid, threads, t.smem, s);
-            return launch_mixed_t<4, 2, false, true>(kp, t.grid, threads, t.smem, s);
+            if (t.SE == 4) return launch_mixed_t<4, 2, false, true>(kp, t.grid, threads, t.smem, s);
+            return launch_mixed_t<8, 2, false, true>(kp, t.grid, threads, t.smem, s);
         }
         if (t.SE == 2) return launch_mixed_t<2, 1, false, true>(kp, t.grid, threads, t.smem, s);
         if (t.SE == 4) return launch_mixed_t<4, 1, false, true>(kp, t.grid, threads, t.smem, s);
@@ -1680,7 +1685,8 @@ static cudaError_t launch_batch_t(const KParams* d_cases, const BatchItem* d_ite
 int batch_blocks_per_sm(int W, int SE, int opw, int rowlen)
 {
     const size_t smem = batch_smem(W, SE, rowlen);
-    if (opw == 2) return SE == 2 ? batch_per_sm_t<2, 2>(W, smem) : batch_per_sm_t<4, 2>(W, smem);
+    if (opw == 2)
+        return SE == 2 ? batch_per_sm_t<2, 2>(W, smem) : SE == 8 ? batch_per_sm_t<8, 2>(W, smem) : batch_per_sm_t<4, 2>(W, smem);
     return SE == 2 ? batch_per_sm_t<2, 1>(W, smem) : SE == 8 ? batch_per_sm_t<8, 1>(W, smem) : batch_per_sm_t<4, 1>(W, smem);
 }
 
@@ -1693,6 +1699,7 @@ cudaError_t launch_tonal_batch(const KParams* d_cases, const BatchItem* d_items,
     if (opw == 2) {
         if (SE == 2) return launch_batch_t<2, 2>(d_cases, d_items, nitems, d_counter, W, rowlen, grid, s);
         if (SE == 4) return launch_batch_t<4, 2>(d_cases, d_items, nitems, d_counter, W, rowlen, grid, s);
+        if (SE == 8) return launch_batch_t<8, 2>(d_cases, d_items, nitems, d_counter, W, rowlen, grid, s);
         return cudaErrorInvalidValue;
     }
     if (SE == 2) return launch_batch_t<2, 1>(d_cases, d_items, nitems, d_counter, W, rowlen, grid, s);

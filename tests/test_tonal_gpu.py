@@ -172,7 +172,7 @@ def test_timing_and_launch_count(ctx):
 
 @pytest.mark.parametrize("W,SE,opw,tm,rows", [
     # the ring kernel
-    (32, 4, 2, 2, 0), (32, 2, 2, 2, 0), (16, 4, 2, 2, 0), (6, 4, 2, 2, 0),
+    (32, 8, 2, 2, 0), (32, 4, 2, 2, 0), (32, 2, 2, 2, 0), (16, 8, 2, 2, 0), (6, 4, 2, 2, 0),
     (16, 8, 1, 2, 0), (16, 4, 1, 2, 0), (16, 2, 1, 2, 0), (7, 8, 1, 2, 0),
     # whole rows only
     (16, 8, 1, 2, 1), (16, 4, 1, 2, 1), (16, 2, 1, 2, 1), (7, 8, 1, 2, 1),
@@ -202,6 +202,30 @@ def test_mixed_tile_shapes_against_oracle(ctx, W, SE, opw, tm, rows):
     assert per_bin_rms(mA, oA).max() < MIXED_RMS_TOL
     assert np.abs(oaspl_db(mA) - oaspl_db(oA)).max() < OASPL_TOL_DB
     assert ctx.error_word(reset=True) == 0
+
+
+def test_observer_near_the_origin_in_forward_flight(ctx):
+    """An observer 9 cm from the hub of a rotor in forward flight (Mach 0.1): the ring
+    kernel's bound on the observer-time offset needs every observer farther from the
+    origin than 1.01 x |x|max x M / sqrt(1 - M^2) (10 cm here), so the whole-row kernel,
+    which checks every sample's range, does the work; it matches the oracle."""
+    from acum3_periodic_gb300 import native
+    d = synth.config_deck(0, replicate=38, scale=dict(n_span=4, n_chord_side=3, ntime=72, nobs=4, minf=0.1))
+    obs = d.obs_file.copy()
+    obs[1] = np.array([0.0, 0.0, 0.09], np.float32) / np.float32(d.OBSscale)
+    d.obs_file = obs
+    oT, oL, oA, bad = O.tonal(d)
+    assert bad == 0
+    ctx.set_deck(d, bb=False)
+    _, _, mA = ctx.tonal(native.MIXED)
+    plan = ctx.last_plan()
+    assert plan["ring_slots"] == 512 and plan["ring_used"] == 0
+    assert per_bin_rms(mA, oA).max() < MIXED_RMS_TOL
+    assert ctx.error_word(reset=True) == 0
+    far = d.subset_observers([0, 2, 3])
+    ctx.set_deck(far, bb=False)
+    ctx.tonal(native.MIXED)
+    assert ctx.last_plan()["ring_used"] == 1
 
 
 def test_records_reaching_past_the_ring(ctx):
