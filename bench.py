@@ -337,7 +337,7 @@ def profile_case(name, device=0):
     bpm: the broadband kernels on workload 1's broadband deck (4 x 50 sections, 720
     steps, 1024 observers); batch: four workload-4 cases shrunk to 30 x 2 x 12 panels per
     blade and 400 observers (376 MB of records) in one persistent launch (32 observers per
-    block, two per warp, 4 elements per stage, 8 items per SM); tonal-small: the mixed kernel on
+    block, two per warp, 8 elements per stage, 8 items per SM); tonal-small: the mixed kernel on
     workload 2 reduced to 25 x 2 x 10 panels per blade and 512 observers; tonal-full: the
     mixed kernel on workload 2 (for one-pass captures only)."""
     from acum3_periodic_gb300 import native, synth
@@ -356,7 +356,7 @@ def profile_case(name, device=0):
         b = native.Batch(device)
         for c in (3, 9, 14, 27):
             b.add(synth.batch_deck(c, shrink=dict(n_span=30, n_chord_side=12, nobs=400)))
-        b.set_tile(32, 4, 8, 2)
+        b.set_tile(32, 8, 8, 2)
         b.run(mode=0)
         out.update(batch_ms=b.timing()[0])
     else:
