@@ -303,6 +303,14 @@ struct __align__(16) SmpF {
     float pt, pl;
 };
 
+// A sample of the ring kernel: observer time in bins u = tau + ki + x (ki the observer's
+// anchor, |x| bounded by the reach, ring_ok), from which the deposit takes the floor and
+// the fraction itself
+struct SmpR {
+    float x;
+    float pt, pl;
+};
+
 struct SmpD {
     int nb;     // floor(t / dPsi), as floor(t * (1 / dPsi))
     double t;   // observer time [rad]
@@ -730,10 +738,10 @@ __device__ __forceinline__ MixedGeom mixed_geom(const G2& g0, float ox, float oy
 // g0..g3: the FP32 record groups (x, ATD | M, Ld'x | Md, Ld'y | L', Ld'z).  RANGE: a
 // fraction whose x lies outside the floor's range is made NaN (the ring kernel, whose
 // decks bound x by the reach, ring_ok, leaves that test out)
-template <bool RANGE>
+template <bool RANGE, typename S>
 __device__ __forceinline__ void mixed_source(const MixedGeom& m, const G2& g0, const G2& g1, const G2& g2,
-                                             const G2& g3, const Anchor& an, const KParams& p, int tau, SmpF& oa,
-                                             SmpF& ob)
+                                             const G2& g3, const Anchor& an, const KParams& p, int tau, S& oa,
+                                             S& ob)
 {
     const float2 rx = m.rx, ry = m.ry, rz = m.rz, ir = m.ir;
     // |M|^2 and L'.M from the fields they are made of
@@ -753,13 +761,18 @@ __device__ __forceinline__ void mixed_source(const MixedGeom& m, const G2& g0, c
     // outside the floor's range (or not finite) the fraction is NaN, which the deposit
     // rejects (and reports) whatever the integer part holds
     const float2 x = fma2(m.dt, p.kb2, f2(an.kf));
-    const float2 t = __fadd2_rd(x, f2(kRound));
-    const float2 fr = sub2(x, add2(t, f2(-kRound)));
-    const int kb = tau + an.ki - kRoundBits;
-    oa.k = kb + __float_as_int(t.x);
-    ob.k = kb + __float_as_int(t.y);
-    oa.f = !RANGE || fabsf(x.x) < 4.0e6f ? fr.x : __int_as_float(0x7fc00000);
-    ob.f = !RANGE || fabsf(x.y) < 4.0e6f ? fr.y : __int_as_float(0x7fc00000);
+    if constexpr (std::is_same<S, SmpR>::value) {
+        oa.x = x.x;
+        ob.x = x.y;
+    } else {
+        const float2 t = __fadd2_rd(x, f2(kRound));
+        const float2 fr = sub2(x, add2(t, f2(-kRound)));
+        const int kb = tau + an.ki - kRoundBits;
+        oa.k = kb + __float_as_int(t.x);
+        ob.k = kb + __float_as_int(t.y);
+        oa.f = !RANGE || fabsf(x.x) < 4.0e6f ? fr.x : __int_as_float(0x7fc00000);
+        ob.f = !RANGE || fabsf(x.y) < 4.0e6f ? fr.y : __int_as_float(0x7fc00000);
+    }
     oa.pt = pt.x;
     ob.pt = pt.y;
     oa.pl = pl.x;
@@ -767,9 +780,9 @@ __device__ __forceinline__ void mixed_source(const MixedGeom& m, const G2& g0, c
 }
 
 // g[q] = group q of the pair's FP32 records
-template <bool RANGE>
+template <bool RANGE, typename S>
 __device__ __forceinline__ void sample_mixed2(const G2* g, float ox, float oy, float oz, const Anchor& an,
-                                              const KParams& p, int tau, SmpF& oa, SmpF& ob)
+                                              const KParams& p, int tau, S& oa, S& ob)
 {
     const MixedGeom m = mixed_geom(g[0], ox, oy, oz, an, p);
     mixed_source<RANGE>(m, g[0], g[1], g[2], g[3], an, p, tau, oa, ob);
@@ -873,6 +886,62 @@ __device__ __forceinline__ void deposit_rest(float2* acc, int nb, int T, unsigne
         else if (++i >= T) i -= T;
         if (q >= 2) acc[i] = add2(acc[i], fma2(f2(w1 + (float)q * inv), dp, pa));
     }
+}
+
+// The ring form of deposit / deposit_rest on SmpR samples: a = lane l - 1's sample (step
+// tau - 1), b = this lane's (step tau); base = tau + ki - 1.5 * 2^23 (as an int), so that the
+// first bin of the interval, k(a) + 1 = tau + ki + floor(x_a), is base + the bits of
+// x_a + 1.5 * 2^23 rounded down.  The interval's length in bins is 1 + x_b - x_a (= the
+// whole-row form's cnt + f_b - f_a) and the weight 1 - f_a = floor(x_a) + 1 - x_a.
+__device__ __forceinline__ void deposit_ring(float2* acc, int R, unsigned m, const SmpR& a, const SmpR& b, int base,
+                                             bool active, unsigned& bad, bool& more)
+{
+    const float ta = __fadd_rd(a.x, kRound), tb = __fadd_rd(b.x, kRound);
+    const int cnt = __float_as_int(tb) - __float_as_int(ta) + 1;
+    const float du = (b.x - a.x) + 1.0f;
+    const bool ok = du > 0.0f;  // false for NaN
+    bad |= (active && !ok) ? 1u : 0u;
+    const bool one = active && ok && cnt >= 1, two = one && cnt >= 2;
+    more |= two && cnt > 2;
+    // not finite when !ok; both slots are then the scratch slot, which is never read out
+    const float inv = rcp_ftz(du);
+    const float2 pa = make_float2(a.pt, a.pl), dp = sub2(make_float2(b.pt, b.pl), pa);
+    const int idx = (int)((unsigned)(base + __float_as_int(ta)) & m);  // used only when `one`
+    const float w1 = ((ta - (kRound - 1.0f)) - a.x) * inv;
+    const int i1 = one ? idx : R + 1, i2 = two ? idx + 1 : R + 1;
+    const float2 v1 = acc[i1], v2 = acc[i2];
+    acc[i1] = add2(v1, fma2(f2(w1), dp, pa));
+    acc[i2] = add2(v2, fma2(f2(w1 + inv), dp, pa));
+}
+
+__device__ __forceinline__ void deposit_rest_ring(float2* acc, int R, unsigned m, const SmpR& a, const SmpR& b,
+                                                  int base, bool active, unsigned& bad)
+{
+    const float ta = __fadd_rd(a.x, kRound), tb = __fadd_rd(b.x, kRound);
+    const int cnt = __float_as_int(tb) - __float_as_int(ta) + 1;
+    const float du = (b.x - a.x) + 1.0f;
+    if (!(active && du > 0.0f && cnt > 2)) return;
+    if (cnt > R) {
+        bad = 1u;
+        return;
+    }
+    const float inv = rcp_ftz(du);
+    const float2 pa = make_float2(a.pt, a.pl), dp = sub2(make_float2(b.pt, b.pl), pa);
+    const float w1 = ((ta - (kRound - 1.0f)) - a.x) * inv;
+    int i = (int)((unsigned)(base + __float_as_int(ta)) & m);
+    for (int q = 1; q < cnt; ++q) {
+        i = (int)((unsigned)(i + 1) & m);
+        if (q >= 2) acc[i] = add2(acc[i], fma2(f2(w1 + (float)q * inv), dp, pa));
+    }
+}
+
+__device__ __forceinline__ SmpR shfl_idx(const SmpR& v, int src)
+{
+    SmpR o;
+    o.x = __shfl_sync(0xffffffffu, v.x, src);
+    o.pt = __shfl_sync(0xffffffffu, v.pt, src);
+    o.pl = __shfl_sync(0xffffffffu, v.pl, src);
+    return o;
 }
 
 __device__ __forceinline__ SmpF shfl_idx(const SmpF& v, int src)
@@ -1049,7 +1118,8 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
         // lane 0 holds only the left end of lane 1's interval; lanes past step T hold nothing
         const bool dep_lane = lane > 0 && tau <= T;
         const float* st = stages + (size_t)s * SE * kTile;
-        SmpF cur[OPW][SE];
+        using Smp = typename std::conditional<RING, SmpR, SmpF>::type;
+        Smp cur[OPW][SE];
         if (TM) {
             // records from tensor memory, in two loads per element pair: the positions
             // (columns 0-7) first; the other groups (columns 8-31) load while the retarded
@@ -1093,12 +1163,18 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
         // the left neighbour: lane l - 1 of the same window (lane 0 receives lane 31's
         // sample and deposits nothing)
         const int rot_src = (lane + 31) & 31;
+        int base[OPW];  // ring: tau + ki - 1.5 * 2^23 (deposit_ring)
+#pragma unroll
+        for (int q = 0; q < OPW; ++q) base[q] = tau + anc[q].ki - kRoundBits;
 #pragma unroll
         for (int q = 0; q < OPW; ++q) {
 #pragma unroll
             for (int j = 0; j < SE; ++j) {
-                const SmpF prev = shfl_idx(cur[q][j], rot_src);
-                deposit<RING>(acc[q], nb, T, mm, prev, cur[q][j], ok_obs[q] && dep_lane, bad, more);
+                const Smp prev = shfl_idx(cur[q][j], rot_src);
+                if constexpr (RING)
+                    deposit_ring(acc[q], nb, mm, prev, cur[q][j], base[q], ok_obs[q] && dep_lane, bad, more);
+                else
+                    deposit<false>(acc[q], nb, T, mm, prev, cur[q][j], ok_obs[q] && dep_lane, bad, more);
             }
         }
         // intervals of more than two bins (|Mr| >= 1): their other bins, for the whole warp
@@ -1107,8 +1183,11 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
             for (int q = 0; q < OPW; ++q) {
 #pragma unroll
                 for (int j = 0; j < SE; ++j) {
-                    const SmpF prev = shfl_idx(cur[q][j], rot_src);
-                    deposit_rest<RING>(acc[q], nb, T, mm, prev, cur[q][j], ok_obs[q] && dep_lane, bad);
+                    const Smp prev = shfl_idx(cur[q][j], rot_src);
+                    if constexpr (RING)
+                        deposit_rest_ring(acc[q], nb, mm, prev, cur[q][j], base[q], ok_obs[q] && dep_lane, bad);
+                    else
+                        deposit_rest<false>(acc[q], nb, T, mm, prev, cur[q][j], ok_obs[q] && dep_lane, bad);
                 }
             }
             more = false;
