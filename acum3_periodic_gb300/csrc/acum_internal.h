@@ -268,7 +268,7 @@ struct KParams {
     // instructions): -alpha, -vInf, a0, oM / dPsi.  16-byte aligned: the kernel reads
     // them two pairs at a time (measured 1.1 % slower at an 8-byte offset)
     alignas(16) float2 nalpha2;
-    float2 nvx2, nvy2, nvz2, a02, kb2;
+    float2 nvx2, nvy2, nvz2, a02, kb2, alpha2;
     unsigned tmod;  // ceil(2^32 / T): bin index modulo T by multiply-high
     int toff;       // a multiple of T >= 2^23, added to bin indices before the modulo
     // FP64 constants

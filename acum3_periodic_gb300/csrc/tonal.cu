@@ -648,21 +648,24 @@ __global__ void __launch_bounds__(512, 1) tonal_f64_kernel(const KParams p)
 // FP64; each sample then solves for t = t0 + dt from the difference of the two retarded-
 // time quadratics (core.cu:261-279 form: alpha t^2 + 2 beta t - |d|^2 = 0),
 //     alpha dt^2 + 2 b dt - num = 0,   b = s0 + (d - D0).v,
-//     num = |d|^2 - |D0|^2 - 2 t0 (d - D0).v,   d - D0 = -x,   |d|^2 - |D0|^2 = -x.(d + D0)
-// (D0 = observer, x = source, s0 = alpha t0 + D0.v, x.v carried in the records), whose
-// terms are all of the size of the source's offset from the origin rather than of the
-// observer distance.  The observer time in bins, tau + t0 oM/dPsi + dt oM/dPsi, keeps the
-// first part split exactly (FP64) into an integer and a fraction, so FP32 rounding
-// applies to dt only.  The floor of the remainder x comes from adding 1.5 * 2^23 rounded
-// towards minus infinity (exact for |x| < 2^22, checked), leaving a fraction in [0, 1];
-// bin indices are reduced modulo T by a multiply-high with m = ceil(2^32 / T).
+//     num = |d|^2 - |D0|^2 - 2 t0 (d - D0).v = |x|^2 - 2 x.P,   d - D0 = -x,   P = D0 - t0 v
+// (D0 = observer, x = source, s0 = alpha t0 + D0.v; P with t0 per observer), whose terms
+// are all of the size of the source's offset from the origin rather than of the observer
+// distance; the radiation vector is d - v t = P - x - v dt.  The observer time in bins,
+// tau + t0 oM/dPsi + dt oM/dPsi, keeps the first part split exactly (FP64) into an integer
+// and a fraction, so FP32 rounding applies to dt only.  The floor of the remainder x comes
+// from adding 1.5 * 2^23 rounded towards minus infinity (exact for |x| < 2^22: checked per
+// sample in the whole-row kernel, bounded by the reach in the ring kernel), leaving a
+// fraction in [0, 1]; whole-row bin indices are reduced modulo T by a multiply-high with
+// m = ceil(2^32 / T), ring indices by an AND.
 
 constexpr float kRound = 12582912.0f;  // 1.5 * 2^23
 constexpr int kRoundBits = 0x4B400000;
 
 struct Anchor {
-    float t0, t2, s0, kf;  // t0, 2 t0, alpha t0 + D0.v, frac(t0 * oM / dPsi)
-    int ki;                // round(t0 * oM / dPsi) modulo T, plus p.toff
+    float t0, s0, kf;  // t0, alpha t0 + D0.v, frac(t0 * oM / dPsi)
+    int ki;            // round(t0 * oM / dPsi) modulo T, plus p.toff
+    float px, py, pz;  // D0 - t0 v
 };
 
 __device__ __forceinline__ Anchor make_anchor(const KParams& p, float ox, float oy, float oz)
@@ -676,7 +679,9 @@ __device__ __forceinline__ Anchor make_anchor(const KParams& p, float ox, float 
     const double Kr = rint(K);
     Anchor a;
     a.t0 = (float)t0;
-    a.t2 = (float)(2.0 * t0);
+    a.px = (float)(x - t0 * p.vx);
+    a.py = (float)(y - t0 * p.vy);
+    a.pz = (float)(z - t0 * p.vz);
     a.s0 = (float)s0;
     a.kf = (float)(K - Kr);
     // bins wrap with period T: the index is kept small, plus the offset p.toff (a multiple
@@ -712,25 +717,27 @@ struct MixedGeom {
     float2 dt, rx, ry, rz, ir;
 };
 
-__device__ __forceinline__ MixedGeom mixed_geom(const G2& g0, float ox, float oy, float oz, const Anchor& an,
-                                                const KParams& p)
+__device__ __forceinline__ MixedGeom mixed_geom(const G2& g0, const Anchor& an, const KParams& p)
 {
-    const float2 OX = f2(ox), OY = f2(oy), OZ = f2(oz);
-    const float2 dx = sub2(OX, g0.x), dy = sub2(OY, g0.y), dz = sub2(OZ, g0.z);
-    // x.(-vInf), recomputed from the position (nv = -vInf)
+    // P = D0 - t0 vInf (the anchor's), P - x
+    const float2 dx = sub2(f2(an.px), g0.x), dy = sub2(f2(an.py), g0.y), dz = sub2(f2(an.pz), g0.z);
+    // x.(-vInf) and |x|^2, recomputed from the position (nv = -vInf); the same for every
+    // observer of the element pair
     const float2 xnv = fma2(g0.x, p.nvx2, fma2(g0.y, p.nvy2, mul2(g0.z, p.nvz2)));
-    // anchored retarded time: -num = x.(d + D0) - 2 t0 x.v
-    const float2 S = fma2(g0.x, add2(dx, OX), fma2(g0.y, add2(dy, OY), mul2(g0.z, add2(dz, OZ))));
-    const float2 nnum = fma2(f2(an.t2), xnv, S);
+    const float2 xx = fma2(g0.x, g0.x, fma2(g0.y, g0.y, mul2(g0.z, g0.z)));
+    // anchored retarded time: num = |x|^2 - 2 x.(D0 - t0 vInf)
+    const float2 xp = fma2(g0.x, f2(an.px), fma2(g0.y, f2(an.py), mul2(g0.z, f2(an.pz))));
+    const float2 num = fma2(f2(-2.0f), xp, xx);
     const float2 bp = add2(f2(an.s0), xnv);
-    const float2 q = fma2(p.nalpha2, nnum, mul2(bp, bp));
+    const float2 q = fma2(p.alpha2, num, mul2(bp, bp));
     const float2 den = fma2(q, make_float2(rsqrt_ftz(q.x), rsqrt_ftz(q.y)), bp);
     MixedGeom m;
-    m.dt = mul2(nnum, make_float2(-rcp_ftz(den.x), -rcp_ftz(den.y)));
+    m.dt = mul2(num, make_float2(rcp_ftz(den.x), rcp_ftz(den.y)));
     const float2 tr = add2(f2(an.t0), m.dt);
-    m.rx = fma2(p.nvx2, tr, dx);
-    m.ry = fma2(p.nvy2, tr, dy);
-    m.rz = fma2(p.nvz2, tr, dz);
+    // r = D0 - x - vInf (t0 + dt) = P - x - vInf dt
+    m.rx = fma2(p.nvx2, m.dt, dx);
+    m.ry = fma2(p.nvy2, m.dt, dy);
+    m.rz = fma2(p.nvz2, m.dt, dz);
     m.ir = rcp2(mul2(p.a02, tr));
     return m;
 }
@@ -781,10 +788,10 @@ __device__ __forceinline__ void mixed_source(const MixedGeom& m, const G2& g0, c
 
 // g[q] = group q of the pair's FP32 records
 template <bool RANGE, typename S>
-__device__ __forceinline__ void sample_mixed2(const G2* g, float ox, float oy, float oz, const Anchor& an,
-                                              const KParams& p, int tau, S& oa, S& ob)
+__device__ __forceinline__ void sample_mixed2(const G2* g, const Anchor& an, const KParams& p, int tau, S& oa,
+                                              S& ob)
 {
-    const MixedGeom m = mixed_geom(g[0], ox, oy, oz, an, p);
+    const MixedGeom m = mixed_geom(g[0], an, p);
     mixed_source<RANGE>(m, g[0], g[1], g[2], g[3], an, p, tau, oa, ob);
 }
 
@@ -1138,7 +1145,7 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
                 const G2 g0 = g2_of(ra);
                 MixedGeom m[OPW];
 #pragma unroll
-                for (int q = 0; q < OPW; ++q) m[q] = mixed_geom(g0, ox[q], oy[q], oz[q], anc[q], p);
+                for (int q = 0; q < OPW; ++q) m[q] = mixed_geom(g0, anc[q], p);
                 tmem_wait_ld_tie(rc, rd, m[0].dt, m[0].rx, m[0].ry, m[0].ir);
                 if (jp + 1 < SE / 2) tmem_ld_x8(ta + tm_col<SE>(0, 1), ra);
 #pragma unroll
@@ -1156,8 +1163,7 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
                 for (int q = 0; q < kGroups32; ++q) gg[q] = load_g2(tl + q * 2 * kWin * 4);
 #pragma unroll
                 for (int q = 0; q < OPW; ++q)
-                    sample_mixed2<!RING>(gg, ox[q], oy[q], oz[q], anc[q], p, tau, cur[q][2 * jp],
-                                         cur[q][2 * jp + 1]);
+                    sample_mixed2<!RING>(gg, anc[q], p, tau, cur[q][2 * jp], cur[q][2 * jp + 1]);
             }
         }
         // the left neighbour: lane l - 1 of the same window (lane 0 receives lane 31's
@@ -1666,6 +1672,7 @@ void fill_kparams(const TonalRun& r, const TonalTile& tile, KParams& kp)
     const float vxf = (float)g.vinf[0], vyf = (float)g.vinf[1], vzf = (float)g.vinf[2];
     const float kbf = (float)(g.oM / g.dPsi);  // bins per second of retarded time
     kp.nalpha2 = make_float2(-alphaf, -alphaf);
+    kp.alpha2 = make_float2(alphaf, alphaf);
     kp.nvx2 = make_float2(-vxf, -vxf);
     kp.nvy2 = make_float2(-vyf, -vyf);
     kp.nvz2 = make_float2(-vzf, -vzf);

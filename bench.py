@@ -47,10 +47,10 @@ ALG_FLOPS_PER_EVAL = 102  # FP ops per tonal evaluation (integrand + observer ti
 # 42 bands, 1
 BPM_FLOPS_PER_EVAL = 13
 # DRAM bytes (read + write) of one workload-2 launch of the mixed kernel, measured with ncu
-# (one pass: dram__bytes_read.sum + dram__bytes_write.sum: 11.65 GB + 8.13 GB); the FP64
+# (one pass: dram__bytes_read.sum + dram__bytes_write.sum: 11.66 GB + 8.20 GB); the FP64
 # flushes of the FP32 bins and the reads they cause, the 3.08 GB of records being read
 # about once
-TONAL_TRAFFIC_BYTES = 19.78e9
+TONAL_TRAFFIC_BYTES = 19.86e9
 WORKLOAD = "workload 2: 4-blade rotor, 32000 elements, 1440 steps/rev, 4096 observers, tonal mixed precision"
 
 
