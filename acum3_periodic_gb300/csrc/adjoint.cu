@@ -15,7 +15,9 @@
 //     dJ/dp and dJ/dt of both end samples (the hat weights and their derivatives), takes
 //     its right neighbour's half through one shuffle, and runs the reverse of the
 //     integrand by hand.  The 19 cotangents of its step's record fields accumulate in
-//     registers over all observers and are written once: no atomics.
+//     registers over all observers and are written once: no atomics.  The FP32 form
+//     (adjoint_kernel_f32) forms the observer time from a per-observer FP64 anchor as the
+//     mixed forward does.
 //  3. adjoint_chain_kernel: one block per element, FP64: record cotangents -> cotangents of
 //     x, ds, n, ndot, V, Vdot, P, Pdot -> through the transposes of the periodic central
 //     differences (V = Dx, Vdot = D^2 x, ndot = Dn, Pdot = DP), of make_periodic and of the
@@ -226,20 +228,185 @@ __global__ void __launch_bounds__(128) adjoint_kernel(AdjDev p)
             const R dp = pc - pp;
             const R* grow = gg + (size_t)o * p.T;
             int idx = n0 >= 0 ? wrap_T(n0, p.T, p.tmod) : ((n0 % p.T) + p.T) % p.T;
+            // value = p_a + w (p_b - p_a): d J / d p_b = sum g w, d J / d p_a = sum g (1 - w),
+            // and with d value / d t(tau) = -dp w / dt, d value / d t(tau-1) = -dp (1 - w) / dt
+            // the time derivatives are -(dp / dt) times those sums
+            R sg = 0;
             for (int n = n0; n <= n1 && n - n0 < 4; ++n) {
                 const R g = grow[idx];
                 if (++idx == p.T) idx = 0;
                 const R wgt = ((R)n * dPsi - tp) * inv;
                 rp += g * wgt;
-                lp += g * ((R)1 - wgt);
-                // d value / d t(tau) = -dp w / dt,  d value / d t(tau-1) = -dp (1 - w) / dt
-                rt -= g * dp * wgt * inv;
-                lt -= g * dp * ((R)1 - wgt) * inv;
+                sg += g;
             }
+            lp = sg - rp;
+            rt = -dp * inv * rp;
+            lt = -dp * inv * lp;
         }
         const R pb = rp + __shfl_down_sync(0xffffffffu, lp, 1);
         const R tb = rt + __shfl_down_sync(0xffffffffu, lt, 1);
         if (owner) reverse<R>(f, a, pb, tb, p, acc);
+    }
+    if (owner) {
+        double* out = p.cot + ((size_t)e * p.T + step) * kCot;
+#pragma unroll
+        for (int k = 0; k < kCot; ++k) out[k] = (double)acc[k];
+    }
+}
+
+// ---------------------------------------------------------------- FP32 adjoint
+//
+// The FP32 adjoint forms the observer time as the mixed forward does (tonal.cu): per
+// observer the retarded time t0 of the origin is solved once in FP64 and its observer time
+// t0 oM / dPsi split into an integer ki (with a multiple of T >= 2^23) and a fraction kf;
+// per sample dt = t - t0 solves the difference of the two retarded-time quadratics,
+//     alpha dt^2 + 2 b dt - num = 0,  b = s0 - x.v,  num = |x|^2 - 2 x.P,  P = D0 - t0 v,
+// and the sample's observer time in bins is tau + ki + x with x = kf + dt oM / dPsi, so
+// FP32 rounding applies to dt only (the FP32 observer time in radians of the plain form
+// loses ~6e-5 of a bin).  The reverse pass is the plain one: it needs tr = t0 + dt and
+// s = sqrt(beta^2 + alpha c), which equals alpha tr + beta at the root.
+
+// one observer, three 128-bit loads
+struct __align__(16) AdjAnchor {
+    float t0, s0, kf;   // t0, alpha t0 + D0.v, frac(t0 oM / dPsi)
+    int ki;             // round(t0 oM / dPsi) modulo T, plus toff
+    float px, py, pz;   // P = D0 - t0 v
+    float ox;           // D0
+    float oy, oz, pad0, pad1;
+};
+
+__global__ void adj_anchor_kernel(const float* __restrict__ obs, int O, AdjDev p, int toff, AdjAnchor* out)
+{
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= O) return;
+    const double x = obs[3 * o], y = obs[3 * o + 1], z = obs[3 * o + 2];
+    const double b0 = x * p.vx + y * p.vy + z * p.vz;
+    const double c0 = x * x + y * y + z * z;
+    const double s0 = sqrt(b0 * b0 + p.alpha * c0);
+    const double t0 = c0 / (s0 + b0);  // = (s0 - b0) / alpha without the cancellation
+    const double K = t0 * (p.oM / p.dPsi);
+    const double Kr = rint(K);
+    AdjAnchor a;
+    a.t0 = (float)t0;
+    a.s0 = (float)s0;
+    a.kf = (float)(K - Kr);
+    a.px = (float)(x - t0 * p.vx);
+    a.py = (float)(y - t0 * p.vy);
+    a.pz = (float)(z - t0 * p.vz);
+    a.ki = (int)(Kr - floor(Kr / p.T) * p.T) + toff;
+    a.ox = (float)x;
+    a.oy = (float)y;
+    a.oz = (float)z;
+    a.pad0 = a.pad1 = 0.f;
+    out[o] = a;
+}
+
+constexpr float kRoundA = 12582912.0f;  // 1.5 * 2^23
+constexpr int kRoundBitsA = 0x4B400000;
+
+// forward<float> with the anchored retarded time; *xo = the observer-time offset x
+__device__ __forceinline__ Fwd<float> forward_anchored(const float* f, float ox, float oy, float oz,
+                                                       const AdjAnchor& an, const AdjDev& p, float* xo)
+{
+    Fwd<float> a;
+    const float vx = (float)p.vx, vy = (float)p.vy, vz = (float)p.vz, a0 = (float)p.a0, alpha = (float)p.alpha;
+    a.dx = ox - f[0];
+    a.dy = oy - f[1];
+    a.dz = oz - f[2];
+    a.c = 0.f;  // not needed by the reverse pass
+    a.beta = a.dx * vx + a.dy * vy + a.dz * vz;
+    const float xv = f[0] * vx + f[1] * vy + f[2] * vz;
+    const float xx = f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
+    const float xp = f[0] * an.px + f[1] * an.py + f[2] * an.pz;
+    const float num = xx - 2.0f * xp;
+    const float bp = an.s0 - xv;
+    const float q = alpha * num + bp * bp;
+    const float den = q * rsqrt_ftz(q) + bp;
+    const float dt = num * rcp_ftz(den);
+    a.tr = an.t0 + dt;
+    a.s = alpha * a.tr + a.beta;
+    a.rx = a.dx - vx * a.tr;
+    a.ry = a.dy - vy * a.tr;
+    a.rz = a.dz - vz * a.tr;
+    const float r = a0 * a.tr;
+    a.ir = rcp_ftz(r);
+    a.Mr = (f[4] * a.rx + f[5] * a.ry + f[6] * a.rz) * a.ir;
+    a.Mdr = (f[8] * a.rx + f[9] * a.ry + f[10] * a.rz) * a.ir;
+    a.Lr = (f[12] * a.rx + f[13] * a.ry + f[14] * a.rz) * a.ir;
+    a.Ldr = (f[16] * a.rx + f[17] * a.ry + f[18] * a.rz) * a.ir;
+    a.G = rcp_ftz(1.0f - a.Mr);
+    a.qa = a0 * a.ir;
+    a.K = a.Mdr + a.qa * (a.Mr - f[7]);
+    a.base = a.ir * a.G * a.G;
+    a.Y = a.Ldr + a.qa * (a.Lr - f[15]) + a.Lr * a.G * a.K;
+    a.pt = f[11] * a.base * a.G * a.K;
+    a.pl = f[3] * a.base * a.Y;
+    a.t = 0.f;
+    *xo = an.kf + dt * (float)p.kb;
+    return a;
+}
+
+// The FP32 adjoint: as adjoint_kernel<double>, with the anchored observer time.  The
+// interval of lane l is (u(tau - 1), u(tau)], in bins relative to tau + ki: (x_a - 1, x_b];
+// its bins k(a) + 1 ... k(b), their weights and the derivatives with respect to both ends
+// as the forward's deposit forms them (tonal.cu deposit_ring), at most four bins.
+__global__ void __launch_bounds__(128) adjoint_kernel_f32(AdjDev p, const AdjAnchor* __restrict__ anc)
+{
+    const int warp_g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp_g >= p.E * p.nWa) return;  // warp-uniform
+    const int e = warp_g / p.nWa, w = warp_g % p.nWa;
+    const int tau = kAdjStride * w - 1 + lane;  // unwrapped step of this lane's sample
+    const int step = tau < 0 ? tau + p.T : (tau >= p.T ? tau - p.T : tau);
+    const bool owner = lane >= 1 && lane <= kAdjStride && tau >= 0 && tau < p.T;
+    float f[20];
+    load_rec<float>(reinterpret_cast<const double*>(p.rec), p.nW, e, step, f);
+    float acc[kCot];
+#pragma unroll
+    for (int k = 0; k < kCot; ++k) acc[k] = 0.f;
+    const float* gg = reinterpret_cast<const float*>(p.g);
+    const float idPsi = (float)(1.0 / p.dPsi);
+    for (int o = 0; o < p.O; ++o) {
+        const AdjAnchor an = anc[o];
+        float xb;
+        const Fwd<float> a = forward_anchored(f, an.ox, an.oy, an.oz, an, p, &xb);
+        const float pc = a.pt + a.pl;
+        const float xa = __shfl_up_sync(0xffffffffu, xb, 1);
+        const float pp = __shfl_up_sync(0xffffffffu, pc, 1);
+        const float ta = __fadd_rd(xa, kRoundA), tb = __fadd_rd(xb, kRoundA);
+        const int cnt = __float_as_int(tb) - __float_as_int(ta) + 1;
+        const float du = (xb - xa) + 1.0f;
+        // the interval's bins n: value = p_a + w (p_b - p_a), w = (n - u_a) / du, so
+        // d J / d p_b = sum g w, d J / d p_a = sum g (1 - w), and (d value / d u_b = -dp w / du,
+        // d value / d u_a = -dp (1 - w) / du) d J / d u_b = -(dp / du) sum g w, d J / d u_a =
+        // -(dp / du) sum g (1 - w)
+        float rp = 0.f, lp = 0.f, rt = 0.f, lt = 0.f;
+        if (lane >= 1 && du > 0.0f && cnt >= 1) {
+            const float inv = rcp_ftz(du);
+            const float* grow = gg + (size_t)o * p.T;
+            // first bin k(a) + 1 = tau + ki + floor(x_a) (>= 0: ki carries toff)
+            const int n0 = tau + an.ki - kRoundBitsA + __float_as_int(ta);
+            // (a sample far outside the floor's range gives any n0: reduce it safely)
+            int idx = (n0 >= 0 && n0 < (1 << 24)) ? wrap_T(n0, p.T, p.tmod) : ((n0 % p.T) + p.T) % p.T;
+            float wgt = ((ta - (kRoundA - 1.0f)) - xa) * inv;  // w at the first bin
+            const int nb = cnt < 4 ? cnt : 4;
+            float sg = 0.f;
+            for (int n = 0; n < nb; ++n) {
+                const float g = grow[idx];
+                if (++idx == p.T) idx = 0;
+                rp = fmaf(g, wgt, rp);
+                sg += g;
+                wgt += inv;
+            }
+            lp = sg - rp;
+            const float c = -(pc - pp) * inv;
+            rt = c * rp;
+            lt = c * lp;
+        }
+        const float pb = rp + __shfl_down_sync(0xffffffffu, lp, 1);
+        // d J / d u in bins -> d J / d t in radians (u = t / dPsi)
+        const float tbr = (rt + __shfl_down_sync(0xffffffffu, lt, 1)) * idPsi;
+        if (owner) reverse<float>(f, a, pb, tbr, p, acc);
     }
     if (owner) {
         double* out = p.cot + ((size_t)e * p.T + step) * kCot;
@@ -513,6 +680,7 @@ struct AdjState {
     DBuf<double> cot, g64, jrow, gcp, gx, gn;
     DBuf<float> g32;
     DBuf<double> obs64;
+    DBuf<AdjAnchor> anc;
 };
 
 static AdjState* adj_state(acum_ctx* c)
@@ -526,7 +694,7 @@ void release_adj_state(acum_ctx* c)
     if (!c->adj_state) return;
     AdjState* s = adj_state(c);
     s->cot.release(); s->g64.release(); s->jrow.release(); s->gcp.release(); s->gx.release(); s->gn.release();
-    s->g32.release(); s->obs64.release();
+    s->g32.release(); s->obs64.release(); s->anc.release();
     delete s;
     c->adj_state = nullptr;
 }
@@ -609,7 +777,11 @@ extern "C" int acum_tonal_adjoint(acum_ctx* ctx, int precision, const double* dJ
         p.rec = ctx->d_rec64.p;
         p.obs = ctx->d_obs32.p;
         p.g = s->g32.p;
-        adjoint_kernel<float><<<blocks, 128, 0, st>>>(p);
+        p.kb = p.oM / p.dPsi;
+        CKA(s->anc.ensure((size_t)O));
+        const int toff = (int)(((1 << 23) + T - 1) / T * T);
+        adj_anchor_kernel<<<(O + 127) / 128, 128, 0, st>>>(ctx->d_obs32.p, O, p, toff, s->anc.p);
+        adjoint_kernel_f32<<<blocks, 128, 0, st>>>(p, s->anc.p);
     }
     CKA(cudaEventRecord(ctx->ev[EV_ADJ1], st));
     CKA(cudaGetLastError());

@@ -138,9 +138,11 @@ def test_fp32_adjoint_against_fp64(workload3):
     d, ctx, pA, (J, gcp, gx, gn) = workload3
     J32, g32, x32, n32 = ctx.adjoint(native.MIXED)
     assert abs(J32 - J) / J < 1e-5
+    # the FP32 adjoint forms the observer time from the FP64 anchor as the mixed forward
+    # does: measured 6e-5 in relative norm (8.7e-4 with the observer time in FP32 radians)
     for a, b in ((g32, gcp), (x32, gx), (n32, gn)):
         rel = np.linalg.norm(a - b) / np.linalg.norm(b)
-        assert rel < 1e-3, rel
+        assert rel < 3e-4, rel
 
 
 def test_adjoint_cost_ratio(workload3):
