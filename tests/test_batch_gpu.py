@@ -103,25 +103,63 @@ def test_against_fp64_oracle(batch):
         assert per_bin_rms(got, ref).max() < BIN_RMS
 
 
-@pytest.mark.parametrize("W,SE,ips", [(8, 2, 4), (12, 4, 16), (16, 2, 8), (5, 4, 1), (16, 8, 8), (7, 8, 2)])
-def test_tile_shapes_agree(batch, singles, W, SE, ips):
+@pytest.mark.parametrize("W,SE,ips,opw", [(8, 2, 4, 1), (12, 4, 16, 1), (16, 2, 8, 1), (5, 4, 1, 1), (16, 8, 8, 1),
+                                         (7, 8, 2, 1), (32, 8, 8, 2), (16, 4, 4, 2), (24, 2, 8, 2), (6, 8, 1, 2)])
+def test_tile_shapes_agree(batch, singles, W, SE, ips, opw):
     b, decks = batch
-    b.set_tile(W, SE, ips)
-    assert b.tile() == (W, SE, ips)
+    b.set_tile(W, SE, ips, opw)
+    assert b.tile() == (W, SE, ips) and b.obs_per_warp() == opw
     b.run(mode=0)
     for i in range(len(decks)):
-        assert per_bin_rms(b.result(i), singles[i]).max() < SAME_FORM_RMS, (W, SE, ips, i)
+        assert per_bin_rms(b.result(i), singles[i]).max() < SAME_FORM_RMS, (W, SE, ips, opw, i)
 
 
 def test_autotune(batch, singles):
     b, decks = batch
     est = b.autotune()
     W, SE, ips = b.tile()
-    assert W in (8, 12, 16) and SE in (2, 4, 8) and ips in (4, 8, 16, 32)
+    if b.obs_per_warp() == 1:
+        assert W in (8, 12, 16) and SE in (2, 4, 8)
+    else:
+        assert b.obs_per_warp() == 2 and W in (16, 24, 32) and SE in (2, 4, 8)
+    assert ips in (4, 8, 16, 32)
     assert est > 0
     b.run(mode=2)
     for i in range(len(decks)):
         assert per_bin_rms(b.result(i), singles[i]).max() < SAME_FORM_RMS
+
+
+def test_ring_and_whole_row_cases_in_one_launch():
+    """A batch whose cases take different forms: one in forward flight with an observer
+    9 cm from the hub, which the bin ring's bound does not cover (its items run on whole
+    rows), beside cases that run on the ring; every case matches its single-deck solve and
+    the FP64 oracle."""
+    from acum3_periodic_gb300 import native
+    near = synth.config_deck(0, replicate=39, scale=dict(n_span=4, n_chord_side=3, ntime=72, nobs=5, minf=0.1))
+    obs = near.obs_file.copy()
+    obs[2] = np.array([0.0, 0.0, 0.09], np.float32) / np.float32(near.OBSscale)
+    near.obs_file = obs
+    decks = [shrunk(0), near, shrunk(5)]
+    ctx = native.Context(0)
+    singles, forms = [], []
+    for d in decks:
+        ctx.set_deck(d, bb=False)
+        singles.append(ctx.tonal(native.MIXED)[2])
+        forms.append(ctx.last_plan()["ring_used"])
+    ctx.close()
+    assert forms == [1, 0, 1]
+    b = native.Batch(0)
+    for d in decks:
+        b.add(d)
+    for W, SE, ips, opw in ((32, 8, 8, 2), (16, 8, 8, 1)):
+        b.set_tile(W, SE, ips, opw)
+        b.run(mode=0)
+        for i, d in enumerate(decks):
+            got = b.result(i)
+            assert per_bin_rms(got, singles[i]).max() < SAME_FORM_RMS, (W, i)
+    _, _, ref, _ = O.tonal(near, nthreads=8)
+    assert per_bin_rms(b.result(1), ref).max() < BIN_RMS
+    b.close()
 
 
 def test_errors():
