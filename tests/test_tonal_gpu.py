@@ -233,10 +233,11 @@ def test_records_reaching_past_the_ring(ctx):
     (tip Mach 0.8 over 2048 steps per revolution: the source's distance from the origin
     is worth up to 0.8 x 2048 / 2 pi = 261 bins either side): the whole-row kernel
     launched behind the ring kernel does the work, and matches the oracle; the same rotor
-    at 180 steps (23 bins) runs on the ring."""
+    at 180 steps (23 bins) runs on the ring, and so does tip Mach 0.68 over 2048 steps (224
+    bins either side: the window's live span fills 487 of the ring's 512 slots)."""
     from acum3_periodic_gb300 import native
-    for T, used in ((2048, 0), (180, 1)):
-        d = synth.config_deck(0, replicate=37, scale=dict(n_span=4, n_chord_side=3, ntime=T, nobs=6, tip_mach=0.8,
+    for T, tip, used in ((2048, 0.8, 0), (180, 0.8, 1), (2048, 0.68, 1)):
+        d = synth.config_deck(0, replicate=37, scale=dict(n_span=4, n_chord_side=3, ntime=T, nobs=6, tip_mach=tip,
                                                            minf=0.0))
         oT, oL, oA, bad = O.tonal(d)
         assert bad == 0
