@@ -819,24 +819,10 @@ __device__ __forceinline__ float small_int_to_float(int v)
     return __int_as_float(v + kRoundBits) - kRound;  // exact for |v| < 2^22
 }
 
-// RMW of one bin of a warp's observer row: (pT, pL) += p(a) + w (p(b) - p(a)), packed
-__device__ __forceinline__ void add_bin(float2* acc, int idx, float w, float2 pa, float2 dp)
-{
-    acc[idx] = fma2(f2(w), dp, add2(acc[idx], pa));
-}
-
-// Slot of bin index n >= 0 in a warp's observer row: whole rows hold the T bins of the
-// period (n mod T by multiply-high, m = ceil(2^32 / T)); a ring holds R = m + 1 (a power
-// of two) consecutive bins (n mod R).
-template <bool RING>
-__device__ __forceinline__ int bin_slot(int n, int T, unsigned m)
-{
-    return RING ? (int)((unsigned)n & m) : mod_T(n, T, m);
-}
-
-// A warp's observer row: `nb` slots (the T bins of the period, or the R slots of the
-// ring), then an overflow slot (index nb: the slot after the last, i.e. slot 0, added
-// into it when the row is flushed) and a scratch slot (index nb + 1, never read).
+// A warp's observer row of the whole-row form: the T bins of the period (bin n in slot n
+// mod T, by multiply-high with m = ceil(2^32 / T)), then an overflow slot (index T: bin 0
+// of the next period, added into bin 0 when the row is flushed) and a scratch slot
+// (index T + 1, never read).  (The ring form's rows: deposit_ring.)
 //
 // Bins n with u(a) < n <= u(b): n = k(a) + 1 ... k(b), the value interpolated between the
 // two samples.  For |Mr| < 1 an interval holds at most 2 bins (u(b) - u(a) = 1 - Mr < 2).
@@ -848,9 +834,8 @@ __device__ __forceinline__ int bin_slot(int n, int T, unsigned m)
 // of more than two bins (|Mr| >= 1) set `more`: the caller then adds their other bins
 // with deposit_rest.  The integer parts k carry a multiple of T of at least 2^23 (the
 // anchor's), which keeps the bin index non-negative.
-template <bool RING>
-__device__ __forceinline__ void deposit(float2* acc, int nb, int T, unsigned m, const SmpF& a, const SmpF& b,
-                                        bool active, unsigned& bad, bool& more)
+__device__ __forceinline__ void deposit(float2* acc, int T, unsigned m, const SmpF& a, const SmpF& b, bool active,
+                                        unsigned& bad, bool& more)
 {
     const int cnt = b.k - a.k;
     const float du = small_int_to_float(cnt) + (b.f - a.f);
@@ -861,9 +846,9 @@ __device__ __forceinline__ void deposit(float2* acc, int nb, int T, unsigned m, 
     // not finite when !ok; both slots are then the scratch slot, which is never read out
     const float inv = rcp_ftz(du);
     const float2 pa = make_float2(a.pt, a.pl), dp = sub2(make_float2(b.pt, b.pl), pa);
-    const int idx = bin_slot<RING>(a.k + 1, T, m);  // used only when `one`
+    const int idx = mod_T(a.k + 1, T, m);  // used only when `one`
     const float w1 = (1.0f - a.f) * inv;
-    const int i1 = one ? idx : nb + 1, i2 = two ? idx + 1 : nb + 1;
+    const int i1 = one ? idx : T + 1, i2 = two ? idx + 1 : T + 1;
     // i1 != i2 unless both are the scratch slot, so both bins are read before either is
     // written (one shared-memory round trip per sample instead of two in sequence)
     const float2 v1 = acc[i1], v2 = acc[i2];
@@ -872,30 +857,30 @@ __device__ __forceinline__ void deposit(float2* acc, int nb, int T, unsigned m, 
 }
 
 // The bins after the first two of an interval that holds more (see deposit); an interval
-// of more bins than the row has slots sets `bad` instead.
-template <bool RING>
-__device__ __forceinline__ void deposit_rest(float2* acc, int nb, int T, unsigned m, const SmpF& a, const SmpF& b,
+// of more than T bins sets `bad` instead.
+__device__ __forceinline__ void deposit_rest(float2* acc, int T, unsigned m, const SmpF& a, const SmpF& b,
                                              bool active, unsigned& bad)
 {
     const int cnt = b.k - a.k;
     const float du = small_int_to_float(cnt) + (b.f - a.f);
     if (!(active && du > 0.0f && cnt > 2)) return;
-    if (cnt > nb) {
+    if (cnt > T) {
         bad = 1u;
         return;
     }
     const float inv = rcp_ftz(du);
     const float2 pa = make_float2(a.pt, a.pl), dp = sub2(make_float2(b.pt, b.pl), pa);
     const float w1 = (1.0f - a.f) * inv;
-    int i = bin_slot<RING>(a.k + 1, T, m);
+    int i = mod_T(a.k + 1, T, m);
     for (int q = 1; q < cnt; ++q) {
-        if (RING) i = (int)((unsigned)(i + 1) & m);
-        else if (++i >= T) i -= T;
+        if (++i >= T) i -= T;
         if (q >= 2) acc[i] = add2(acc[i], fma2(f2(w1 + (float)q * inv), dp, pa));
     }
 }
 
-// The ring form of deposit / deposit_rest on SmpR samples: a = lane l - 1's sample (step
+// The ring form of deposit / deposit_rest on SmpR samples, in a row of R slots (bin n in
+// slot n mod R, R a power of two, m = R - 1), an overflow slot R (slot 0's bin, added into
+// it when the slot is flushed) and a scratch slot R + 1: a = lane l - 1's sample (step
 // tau - 1), b = this lane's (step tau); base = tau + ki - 1.5 * 2^23 (as an int), so that the
 // first bin of the interval, k(a) + 1 = tau + ki + floor(x_a), is base + the bits of
 // x_a + 1.5 * 2^23 rounded down.  The interval's length in bins is 1 + x_b - x_a (= the
@@ -1180,7 +1165,7 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
                 if constexpr (RING)
                     deposit_ring(acc[q], nb, mm, prev, cur[q][j], base[q], ok_obs[q] && dep_lane, bad, more);
                 else
-                    deposit<false>(acc[q], nb, T, mm, prev, cur[q][j], ok_obs[q] && dep_lane, bad, more);
+                    deposit(acc[q], T, mm, prev, cur[q][j], ok_obs[q] && dep_lane, bad, more);
             }
         }
         // intervals of more than two bins (|Mr| >= 1): their other bins, for the whole warp
@@ -1193,7 +1178,7 @@ __device__ __forceinline__ void mixed_item(const KParams& __restrict__ p, int ot
                     if constexpr (RING)
                         deposit_rest_ring(acc[q], nb, mm, prev, cur[q][j], base[q], ok_obs[q] && dep_lane, bad);
                     else
-                        deposit_rest<false>(acc[q], nb, T, mm, prev, cur[q][j], ok_obs[q] && dep_lane, bad);
+                        deposit_rest(acc[q], T, mm, prev, cur[q][j], ok_obs[q] && dep_lane, bad);
                 }
             }
             more = false;
