@@ -160,6 +160,8 @@ struct TonalTile {
     int opw;          // observers per warp
     bool tm;          // mixed: record stages copied into tensor memory and read from there
     int ring;         // mixed: bin slots per observer of the sliding ring (a power of 2), 0 = whole rows
+    int ring_lo;      // mixed: slots of the smaller ring launched before this kernel in the same
+                      // plan, which takes the records first when they fit it (0: none)
     size_t smem;
 };
 
@@ -239,8 +241,10 @@ cudaError_t launch_per_rows(const float* raw, const long long* raw_off, const in
 
 struct TonalRun {
     TonalGeom g;
-    TonalTile t;          // the plan; mixed with t.ring > 0: the ring kernel, and
-    TonalTile rows;       // the whole-row kernel launched after it, which runs when the ring is too short
+    TonalTile t;          // the plan; mixed with t.ring > 0: the ring kernel, then
+    TonalTile wide;       // the wide-ring kernel (wide.ring > 0: planned) for records that reach
+                          // past the first ring, and
+    TonalTile rows;       // the whole-row kernel, which runs when every ring is too short
     const unsigned* rmax; // mixed: the records' largest |x| (note_radius bits)
     const void* rec;      // rec64 or rec32
     const double* obs64;  // [O][3]
@@ -259,7 +263,9 @@ struct KParams {
     int Epad, T, nW, O;
     int nW32;               // windows of the FP32 records
     int ring;               // mixed: ring slots per observer (ring kernel), 0 = whole rows
-    int dual;               // mixed: a ring kernel and a whole-row kernel are both launched
+    int ring_lo;            // mixed: slots of the smaller ring launched before (TonalTile::ring_lo)
+    int dual;               // mixed: ring kernels and a whole-row kernel are all launched, and
+                            // each tests the records' reach
     const unsigned* rmax;   // mixed: the records' largest |x| (note_radius bits)
     double obs_rmin;        // mixed: the smallest observer distance from the origin (ring_ok)
     const float* obs32;
@@ -296,6 +302,17 @@ size_t batch_static_smem(int SE, int opw);  // static shared memory to keep besi
 cudaError_t launch_tonal_batch(const KParams* d_cases, const BatchItem* d_items, int nitems, int* d_counter, int W,
                                int SE, int opw, int rowlen, int grid, cudaStream_t s);
 constexpr int kRingSlots = 512;  // bin slots per observer of the mixed ring kernels (single deck and batched)
+// Bin slots per observer of the wide ring, for records that reach past kRingSlots, in decks
+// of more than kRingSlotsWide steps (whole rows of a shorter period hold no more bins).
+constexpr int kRingSlotsWide = 1024;
+// the ring that serves records of largest |x| r (ring_ok), for a deck of T steps: the
+// first ring, else the wide ring, else 0 (whole rows)
+inline int ring_for(float r, double vx, double vy, double vz, double a0, double kb, double obs_rmin, int T)
+{
+    if (ring_ok(r, vx, vy, vz, a0, kb, obs_rmin, kRingSlots)) return kRingSlots;
+    if (T > kRingSlotsWide && ring_ok(r, vx, vy, vz, a0, kb, obs_rmin, kRingSlotsWide)) return kRingSlotsWide;
+    return 0;
+}
 // acc [O][T][2] of every case -> pA [T][O] (overwrite)
 struct FinCase {
     const double* acc;

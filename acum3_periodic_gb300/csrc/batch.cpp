@@ -32,9 +32,11 @@ struct acum_batch {
     // tile shape and plan: W observers per block, opw per warp, SE elements per stage;
     // rowlen = slots per bin row (the longest whole-row case's nTime, or the ring's)
     int W = 32, SE = 8, opw = 2, ips = 8;
+    bool tile_set = false;  // the shape was set (or autotuned); else the default, with fewer
+                            // observers per block where its rows do not fit
     bool planned = false;
     int Tmax = 0, rowlen = 0;
-    std::vector<char> ring;  // per case: its records fit the bin ring
+    std::vector<int> ring;  // per case: slots of the bin ring its records fit (ring_for), 0 = whole rows
     int nitems = 0;
     std::vector<BatchItem> items;
     std::vector<size_t> acc_off, out_off;
@@ -163,7 +165,7 @@ bool shape_fits(const acum_batch* b, int W, int SE, int opw)
     return batch_smem(W, SE, b->rowlen) + batch_static_smem(SE, opw) <= b->smem_optin;
 }
 
-// Which cases' records fit the bin ring (from each case's largest |x|, read once), and
+// Which bin ring each case's records fit (from the case's largest |x|, read once), and
 // the slots per bin row the batch needs.
 int ring_cases(acum_batch* b)
 {
@@ -176,17 +178,15 @@ int ring_cases(acum_batch* b)
             BK(b, cudaMemcpy(&bits, c->d_rmax.p, sizeof(bits), cudaMemcpyDeviceToHost));
             float r;
             memcpy(&r, &bits, sizeof(r));
-            b->ring[i] = ring_ok(r, c->der.vinf[0], c->der.vinf[1], c->der.vinf[2], c->in.a0,
-                                 c->der.oM / c->der.dPsi, c->obs_rmin, kRingSlots)
-                             ? 1
-                             : 0;
+            b->ring[i] = ring_for(r, c->der.vinf[0], c->der.vinf[1], c->der.vinf[2], c->in.a0,
+                                  c->der.oM / c->der.dPsi, c->obs_rmin, c->T);
         }
     }
     b->Tmax = 0;
     b->rowlen = 0;
     for (size_t i = 0; i < n; ++i) {
         b->Tmax = std::max(b->Tmax, b->cases[i]->T);
-        b->rowlen = std::max(b->rowlen, b->ring[i] ? kRingSlots : b->cases[i]->T);
+        b->rowlen = std::max(b->rowlen, b->ring[i] > 0 ? b->ring[i] : b->cases[i]->T);
     }
     return ACUM_OK;
 }
@@ -197,6 +197,14 @@ int plan(acum_batch* b)
     DeviceGuard g(b->device);
     int rc0 = ring_cases(b);
     if (rc0) return rc0;
+    if (!b->tile_set) {
+        // the default shape, with as many observers per block as the longest rows leave
+        // room for
+        b->W = 32;
+        b->SE = 8;
+        b->opw = 2;
+        while (b->W > b->opw && !shape_fits(b, b->W, b->SE, b->opw)) b->W -= b->opw;
+    }
     if (!shape_fits(b, b->W, b->SE, b->opw))
         return bfail(b, ACUM_ERR_INVALID, "tile shape does not fit in shared memory for the longest case");
     // pools of sums and results
@@ -222,7 +230,7 @@ int plan(acum_batch* b)
         const acum_ctx* c = b->cases[i];
         TonalRun r = case_run(b, c, b->d_acc.p + b->acc_off[i]);
         fill_kparams(r, kp[i]);
-        kp[i].ring = b->ring[i] ? kRingSlots : 0;  // the batched kernel picks the form per case
+        kp[i].ring = b->ring[i];  // the batched kernel picks the form per case
         kp[i].dual = 0;
         fin[i].acc = b->d_acc.p + b->acc_off[i];
         fin[i].pA = b->d_out.p + b->out_off[i];
@@ -481,6 +489,7 @@ extern "C" int acum_batch_set_tile(acum_batch* b, int obs_per_block, int elems_p
     if (elems_per_stage) b->SE = elems_per_stage;
     if (items_per_sm) b->ips = items_per_sm;
     b->opw = 1;
+    b->tile_set = true;
     b->planned = false;
     b->drop_graph();
     return ACUM_OK;
@@ -501,6 +510,7 @@ extern "C" int acum_batch_set_tile2(acum_batch* b, int obs_per_block, int elems_
     b->SE = elems_per_stage ? elems_per_stage : 8;
     if (items_per_sm) b->ips = items_per_sm;
     b->opw = 2;
+    b->tile_set = true;
     b->planned = false;
     b->drop_graph();
     return ACUM_OK;
@@ -620,6 +630,7 @@ extern "C" int acum_batch_autotune(acum_batch* b, int probe_per_sm, double* best
         for (int SE : {2, 4, 8}) shapes.push_back({W, SE, 2});
     double best_rate = 0;
     int bw = b->W, bse = b->SE, bopw = b->opw;
+    b->tile_set = true;  // plan() keeps each probed shape
     DBuf<BatchItem> d_probe;
     std::vector<BatchItem> probe;
     for (const Shape& sh : shapes) {
@@ -647,6 +658,7 @@ extern "C" int acum_batch_autotune(acum_batch* b, int probe_per_sm, double* best
     b->W = bw;
     b->SE = bse;
     b->opw = bopw;
+    b->tile_set = true;
     int rc = plan(b);
     if (rc) return rc;
     double ev1 = probe_items(b, bw, bse, 64, target, probe), ms1 = 0;

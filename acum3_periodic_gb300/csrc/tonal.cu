@@ -1270,14 +1270,20 @@ __device__ __forceinline__ void mixed_drain(unsigned char* smem, size_t stage_of
 // element chunk, then tile within the group, one at a time from a counter in global
 // memory.  The blocks running at any time therefore share one or two chunks of records
 // in L2 (each record is read from HBM about once per group), and the FP64 sums they add
-// into belong to one group of tiles.  A ring kernel (RING) and a whole-row kernel are
-// launched one after the other when the plan has a ring (p.dual): each tests the
-// records' reach against the ring, and the one that does not match returns at once.
+// into belong to one group of tiles.  When the plan has a ring (p.dual) the ring kernel,
+// the wide-ring kernel (if planned) and the whole-row kernel are launched one after the
+// other: each tests the records' reach, and all but the first that serves them return at
+// once (a ring kernel needs the records to fit its ring, and every kernel leaves them to
+// the smaller ring launched before it when they fit that one).
 template <int SE, int OPW, bool TM, bool RING>
 __global__ void __launch_bounds__(512, 1) tonal_mixed_kernel(const KParams p)
 {
-    if (p.dual && ring_ok(__uint_as_float(*p.rmax), p.vx, p.vy, p.vz, p.a0, p.oM / p.dPsi, p.obs_rmin, p.ring) != RING)
-        return;
+    if (p.dual) {
+        const float rm = __uint_as_float(*p.rmax);
+        const double kb = p.oM / p.dPsi;
+        if (RING && !ring_ok(rm, p.vx, p.vy, p.vz, p.a0, kb, p.obs_rmin, p.ring)) return;
+        if (p.ring_lo > 0 && ring_ok(rm, p.vx, p.vy, p.vz, p.a0, kb, p.obs_rmin, p.ring_lo)) return;
+    }
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ MixedShared<SE, OPW> sh;
     __shared__ int s_item;
@@ -1373,7 +1379,7 @@ __global__ void __launch_bounds__(512, 1)
 
 constexpr int kMixedSE = 8;   // elements per stage of the whole-row mixed kernel (one observer per warp)
 constexpr int kRingSE = 8;    // elements per stage of the ring kernel
-constexpr int kRingOPW = 2;   // observers per warp of the ring kernel
+constexpr int kRingOPW = 2;   // observers per warp of the ring and wide-ring kernels
 constexpr bool kMixedTmem = false;  // record stages read from tensor memory by default
 static_assert(kMaxStages >= 4, "stage bookkeeping");
 static_assert(sizeof(SmpF) == 16, "sample record");
@@ -1481,6 +1487,7 @@ static cudaError_t plan_mixed_tile(const TonalRun& r, TonalTile& t, int W_req, i
     t.opw = opw;
     t.tm = tm;
     t.ring = ring;
+    t.ring_lo = 0;
     t.smem = tonal_smem(W, rowlen, NS, SE, 4);
     // more than half of the shared memory keeps a second block off the SM (a second
     // allocation of the tensor-memory columns would wait for the first block to end)
@@ -1518,11 +1525,13 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
 {
     const bool f64 = r.precision == ACUM_PLAIN_FP64;
     memset(&r.rows, 0, sizeof(r.rows));
+    memset(&r.wide, 0, sizeof(r.wide));
     if (!f64) {
         // Mixed: the ring kernel (observers per warp 1 or 2, default 2; elements per stage
-        // 2 or 4, or 8 with one observer) with the whole-row kernel (one observer per warp)
-        // behind it for records that reach too far for the ring; whole rows alone when
-        // asked for, with tensor-memory stages, or without the records' reach.
+        // 2, 4 or 8), with the wide-ring kernel behind it in decks of more than
+        // kRingSlotsWide steps, and the whole-row kernel (one observer per warp) last, for
+        // records that reach too far for every ring; whole rows alone when asked for, with
+        // tensor-memory stages, or without the records' reach.
         const bool tm = tm_req == 1 || (tm_req == 0 && kMixedTmem);
         TonalTile rows;
         memset(&rows, 0, sizeof(rows));
@@ -1540,6 +1549,22 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
             cudaSuccess) {
             r.t = rows;
             return cudaSuccess;
+        }
+        ring.ring_lo = 0;
+        rows.ring_lo = ring.ring;
+        if (r.g.T > kRingSlotsWide) {
+            // the wide ring, with the ring's observers per warp: as many observers per
+            // block as its rows leave room for (24 in 12 warps at two per warp, two
+            // stages: 13.7 ms against 15.1 ms for 16 warps of one, six stages, on 1024
+            // observers of a 2048-step deck)
+            TonalTile wide;
+            memset(&wide, 0, sizeof(wide));
+            if (plan_mixed_tile(r, wide, W_req, SE_req, opw, false, kRingSlotsWide, items_per_sm, num_sms,
+                                smem_optin) == cudaSuccess) {
+                wide.ring_lo = ring.ring;
+                rows.ring_lo = wide.ring;
+                r.wide = wide;
+            }
         }
         r.t = ring;
         r.rows = rows;
@@ -1563,6 +1588,7 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
     t.opw = 1;
     t.tm = false;
     t.ring = 0;
+    t.ring_lo = 0;
     t.smem = tonal_smem(W, T, NSmin, SE, 8);
     const int obs_tiles = (r.g.O + W - 1) / W;
     // resident blocks per SM: shared memory, and registers (~128 per thread)
@@ -1635,7 +1661,8 @@ void fill_kparams(const TonalRun& r, const TonalTile& tile, KParams& kp)
     kp.T = g.T;
     kp.nW = g.nW;
     kp.nW32 = nwin32(g.T);
-    kp.ring = r.t.ring;  // the ring kernel's slots, also in the whole-row kernel launched behind it
+    kp.ring = tile.ring;
+    kp.ring_lo = tile.ring_lo;
     kp.dual = r.t.ring > 0 ? 1 : 0;
     kp.rmax = r.rmax;
     kp.obs_rmin = g.obs_rmin;
@@ -1706,9 +1733,14 @@ cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s)
     if (r.precision == ACUM_PLAIN_FP64) return launch_f64_t<kSE64>(kp, r.t.items, 32 * r.t.W, r.t.smem, s);
     cudaError_t e = launch_mixed_tile(kp, r.t, s);
     if (e != cudaSuccess || r.t.ring == 0) return e;
-    // the whole-row kernel behind the ring kernel: it runs when the records reach too far
-    // for the ring, and returns at once otherwise
+    // the wide-ring and whole-row kernels behind the ring kernel: each runs when the
+    // records reach too far for the rings before it, and returns at once otherwise
     KParams kr;
+    if (r.wide.ring > 0) {
+        fill_kparams(r, r.wide, kr);
+        e = launch_mixed_tile(kr, r.wide, s);
+        if (e != cudaSuccess) return e;
+    }
     fill_kparams(r, r.rows, kr);
     return launch_mixed_tile(kr, r.rows, s);
 }

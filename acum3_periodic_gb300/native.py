@@ -326,17 +326,19 @@ class Context:
         self._ck(self.L.acum_set_ring(self.h, whole_rows))
 
     def last_plan(self) -> dict:
-        """The last tonal plan; for the mixed form also `ring_slots` (0: whole rows only)
-        and `ring_used` (the records fit the ring, so the ring kernel did the work)."""
+        """The last tonal plan; for the mixed form also `ring_slots` (0: whole rows only),
+        `wide_ring_slots` (0: no wide ring planned) and `ring_used` (the slots of the ring
+        whose kernel did the work, 0: the whole-row kernel)."""
         v = (C.c_int * 8)()
         self._ck(self.L.acum_last_plan(self.h, v))
         keys = ("obs_per_block", "elems_per_stage", "stages", "elems_per_item", "element_chunks", "work_items",
                 "obs_per_warp", "tensor_memory")
         out = dict(zip(keys, (int(x) for x in v)))
-        r = (C.c_int * 5)()
+        r = (C.c_int * 8)()
         self._ck(self.L.acum_last_plan_ring(self.h, r))
         out.update(ring_slots=int(r[0]), rows_obs_per_block=int(r[1]), rows_elems_per_stage=int(r[2]),
-                   rows_stages=int(r[3]), ring_used=int(r[4]))
+                   rows_stages=int(r[3]), ring_used=int(r[4]), wide_ring_slots=int(r[5]),
+                   wide_obs_per_block=int(r[6]), wide_stages=int(r[7]))
         return out
 
     def timing(self, which: int):

@@ -90,7 +90,9 @@ def test_one_launch_per_case_matches(batch, singles):
         assert per_bin_rms(b.result(i), singles[i]).max() < 1e-12
         assert b.case_ms(i) > 0
     _, launches = b.timing()
-    assert launches == 3 * len(decks)  # per case the ring kernel, the whole-row kernel behind it, finalize
+    # per case the ring kernel, the wide-ring kernel (cases of more than 1024 steps), the
+    # whole-row kernel, finalize
+    assert launches == sum(4 if d.nTime > 1024 else 3 for d in decks)
 
 
 def test_against_fp64_oracle(batch):
@@ -147,7 +149,7 @@ def test_ring_and_whole_row_cases_in_one_launch():
         singles.append(ctx.tonal(native.MIXED)[2])
         forms.append(ctx.last_plan()["ring_used"])
     ctx.close()
-    assert forms == [1, 0, 1]
+    assert forms == [512, 0, 512]
     b = native.Batch(0)
     for d in decks:
         b.add(d)
@@ -183,4 +185,41 @@ def test_errors():
         b.result(1)
     with pytest.raises(native.AcumError):
         b.case_ms(0)  # last run was not one launch per case
+    b.close()
+
+
+def test_wide_ring_case_in_a_batch():
+    """A case whose records reach past the bin ring (2048 steps at tip Mach 0.8: a live
+    span of 514 bins) runs on the wide ring of 1024 slots beside a case on the ring.  The
+    default shape then holds fewer than 32 observers per block, an explicit shape whose
+    rows do not fit is refused, and every case matches its single-deck solve and the FP64
+    oracle."""
+    from acum3_periodic_gb300 import native
+    wide = synth.config_deck(0, replicate=37, scale=dict(n_span=4, n_chord_side=3, ntime=2048, nobs=6, tip_mach=0.8,
+                                                         minf=0.0))
+    decks = [shrunk(0), wide]
+    ctx = native.Context(0)
+    singles, forms = [], []
+    for d in decks:
+        ctx.set_deck(d, bb=False)
+        singles.append(ctx.tonal(native.MIXED)[2])
+        forms.append(ctx.last_plan()["ring_used"])
+    ctx.close()
+    assert forms == [512, 1024]
+    b = native.Batch(0)
+    for d in decks:
+        b.add(d)
+    b.run(mode=0)
+    assert b.tile()[0] < 32
+    for i in range(len(decks)):
+        assert per_bin_rms(b.result(i), singles[i]).max() < SAME_FORM_RMS, i
+    b.set_tile(32, 8, 8, 2)
+    with pytest.raises(native.AcumError):
+        b.run(mode=0)
+    b.set_tile(16, 8, 8, 1)
+    b.run(mode=0)
+    for i in range(len(decks)):
+        assert per_bin_rms(b.result(i), singles[i]).max() < SAME_FORM_RMS, (16, i)
+    _, _, ref, _ = O.tonal(wide, nthreads=8)
+    assert per_bin_rms(b.result(1), ref).max() < BIN_RMS
     b.close()

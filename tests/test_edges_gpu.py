@@ -53,11 +53,23 @@ def test_smallest_deck(ctx):
 
 def test_longest_period(ctx):
     """4096 steps per period: the retarded times spread over more bins than the mixed
-    ring holds, and the whole-row kernel's blocks hold only as many observer rows as fit
-    in shared memory (fewer than 16)."""
+    ring holds (a live span of 671 bins), and the wide ring does the work; with whole rows
+    asked for, the whole-row kernel's blocks hold only as many observer rows as fit in
+    shared memory (fewer than 16).  Both match the oracle."""
+    from acum3_periodic_gb300 import native
     d = synth.config_deck(0, replicate=81, scale=dict(n_span=2, n_chord_side=2, ntime=4096, nobs=9))
     plan = _against_oracle(ctx, d, rms_norm=True)
-    assert plan["ring_used"] == 0 and plan["rows_obs_per_block"] < 9
+    assert plan["ring_used"] == 1024 and plan["wide_obs_per_block"] == 10  # 9 observers, two per warp
+    _, _, oA, _ = O.tonal(d)
+    ctx.set_tile(whole_rows=1)
+    try:
+        _, _, mA = ctx.tonal(native.MIXED)
+        plan = ctx.last_plan()
+    finally:
+        ctx.set_tile()
+    assert plan["ring_slots"] == 0 and plan["ring_used"] == 0 and plan["obs_per_block"] < 9
+    assert per_bin_rms(mA, oA).max() < MIXED_RMS_TOL
+    assert ctx.error_word(reset=True) == 0
 
 
 def test_refused_decks(ctx):

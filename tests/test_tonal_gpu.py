@@ -20,6 +20,14 @@ pytestmark = pytest.mark.gpu
 
 F64_TOL = 1e-10
 MIXED_RMS_TOL = 1e-4
+# The mixed form at 4096 steps per revolution: its FP32 observer-time offsets carry a
+# relative error of a few 1e-7, i.e. an absolute error that grows with the records' reach
+# in bins (up to ~500 here), and the bins of a long period resolve the sharp thickness
+# pulses of a fast blade; measured 1.3e-4 (tip Mach 0.6) to 3.9e-4 (0.8) of the observer
+# RMS, alike on the ring, the wide ring and whole rows (the FP64 form: < 4e-11).
+LONG_PERIOD_RMS_TOL = 6e-4
+# a ring form against whole rows on the same deck (summation orders differ)
+SAME_DECK_RMS_TOL = 1e-5
 OASPL_TOL_DB = 0.05
 
 TONAL = ["tonal_hover", "tonal_flight_lowpass", "bb_tdel2", "bb_tdel1_lbl_cw", "bb_tdel0_hover"]
@@ -198,7 +206,7 @@ def test_mixed_tile_shapes_against_oracle(ctx, W, SE, opw, tm, rows):
     assert plan["tensor_memory"] == (1 if tm == 1 else 0)
     ring = tm != 1 and not rows
     assert plan["ring_slots"] == (512 if ring else 0)
-    assert plan["ring_used"] == (1 if ring else 0)
+    assert plan["ring_used"] == (512 if ring else 0)
     assert per_bin_rms(mA, oA).max() < MIXED_RMS_TOL
     assert np.abs(oaspl_db(mA) - oaspl_db(oA)).max() < OASPL_TOL_DB
     assert ctx.error_word(reset=True) == 0
@@ -225,18 +233,22 @@ def test_observer_near_the_origin_in_forward_flight(ctx):
     far = d.subset_observers([0, 2, 3])
     ctx.set_deck(far, bb=False)
     ctx.tonal(native.MIXED)
-    assert ctx.last_plan()["ring_used"] == 1
+    assert ctx.last_plan()["ring_used"] == 512
 
 
 def test_records_reaching_past_the_ring(ctx):
-    """A hovering rotor whose retarded times spread over more bins than the ring holds
-    (tip Mach 0.8 over 2048 steps per revolution: the source's distance from the origin
-    is worth up to 0.8 x 2048 / 2 pi = 261 bins either side): the whole-row kernel
-    launched behind the ring kernel does the work, and matches the oracle; the same rotor
-    at 180 steps (23 bins) runs on the ring, and so does tip Mach 0.68 over 2048 steps (224
-    bins either side: the window's live span fills 487 of the ring's 512 slots)."""
+    """Hovering rotors whose retarded times spread over more bins than a ring holds: the
+    reach of a source point is |x| x (bins per second) / a0, and the live span of a
+    window 2 x reach + 40 bins (with the largest |x| of these blades, 0.90 of the tip
+    radius: 588 x tip Mach bins either side at 4096 steps per revolution, 294 x tip Mach
+    at 2048).  Each runs on the kernel the span selects, and matches the oracle:
+    * 180 steps at tip Mach 0.8 (span 85) and 2048 at 0.68 (444 of 512): the ring;
+    * 2048 steps at tip Mach 0.8 (514, just past the ring) and 4096 at 0.8 (984 of the
+      wide ring's 1024): the wide ring launched behind it;
+    * 4096 steps at tip Mach 0.9 (1102): the whole-row kernel launched last.
+    A ring's result also agrees with whole rows asked for on the same deck."""
     from acum3_periodic_gb300 import native
-    for T, tip, used in ((2048, 0.8, 0), (180, 0.8, 1), (2048, 0.68, 1)):
+    for T, tip, used in ((180, 0.8, 512), (2048, 0.68, 512), (2048, 0.8, 1024), (4096, 0.8, 1024), (4096, 0.9, 0)):
         d = synth.config_deck(0, replicate=37, scale=dict(n_span=4, n_chord_side=3, ntime=T, nobs=6, tip_mach=tip,
                                                            minf=0.0))
         oT, oL, oA, bad = O.tonal(d)
@@ -245,11 +257,22 @@ def test_records_reaching_past_the_ring(ctx):
         pT, pL, mA = ctx.tonal(native.MIXED)
         plan = ctx.last_plan()
         assert plan["ring_slots"] == 512 and plan["ring_used"] == used, T
+        assert plan["wide_ring_slots"] == (1024 if T > 1024 else 0), T
         assert plan["rows_obs_per_block"] > 0
-        assert per_bin_rms(mA, oA).max() < MIXED_RMS_TOL, T
+        tol = LONG_PERIOD_RMS_TOL if T > 2048 else MIXED_RMS_TOL
+        assert per_bin_rms(mA, oA).max() < tol, T
+        assert np.abs(oaspl_db(mA) - oaspl_db(oA)).max() < OASPL_TOL_DB, T
         rms = np.sqrt(np.mean(oA ** 2, axis=0, keepdims=True))
-        assert (np.abs(pT - oT) / rms).max() < MIXED_RMS_TOL, T
+        assert (np.abs(pT - oT) / rms).max() < tol, T
         assert ctx.error_word(reset=True) == 0
+        if used:
+            ctx.set_tile(whole_rows=1)
+            try:
+                _, _, rA = ctx.tonal(native.MIXED)
+                assert ctx.last_plan()["ring_used"] == 0
+            finally:
+                ctx.set_tile()
+            assert per_bin_rms(mA, rA).max() < SAME_DECK_RMS_TOL, T
 
 
 def test_decks_in_sequence_on_one_context(ctx):
