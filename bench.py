@@ -340,7 +340,11 @@ def profile_case(name, device=0):
     blade and 400 observers (376 MB of records) in one persistent launch (32 observers per
     block, two per warp, 8 elements per stage, 8 items per SM); tonal-small: the mixed kernel on
     workload 2 reduced to 25 x 2 x 10 panels per blade and 512 observers; tonal-full: the
-    mixed kernel on workload 2 (for one-pass captures only)."""
+    mixed kernel on workload 2 (for one-pass captures only); tonal-long: hovering rotors
+    of long periods (workload 0's blades at 40 x 2 x 10 panels, 1024 observers; 2048 steps
+    at tip Mach 0.8 and 0.6, 4096 steps at tip Mach 0.6) on the plan's kernel and on
+    whole rows asked for, median of 5 runs each, with their largest difference in units
+    of the observer RMS."""
     from acum3_periodic_gb300 import native, synth
     out = {"case": name}
     if name.startswith("adjoint"):
@@ -360,6 +364,30 @@ def profile_case(name, device=0):
         b.set_tile(32, 8, 8, 2)
         b.run(mode=0)
         out.update(batch_ms=b.timing()[0])
+    elif name == "tonal-long":
+        ctx = native.Context(device)
+        out["decks"] = []
+        for T, tip in ((2048, 0.8), (4096, 0.6), (2048, 0.6)):
+            d = synth.config_deck(0, replicate=37, scale=dict(n_span=40, n_chord_side=10, ntime=T, nobs=1024,
+                                                               tip_mach=tip, minf=0.0))
+            ctx.set_deck(d, bb=False)
+            row = {"steps": T, "tip_mach": tip, "evals": d.tonal_evals()}
+            res = {}
+            for rows in (0, 1):
+                ctx.set_tile(whole_rows=rows)
+                ctx.tonal(native.MIXED)
+                ts = []
+                for _ in range(5):
+                    _, _, res[rows] = ctx.tonal(native.MIXED)
+                    ts.append(ctx.timing(0)[0])
+                ms = float(np.median(ts))
+                plan = ctx.last_plan()
+                row["whole_rows" if rows else "plan"] = {"ms": ms, "evals_per_s": row["evals"] / ms * 1e3,
+                                                         "ring_used": plan["ring_used"]}
+            ctx.set_tile()
+            rms = np.sqrt(np.mean(res[1] ** 2, axis=0, keepdims=True))
+            row["max_diff_over_rms"] = float((np.abs(res[0] - res[1]) / rms).max())
+            out["decks"].append(row)
     else:
         ctx = native.Context(device)
         scale = None if name == "tonal-full" else dict(n_span=25, n_chord_side=10, ntime=1440, nobs=512)
@@ -369,7 +397,7 @@ def profile_case(name, device=0):
     print(json.dumps(out))
 
 
-PROFILE_CASES = ("adjoint-fp64", "adjoint-mixed", "bpm", "batch", "tonal-small", "tonal-full")
+PROFILE_CASES = ("adjoint-fp64", "adjoint-mixed", "bpm", "batch", "tonal-small", "tonal-full", "tonal-long")
 
 
 def batch_leg(native, device, steps=1, inflight=6):
