@@ -32,6 +32,27 @@ def test_noalloc_matches_allocating_entry_point_twice():
             assert per_bin_rms(a, b).max() < MIXED_RMS_TOL
 
 
+def test_noalloc_long_period_on_the_wide_ring():
+    """2048 steps at tip Mach 0.8: the records reach past the 512-slot ring (a live span of
+    514 bins), so both drop-in entry points solve on the wide ring; they agree with each
+    other and with the oracle."""
+    torch = pytest.importorskip("torch")
+    from acum3_periodic_gb300 import native
+    L = native.lib()
+    d = synth.config_deck(0, replicate=37, scale=dict(n_span=4, n_chord_side=3, ntime=2048, nobs=6, tip_mach=0.8,
+                                                       minf=0.0))
+    f = O.preprocess(d)
+    _, _, oA, bad = O.tonal(d)
+    assert bad == 0
+    rc, rT, rL, rA = call_dropin(L.acum_find_pressure_time_history, d, f, np.float32, torch)
+    assert rc == 0, L.acum_last_global_error()
+    rc, nT, nL, nA = call_dropin(L.acum_find_pressure_time_history_noalloc, d, f, np.float32, torch)
+    assert rc == 0, L.acum_noalloc_last_error()
+    for a, b in ((nT, rT), (nL, rL), (nA, rA)):
+        assert per_bin_rms(a, b).max() < MIXED_RMS_TOL
+    assert per_bin_rms(nA, oA).max() < MIXED_RMS_TOL
+
+
 def test_noalloc_rejects_oversized_problems():
     torch = pytest.importorskip("torch")
     from acum3_periodic_gb300 import native
