@@ -9,7 +9,7 @@ import pytest
 from acum3_periodic_gb300 import synth
 from oracle import oracle as O
 
-from metrics import per_bin_rms
+from metrics import oaspl_db, per_bin_rms
 from test_dropin_gpu import call_dropin
 
 pytestmark = pytest.mark.gpu
@@ -35,7 +35,13 @@ def test_noalloc_matches_allocating_entry_point_twice():
 def test_noalloc_long_period_on_the_wide_ring():
     """2048 steps at tip Mach 0.8: the records reach past the 512-slot ring (a live span of
     514 bins), so both drop-in entry points solve on the wide ring; they agree with each
-    other and with the oracle."""
+    other, and with the oracle within the float interface's bound.  The scalars arrive as
+    float32, as the reference passes them, so oM / dPsi (bins per second) carries a
+    relative error of ~1e-7; an observer ~5000 bins of travel time away (20 radii at 2048
+    steps) then has its whole signal shifted by ~5e-4 bins.  Measured against the oracle:
+    the FP64 drop-in given the same float32 scalars 2.3e-3 of the observer RMS, with
+    float32 fields and exact scalars 4e-7; the mixed drop-in 1.4e-3; the context entry
+    point (FP64 scalars) 8.7e-5."""
     torch = pytest.importorskip("torch")
     from acum3_periodic_gb300 import native
     L = native.lib()
@@ -50,7 +56,8 @@ def test_noalloc_long_period_on_the_wide_ring():
     assert rc == 0, L.acum_noalloc_last_error()
     for a, b in ((nT, rT), (nL, rL), (nA, rA)):
         assert per_bin_rms(a, b).max() < MIXED_RMS_TOL
-    assert per_bin_rms(nA, oA).max() < MIXED_RMS_TOL
+    assert per_bin_rms(nA, oA).max() < 3e-3
+    assert np.abs(oaspl_db(nA) - oaspl_db(oA)).max() < 0.05
 
 
 def test_noalloc_rejects_oversized_problems():
