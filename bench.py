@@ -6,8 +6,9 @@ rotor, see acum3_periodic_gb300/synth.py).
 
 GB300 arm (default).  One step = one pass of the tonal path over the deck with the
 surface rows already resident in HBM: GPU preprocessing (preprocess_imper) + the
-mixed-precision tonal kernel (the ring kernel, and the whole-row kernel launched behind it,
-which returns at once on this deck) + the finalize transpose, i.e. acum_tonal_device.
+mixed-precision tonal kernel (the ring kernel, and the wide-ring and whole-row kernels
+launched behind it, which return at once on this deck) + the finalize transpose, i.e.
+acum_tonal_device.
 `value` is element*observer*step evaluations per second over K timed steps (inputs larger
 than L2: 1.47 GB of surface rows and 3.08 GB of records per step).  `e2e` times the same
 metric through acum_tonal_from_host_async: pinned host rows in, pA out, copies inside
