@@ -485,7 +485,8 @@ extern "C" int acum_batch_set_tile(acum_batch* b, int obs_per_block, int elems_p
     if (obs_per_block < 0 || obs_per_block > 16 || items_per_sm < 0 ||
         (elems_per_stage != 0 && elems_per_stage != 2 && elems_per_stage != 4 && elems_per_stage != 8))
         return bfail(b, ACUM_ERR_INVALID, "acum_batch_set_tile: obs_per_block 1..16, elems_per_stage 2, 4 or 8");
-    if (obs_per_block) b->W = obs_per_block;
+    // a kept shape of two observers per warp may hold more observers than 16 warps of one
+    b->W = obs_per_block ? obs_per_block : std::min(b->W, 16);
     if (elems_per_stage) b->SE = elems_per_stage;
     if (items_per_sm) b->ips = items_per_sm;
     b->opw = 1;

@@ -386,7 +386,7 @@ int acum_batch_timing(const acum_batch* b, double* ms, long long* launches);
 /* Device time of one case's tonal kernel in the last mode-1 run. */
 int acum_batch_case_timing(const acum_batch* b, int case_id, double* ms);
 /* One observer per warp: obs_per_block 1..16, elems_per_stage 2, 4 or 8, items_per_sm >= 1
- * (0 keeps a value). */
+ * (0 keeps a value; a kept obs_per_block above 16 becomes 16). */
 int acum_batch_set_tile(acum_batch* b, int obs_per_block, int elems_per_stage, int items_per_sm);
 /* As acum_batch_set_tile with obs_per_warp 1 or 2; two: obs_per_block 2..32 (even; 0 =
  * 32), elems_per_stage 2 or 4 (0 = 4). */

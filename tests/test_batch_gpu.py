@@ -116,6 +116,19 @@ def test_tile_shapes_agree(batch, singles, W, SE, ips, opw):
         assert per_bin_rms(b.result(i), singles[i]).max() < SAME_FORM_RMS, (W, SE, ips, opw, i)
 
 
+def test_tile_with_kept_values(batch, singles):
+    """A shape of one observer per warp set with 0 observers per block after a shape of 32
+    (two per warp) keeps 16, the most one-observer warps a block holds; 0 elements per stage
+    and items per SM keep theirs."""
+    b, decks = batch
+    b.set_tile(32, 8, 8, 2)
+    b.set_tile(0, 4, 0, 1)
+    assert b.tile() == (16, 4, 8) and b.obs_per_warp() == 1
+    b.run(mode=0)
+    for i in range(len(decks)):
+        assert per_bin_rms(b.result(i), singles[i]).max() < SAME_FORM_RMS, i
+
+
 def test_autotune(batch, singles):
     b, decks = batch
     est = b.autotune()
