@@ -374,9 +374,11 @@ extern "C" int acum_last_plan_ring(acum_ctx* ctx, int* out)
     out[2] = ctx->last_rows.SE;
     out[3] = ctx->last_rows.NS;
     out[4] = 0;
-    out[5] = ctx->last_wide.ring;
-    out[6] = ctx->last_wide.W;
-    out[7] = ctx->last_wide.NS;
+    for (int k = 0; k < kWideTiers; ++k) {
+        out[5 + 3 * k] = ctx->last_wide[k].ring;
+        out[6 + 3 * k] = ctx->last_wide[k].W;
+        out[7 + 3 * k] = ctx->last_wide[k].NS;
+    }
     if (ctx->last_tile.ring > 0) {
         // the tests the kernels make, from the same radius
         DeviceGuard g(ctx->device);
@@ -386,7 +388,9 @@ extern "C" int acum_last_plan_ring(acum_ctx* ctx, int* out)
         float r;
         memcpy(&r, &bits, sizeof(r));
         const double kb = ctx->der.oM / ctx->der.dPsi;
-        for (int R : {ctx->last_tile.ring, ctx->last_wide.ring})
+        int rings[1 + kWideTiers] = {ctx->last_tile.ring};
+        for (int k = 0; k < kWideTiers; ++k) rings[1 + k] = ctx->last_wide[k].ring;
+        for (int R : rings)
             if (R > 0 && ring_ok(r, ctx->der.vinf[0], ctx->der.vinf[1], ctx->der.vinf[2], ctx->in.a0, kb,
                                  ctx->obs_rmin, R)) {
                 out[4] = R;
@@ -549,7 +553,7 @@ int acum_ctx::run_tonal(int precision, double* d_pT, double* d_pL, double* d_pA)
     r.acc = d_acc.p;
     r.err = d_err.p;
     last_tile = r.t;
-    last_wide = r.wide;
+    for (int k = 0; k < kWideTiers; ++k) last_wide[k] = r.wide[k];
     last_rows = r.rows;
     have_tonal_plan = true;
     // the mixed form always adds into the FP64 sums; the FP64 form stores when one block
@@ -560,7 +564,8 @@ int acum_ctx::run_tonal(int precision, double* d_pT, double* d_pL, double* d_pA)
     CK(this, cudaEventRecord(ev[EV_TONAL1], stream));
     CK(this, launch_finalize(d_acc.p, nobs, T, d_pT, d_pL, d_pA, 0, stream));
     CK(this, cudaEventRecord(ev[EV_FIN1], stream));
-    launches += r.t.ring > 0 ? (r.wide.ring > 0 ? 4 : 3) : 2;
+    launches += r.t.ring > 0 ? 3 : 2;
+    for (int k = 0; k < kWideTiers; ++k) launches += r.wide[k].ring > 0 ? 1 : 0;
     tonal_timed = true;
     return ACUM_OK;
 }

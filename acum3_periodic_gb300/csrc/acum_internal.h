@@ -242,8 +242,8 @@ cudaError_t launch_per_rows(const float* raw, const long long* raw_off, const in
 struct TonalRun {
     TonalGeom g;
     TonalTile t;          // the plan; mixed with t.ring > 0: the ring kernel, then
-    TonalTile wide;       // the wide-ring kernel (wide.ring > 0: planned) for records that reach
-                          // past the first ring, and
+    TonalTile wide[2];    // the wide-ring kernels (ring > 0: planned; kRingSlotsWide) for records
+                          // that reach past the rings before them, and
     TonalTile rows;       // the whole-row kernel, which runs when every ring is too short
     const unsigned* rmax; // mixed: the records' largest |x| (note_radius bits)
     const void* rec;      // rec64 or rec32
@@ -302,15 +302,20 @@ size_t batch_static_smem(int SE, int opw);  // static shared memory to keep besi
 cudaError_t launch_tonal_batch(const KParams* d_cases, const BatchItem* d_items, int nitems, int* d_counter, int W,
                                int SE, int opw, int rowlen, int grid, cudaStream_t s);
 constexpr int kRingSlots = 512;  // bin slots per observer of the mixed ring kernels (single deck and batched)
-// Bin slots per observer of the wide ring, for records that reach past kRingSlots, in decks
-// of more than kRingSlotsWide steps (whole rows of a shorter period hold no more bins).
-constexpr int kRingSlotsWide = 1024;
+// Bin slots per observer of the wide rings, each for records that reach past the ring
+// before it, in decks of more steps than its slots (whole rows of a shorter period hold no
+// more bins).
+constexpr int kWideTiers = 2;
+constexpr int kRingSlotsWide[kWideTiers] = {1024, 2048};
+static_assert(sizeof(TonalRun::wide) / sizeof(TonalTile) == kWideTiers, "one plan per wide ring");
 // the ring that serves records of largest |x| r (ring_ok), for a deck of T steps: the
-// first ring, else the wide ring, else 0 (whole rows)
+// first ring, else the first wide ring that does, else 0 (whole rows)
 inline int ring_for(float r, double vx, double vy, double vz, double a0, double kb, double obs_rmin, int T)
 {
     if (ring_ok(r, vx, vy, vz, a0, kb, obs_rmin, kRingSlots)) return kRingSlots;
-    if (T > kRingSlotsWide && ring_ok(r, vx, vy, vz, a0, kb, obs_rmin, kRingSlotsWide)) return kRingSlotsWide;
+    for (int k = 0; k < kWideTiers; ++k)
+        if (T > kRingSlotsWide[k] && ring_ok(r, vx, vy, vz, a0, kb, obs_rmin, kRingSlotsWide[k]))
+            return kRingSlotsWide[k];
     return 0;
 }
 // acc [O][T][2] of every case -> pA [T][O] (overwrite)

@@ -199,11 +199,20 @@ int plan(acum_batch* b)
     if (rc0) return rc0;
     if (!b->tile_set) {
         // the default shape, with as many observers per block as the longest rows leave
-        // room for
+        // room for; where that leaves fewer than 12 warps of two, one observer per warp if
+        // that gives more warps (the single-deck wide rings measured likewise)
         b->W = 32;
         b->SE = 8;
         b->opw = 2;
         while (b->W > b->opw && !shape_fits(b, b->W, b->SE, b->opw)) b->W -= b->opw;
+        if (b->W / 2 < 12) {
+            int W1 = 16;
+            while (W1 > 1 && !shape_fits(b, W1, b->SE, 1)) --W1;
+            if (W1 > b->W / 2 && shape_fits(b, W1, b->SE, 1)) {
+                b->W = W1;
+                b->opw = 1;
+            }
+        }
     }
     if (!shape_fits(b, b->W, b->SE, b->opw))
         return bfail(b, ACUM_ERR_INVALID, "tile shape does not fit in shared memory for the longest case");

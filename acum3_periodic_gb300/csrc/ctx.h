@@ -134,7 +134,7 @@ struct acum_ctx {
     long long launches = 0;
     bool prep_timed = false, tonal_timed = false, bpm_timed = false, adj_timed = false, call_timed = false;
     int tile_W = 0, tile_SE = 0, tile_ips = 0, tile_opw = 0, tile_tm = 0, tile_rows = 0;
-    acum::TonalTile last_tile, last_wide, last_rows;
+    acum::TonalTile last_tile, last_wide[acum::kWideTiers], last_rows;
     bool have_tonal_plan = false;
 
     // broadband / adjoint state lives in their own translation units

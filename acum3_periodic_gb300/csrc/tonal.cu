@@ -1379,7 +1379,12 @@ __global__ void __launch_bounds__(512, 1)
 
 constexpr int kMixedSE = 8;   // elements per stage of the whole-row mixed kernel (one observer per warp)
 constexpr int kRingSE = 8;    // elements per stage of the ring kernel
-constexpr int kRingOPW = 2;   // observers per warp of the ring and wide-ring kernels
+constexpr int kRingOPW = 2;   // observers per warp of the ring kernel
+// observers per warp of the wide-ring kernels (1024 and 2048 slots): both then run 12 warps
+// of 24 and 12 observers (two per warp at 2048 slots would leave 6 warps: 40.3 ms against
+// 31.0 ms on 1024 observers of a 4096-step deck; one per warp at 1024 slots 15.1 ms
+// against 13.7 ms on a 2048-step deck)
+constexpr int kWideOPW[kWideTiers] = {2, 1};
 constexpr bool kMixedTmem = false;  // record stages read from tensor memory by default
 static_assert(kMaxStages >= 4, "stage bookkeeping");
 static_assert(sizeof(SmpF) == 16, "sample record");
@@ -1525,12 +1530,12 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
 {
     const bool f64 = r.precision == ACUM_PLAIN_FP64;
     memset(&r.rows, 0, sizeof(r.rows));
-    memset(&r.wide, 0, sizeof(r.wide));
+    memset(r.wide, 0, sizeof(r.wide));
     if (!f64) {
         // Mixed: the ring kernel (observers per warp 1 or 2, default 2; elements per stage
-        // 2, 4 or 8), with the wide-ring kernel behind it in decks of more than
-        // kRingSlotsWide steps, and the whole-row kernel (one observer per warp) last, for
-        // records that reach too far for every ring; whole rows alone when asked for, with
+        // 2, 4 or 8), with the wide-ring kernels behind it (each in decks of more steps than
+        // its slots), and the whole-row kernel (one observer per warp) last, for records
+        // that reach too far for every ring; whole rows alone when asked for, with
         // tensor-memory stages, or without the records' reach.
         const bool tm = tm_req == 1 || (tm_req == 0 && kMixedTmem);
         TonalTile rows;
@@ -1551,21 +1556,21 @@ cudaError_t plan_tonal(TonalRun& r, int W_req, int SE_req, int items_per_sm, int
             return cudaSuccess;
         }
         ring.ring_lo = 0;
-        rows.ring_lo = ring.ring;
-        if (r.g.T > kRingSlotsWide) {
-            // the wide ring, with the ring's observers per warp: as many observers per
-            // block as its rows leave room for (24 in 12 warps at two per warp, two
-            // stages: 13.7 ms against 15.1 ms for 16 warps of one, six stages, on 1024
-            // observers of a 2048-step deck)
+        int below = ring.ring;  // the largest ring planned so far
+        for (int k = 0; k < kWideTiers; ++k) {
+            if (r.g.T <= kRingSlotsWide[k]) break;
+            // a wide ring: as many observers per block as its rows leave room for (one per
+            // warp when one is asked for)
             TonalTile wide;
             memset(&wide, 0, sizeof(wide));
-            if (plan_mixed_tile(r, wide, W_req, SE_req, opw, false, kRingSlotsWide, items_per_sm, num_sms,
-                                smem_optin) == cudaSuccess) {
-                wide.ring_lo = ring.ring;
-                rows.ring_lo = wide.ring;
-                r.wide = wide;
-            }
+            if (plan_mixed_tile(r, wide, W_req, SE_req, opw_req == 1 ? 1 : kWideOPW[k], false, kRingSlotsWide[k],
+                                items_per_sm, num_sms, smem_optin) != cudaSuccess)
+                break;
+            wide.ring_lo = below;
+            below = wide.ring;
+            r.wide[k] = wide;
         }
+        rows.ring_lo = below;
         r.t = ring;
         r.rows = rows;
         return cudaSuccess;
@@ -1736,9 +1741,9 @@ cudaError_t launch_tonal(const TonalRun& r, cudaStream_t s)
     // the wide-ring and whole-row kernels behind the ring kernel: each runs when the
     // records reach too far for the rings before it, and returns at once otherwise
     KParams kr;
-    if (r.wide.ring > 0) {
-        fill_kparams(r, r.wide, kr);
-        e = launch_mixed_tile(kr, r.wide, s);
+    for (int k = 0; k < kWideTiers && r.wide[k].ring > 0; ++k) {
+        fill_kparams(r, r.wide[k], kr);
+        e = launch_mixed_tile(kr, r.wide[k], s);
         if (e != cudaSuccess) return e;
     }
     fill_kparams(r, r.rows, kr);

@@ -327,18 +327,20 @@ class Context:
 
     def last_plan(self) -> dict:
         """The last tonal plan; for the mixed form also `ring_slots` (0: whole rows only),
-        `wide_ring_slots` (0: no wide ring planned) and `ring_used` (the slots of the ring
-        whose kernel did the work, 0: the whole-row kernel)."""
+        `wide_ring_slots` and `wide2_ring_slots` (the 1024- and 2048-slot wide rings; 0:
+        not planned) and `ring_used` (the slots of the ring whose kernel did the work, 0:
+        the whole-row kernel)."""
         v = (C.c_int * 8)()
         self._ck(self.L.acum_last_plan(self.h, v))
         keys = ("obs_per_block", "elems_per_stage", "stages", "elems_per_item", "element_chunks", "work_items",
                 "obs_per_warp", "tensor_memory")
         out = dict(zip(keys, (int(x) for x in v)))
-        r = (C.c_int * 8)()
+        r = (C.c_int * 11)()
         self._ck(self.L.acum_last_plan_ring(self.h, r))
         out.update(ring_slots=int(r[0]), rows_obs_per_block=int(r[1]), rows_elems_per_stage=int(r[2]),
                    rows_stages=int(r[3]), ring_used=int(r[4]), wide_ring_slots=int(r[5]),
-                   wide_obs_per_block=int(r[6]), wide_stages=int(r[7]))
+                   wide_obs_per_block=int(r[6]), wide_stages=int(r[7]), wide2_ring_slots=int(r[8]),
+                   wide2_obs_per_block=int(r[9]), wide2_stages=int(r[10]))
         return out
 
     def timing(self, which: int):

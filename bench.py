@@ -343,7 +343,7 @@ def profile_case(name, device=0):
     workload 2 reduced to 25 x 2 x 10 panels per blade and 512 observers; tonal-full: the
     mixed kernel on workload 2 (for one-pass captures only); tonal-long: hovering rotors
     of long periods (workload 0's blades at 40 x 2 x 10 panels, 1024 observers; 2048 steps
-    at tip Mach 0.8 and 0.6, 4096 steps at tip Mach 0.6) on the plan's kernel and on
+    at tip Mach 0.8 and 0.6, 4096 steps at tip Mach 0.6 and 0.9) on the plan's kernel and on
     whole rows asked for, median of 5 runs each, with their largest difference in units
     of the observer RMS."""
     from acum3_periodic_gb300 import native, synth
@@ -368,7 +368,7 @@ def profile_case(name, device=0):
     elif name == "tonal-long":
         ctx = native.Context(device)
         out["decks"] = []
-        for T, tip in ((2048, 0.8), (4096, 0.6), (2048, 0.6)):
+        for T, tip in ((2048, 0.8), (4096, 0.6), (2048, 0.6), (4096, 0.9)):
             d = synth.config_deck(0, replicate=37, scale=dict(n_span=40, n_chord_side=10, ntime=T, nobs=1024,
                                                                tip_mach=tip, minf=0.0))
             ctx.set_deck(d, bb=False)

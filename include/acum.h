@@ -214,17 +214,17 @@ int acum_set_obs_per_warp(acum_ctx* ctx, int obs_per_warp);
  * from shared memory: 1 = yes, 2 = no, 0 = let the library choose. */
 int acum_set_tensor_memory(acum_ctx* ctx, int use);
 /* Bins of the mixed tonal kernel: 0 = a sliding ring of bins per observer (the ring
- * kernel, 512 slots), with a wide-ring kernel (1024 slots, in decks of more than 1024
- * steps) and the whole-row kernel launched behind it for records whose retarded times
- * spread too far for the rings before them (the default); 1 = whole rows of the period
- * only. */
+ * kernel, 512 slots), with wide-ring kernels (1024 slots in decks of more than 1024 steps,
+ * 2048 slots in decks of more than 2048) and the whole-row kernel launched behind it, each
+ * for records whose retarded times spread too far for the rings before it (the default);
+ * 1 = whole rows of the period only. */
 int acum_set_ring(acum_ctx* ctx, int mode);
-/* The ring side of the last tonal plan (out holds 8 ints): out[0] ring slots per
+/* The ring side of the last tonal plan (out holds 11 ints): out[0] ring slots per
  * observer (0: whole rows only), [1] observers per block, [2] elements per stage and [3]
  * pipeline stages of the whole-row kernel behind the ring kernels, [4] the slots of the
  * ring whose kernel did the work (0: the whole-row kernel; synchronises the context's
- * stream), [5] slots of the wide ring (0: not planned), [6] observers per block and [7]
- * pipeline stages of its kernel. */
+ * stream), [5] slots of the 1024-slot wide ring (0: not planned), [6] observers per block
+ * and [7] pipeline stages of its kernel, [8], [9], [10] the same for the 2048-slot one. */
 int acum_last_plan_ring(acum_ctx* ctx, int* out);
 /* The plan of the last tonal run (out holds 8 ints): out[0] observers per block,
  * [1] elements per stage, [2] pipeline stages, [3] elements per work item, [4] element
@@ -352,13 +352,13 @@ int acum_find_bb_noise(int nSurf_BB, int nObs, int nTime, float dTau, const floa
  * holds many independent decks ("cases") resident on one device and runs all their tonal
  * solves (mixed precision) in one persistent launch: one block per SM takes work items
  * (case, observer tile, element range) from a device counter, largest first.  A case
- * whose records fit the mixed bin ring (or, in a case of more than 1024 steps, the wide
- * ring) runs the ring form on that ring, the others whole rows (the tests of
+ * whose records fit the mixed bin ring (or, in a case of more steps than its slots, a
+ * wide ring of 1024 or 2048 slots) runs the ring form on that ring, the others whole rows (the tests of
  * acum_set_ring, per case).  The tile shape -- observers per block, observers per warp,
  * elements per pipeline stage, work items per SM -- is set by acum_batch_set_tile /
  * acum_batch_set_tile2 or chosen by acum_batch_autotune (default 32 observers per block,
  * two per warp, 8 elements per stage; fewer observers per block where the longest rows
- * leave no room for 32). */
+ * leave no room for 32, and one per warp where two would leave fewer than 12 warps). */
 typedef struct acum_batch acum_batch;
 
 int acum_batch_create(acum_batch** out, int device);

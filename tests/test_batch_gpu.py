@@ -236,3 +236,30 @@ def test_wide_ring_case_in_a_batch():
     _, _, ref, _ = O.tonal(wide, nthreads=8)
     assert per_bin_rms(b.result(1), ref).max() < BIN_RMS
     b.close()
+
+
+def test_cases_on_every_ring_in_one_launch():
+    """Cases on the ring (512 slots), the wide ring (1024: 2048 steps at tip Mach 0.8) and
+    the widest (2048: 4096 steps at tip Mach 0.9) in one launch of the default shape, which
+    then holds 12 observers per block, one per warp; each case matches its single-deck
+    solve."""
+    from acum3_periodic_gb300 import native
+    decks = [shrunk(0)] + [synth.config_deck(0, replicate=37, scale=dict(n_span=4, n_chord_side=3, ntime=T, nobs=6,
+                                                                           tip_mach=tip, minf=0.0))
+                           for T, tip in ((2048, 0.8), (4096, 0.9))]
+    ctx = native.Context(0)
+    singles, forms = [], []
+    for d in decks:
+        ctx.set_deck(d, bb=False)
+        singles.append(ctx.tonal(native.MIXED)[2])
+        forms.append(ctx.last_plan()["ring_used"])
+    ctx.close()
+    assert forms == [512, 1024, 2048]
+    b = native.Batch(0)
+    for d in decks:
+        b.add(d)
+    b.run(mode=0)
+    assert b.tile()[0] == 12 and b.obs_per_warp() == 1
+    for i in range(len(decks)):
+        assert per_bin_rms(b.result(i), singles[i]).max() < SAME_FORM_RMS, i
+    b.close()

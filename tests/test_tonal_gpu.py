@@ -244,11 +244,12 @@ def test_records_reaching_past_the_ring(ctx):
     at 2048).  Each runs on the kernel the span selects, and matches the oracle:
     * 180 steps at tip Mach 0.8 (span 85) and 2048 at 0.68 (444 of 512): the ring;
     * 2048 steps at tip Mach 0.8 (514, just past the ring) and 4096 at 0.8 (984 of the
-      wide ring's 1024): the wide ring launched behind it;
-    * 4096 steps at tip Mach 0.9 (1102): the whole-row kernel launched last.
-    A ring's result also agrees with whole rows asked for on the same deck."""
+      wide ring's 1024): the 1024-slot wide ring launched behind it;
+    * 4096 steps at tip Mach 0.9 (1102): the 2048-slot wide ring launched after that.
+    Each agrees with whole rows asked for on the same deck."""
     from acum3_periodic_gb300 import native
-    for T, tip, used in ((180, 0.8, 512), (2048, 0.68, 512), (2048, 0.8, 1024), (4096, 0.8, 1024), (4096, 0.9, 0)):
+    for T, tip, used in ((180, 0.8, 512), (2048, 0.68, 512), (2048, 0.8, 1024), (4096, 0.8, 1024),
+                         (4096, 0.9, 2048)):
         d = synth.config_deck(0, replicate=37, scale=dict(n_span=4, n_chord_side=3, ntime=T, nobs=6, tip_mach=tip,
                                                            minf=0.0))
         oT, oL, oA, bad = O.tonal(d)
@@ -258,6 +259,7 @@ def test_records_reaching_past_the_ring(ctx):
         plan = ctx.last_plan()
         assert plan["ring_slots"] == 512 and plan["ring_used"] == used, T
         assert plan["wide_ring_slots"] == (1024 if T > 1024 else 0), T
+        assert plan["wide2_ring_slots"] == (2048 if T > 2048 else 0), T
         assert plan["rows_obs_per_block"] > 0
         tol = LONG_PERIOD_RMS_TOL if T > 2048 else MIXED_RMS_TOL
         assert per_bin_rms(mA, oA).max() < tol, T
