@@ -1,34 +1,44 @@
 // tonal.cu -- sm_103a kernels of the tonal (FW-H thickness + loading) path.
 //
-//  prep_kernel          preprocess_imper (preprocess.cu:228-413) on the GPU in FP64, one
-//                       block per element: scaling, make_periodic, optional lowpass,
-//                       periodic d/dtau of P, n, x and of the velocity; writes the tiled
-//                       FP64 and FP32 records the tonal kernels stream.
+//  prep_kernel          preprocess_imper (preprocess.cu:228-413) on the GPU, one block per
+//                       element: scaling, make_periodic, optional lowpass, periodic
+//                       d/dtau of P, n, x and of the velocity; in FP64 for the plain
+//                       form's records, with the geometry in FP32 for the mixed form's
+//                       (the pressure path FP64 in both); writes the tiled records the
+//                       tonal kernels stream, and the records' largest |x| (the reach test
+//                       of the ring kernels).
 //  aos_record_kernel    the same records from the reference's AoS arrays (drop-in entry).
-//  tonal_mixed_kernel   the hot loop of the mixed form (core.cu:18-259 semantics).  A
-//                       block owns W observers, one warp each, and a range of elements.
-//                       Lane = source step inside a 32-step window.  Element tiles are
-//                       moved into shared memory by bulk TMA copies (cp.async.bulk +
-//                       mbarrier complete_tx) into a ring of NS stages shared by the W
-//                       observer warps; the last warp done with a stage refills it.  Each
-//                       lane evaluates the Farassat-1A integrand and the observer time of
-//                       its step; the periodic hat-function binning of core.cu:166-231 is
-//                       done as its equivalent, the piecewise-linear interpolation of the
-//                       retarded-time signal onto the bin grid: lane tau fills the bins in
-//                       (t(tau-1), t(tau)] from its own sample and its left neighbour's
-//                       (one warp shuffle), so lanes never collide and each warp adds into
-//                       its own observer's bins in shared memory with plain read-modify-
-//                       writes -- no atomics.
+//  tonal_mixed_kernel   the hot loop of the mixed form (core.cu:18-259 semantics): one
+//                       persistent block per SM takes work items (observer tile, element
+//                       chunk) from a counter.  A block owns W observers, one or two per
+//                       warp (two share each record load).  Lane = source step inside a
+//                       32-step window (windows overlap by one step, so the periodic wrap
+//                       is an ordinary interval).  Element stages are moved into shared
+//                       memory by bulk copies (cp.async.bulk + mbarrier complete_tx) into a
+//                       ring of NS stages shared by the block's warps; the last warp done
+//                       with a stage refills it.  Each lane evaluates the Farassat-1A
+//                       integrand and the observer time of its step; the periodic
+//                       hat-function binning of core.cu:166-231 is done as its equivalent,
+//                       the piecewise-linear interpolation of the retarded-time signal onto
+//                       the bin grid: lane tau fills the bins in (t(tau-1), t(tau)] from
+//                       its own sample and its left neighbour's (one warp shuffle), so lanes
+//                       never collide and each warp adds into its own observers' bins in
+//                       shared memory with plain read-modify-writes -- no atomics.  The bins
+//                       of an observer are a sliding ring of 512 slots (1024 or 2048 for
+//                       long periods) flushed into the FP64 sums window by window, or whole
+//                       rows of the period for records that reach too far for every ring.
 //  tonal_batch_kernel   the same work items of many decks in one persistent launch.
-//  tonal_f64_kernel     the plain FP64 form, same structure.
+//  tonal_f64_kernel     the plain FP64 form (whole rows, one observer per warp).
 //  finalize_kernel      [obs][bin][2] sums -> pT/pL/pA [bin][obs] (main.cu:123-130 layout).
 //
 // Precision forms.  FP64: every quantity in double, observer time in radians as the
 // reference forms it; matches the reference's FP64 build.  Mixed: the integrand in FP32;
-// the observer time carried as an integer bin index plus an FP32 fraction built from a
-// float-float product (no rounding beyond that of the FP32 retarded time); bin sums in
-// FP32 in shared memory over at most 64 elements, then added into FP64 sums in global
-// memory.
+// per observer the retarded time of the origin is solved once in FP64 and its observer
+// time split into an integer bin and a fraction, and each sample's observer-time offset
+// from it comes from the difference of the two retarded-time quadratics in FP32 (every
+// term of the size of the source's offset from the origin); bin sums in FP32 in shared
+// memory over one work item (at most 512 elements; the ring flushes each bin once the
+// windows that reach it have passed), then added into FP64 sums in global memory.
 #include <cuda_runtime.h>
 #include <stdint.h>
 

@@ -45,7 +45,7 @@ extern "C" {
 
 /* precision of the tonal forms */
 #define ACUM_PLAIN_FP64 0 /* FP64 end to end; matches the reference's FP64 build */
-#define ACUM_MIXED 1      /* FP32 integrand, float-float observer time, compensated bin sums */
+#define ACUM_MIXED 1      /* FP32 integrand, FP64-anchored observer time, FP32 bins summed in FP64 */
 
 /* bits of the device error word (acum_device_error_word) */
 #define ACUM_DEVERR_DISC 0x1u       /* negative discriminant in the retarded-time solve */
