@@ -85,10 +85,21 @@ __device__ __forceinline__ double series_deriv(const double* src, int t, int T, 
     return __dadd_rn(__dsub_rn(__dmul_rn(3.0, d1), __dmul_rn(3.0, d2)), d3);
 }
 
+// Outputs of the 13-tap Gaussian per thread.  The taps are symmetric and bit-identical in
+// pairs (w[k] = w[12 - k]: gauss_taps forms both from the same (k - 6)^2), so the product
+// w[k] Q[q] of output t is also the product w[12 - k] Q[q] of output t + 2k - 12; within a
+// run of consecutive outputs each product is formed once (7 + 42 / kGaussRun per output
+// instead of 13), while every output still adds its 13 products in the reference's order.
+constexpr int kGaussRun = 16;
+
 // two passes of (3-point periodic median, 13-tap periodic Gaussian) on row P, Q scratch
-// (mathfunc.cu:208-341 and 375-421)
+// (mathfunc.cu:208-341 and 375-421); T >= 6, so that one wrap brings every tap of an
+// output into the period
 __device__ void lowpass_rows(double* P, double* Q, int T, const double* w)
 {
+    double wr[7];  // the distinct taps, in registers: their products then repeat exactly
+#pragma unroll
+    for (int j = 0; j < 7; ++j) wr[j] = w[j];
     for (int pass = 0; pass < 2; ++pass) {
         for (int t = threadIdx.x; t < T; t += blockDim.x) {
             const double l = P[t == 0 ? T - 1 : t - 1], m = P[t], r = P[t == T - 1 ? 0 : t + 1];
@@ -97,16 +108,25 @@ __device__ void lowpass_rows(double* P, double* Q, int T, const double* w)
             Q[t] = (kl < hi && kl > lo) ? l : ((km < hi && km > lo) ? m : r);
         }
         __syncthreads();
-        for (int t = threadIdx.x; t < T; t += blockDim.x) {
-            double acc = 0.0;
+        const int nruns = (T + kGaussRun - 1) / kGaussRun;
+        for (int r = threadIdx.x; r < nruns; r += blockDim.x) {
+            const int t0 = r * kGaussRun;
+            // qw[i] = Q[t0 - 6 + i] (periodic); the loads past one wrap feed only outputs
+            // past the period's end, which are not stored
+            double qw[kGaussRun + 12];
 #pragma unroll
-            for (int k = 0; k < 13; ++k) {
-                int q = t + k - 6;
-                if (q < 0) q += T;
-                else if (q > T - 1) q -= T;
-                acc = __dadd_rn(acc, __dmul_rn(w[k], Q[q]));
+            for (int i = 0; i < kGaussRun + 12; ++i) {
+                int q = t0 - 6 + i;
+                q = q < 0 ? q + T : (q > T - 1 ? q - T : q);
+                qw[i] = Q[min(q, T - 1)];
             }
-            P[t] = acc;
+#pragma unroll
+            for (int s = 0; s < kGaussRun; ++s) {
+                double acc = 0.0;
+#pragma unroll
+                for (int k = 0; k < 13; ++k) acc = __dadd_rn(acc, __dmul_rn(wr[k < 6 ? k : 12 - k], qw[s + k]));
+                if (t0 + s < T) P[t0 + s] = acc;
+            }
         }
         __syncthreads();
     }

@@ -229,10 +229,10 @@ def adjoint_leg(native, device):
 
 PER_BYTES_PER_ELEMENT_STEP = 140  # float storage: 12 values read (x, y, z, ds, n, u, P, rho), 23 written
 # FP64 instructions per element-step of per_prep_kernel with the filters on: 2 passes x 5
-# series x 13-tap Gaussian (13 DMUL + 13 DADD) = 260, 14 central differences x (1 DADD +
-# 1 DMUL + 4 DFMA + ...) ~ 84, scaling ~ 13 (SASS opcode counters: DMUL 157, DADD 144,
-# DFMA 56)
-PER_FP64_INSTR_PER_ELEMENT_STEP = 357
+# series x 13-tap Gaussian (13 DADD + 9.625 DMUL: each product shared by two outputs of a
+# run of 16) = 226.25, 14 central differences x (1 DADD + 1 DMUL + 4 DFMA + ...) ~ 84,
+# scaling ~ 13 (SASS thread-instruction counters: DMUL 123.25, DADD 144, DFMA 56)
+PER_FP64_INSTR_PER_ELEMENT_STEP = 323.25
 
 
 def permeable_leg(native, device, steps=3, cpu=True, n_elem=8192, ntime=1440, fp64_peak_tflops=None):
