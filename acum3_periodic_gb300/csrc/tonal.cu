@@ -1373,7 +1373,8 @@ __global__ void __launch_bounds__(512, 1)
         __syncthreads();
         // the item works on a copy, whose constants the compiler keeps in registers instead
         // of reading them from shared memory in the integrand (7334 -> 7173 ms at
-        // workload 4, and no spill at two observers per warp)
+        // workload 4; at two observers per warp and 8 elements per stage ptxas keeps a
+        // 4-byte spill)
         const KParams lp = sp;
         if (lp.ring > 0)
             mixed_item<SE, OPW, false, true>(lp, it.ot, it.e0, it.e1, smem, stage_off, sh, gbase);
