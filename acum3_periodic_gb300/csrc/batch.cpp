@@ -191,29 +191,33 @@ int ring_cases(acum_batch* b)
     return ACUM_OK;
 }
 
+// The default shape (after ring_cases): 32 observers per block, two per warp, 8 elements
+// per stage, with as many observers per block as the longest rows leave room for; where
+// that leaves fewer than 12 warps of two, one observer per warp if that gives more warps
+// (the single-deck wide rings measured likewise).
+void default_shape(acum_batch* b)
+{
+    b->W = 32;
+    b->SE = 8;
+    b->opw = 2;
+    while (b->W > b->opw && !shape_fits(b, b->W, b->SE, b->opw)) b->W -= b->opw;
+    if (b->W / 2 < 12) {
+        int W1 = 16;
+        while (W1 > 1 && !shape_fits(b, W1, b->SE, 1)) --W1;
+        if (W1 > b->W / 2 && shape_fits(b, W1, b->SE, 1)) {
+            b->W = W1;
+            b->opw = 1;
+        }
+    }
+}
+
 int plan(acum_batch* b)
 {
     if (b->cases.empty()) return bfail(b, ACUM_ERR_STATE, "the batch has no cases");
     DeviceGuard g(b->device);
     int rc0 = ring_cases(b);
     if (rc0) return rc0;
-    if (!b->tile_set) {
-        // the default shape, with as many observers per block as the longest rows leave
-        // room for; where that leaves fewer than 12 warps of two, one observer per warp if
-        // that gives more warps (the single-deck wide rings measured likewise)
-        b->W = 32;
-        b->SE = 8;
-        b->opw = 2;
-        while (b->W > b->opw && !shape_fits(b, b->W, b->SE, b->opw)) b->W -= b->opw;
-        if (b->W / 2 < 12) {
-            int W1 = 16;
-            while (W1 > 1 && !shape_fits(b, W1, b->SE, 1)) --W1;
-            if (W1 > b->W / 2 && shape_fits(b, W1, b->SE, 1)) {
-                b->W = W1;
-                b->opw = 1;
-            }
-        }
-    }
+    if (!b->tile_set) default_shape(b);
     if (!shape_fits(b, b->W, b->SE, b->opw))
         return bfail(b, ACUM_ERR_INVALID, "tile shape does not fit in shared memory for the longest case");
     // pools of sums and results
@@ -639,6 +643,7 @@ extern "C" int acum_batch_autotune(acum_batch* b, int probe_per_sm, double* best
     for (int W : {16, 24, 32})
         for (int SE : {2, 4, 8}) shapes.push_back({W, SE, 2});
     double best_rate = 0;
+    default_shape(b);  // kept when no probed shape fits the longest rows
     int bw = b->W, bse = b->SE, bopw = b->opw;
     b->tile_set = true;  // plan() keeps each probed shape
     DBuf<BatchItem> d_probe;

@@ -394,10 +394,11 @@ int acum_batch_set_tile2(acum_batch* b, int obs_per_block, int elems_per_stage, 
 int acum_batch_get_tile(const acum_batch* b, int* obs_per_block, int* elems_per_stage, int* items_per_sm);
 int acum_batch_get_obs_per_warp(const acum_batch* b, int* obs_per_warp);
 /* Chooses the tile shape.  (1) For every observers-per-block in {8, 12, 16} x elements-per-
- * stage in {2, 4, 8} (one observer per warp) and {16, 24, 32} x {2, 4} (two per warp)
+ * stage in {2, 4, 8} (one observer per warp) and {16, 24, 32} x {2, 4, 8} (two per warp)
  * whose shared memory fits, one persistent launch over a probe of
  * 128-element work items spread over all cases (about probe_per_sm items per SM; 0 = 8)
- * gives the kernel's throughput; the fastest shape is kept.  (2) Two probes of that shape
+ * gives the kernel's throughput; the fastest shape is kept (where none fits the longest
+ * rows, the default shape shrunk to fit them).  (2) Two probes of that shape
  * with 64- and 256-element items give its cost per work item and per evaluation, from
  * which the largest-first dynamic schedule of the real work list is simulated for
  * items_per_sm in {4, 8, 16, 32}; the shortest predicted makespan is kept and returned in

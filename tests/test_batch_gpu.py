@@ -263,3 +263,33 @@ def test_cases_on_every_ring_in_one_launch():
     for i in range(len(decks)):
         assert per_bin_rms(b.result(i), singles[i]).max() < SAME_FORM_RMS, i
     b.close()
+
+
+def test_autotune_with_rows_no_probed_shape_holds():
+    """A case whose records need whole rows of 4096 steps (an observer 9 cm from the hub in
+    forward flight, outside every ring's bound) leaves room for at most 6 observer rows per
+    block, fewer than any shape the autotuner probes: it keeps the default shape shrunk to
+    fit, and every case matches its single-deck solve."""
+    from acum3_periodic_gb300 import native
+    near = synth.config_deck(0, replicate=39, scale=dict(n_span=4, n_chord_side=3, ntime=4096, nobs=3, minf=0.1))
+    obs = near.obs_file.copy()
+    obs[1] = np.array([0.0, 0.0, 0.09], np.float32) / np.float32(near.OBSscale)
+    near.obs_file = obs
+    decks = [near, shrunk(5)]
+    ctx = native.Context(0)
+    singles, forms = [], []
+    for d in decks:
+        ctx.set_deck(d, bb=False)
+        singles.append(ctx.tonal(native.MIXED)[2])
+        forms.append(ctx.last_plan()["ring_used"])
+    ctx.close()
+    assert forms == [0, 512]
+    b = native.Batch(0)
+    for d in decks:
+        b.add(d)
+    assert b.autotune() > 0
+    assert b.tile()[0] <= 6
+    b.run(mode=2)
+    for i in range(len(decks)):
+        assert per_bin_rms(b.result(i), singles[i]).max() < SAME_FORM_RMS, i
+    b.close()
